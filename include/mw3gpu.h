@@ -1,0 +1,161 @@
+/*
+ * mw3gpu.h -- C-ABI of the GB300 Chebyshev wave-packet propagator.
+ *
+ * Drop-in for the H.psi application and the Chebyshev loop that madwave3's
+ * main program drives.  In the reference these are argument-less Fortran
+ * module routines sharing module state; here they are functions on an opaque
+ * context.  Every entry point returns 0 (MW3_OK) on success, a positive
+ * MW3_ERR_* code otherwise; mw3_last_error() gives the message.  The host
+ * (Fortran through iso_c_binding, or C/C++/Python) owns every input array and
+ * may free it after the call that takes it: the library copies what it needs.
+ *
+ * Array conventions: all arrays are C row-major, slowest index first.  A
+ * Fortran array A(n1,n2,n3) passes unchanged as C A[n3][n2][n1].  Grid indices
+ * stored in arrays (indr1, indr2, jbas) keep the reference's 1-based values.
+ * State vectors use the reference's flat layout for one process
+ * (indtotproc, SRC/mod_pot_01y2.f:435-455): angles in the order
+ * nangu, nangu-1, ..., 1, then Omega/electronic block, then stored point.
+ *
+ * Threading: one host thread per context; calls on one context must not
+ * overlap.  All device work of a context runs on its own CUDA stream.
+ */
+#ifndef MW3GPU_H
+#define MW3GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MW3_OK 0
+#define MW3_ERR_ARG 1          /* invalid argument or inconsistent sizes */
+#define MW3_ERR_CUDA 2         /* CUDA runtime error */
+#define MW3_ERR_UNSUPPORTED 3  /* input the library does not implement */
+#define MW3_ERR_STATE 4        /* call out of order */
+#define MW3_ERR_NOMEM 5        /* device allocation failed */
+#define MW3_ERR_NUMERIC 6      /* non-finite values detected in the state */
+
+#define MW3_PREC_FP64 0        /* FP64 throughout (the reference's arithmetic) */
+#define MW3_PREC_MIXED 1       /* FP32 transforms, FP64 recursion and accumulators */
+
+typedef struct mw3_ctx mw3_ctx;
+
+/* Grid, masses, cut-offs and the compressed potential grid shared by every
+ * partial wave of a context.  Replaces what mod_gridYpara_01y2 and
+ * mod_pot_01y2 (pot0, pot2) hold for mod_Hphi_01y2
+ * (SRC/mod_gridYpara_01y2.f:38-77, SRC/mod_pot_01y2.f:16-48). */
+typedef struct {
+    int32_t npun1, npun2, nangu, nelec;   /* r1 points, r2 points, angles, electronic states */
+    int32_t npun1min;                     /* minimum DST length in r1 (&inputgridbase) */
+    int32_t npuntot;                      /* max(npunreal): leading dimension of indr1/indr2/vvv */
+    double rmis1, rfin1, rmis2, rfin2;    /* radial grid ends, angstrom */
+    double hbr;                           /* hbar in zot units (mod_gridYpara_01y2.f:21) */
+    double xm1red, xm2red;                /* reduced masses, amu */
+    double radcutmax, rotcutmax;          /* kinetic cut-offs, zots */
+    double emindlt, delta2;               /* Chebyshev centre and half width, zots (pot2 :502-505) */
+    int32_t precision;                    /* MW3_PREC_FP64 or MW3_PREC_MIXED */
+} mw3_grid;
+
+/* One partial wave J: its basis and the namelist values of the modules the
+ * library replaces (mod_absorcion_01y2, mod_flux_01y2, mod_colini's packet
+ * parameters for Smatini_col). */
+typedef struct {
+    int32_t Jtot, iparity, inc, j0, iommin, iommax;
+    int32_t ncan;                         /* number of (electronic state, Omega) blocks */
+    const int32_t *iombas, *nelebas;      /* [ncan]; nelebas 1-based */
+    const int32_t *nojbas, *j00;          /* [ncan] */
+    const int32_t *jbas;                  /* [ncan][nangu] */
+    const int32_t *iomdiat, *iomatom;     /* [nelec] */
+    const double *sigdiat, *sigatom;      /* [nelec] */
+    int32_t nangu2;                       /* nangu*inc */
+    const double *djmmp;                  /* Djmmp(nangu,0:nangu2,nelec,0:Jtot) = [Jtot+1][nelec][nangu2+1][nangu] */
+    int32_t proj_j2_up;                   /* must be 0 */
+    /* &inputabsorcion */
+    double absr1, absalp1, absr2, absalp2;
+    int32_t n1expo, ninterv1, n2expo, ninterv2;
+    /* &inputflux, reference state and process */
+    double r1flux_ang, ekinmin, ekinmax;  /* ekin in zots */
+    int32_t netot, kminelastic, iphoto, iprod;
+    int32_t nvini, nvmax, jini, jmax, nvref, jref, iomref, ielecref;
+    const int32_t *nobc;                  /* noBCstates(jini:jmax,nelec) = [nelec][nj] */
+    const double *ediat;                  /* ediat(nvini:nvmax,jini:jmax,nelec) = [nelec][nj][nv] */
+    const double *fd;                     /* fd(npun1,nvini:nvmax,jini:jmax,nelec) = [nelec][nj][nv][npun1] */
+    double xm1reac, xm2reac;
+    double rcolini, alpha0, xk0, factor0, xmasa0;   /* mod_colini_01y2 */
+    int32_t il0;
+    int32_t nofe;                         /* &inputPsiE: number of energies, 0 = off */
+    const double *efe;                    /* [nofe] zots */
+} mw3_wave;
+
+/* Create a context on the current CUDA device.  npunreal[nangu],
+ * indr1/indr2[nangu][npuntot], vvv[nelec][nelec][nangu][npuntot] with
+ * vvv[je][ie][iang][ir] = VVV(ir,iang,ie,je).
+ * Replaces pot2's device-side state (SRC/mod_pot_01y2.f:344-533). */
+int mw3_create(mw3_ctx **ctx, const mw3_grid *grid, const int32_t *npunreal,
+               const int32_t *indr1, const int32_t *indr2, const double *vvv);
+
+/* Add one partial wave; builds the kinetic, absorption and flux tables
+ * (set_vectors_Hphi SRC/mod_Hphi_01y2.f:38-163, ini_absorcion
+ * SRC/mod_absorcion_01y2.f:28-107, ini_flux/Smatini_col
+ * SRC/mod_flux_01y2.f:54-524, input_PsiE SRC/mod_PsiE_01y2.f:19-88).
+ * *wave_id receives its index (0, 1, ...). */
+int mw3_add_wave(mw3_ctx *ctx, const mw3_wave *wave, int32_t *wave_id);
+
+/* Number of doubles in a wave's state vector (ntotproc, one process). */
+int mw3_wave_size(mw3_ctx *ctx, int32_t wave_id, int64_t *ntot);
+
+/* difs: hpsi = H psi for one wave, host arrays in and out
+ * (SRC/mod_Hphi_01y2.f:623-943).  Leaves the propagation state unchanged. */
+int mw3_hphi(mw3_ctx *ctx, int32_t wave_id, const double *psi, double *hpsi);
+
+/* Fresh start of every wave from its initial packet psi0 (host array):
+ * psi_{k-1} = psi0, psi_k = (H psi0 - emindlt psi0)/delta2, k = 1
+ * (SRC/main_madwave3.f:238-250).  psi0s[w] points at wave w's vector. */
+int mw3_start(mw3_ctx *ctx, const double *const *psi0s);
+
+/* Restart from stored vectors (cont##.paq, SRC/main_madwave3.f:253-260). */
+int mw3_upload_state(mw3_ctx *ctx, int32_t wave_id, const double *psi_km1,
+                     const double *psi_k, int64_t it);
+
+/* n Chebyshev iterations of every wave, device resident: difs, the damped
+ * three-term update, CoefEcheby, totalflux_k, Cvjflux_k, check and funE
+ * (SRC/main_madwave3.f:324-352). */
+int mw3_run(mw3_ctx *ctx, int64_t n_iter);
+
+/* Wait for queued work; reports a deferred CUDA error. */
+int mw3_sync(mw3_ctx *ctx);
+
+int mw3_download_state(mw3_ctx *ctx, int32_t wave_id, double *psi_km1, double *psi_k,
+                       int64_t *it);
+
+/* ||psi_k||^2 after each iteration since the last mw3_start/upload
+ * (check, SRC/main_madwave3.f:431-442): norms[0..*n-1]; *n in: capacity,
+ * out: number written. */
+int mw3_norms(mw3_ctx *ctx, int32_t wave_id, double *norms, int64_t *n);
+
+/* totalflux (SRC/mod_flux_01y2.f:778-816): P(E) and per-state split.
+ * s2prodtot[netot], s2prodelec[nelec][netot] (may be NULL). */
+int mw3_totalflux(mw3_ctx *ctx, int32_t wave_id, double *s2prodtot, double *s2prodelec);
+
+/* Raw accumulators, complex as (re,im) pairs: zcr/zcdr [nflux][netot],
+ * zs2 [ncan][nj][nv][netot], cvj [ncan][nj][nv] of the last iteration,
+ * zfe [nofe][ntot].  Any pointer may be NULL. */
+int mw3_flux_count(mw3_ctx *ctx, int32_t wave_id, int32_t *nflux);
+int mw3_download_accumulators(mw3_ctx *ctx, int32_t wave_id, double *zcr, double *zcdr,
+                              double *zs2, double *cvj, double *zfe);
+
+/* Set-up tables for inspection: nopr1[nangu], reacfct[netot], S2factor
+ * [nelec][nj][nv][netot], etot[netot], absfr1[npun1], absfr2[npun2]. */
+int mw3_tables(mw3_ctx *ctx, int32_t wave_id, int32_t *nopr1, double *etot, double *reacfct,
+               double *s2factor, double *absfr1, double *absfr2);
+
+/* Number of CUDA kernels this context has launched so far. */
+int mw3_kernel_launches(mw3_ctx *ctx, int64_t *count);
+
+const char *mw3_last_error(const mw3_ctx *ctx);
+int mw3_destroy(mw3_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

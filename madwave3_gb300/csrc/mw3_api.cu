@@ -1,0 +1,779 @@
+// C-ABI of libmw3gpu (include/mw3gpu.h): context management, device-side
+// assembly of the per-wave tables and the Chebyshev driver loop
+// (SRC/main_madwave3.f:238-368 for one process, every partial wave of the
+// context advancing together).
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <new>
+
+#include "mw3_internal.h"
+
+using mw3::Ctx;
+using mw3::WaveDev;
+using mw3::WaveTables;
+
+struct mw3_ctx {
+    Ctx c;
+};
+
+namespace {
+
+constexpr int kAngCW = 64;   // column chunk of the angular kernels (must match mw3_kernels.cu)
+
+template <typename V>
+int dupload(Ctx &c, V **dst, const V *src, size_t n)
+{
+    *dst = nullptr;
+    size_t bytes = sizeof(V) * std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc((void **)dst, bytes);
+    if (e != cudaSuccess) {
+        c.err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return MW3_ERR_NOMEM;
+    }
+    c.allocs.push_back(*dst);
+    if (n && src) {
+        e = cudaMemcpy(*dst, src, sizeof(V) * n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            c.err = std::string("cudaMemcpy: ") + cudaGetErrorString(e);
+            return MW3_ERR_CUDA;
+        }
+    }
+    return MW3_OK;
+}
+
+template <typename V>
+int dupload(Ctx &c, V **dst, const std::vector<V> &v)
+{
+    return dupload(c, dst, v.data(), v.size());
+}
+
+template <typename V>
+int dalloc(Ctx &c, V **dst, size_t n, bool zero = true)
+{
+    int rc = dupload<V>(c, dst, nullptr, n);
+    if (rc) return rc;
+    if (zero) {
+        cudaError_t e = cudaMemset(*dst, 0, sizeof(V) * std::max<size_t>(n, 1));
+        if (e != cudaSuccess) {
+            c.err = std::string("cudaMemset: ") + cudaGetErrorString(e);
+            return MW3_ERR_CUDA;
+        }
+    }
+    return MW3_OK;
+}
+
+void free_device(Ctx &c)
+{
+    for (void *p : c.allocs) cudaFree(p);
+    c.allocs.clear();
+    c.built = false;
+}
+
+#define TRY(x)                 \
+    do {                       \
+        int rc_ = (x);         \
+        if (rc_) return rc_;   \
+    } while (0)
+
+// DST-I matrix of length n, the unnormalised RODFT00 of FFTW: S[i][k] = 2 sin(pi (i+1)(k+1)/(n+1))
+std::vector<double> dst_matrix(int n)
+{
+    std::vector<double> s((size_t)n * n);
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < n; k++) {
+            long long m = ((long long)(i + 1) * (k + 1)) % (2LL * (n + 1));
+            s[(size_t)i * n + k] = 2.0 * sin(pi * (double)m / (double)(n + 1));
+        }
+    return s;
+}
+
+template <typename T>
+std::vector<T> cast(const std::vector<double> &v)
+{
+    return std::vector<T>(v.begin(), v.end());
+}
+
+template <typename T>
+int build_typed(Ctx &c)
+{
+    int na = c.na, n1 = c.n1, n2 = c.n2;
+    int W = (int)c.waves.size();
+    // DST matrices
+    {
+        std::vector<T> s2 = cast<T>(dst_matrix(n2));
+        T *d;
+        TRY(dupload(c, &d, s2));
+        c.d_S2 = d;
+        std::map<int, int64_t> off;
+        std::vector<T> s1all;
+        std::vector<int64_t> s1off((size_t)W * na);
+        for (int w = 0; w < W; w++)
+            for (int a = 0; a < na; a++) {
+                int nn = c.waves[w].nopr1[a];
+                auto it = off.find(nn);
+                if (it == off.end()) {
+                    int64_t o = (int64_t)s1all.size();
+                    std::vector<T> m = cast<T>(dst_matrix(nn));
+                    s1all.insert(s1all.end(), m.begin(), m.end());
+                    it = off.emplace(nn, o).first;
+                }
+                s1off[(size_t)w * na + a] = it->second;
+            }
+        T *d1;
+        TRY(dupload(c, &d1, s1all));
+        c.d_S1 = d1;
+        TRY(dupload(c, &c.d_S1off, s1off));
+    }
+    // rectangles, zero outside the stored points
+    size_t rect = (size_t)c.G * na * n1 * n2;
+    T *x, *y;
+    TRY(dalloc(c, &x, rect));
+    TRY(dalloc(c, &y, rect));
+    c.d_X = x;
+    c.d_Y = y;
+    // explicit angular matrices
+    T *xj2, *xl2p;
+    TRY(dalloc(c, &xj2, (size_t)c.G * n1 * na * na));
+    TRY(dalloc(c, &xl2p, (size_t)c.G * 3 * n2 * na * na));
+    c.d_xj2 = xj2;
+    c.d_xl2p = xl2p;
+    mw3::launch_build_kinetic<T>(c);
+    return MW3_OK;
+}
+
+int build_device(Ctx &c)
+{
+    if (c.built) return MW3_OK;
+    if (c.waves.empty()) {
+        c.err = "no partial wave added";
+        return MW3_ERR_STATE;
+    }
+    free_device(c);
+    int na = c.na, n1 = c.n1, n2 = c.n2, ne = c.ne;
+    int W = (int)c.waves.size();
+    // ---- shared grid ----
+    TRY(dupload(c, &c.d_indr1, c.indr1));
+    TRY(dupload(c, &c.d_indr2, c.indr2));
+    TRY(dupload(c, &c.d_npunreal, c.npunreal));
+    TRY(dupload(c, &c.d_vvv, c.vvv));
+    {
+        std::vector<int> map((size_t)na * n1 * n2, -1);
+        for (int a = 0; a < na; a++)
+            for (int ir = 0; ir < c.npunreal[a]; ir++) {
+                int ir1 = c.indr1[(size_t)a * c.npt + ir] - 1, ir2 = c.indr2[(size_t)a * c.npt + ir] - 1;
+                map[((size_t)a * n1 + ir1) * n2 + ir2] = ir;
+            }
+        TRY(dupload(c, &c.d_map, map));
+    }
+    // ---- layout of the wave set ----
+    int G = 0;
+    int64_t NT = 0;
+    for (auto &t : c.waves) {
+        t.g0 = G;
+        t.flat0 = NT;
+        G += t.ncan;
+        NT += t.ntot;
+    }
+    c.G = G;
+    c.NT = NT;
+    c.nseg = G * na;
+    std::vector<int> bw(G), be(G), bo(G), bnoj(G), bjb((size_t)G * na);
+    std::vector<int64_t> foff((size_t)G * na);
+    std::vector<int> cpl((size_t)G * 6, -1), vsrc((size_t)G * ne, -1);
+    std::vector<double> byj2((size_t)G * n1 * na);
+    c.h_slot_used.assign((size_t)G * 3, 0);
+    std::vector<int64_t> wflat0(W + 1);
+    std::vector<int> wseg0(W), wseg1(W);
+    for (int w = 0; w < W; w++) {
+        WaveTables &t = c.waves[w];
+        wflat0[w] = t.flat0;
+        wseg0[w] = t.g0 * na;
+        wseg1[w] = (t.g0 + t.ncan) * na;
+        for (int b = 0; b < t.ncan; b++) {
+            int g = t.g0 + b;
+            bw[g] = w;
+            be[g] = t.nelebas[b];
+            bo[g] = t.iombas[b];
+            bnoj[g] = t.nojbas[b];
+            for (int k = 0; k < na; k++) bjb[(size_t)g * na + k] = t.jbas[(size_t)b * na + k];
+            for (int a = 0; a < na; a++) foff[(size_t)g * na + a] = t.flat0 + t.offs[(size_t)a * t.ncan + b];
+            std::copy(t.yj2.begin() + (size_t)b * n1 * na, t.yj2.begin() + (size_t)(b + 1) * n1 * na,
+                      byj2.begin() + (size_t)g * n1 * na);
+            int nv = 0;
+            for (int s = 0; s < t.ncan; s++) {
+                if (t.iombas[s] == t.iombas[b] && nv < ne) vsrc[(size_t)g * ne + nv++] = t.g0 + s;
+                if (t.nelebas[s] == t.nelebas[b] && abs(t.iombas[s] - t.iombas[b]) <= 1) {
+                    int q = t.iombas[s] - t.iombas[b];
+                    cpl[((size_t)g * 3 + (q + 1)) * 2] = t.g0 + s;
+                    cpl[((size_t)g * 3 + (q + 1)) * 2 + 1] = q;
+                    c.h_slot_used[(size_t)(t.g0 + s) * 3 + (q + 1)] = 1;
+                }
+            }
+        }
+    }
+    wflat0[W] = NT;
+    TRY(dupload(c, &c.d_blk_wave, bw));
+    TRY(dupload(c, &c.d_blk_elec, be));
+    TRY(dupload(c, &c.d_blk_om, bo));
+    TRY(dupload(c, &c.d_blk_nojb, bnoj));
+    TRY(dupload(c, &c.d_blk_jbas, bjb));
+    TRY(dupload(c, &c.d_blk_yj2, byj2));
+    TRY(dupload(c, &c.d_foff, foff));
+    TRY(dupload(c, &c.d_cpl, cpl));
+    TRY(dupload(c, &c.d_vsrc, vsrc));
+    TRY(dupload(c, &c.d_wflat0, wflat0));
+    TRY(dupload(c, &c.d_wseg0, wseg0));
+    TRY(dupload(c, &c.d_wseg1, wseg1));
+    // ---- per-wave tables concatenated ----
+    std::vector<int> nopr1((size_t)W * na);
+    std::vector<double> p2r1((size_t)W * na * n1), p2r2((size_t)W * na * n2), a1((size_t)W * n1),
+        a2((size_t)W * n2);
+    std::vector<double> djall, l2all;
+    std::vector<char> l2used;
+    std::vector<int64_t> djoff(W), l2off(W), l2uoff(W);
+    std::vector<int> wn2(W), wj0(W), winc(W), wmin(W), wmax(W), wnom(W), wnj2(W);
+    std::vector<int> qptr((size_t)W * na + 1, 0), qlist;
+    for (int w = 0; w < W; w++) {
+        WaveTables &t = c.waves[w];
+        std::copy(t.nopr1.begin(), t.nopr1.end(), nopr1.begin() + (size_t)w * na);
+        std::copy(t.p2r1.begin(), t.p2r1.end(), p2r1.begin() + (size_t)w * na * n1);
+        std::copy(t.p2r2.begin(), t.p2r2.end(), p2r2.begin() + (size_t)w * na * n2);
+        std::copy(t.absfr1.begin(), t.absfr1.end(), a1.begin() + (size_t)w * n1);
+        std::copy(t.absfr2.begin(), t.absfr2.end(), a2.begin() + (size_t)w * n2);
+        djoff[w] = (int64_t)djall.size();
+        djall.insert(djall.end(), t.djmmp.begin(), t.djmmp.end());
+        l2off[w] = (int64_t)l2all.size();
+        l2all.insert(l2all.end(), t.l2tab.begin(), t.l2tab.end());
+        l2uoff[w] = (int64_t)l2used.size();
+        l2used.insert(l2used.end(), t.l2used.begin(), t.l2used.end());
+        wn2[w] = t.nangu2; wj0[w] = t.j0; winc[w] = t.inc; wmin[w] = t.iommin; wmax[w] = t.iommax;
+        wnom[w] = t.nom; wnj2[w] = t.nj2;
+        for (int a = 0; a < na; a++) {
+            for (int ir = 0; ir < c.npunreal[a]; ir++)
+                if (c.indr1[(size_t)a * c.npt + ir] > t.nopr1[a]) qlist.push_back(ir);
+            qptr[(size_t)w * na + a + 1] = (int)qlist.size();
+        }
+    }
+    TRY(dupload(c, &c.d_nopr1, nopr1));
+    TRY(dupload(c, &c.d_p2r1, p2r1));
+    TRY(dupload(c, &c.d_p2r2, p2r2));
+    TRY(dupload(c, &c.d_absfr1, a1));
+    TRY(dupload(c, &c.d_absfr2, a2));
+    TRY(dupload(c, &c.d_djall, djall));
+    TRY(dupload(c, &c.d_djoff, djoff));
+    TRY(dupload(c, &c.d_l2all, l2all));
+    TRY(dupload(c, &c.d_l2off, l2off));
+    TRY(dupload(c, &c.d_l2used, l2used));
+    TRY(dupload(c, &c.d_l2uoff, l2uoff));
+    TRY(dupload(c, &c.d_wnangu2, wn2));
+    TRY(dupload(c, &c.d_wj0, wj0));
+    TRY(dupload(c, &c.d_winc, winc));
+    TRY(dupload(c, &c.d_wiommin, wmin));
+    TRY(dupload(c, &c.d_wiommax, wmax));
+    TRY(dupload(c, &c.d_wnom, wnom));
+    TRY(dupload(c, &c.d_wnj2, wnj2));
+    TRY(dupload(c, &c.d_quirk_ptr, qptr));
+    TRY(dupload(c, &c.d_quirk, qlist));
+    // ---- target lists of the angular kernels ----
+    {
+        c.ncj = (n2 + kAngCW - 1) / kAngCW;
+        c.ncl = (n1 + kAngCW - 1) / kAngCW;
+        std::vector<std::vector<int>> bj((size_t)n1 * c.ncj), bl((size_t)n2 * c.ncl);
+        for (int a = 0; a < na; a++)
+            for (int ir = 0; ir < c.npunreal[a]; ir++) {
+                int ir1 = c.indr1[(size_t)a * c.npt + ir] - 1, ir2 = c.indr2[(size_t)a * c.npt + ir] - 1;
+                int ent = (a << 20) | ir;
+                bj[(size_t)ir1 * c.ncj + ir2 / kAngCW].push_back(ent);
+                bl[(size_t)ir2 * c.ncl + ir1 / kAngCW].push_back(ent);
+            }
+        auto flatten = [](std::vector<std::vector<int>> &b, std::vector<int> &ptr, std::vector<int> &lst) {
+            ptr.assign(b.size() + 1, 0);
+            for (size_t i = 0; i < b.size(); i++) {
+                lst.insert(lst.end(), b[i].begin(), b[i].end());
+                ptr[i + 1] = (int)lst.size();
+            }
+        };
+        std::vector<int> pj, lj, pl, ll;
+        flatten(bj, pj, lj);
+        flatten(bl, pl, ll);
+        TRY(dupload(c, &c.d_tj_ptr, pj));
+        TRY(dupload(c, &c.d_tj, lj));
+        TRY(dupload(c, &c.d_tl_ptr, pl));
+        TRY(dupload(c, &c.d_tl, ll));
+    }
+    // ---- recursion vectors and scratch ----
+    TRY(dalloc(c, &c.d_psiA, NT));
+    TRY(dalloc(c, &c.d_psiB, NT));
+    c.d_pk = c.d_psiA;
+    c.d_pkm1 = c.d_psiB;
+    TRY(dalloc(c, &c.d_h, NT));
+    TRY(dalloc(c, &c.d_tmp, NT));
+    c.tmp_cap = NT;
+    TRY(dalloc(c, &c.d_normpart, (size_t)c.nseg));
+    // ---- per-wave accumulators ----
+    c.wdev.assign(W, WaveDev());
+    c.nofemax = 0;
+    for (auto &t : c.waves) c.nofemax = std::max(c.nofemax, t.nofe);
+    TRY(dalloc(c, &c.d_zcke, (size_t)W * std::max(c.nofemax, 1) * 2));
+    std::vector<double *> zfeptr(W, nullptr), normptr(W, nullptr);
+    std::vector<int64_t> normcap(W, 0);
+    for (int w = 0; w < W; w++) {
+        WaveTables &t = c.waves[w];
+        WaveDev &d = c.wdev[w];
+        TRY(dalloc(c, &d.zck, (size_t)t.netot * 2));
+        TRY(dupload(c, &d.etot, t.etot));
+        TRY(dupload(c, &d.reacfct, t.reacfct));
+        TRY(dupload(c, &d.nelebas, t.nelebas));
+        TRY(dupload(c, &d.zar1flux, t.zar1flux));
+        TRY(dupload(c, &d.potiflux, t.potiflux));
+        TRY(dupload(c, &d.fl_idx, t.fl_idx));
+        TRY(dupload(c, &d.fl_block, t.fl_block));
+        TRY(dupload(c, &d.fl_dptr, t.fl_dptr));
+        TRY(dupload(c, &d.fl_didx, t.fl_didx));
+        TRY(dupload(c, &d.fl_dir1, t.fl_dir1));
+        TRY(dalloc(c, &d.zcr, (size_t)t.nflux * t.netot * 2));
+        TRY(dalloc(c, &d.zcdr, (size_t)t.nflux * t.netot * 2));
+        TRY(dalloc(c, &d.zs2, (size_t)t.ncan * t.nj * t.nv * t.netot * 2));
+        TRY(dalloc(c, &d.cvj, (size_t)t.ncan * t.nj * t.nv));
+        TRY(dupload(c, &d.fd, t.fd));
+        TRY(dupload(c, &d.nobc, t.nobc));
+        TRY(dupload(c, &d.r2abs_map, t.r2abs_map));
+        d.djmmp = c.d_djall + djoff[w];
+        if (t.nofe > 0) {
+            TRY(dupload(c, &d.efe, t.efe));
+            TRY(dalloc(c, &d.zfe, (size_t)t.nofe * t.ntot * 2));
+            zfeptr[w] = d.zfe;
+        }
+        d.norms_cap = 1024;
+        TRY(dalloc(c, &d.norms, (size_t)d.norms_cap));
+        normptr[w] = d.norms;
+        normcap[w] = d.norms_cap;
+    }
+    TRY(dupload(c, &c.d_zfe_ptrs, zfeptr));
+    TRY(dupload(c, &c.d_norm_ptrs, normptr));
+    TRY(dupload(c, &c.d_norm_cap, normcap));
+    // ---- typed tables ----
+    mw3::set_kernel_attributes(c);
+    int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        c.err = std::string("building device tables: ") + cudaGetErrorString(e);
+        return MW3_ERR_CUDA;
+    }
+    c.built = true;
+    c.started = false;
+    return MW3_OK;
+}
+
+int grow_norms(Ctx &c, int64_t need)
+{
+    int W = (int)c.waves.size();
+    bool changed = false;
+    std::vector<double *> ptr(W);
+    std::vector<int64_t> cap(W);
+    for (int w = 0; w < W; w++) {
+        WaveDev &d = c.wdev[w];
+        if (need > d.norms_cap) {
+            int64_t nc = std::max(need, 2 * d.norms_cap);
+            double *p;
+            TRY(dalloc(c, &p, (size_t)nc));
+            MW3_CUDA_TRY(cudaMemcpyAsync(p, d.norms, sizeof(double) * d.norms_cap, cudaMemcpyDeviceToDevice,
+                                         c.stream));
+            d.norms = p;
+            d.norms_cap = nc;
+            changed = true;
+        }
+        ptr[w] = d.norms;
+        cap[w] = d.norms_cap;
+    }
+    if (changed) {
+        MW3_CUDA_TRY(cudaMemcpyAsync(c.d_norm_ptrs, ptr.data(), sizeof(double *) * W, cudaMemcpyHostToDevice,
+                                     c.stream));
+        MW3_CUDA_TRY(cudaMemcpyAsync(c.d_norm_cap, cap.data(), sizeof(int64_t) * W, cudaMemcpyHostToDevice,
+                                     c.stream));
+        MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
+    return MW3_OK;
+}
+
+template <typename T>
+void hphi_typed(Ctx &c, const double *psi, int g0, int g1)
+{
+    mw3::launch_hphi<T>(c, psi, g0, g1);
+}
+
+template <typename T>
+void scatter_typed(Ctx &c, const double *psi, int g0, int g1)
+{
+    mw3::launch_scatter<T>(c, psi, g0, g1);
+}
+
+void scatter(Ctx &c, const double *psi, int g0, int g1)
+{
+    if (c.fp64) scatter_typed<double>(c, psi, g0, g1);
+    else scatter_typed<float>(c, psi, g0, g1);
+}
+
+void hphi_all(Ctx &c, const double *psi, int g0, int g1)
+{
+    if (c.fp64) hphi_typed<double>(c, psi, g0, g1);
+    else hphi_typed<float>(c, psi, g0, g1);
+}
+
+void update(Ctx &c, int first)
+{
+    if (c.fp64) mw3::launch_update<double>(c, first);
+    else mw3::launch_update<float>(c, first);
+}
+
+int check_launch(Ctx &c, const char *where)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        c.err = std::string(where) + ": " + cudaGetErrorString(e);
+        return MW3_ERR_CUDA;
+    }
+    return MW3_OK;
+}
+
+int reset_accumulators(Ctx &c)
+{
+    for (size_t w = 0; w < c.waves.size(); w++) {
+        WaveTables &t = c.waves[w];
+        WaveDev &d = c.wdev[w];
+        MW3_CUDA_TRY(cudaMemsetAsync(d.zcr, 0, sizeof(double) * 2 * std::max<size_t>((size_t)t.nflux * t.netot, 1),
+                                     c.stream));
+        MW3_CUDA_TRY(cudaMemsetAsync(d.zcdr, 0, sizeof(double) * 2 * std::max<size_t>((size_t)t.nflux * t.netot, 1),
+                                     c.stream));
+        MW3_CUDA_TRY(cudaMemsetAsync(d.zs2, 0, sizeof(double) * 2 * (size_t)t.ncan * t.nj * t.nv * t.netot,
+                                     c.stream));
+        if (d.zfe) MW3_CUDA_TRY(cudaMemsetAsync(d.zfe, 0, sizeof(double) * 2 * (size_t)t.nofe * t.ntot, c.stream));
+    }
+    return MW3_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+int mw3_create(mw3_ctx **out, const mw3_grid *g, const int32_t *npunreal, const int32_t *indr1,
+               const int32_t *indr2, const double *vvv)
+{
+    if (!out || !g || !npunreal || !indr1 || !indr2 || !vvv) return MW3_ERR_ARG;
+    *out = nullptr;
+    if (g->npun1 < 2 || g->npun2 < 2 || g->nangu < 1 || g->nelec < 1 || g->nelec > 8 || g->npuntot < 1 ||
+        g->npun1 > 256 || g->nangu > 2047 || g->npuntot >= (1 << 20) ||
+        (g->precision != MW3_PREC_FP64 && g->precision != MW3_PREC_MIXED))
+        return MW3_ERR_ARG;
+    if (!(g->delta2 > 0.0) || !(g->rfin1 > g->rmis1) || !(g->rfin2 > g->rmis2)) return MW3_ERR_ARG;
+    mw3_ctx *h = new (std::nothrow) mw3_ctx();
+    if (!h) return MW3_ERR_NOMEM;
+    Ctx &c = h->c;
+    c.grid = *g;
+    c.n1 = g->npun1;
+    c.n2 = g->npun2;
+    c.na = g->nangu;
+    c.ne = g->nelec;
+    c.npt = g->npuntot;
+    c.fp64 = (g->precision == MW3_PREC_FP64);
+    c.npunreal.assign(npunreal, npunreal + c.na);
+    c.indr1.assign(indr1, indr1 + (size_t)c.na * c.npt);
+    c.indr2.assign(indr2, indr2 + (size_t)c.na * c.npt);
+    c.vvv.assign(vvv, vvv + (size_t)c.ne * c.ne * c.na * c.npt);
+    for (int a = 0; a < c.na; a++) {
+        if (c.npunreal[a] < 1 || c.npunreal[a] > c.npt) {
+            delete h;
+            return MW3_ERR_ARG;
+        }
+        for (int ir = 0; ir < c.npunreal[a]; ir++) {
+            int r1 = c.indr1[(size_t)a * c.npt + ir], r2 = c.indr2[(size_t)a * c.npt + ir];
+            if (r1 < 1 || r1 > c.n1 || r2 < 1 || r2 > c.n2) {
+                delete h;
+                return MW3_ERR_ARG;
+            }
+        }
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return MW3_ERR_CUDA;
+    }
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) {
+        // the dynamic shared memory the kernels need must fit the device
+        size_t need = mw3::max_smem_needed(c);
+        if (need > prop.sharedMemPerBlockOptin) {
+            cudaStreamDestroy(c.stream);
+            delete h;
+            return MW3_ERR_UNSUPPORTED;
+        }
+    }
+    *out = h;
+    return MW3_OK;
+}
+
+int mw3_add_wave(mw3_ctx *h, const mw3_wave *w, int32_t *wave_id)
+{
+    if (!h || !w) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (!w->iombas || !w->nelebas || !w->nojbas || !w->j00 || !w->jbas || !w->iomdiat || !w->iomatom ||
+        !w->sigdiat || !w->sigatom || !w->djmmp || !w->nobc || !w->ediat || !w->fd || (w->nofe > 0 && !w->efe)) {
+        c.err = "mw3_add_wave: null array";
+        return MW3_ERR_ARG;
+    }
+    WaveTables t;
+    std::string err;
+    int rc = mw3::build_wave_tables(c, *w, t, err);
+    if (rc) {
+        c.err = "mw3_add_wave: " + err;
+        return rc;
+    }
+    c.waves.push_back(std::move(t));
+    c.built = false;
+    c.started = false;
+    if (wave_id) *wave_id = (int32_t)c.waves.size() - 1;
+    return MW3_OK;
+}
+
+int mw3_wave_size(mw3_ctx *h, int32_t w, int64_t *ntot)
+{
+    if (!h || !ntot || w < 0 || w >= (int)h->c.waves.size()) return MW3_ERR_ARG;
+    *ntot = h->c.waves[w].ntot;
+    return MW3_OK;
+}
+
+int mw3_hphi(mw3_ctx *h, int32_t w, const double *psi, double *hpsi)
+{
+    if (!h || !psi || !hpsi) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) return MW3_ERR_ARG;
+    int rc = build_device(c);
+    if (rc) return rc;
+    WaveTables &t = c.waves[w];
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_tmp + t.flat0, psi, sizeof(double) * t.ntot, cudaMemcpyHostToDevice, c.stream));
+    scatter(c, c.d_tmp, t.g0, t.g0 + t.ncan);
+    hphi_all(c, c.d_tmp, t.g0, t.g0 + t.ncan);
+    // V psi (the update kernel adds it during propagation)
+    mw3::launch_addv(c, c.d_tmp, t.g0, t.g0 + t.ncan);
+    MW3_CUDA_TRY(cudaMemcpyAsync(hpsi, c.d_h + t.flat0, sizeof(double) * t.ntot, cudaMemcpyDeviceToHost, c.stream));
+    if (c.started) scatter(c, c.d_pk, t.g0, t.g0 + t.ncan);   // restore the propagation rectangle
+    rc = check_launch(c, "mw3_hphi");
+    if (rc) return rc;
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return MW3_OK;
+}
+
+int mw3_start(mw3_ctx *h, const double *const *psi0s)
+{
+    if (!h || !psi0s) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    int rc = build_device(c);
+    if (rc) return rc;
+    for (size_t w = 0; w < c.waves.size(); w++) {
+        WaveTables &t = c.waves[w];
+        if (!psi0s[w]) return MW3_ERR_ARG;
+        MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pk + t.flat0, psi0s[w], sizeof(double) * t.ntot, cudaMemcpyHostToDevice,
+                                     c.stream));
+    }
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, c.d_pk, sizeof(double) * c.NT, cudaMemcpyDeviceToDevice, c.stream));
+    rc = reset_accumulators(c);
+    if (rc) return rc;
+    scatter(c, c.d_pk, 0, c.G);
+    hphi_all(c, c.d_pk, 0, c.G);
+    update(c, 1);
+    std::swap(c.d_pk, c.d_pkm1);
+    mw3::launch_norms(c, 0);
+    c.it = 1;
+    c.norm_slot = 1;
+    c.started = true;
+    return check_launch(c, "mw3_start");
+}
+
+int mw3_upload_state(mw3_ctx *h, int32_t w, const double *psi_km1, const double *psi_k, int64_t it)
+{
+    if (!h || !psi_km1 || !psi_k || it < 1) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) return MW3_ERR_ARG;
+    int rc = build_device(c);
+    if (rc) return rc;
+    if (c.started && it != c.it && c.waves.size() > 1) {
+        c.err = "all partial waves of a context share the iteration index";
+        return MW3_ERR_STATE;
+    }
+    WaveTables &t = c.waves[w];
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1 + t.flat0, psi_km1, sizeof(double) * t.ntot, cudaMemcpyHostToDevice,
+                                 c.stream));
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pk + t.flat0, psi_k, sizeof(double) * t.ntot, cudaMemcpyHostToDevice,
+                                 c.stream));
+    scatter(c, c.d_pk, t.g0, t.g0 + t.ncan);
+    if (!c.started) {
+        rc = reset_accumulators(c);
+        if (rc) return rc;
+    }
+    c.it = it;
+    c.norm_slot = 0;
+    c.started = true;
+    rc = check_launch(c, "mw3_upload_state");
+    if (rc) return rc;
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return MW3_OK;
+}
+
+int mw3_run(mw3_ctx *h, int64_t n)
+{
+    if (!h || n < 0) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (!c.started) {
+        c.err = "mw3_run before mw3_start/mw3_upload_state";
+        return MW3_ERR_STATE;
+    }
+    int rc = grow_norms(c, c.norm_slot + n);
+    if (rc) return rc;
+    for (int64_t s = 0; s < n; s++) {
+        int64_t it = c.it + 1;
+        hphi_all(c, c.d_pk, 0, c.G);
+        update(c, 0);
+        std::swap(c.d_pk, c.d_pkm1);
+        mw3::launch_accumulators(c, it);
+        mw3::launch_norms(c, c.norm_slot);
+        c.it = it;
+        c.norm_slot++;
+    }
+    return check_launch(c, "mw3_run");
+}
+
+int mw3_sync(mw3_ctx *h)
+{
+    if (!h) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return check_launch(c, "mw3_sync");
+}
+
+int mw3_download_state(mw3_ctx *h, int32_t w, double *km1, double *k, int64_t *it)
+{
+    if (!h) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size() || !c.started) return MW3_ERR_STATE;
+    WaveTables &t = c.waves[w];
+    if (km1)
+        MW3_CUDA_TRY(cudaMemcpyAsync(km1, c.d_pkm1 + t.flat0, sizeof(double) * t.ntot, cudaMemcpyDeviceToHost,
+                                     c.stream));
+    if (k)
+        MW3_CUDA_TRY(cudaMemcpyAsync(k, c.d_pk + t.flat0, sizeof(double) * t.ntot, cudaMemcpyDeviceToHost,
+                                     c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    if (it) *it = c.it;
+    return MW3_OK;
+}
+
+int mw3_norms(mw3_ctx *h, int32_t w, double *norms, int64_t *n)
+{
+    if (!h || !n) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size() || !c.started) return MW3_ERR_STATE;
+    int64_t m = std::min(*n, c.norm_slot);
+    if (norms && m > 0)
+        MW3_CUDA_TRY(cudaMemcpyAsync(norms, c.wdev[w].norms, sizeof(double) * m, cudaMemcpyDeviceToHost, c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    *n = m;
+    return MW3_OK;
+}
+
+int mw3_totalflux(mw3_ctx *h, int32_t w, double *tot, double *elec)
+{
+    if (!h || !tot) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size() || !c.built) return MW3_ERR_STATE;
+    WaveTables &t = c.waves[w];
+    double *d = nullptr;
+    MW3_CUDA_TRY(cudaMallocAsync(&d, sizeof(double) * (size_t)t.netot * (1 + c.ne), c.stream));
+    mw3::launch_totalflux(c, w, d, d + t.netot);
+    MW3_CUDA_TRY(cudaMemcpyAsync(tot, d, sizeof(double) * t.netot, cudaMemcpyDeviceToHost, c.stream));
+    if (elec)
+        MW3_CUDA_TRY(cudaMemcpyAsync(elec, d + t.netot, sizeof(double) * (size_t)t.netot * c.ne,
+                                     cudaMemcpyDeviceToHost, c.stream));
+    MW3_CUDA_TRY(cudaFreeAsync(d, c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return check_launch(c, "mw3_totalflux");
+}
+
+int mw3_flux_count(mw3_ctx *h, int32_t w, int32_t *nflux)
+{
+    if (!h || !nflux || w < 0 || w >= (int)h->c.waves.size()) return MW3_ERR_ARG;
+    *nflux = h->c.waves[w].nflux;
+    return MW3_OK;
+}
+
+int mw3_download_accumulators(mw3_ctx *h, int32_t w, double *zcr, double *zcdr, double *zs2, double *cvj,
+                              double *zfe)
+{
+    if (!h) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size() || !c.built) return MW3_ERR_STATE;
+    WaveTables &t = c.waves[w];
+    WaveDev &d = c.wdev[w];
+    size_t nf = (size_t)t.nflux * t.netot * 2;
+    size_t ns = (size_t)t.ncan * t.nj * t.nv;
+    if (zcr && nf) MW3_CUDA_TRY(cudaMemcpyAsync(zcr, d.zcr, sizeof(double) * nf, cudaMemcpyDeviceToHost, c.stream));
+    if (zcdr && nf)
+        MW3_CUDA_TRY(cudaMemcpyAsync(zcdr, d.zcdr, sizeof(double) * nf, cudaMemcpyDeviceToHost, c.stream));
+    if (zs2)
+        MW3_CUDA_TRY(cudaMemcpyAsync(zs2, d.zs2, sizeof(double) * ns * t.netot * 2, cudaMemcpyDeviceToHost, c.stream));
+    if (cvj) MW3_CUDA_TRY(cudaMemcpyAsync(cvj, d.cvj, sizeof(double) * ns, cudaMemcpyDeviceToHost, c.stream));
+    if (zfe && d.zfe)
+        MW3_CUDA_TRY(cudaMemcpyAsync(zfe, d.zfe, sizeof(double) * 2 * (size_t)t.nofe * t.ntot, cudaMemcpyDeviceToHost,
+                                     c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return MW3_OK;
+}
+
+int mw3_tables(mw3_ctx *h, int32_t w, int32_t *nopr1, double *etot, double *reacfct, double *s2factor,
+               double *absfr1, double *absfr2)
+{
+    if (!h || w < 0 || w >= (int)h->c.waves.size()) return MW3_ERR_ARG;
+    WaveTables &t = h->c.waves[w];
+    if (nopr1) std::copy(t.nopr1.begin(), t.nopr1.end(), nopr1);
+    if (etot) std::copy(t.etot.begin(), t.etot.end(), etot);
+    if (reacfct) std::copy(t.reacfct.begin(), t.reacfct.end(), reacfct);
+    if (s2factor) std::copy(t.s2factor.begin(), t.s2factor.end(), s2factor);
+    if (absfr1) std::copy(t.absfr1.begin(), t.absfr1.end(), absfr1);
+    if (absfr2) std::copy(t.absfr2.begin(), t.absfr2.end(), absfr2);
+    return MW3_OK;
+}
+
+int mw3_kernel_launches(mw3_ctx *h, int64_t *count)
+{
+    if (!h || !count) return MW3_ERR_ARG;
+    *count = h->c.launches;
+    return MW3_OK;
+}
+
+const char *mw3_last_error(const mw3_ctx *h)
+{
+    if (!h) return "null context";
+    return h->c.err.c_str();
+}
+
+int mw3_destroy(mw3_ctx *h)
+{
+    if (!h) return MW3_OK;
+    Ctx &c = h->c;
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    free_device(c);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete h;
+    return MW3_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,202 @@
+// Internal declarations of libmw3gpu: context layout, device tables and the
+// kernel launchers shared by mw3_api.cu, mw3_setup.cu and mw3_kernels.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mw3gpu.h"
+
+namespace mw3 {
+
+// ---------------------------------------------------------------------------
+// host-side tables of one partial wave (what set_vectors_Hphi, ini_absorcion,
+// ini_flux/Smatini_col and input_PsiE leave in module state)
+// ---------------------------------------------------------------------------
+struct WaveTables {
+    // scalars copied from mw3_wave
+    int Jtot, iparity, inc, j0, iommin, iommax, ncan, nangu2, proj_j2_up;
+    double absr1, absalp1, absr2, absalp2;
+    int n1expo, ninterv1, n2expo, ninterv2;
+    double r1flux_ang, ekinmin, ekinmax;
+    int netot, kminelastic, iphoto, iprod;
+    int nvini, nvmax, jini, jmax, nvref, jref, iomref, ielecref;
+    double xm1reac, xm2reac, rcolini, alpha0, xk0, factor0, xmasa0;
+    int il0, nofe;
+    std::vector<int> iombas, nelebas, nojbas, j00, jbas;   // jbas [ncan][nangu]
+    std::vector<int> iomdiat, iomatom;
+    std::vector<double> sigdiat, sigatom;
+    std::vector<double> djmmp;                              // [Jtot+1][nelec][nangu2+1][nangu]
+    std::vector<int> nobc;
+    std::vector<double> ediat, fd, efe;
+    int nj = 0, nv = 0;
+
+    // layout
+    int64_t ntot = 0;            // points of this wave
+    int64_t flat0 = 0;           // start in the context-wide flat arrays
+    int g0 = 0;                  // first context-wide block
+    std::vector<int64_t> offs;   // [nangu][ncan] flat start relative to flat0
+
+    // Tradial (mod_Hphi_01y2.f:487-620)
+    std::vector<int> nopr1;                 // [nangu]
+    std::vector<double> p2r1, p2r2;         // [nangu][npun1], [nangu][npun2]
+    // angkinj2 scalar part: yyy(ir1, k) for the block's j list, [ncan][npun1][nangu]
+    std::vector<double> yj2;
+    // bfgridl2mat scalar part: xl2mat for (ielec, j, ir2, iom, jom)
+    //   l2tab[((ielec*nj2 + jidx)*npun2 + ir2)*nom*nom + (iom-iommin)*nom + (jom-iommin)]
+    int nj2 = 0, nom = 0;
+    std::vector<double> l2tab;
+    std::vector<char> l2used;               // [ielec][jidx][iom][jom] combination present
+    // ini_absorcion
+    std::vector<double> absfr1, absfr2;
+    int ir1abs = 0, ir2abs = 0;
+    // ini_flux
+    int ir4flux = 0;
+    std::vector<double> zar1flux;           // [npun1][2]
+    std::vector<int> ir1flux;               // [nangu]
+    int nflux = 0;
+    std::vector<int64_t> fl_idx;            // flat index (wave-relative) of each flux point
+    std::vector<int> fl_block;              // block of each flux point
+    std::vector<double> potiflux;
+    std::vector<int> fl_dptr;               // CSR over flux points of the r1-derivative terms
+    std::vector<int64_t> fl_didx;           // wave-relative flat index of each term
+    std::vector<int> fl_dir1;               // ir1 (0-based) of each term
+    // Smatini_col
+    std::vector<double> etot, reacfct, apaqini, s2factor;
+    int icanref = -1;
+    // Cvjflux_k
+    std::vector<int> r2abs_map;             // [nangu][npun1] local point index at ir2abs, or -1
+};
+
+// device pointers of one wave
+struct WaveDev {
+    double *norms = nullptr;                     // norm trace
+    int64_t norms_cap = 0;
+    double *zck = nullptr;                       // [netot][2]
+    double *etot = nullptr, *potiflux = nullptr, *zar1flux = nullptr, *reacfct = nullptr;
+    int64_t *fl_idx = nullptr, *fl_didx = nullptr;
+    int *fl_dptr = nullptr, *fl_dir1 = nullptr, *fl_block = nullptr, *nelebas = nullptr;
+    double *zcr = nullptr, *zcdr = nullptr;      // [nflux][netot][2]
+    double *zs2 = nullptr, *cvj = nullptr;       // [ncan][nj][nv][netot][2], [ncan][nj][nv]
+    double *fd = nullptr;                        // [nelec][nj][nv][npun1]
+    int *nobc = nullptr, *r2abs_map = nullptr;
+    double *djmmp = nullptr;                     // wave's Djmmp
+    double *efe = nullptr, *zfe = nullptr;       // PsiE
+};
+
+struct Ctx {
+    mw3_grid grid;
+    int n1, n2, na, ne, npt;
+    bool fp64;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0;
+    bool started = false;
+    int64_t it = 0;                  // Chebyshev index of psi_k (all waves advance together)
+    int64_t norm_slot = 0;           // iterations recorded since the last start/upload
+
+    // host copies of the shared grid
+    std::vector<int> npunreal, indr1, indr2;
+    std::vector<double> vvv;
+
+    std::vector<WaveTables> waves;
+    std::vector<WaveDev> wdev;
+
+    // context-wide block list (all waves)
+    int G = 0;                       // total blocks
+    int64_t NT = 0;                  // total flat points
+    bool built = false;              // device tables built for the current wave set
+
+    // shared grid on the device
+    int *d_indr1 = nullptr, *d_indr2 = nullptr, *d_npunreal = nullptr;
+    double *d_vvv = nullptr;
+    int *d_map = nullptr;            // [na][n1][n2] local point index, -1 = not stored
+    // block tables
+    int *d_blk_wave = nullptr, *d_blk_elec = nullptr, *d_blk_om = nullptr;
+    int64_t *d_foff = nullptr;       // [G][na] context-wide flat start of (block, angle)
+    int *d_cpl = nullptr;            // [G][3][2]: (source block, q) of the l^2 couplings, -1 = none
+    int *d_vsrc = nullptr;           // [G][nelec]: same-Omega source blocks of V, -1 = none
+    int *d_nopr1 = nullptr;          // [W][na]
+    double *d_p2r1 = nullptr, *d_p2r2 = nullptr;     // [W][na][n1], [W][na][n2]
+    double *d_absfr1 = nullptr, *d_absfr2 = nullptr; // [W][n1], [W][n2]
+    // recursion vectors (context-wide flat layout), H accumulator, norm partials
+    double *d_psiA = nullptr, *d_psiB = nullptr;
+    double *d_pk = nullptr, *d_pkm1 = nullptr;       // aliases, swapped every iteration
+    double *d_h = nullptr;
+    double *d_normpart = nullptr;    // [G*na]
+    // per-wave device tables
+    int64_t *d_wflat0 = nullptr;     // [W+1]
+    int *d_wseg0 = nullptr, *d_wseg1 = nullptr;      // segment range of each wave
+    double **d_norm_ptrs = nullptr;  // [W]
+    int64_t *d_norm_cap = nullptr;   // [W]
+    double **d_zfe_ptrs = nullptr;   // [W]
+    double *d_zcke = nullptr;        // [W][nofemax][2]
+    int nofemax = 0;
+    // rectangles of type T (double or float): X = psi, Y = transform scratch
+    void *d_X = nullptr, *d_Y = nullptr;
+    // DST matrices (type T): S2 [n2][n2]; S1 of every (wave, angle) length, packed
+    void *d_S2 = nullptr, *d_S1 = nullptr;
+    int64_t *d_S1off = nullptr;      // [W][na]
+    // explicit angular kinetic matrices (type T)
+    void *d_xj2 = nullptr;           // [G][n1][na][na]
+    void *d_xl2p = nullptr;          // [G][3][n2][na][na]
+    std::vector<char> h_slot_used;   // [G][3]
+    // inputs of the device-side assembly of xj2/xl2p
+    int *d_blk_nojb = nullptr, *d_blk_jbas = nullptr;
+    double *d_blk_yj2 = nullptr;
+    double *d_djall = nullptr;
+    int64_t *d_djoff = nullptr;
+    int *d_wnangu2 = nullptr, *d_wj0 = nullptr, *d_winc = nullptr, *d_wiommin = nullptr, *d_wiommax = nullptr,
+        *d_wnom = nullptr, *d_wnj2 = nullptr;
+    double *d_l2all = nullptr;
+    int64_t *d_l2off = nullptr, *d_l2uoff = nullptr;
+    char *d_l2used = nullptr;
+    // target lists of the angular kernels
+    int *d_tj_ptr = nullptr, *d_tj = nullptr;   // per (ir1, chunk of ir2): (a<<20 | ir)
+    int *d_tl_ptr = nullptr, *d_tl = nullptr;   // per (ir2, chunk of ir1)
+    int *d_quirk_ptr = nullptr, *d_quirk = nullptr;  // per (wave, angle): local points with ir1 > nopr1
+    int ncj = 0, ncl = 0;
+    // scratch for mw3_hphi
+    double *d_tmp = nullptr;
+    int64_t tmp_cap = 0;
+    int nseg = 0;                    // G*na segments, block-major
+    std::vector<void *> allocs;      // everything allocated for the wave set
+};
+
+// ---------------------------------------------------------------------------
+// setup (mw3_setup.cu)
+// ---------------------------------------------------------------------------
+int build_wave_tables(Ctx &c, const mw3_wave &w, WaveTables &t, std::string &err);
+int noptfft(int nin, int ntot);
+void riccati_fg(int l, double x, double *f, double *g);
+
+// ---------------------------------------------------------------------------
+// kernels (mw3_kernels.cu)
+// ---------------------------------------------------------------------------
+template <typename T>
+void launch_scatter(Ctx &c, const double *psi, int g_begin, int g_end);
+template <typename T>
+void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end);
+template <typename T>
+void launch_update(Ctx &c, int first);
+template <typename T>
+void launch_build_kinetic(Ctx &c);
+void launch_accumulators(Ctx &c, int64_t it);
+void launch_norms(Ctx &c, int64_t slot);
+void launch_addv(Ctx &c, const double *psi, int g0, int g1);
+void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec);
+void set_kernel_attributes(Ctx &c);
+size_t max_smem_needed(Ctx &c);
+
+}  // namespace mw3
+
+#define MW3_CUDA_TRY(expr)                                                            \
+    do {                                                                              \
+        cudaError_t e_ = (expr);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            c.err = std::string(#expr) + ": " + cudaGetErrorString(e_);               \
+            return MW3_ERR_CUDA;                                                      \
+        }                                                                             \
+    } while (0)

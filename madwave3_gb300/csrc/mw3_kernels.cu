@@ -1,0 +1,877 @@
+// CUDA kernels of the Chebyshev hot path (sm_103a).
+//
+// One H.psi application (difs, SRC/mod_Hphi_01y2.f:623-943) is five stages over
+// every Omega/electronic block of every partial wave at once:
+//   1. k_dst_rows   psi rectangle x S2            (DST-I along R, all angles)
+//   2. k_dst_cols   S1 (E o (S1 Y))                (DST-I along r twice, k-space scaling between)
+//   3. k_dst_rows   Y x S2 with a gather epilogue  (kinetic part at the stored points)
+//      k_quirk      stored points with ir1 > nopr1 keep psi (the reference's DST never
+//                   reaches them, mod_Hphi_01y2.f:768-831)
+//   4. k_ang_j      j^2 part: per r1, dense angle x angle matrix (xj2)
+//      k_ang_l      l^2 part incl. Omega+-1 Coriolis coupling: per R (xl2p)
+//   5. k_update     V psi, damped three-term recursion, next rectangle, norm partials
+// followed by the accumulators (CoefEcheby, totalflux_k, Cvjflux_k).
+// T is the transform type: double (plain FP64 path) or float (mixed path); the
+// recursion vectors, potential, absorption and accumulators are always FP64.
+#include <math.h>
+#include <stdio.h>
+
+#include "mw3_internal.h"
+
+namespace mw3 {
+
+// device-side views of the context (passed by value)
+struct DevGrid {
+    int n1, n2, na, ne, npt, G;
+    const int *indr1, *indr2, *npunreal;
+    const double *vvv;
+    const int *map;
+    const int64_t *foff;
+    const int *blk_wave, *blk_elec, *blk_om;
+};
+
+static DevGrid devgrid(Ctx &c)
+{
+    DevGrid d;
+    d.n1 = c.n1; d.n2 = c.n2; d.na = c.na; d.ne = c.ne; d.npt = c.npt; d.G = c.G;
+    d.indr1 = c.d_indr1; d.indr2 = c.d_indr2; d.npunreal = c.d_npunreal; d.vvv = c.d_vvv;
+    d.map = c.d_map; d.foff = c.d_foff;
+    d.blk_wave = c.d_blk_wave; d.blk_elec = c.d_blk_elec; d.blk_om = c.d_blk_om;
+    return d;
+}
+
+#define LAUNCH_CHECK(c) do { (c).launches++; } while (0)
+
+// ---------------------------------------------------------------------------
+// scatter: compressed psi -> rectangle X[g][a][ir1][ir2]
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict__ psi, int seg0)
+{
+    int seg = seg0 + blockIdx.x;
+    int g = seg / d.na, a = seg % d.na;
+    int64_t off = d.foff[seg];
+    int n = d.npunreal[a];
+    T *base = X + (size_t)seg * d.n1 * d.n2;
+    for (int ir = threadIdx.x; ir < n; ir += blockDim.x) {
+        int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
+        int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
+        base[(size_t)ir1 * d.n2 + ir2] = (T)psi[off + ir];
+    }
+    (void)g;
+}
+
+// ---------------------------------------------------------------------------
+// row DST: C[r][:] = A[r][:] x S2 for the rows r = (g, a, ir1) with ir1 < nopr1
+// register-tiled GEMM; epilogue either stores C or gathers it into H
+// ---------------------------------------------------------------------------
+template <typename T> struct RowCfg;
+template <> struct RowCfg<double> { enum { BM = 64, BN = 64, BK = 16, TM = 4, TN = 4 }; };
+template <> struct RowCfg<float> { enum { BM = 128, BN = 128, BK = 8, TM = 8, TN = 8 }; };
+
+template <typename T, bool GATHER>
+__global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict__ A, const T *__restrict__ S,
+                                                  T *__restrict__ C, double *__restrict__ H,
+                                                  const int *__restrict__ nopr1, int64_t row0, int64_t nrows)
+{
+    constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN, BK = RowCfg<T>::BK;
+    constexpr int TM = RowCfg<T>::TM, TN = RowCfg<T>::TN;
+    constexpr int TX = BN / TN, TY = BM / TM;
+    static_assert(TX * TY == 256, "256 threads");
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN];
+    const int n1 = d.n1, n2 = d.n2, na = d.na;
+    int64_t rbase = row0 + (int64_t)blockIdx.y * BM;
+    int cbase = blockIdx.x * BN;
+    int tid = threadIdx.x;
+    // skip tiles whose rows all lie beyond the DST length of their angle
+    __shared__ int any;
+    if (tid == 0) any = 0;
+    __syncthreads();
+    if (tid < BM) {
+        int64_t r = rbase + tid;
+        if (r < row0 + nrows) {
+            int64_t ga = r / n1;
+            int ir1 = (int)(r % n1);
+            int g = (int)(ga / na), a = (int)(ga % na);
+            if (ir1 < nopr1[d.blk_wave[g] * na + a]) any = 1;
+        }
+    }
+    __syncthreads();
+    if (!any) return;
+    int tx = tid % TX, ty = tid / TX;
+    T acc[TM][TN];
+#pragma unroll
+    for (int m = 0; m < TM; m++)
+#pragma unroll
+        for (int n = 0; n < TN; n++) acc[m][n] = (T)0;
+    for (int k0 = 0; k0 < n2; k0 += BK) {
+        for (int e = tid; e < BM * BK; e += 256) {
+            int i = e / BK, kk = e % BK;
+            int64_t r = rbase + i;
+            T v = 0;
+            if (r < row0 + nrows && k0 + kk < n2) v = A[r * n2 + k0 + kk];
+            As[kk][i] = v;
+        }
+        for (int e = tid; e < BK * BN; e += 256) {
+            int kk = e / BN, j = e % BN;
+            T v = 0;
+            if (k0 + kk < n2 && cbase + j < n2) v = S[(size_t)(k0 + kk) * n2 + cbase + j];
+            Bs[kk][j] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; kk++) {
+            T av[TM], bv[TN];
+#pragma unroll
+            for (int m = 0; m < TM; m++) av[m] = As[kk][ty + m * TY];
+#pragma unroll
+            for (int n = 0; n < TN; n++) bv[n] = Bs[kk][tx + n * TX];
+#pragma unroll
+            for (int m = 0; m < TM; m++)
+#pragma unroll
+                for (int n = 0; n < TN; n++) acc[m][n] += av[m] * bv[n];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int m = 0; m < TM; m++) {
+        int64_t r = rbase + ty + m * TY;
+        if (r >= row0 + nrows) continue;
+        int64_t ga = r / n1;
+        int ir1 = (int)(r % n1);
+        int g = (int)(ga / na), a = (int)(ga % na);
+        if (ir1 >= nopr1[d.blk_wave[g] * na + a]) continue;
+#pragma unroll
+        for (int n = 0; n < TN; n++) {
+            int col = cbase + tx + n * TX;
+            if (col >= n2) continue;
+            if (GATHER) {
+                int idx = d.map[((size_t)a * n1 + ir1) * n2 + col];
+                if (idx >= 0) H[d.foff[ga] + idx] = (double)acc[m][n];
+            } else {
+                C[r * n2 + col] = acc[m][n];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// column DSTs: for one (block, angle) and a tile of W columns,
+// Y[0:nn][cols] <- S1 ( E o (S1 Y[0:nn][cols]) ),  E = min(p2r1+p2r2, radcut)/(4(nn+1)(n2+1))
+// ---------------------------------------------------------------------------
+constexpr int COL_W = 32;
+constexpr int COL_KC = 32;
+constexpr int COL_RMAX = 32;   // rows per thread (n1 <= 256)
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, const T *__restrict__ S1all,
+                                                  const int64_t *__restrict__ s1off, const int *__restrict__ nopr1,
+                                                  const double *__restrict__ p2r1, const double *__restrict__ p2r2,
+                                                  double radcut, int seg0)
+{
+    extern __shared__ unsigned char smraw[];
+    T *Yt = reinterpret_cast<T *>(smraw);                 // [n1][COL_W]
+    T *Sc = Yt + (size_t)d.n1 * COL_W;                    // [n1][COL_KC]
+    int seg = seg0 + blockIdx.y;
+    int g = seg / d.na, a = seg % d.na;
+    int w = d.blk_wave[g];
+    int nn = nopr1[w * d.na + a];
+    const T *S1 = S1all + s1off[w * d.na + a];
+    int n1 = d.n1, n2 = d.n2;
+    int c0 = blockIdx.x * COL_W;
+    int tx = threadIdx.x % COL_W, ty = threadIdx.x / COL_W;   // 8 row groups
+    T *base = Y + (size_t)seg * n1 * n2;
+    for (int e = threadIdx.x; e < nn * COL_W; e += 256) {
+        int k = e / COL_W, cc = e % COL_W;
+        Yt[k * COL_W + cc] = (c0 + cc < n2) ? base[(size_t)k * n2 + c0 + cc] : (T)0;
+    }
+    const double *p1 = p2r1 + ((size_t)w * d.na + a) * n1;
+    const double *p2 = p2r2 + ((size_t)w * d.na + a) * n2;
+    const T divi = (T)(1.0 / (4.0 * (double)(nn + 1) * (double)(n2 + 1)));
+    const T rcut = (T)radcut;
+    T acc[COL_RMAX];
+    for (int pass = 0; pass < 2; pass++) {
+#pragma unroll
+        for (int r = 0; r < COL_RMAX; r++) acc[r] = (T)0;
+        for (int kc = 0; kc < nn; kc += COL_KC) {
+            __syncthreads();
+            for (int e = threadIdx.x; e < nn * COL_KC; e += 256) {
+                int i = e / COL_KC, kk = e % COL_KC;
+                Sc[i * COL_KC + kk] = (kc + kk < nn) ? S1[(size_t)i * nn + kc + kk] : (T)0;
+            }
+            __syncthreads();
+            int kmax = min(COL_KC, nn - kc);
+            for (int kk = 0; kk < kmax; kk++) {
+                T y = Yt[(kc + kk) * COL_W + tx];
+#pragma unroll
+                for (int r = 0; r < COL_RMAX; r++) {
+                    int i = ty + 8 * r;
+                    if (i < nn) acc[r] += Sc[i * COL_KC + kk] * y;
+                }
+            }
+        }
+        __syncthreads();
+        if (pass == 0) {
+            int col = c0 + tx;
+#pragma unroll
+            for (int r = 0; r < COL_RMAX; r++) {
+                int i = ty + 8 * r;
+                if (i < nn && col < n2) {
+                    T ek = (T)p1[i] + (T)p2[col];
+                    if (ek > rcut) ek = rcut;
+                    Yt[i * COL_W + tx] = acc[r] * ek * divi;
+                } else if (i < nn) {
+                    Yt[i * COL_W + tx] = (T)0;
+                }
+            }
+        }
+    }
+    int col = c0 + tx;
+    if (col < n2)
+#pragma unroll
+        for (int r = 0; r < COL_RMAX; r++) {
+            int i = ty + 8 * r;
+            if (i < nn) base[(size_t)i * n2 + col] = acc[r];
+        }
+}
+
+// stored points with ir1 beyond the DST length keep psi as their "kinetic" term
+__global__ void k_quirk(DevGrid d, const double *__restrict__ psi, double *__restrict__ H,
+                        const int *__restrict__ qptr, const int *__restrict__ qlist, int seg0)
+{
+    int seg = seg0 + blockIdx.x;
+    int g = seg / d.na, a = seg % d.na;
+    int w = d.blk_wave[g];
+    int b = qptr[w * d.na + a], e = qptr[w * d.na + a + 1];
+    int64_t off = d.foff[seg];
+    for (int q = b + threadIdx.x; q < e; q += blockDim.x) {
+        int ir = qlist[q];
+        H[off + ir] = psi[off + ir];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// angular kinetic terms in the grid representation
+// ---------------------------------------------------------------------------
+constexpr int ANG_CW = 64;
+
+// j^2: H(g, a, r1, r2) += sum_j' X(g, j', r1, r2) xj2(g, r1, a, j')
+template <typename T>
+__global__ void __launch_bounds__(256) k_ang_j(DevGrid d, const T *__restrict__ X, const T *__restrict__ xj2,
+                                               double *__restrict__ H, const int *__restrict__ tptr,
+                                               const int *__restrict__ tlist, int ncj, int g0)
+{
+    extern __shared__ unsigned char smraw[];
+    int chunk = blockIdx.x, ir1 = blockIdx.y, g = g0 + blockIdx.z;
+    int b = tptr[ir1 * ncj + chunk], e = tptr[ir1 * ncj + chunk + 1];
+    if (b == e) return;
+    int na = d.na, n1 = d.n1, n2 = d.n2;
+    T *Xs = reinterpret_cast<T *>(smraw);       // [na][ANG_CW]
+    T *xs = Xs + (size_t)na * ANG_CW;           // [na][na+1]
+    int c0 = chunk * ANG_CW;
+    for (int i = threadIdx.x; i < na * ANG_CW; i += blockDim.x) {
+        int j = i / ANG_CW, cc = i % ANG_CW;
+        Xs[i] = (c0 + cc < n2) ? X[(((size_t)g * na + j) * n1 + ir1) * n2 + c0 + cc] : (T)0;
+    }
+    const T *xm = xj2 + ((size_t)g * n1 + ir1) * na * na;
+    for (int i = threadIdx.x; i < na * na; i += blockDim.x) xs[(i / na) * (na + 1) + (i % na)] = xm[i];
+    __syncthreads();
+    for (int q = b + threadIdx.x; q < e; q += blockDim.x) {
+        int ent = tlist[q];
+        int a = ent >> 20, ir = ent & 0xFFFFF;
+        int col = d.indr2[(size_t)a * d.npt + ir] - 1 - c0;
+        T acc = (T)0;
+        const T *row = xs + (size_t)a * (na + 1);
+        for (int j = 0; j < na; j++) acc += Xs[j * ANG_CW + col] * row[j];
+        H[d.foff[(size_t)g * na + a] + ir] += (double)acc;
+    }
+}
+
+// l^2 with Omega coupling: H(t, a, r1, r2) += sum_(s,q) sum_j' X(s, j', r1, r2) xl2p(s, q, r2, a, j')
+template <typename T>
+__global__ void __launch_bounds__(256) k_ang_l(DevGrid d, const T *__restrict__ X, const T *__restrict__ xl2p,
+                                               double *__restrict__ H, const int *__restrict__ tptr,
+                                               const int *__restrict__ tlist, const int *__restrict__ cpl, int ncl,
+                                               int g0)
+{
+    extern __shared__ unsigned char smraw[];
+    int chunk = blockIdx.x, ir2 = blockIdx.y, t = g0 + blockIdx.z;
+    int b = tptr[ir2 * ncl + chunk], e = tptr[ir2 * ncl + chunk + 1];
+    if (b == e) return;
+    int na = d.na, n1 = d.n1, n2 = d.n2;
+    T *acc = reinterpret_cast<T *>(smraw);                     // [e-b]
+    T *Xs = reinterpret_cast<T *>(acc + (na * ANG_CW));         // [na][ANG_CW]
+    T *xs = Xs + (size_t)na * ANG_CW;                           // [na][na+1]
+    int c0 = chunk * ANG_CW;
+    int nt = e - b;
+    for (int q = threadIdx.x; q < nt; q += blockDim.x) acc[q] = (T)0;
+    for (int slot = 0; slot < 3; slot++) {
+        int s = cpl[(t * 3 + slot) * 2], qq = cpl[(t * 3 + slot) * 2 + 1];
+        if (s < 0) continue;
+        __syncthreads();
+        for (int i = threadIdx.x; i < na * ANG_CW; i += blockDim.x) {
+            int j = i / ANG_CW, cc = i % ANG_CW;
+            Xs[i] = (c0 + cc < n1) ? X[(((size_t)s * na + j) * n1 + c0 + cc) * n2 + ir2] : (T)0;
+        }
+        const T *xm = xl2p + (((size_t)s * 3 + (qq + 1)) * n2 + ir2) * na * na;
+        for (int i = threadIdx.x; i < na * na; i += blockDim.x) xs[(i / na) * (na + 1) + (i % na)] = xm[i];
+        __syncthreads();
+        for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+            int ent = tlist[b + q];
+            int a = ent >> 20, ir = ent & 0xFFFFF;
+            int col = d.indr1[(size_t)a * d.npt + ir] - 1 - c0;
+            T s_ = (T)0;
+            const T *row = xs + (size_t)a * (na + 1);
+            for (int j = 0; j < na; j++) s_ += Xs[j * ANG_CW + col] * row[j];
+            acc[q] += s_;
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+        int ent = tlist[b + q];
+        int a = ent >> 20, ir = ent & 0xFFFFF;
+        H[d.foff[(size_t)t * na + a] + ir] += (double)acc[q];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// potential, damped Chebyshev recursion (main_madwave3.f:332-339, first step
+// :245-248), next rectangle, norm partials and funE (mod_PsiE_01y2.f:108-120)
+// ---------------------------------------------------------------------------
+struct UpdArgs {
+    const double *H, *pk, *pkm1;
+    double *out;
+    const int *vsrc;               // [G][ne]
+    const double *absfr1, *absfr2; // [W][n1], [W][n2]
+    double emindlt, delta2;
+    int first;
+    double *normpart;              // [G*na]
+    int nofe;                      // max over waves; 0 = funE off
+    const double *zcke;            // [W][nofe][2]
+    double *const *zfe;            // per wave [nofe][ntot_w][2] (null when the wave has none)
+    const int64_t *wflat0;         // [W+1]
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
+{
+    int seg = blockIdx.x;
+    int g = seg / d.na, a = seg % d.na;
+    int w = d.blk_wave[g];
+    int et = d.blk_elec[g];
+    int64_t off = d.foff[seg];
+    int n = d.npunreal[a];
+    int n1 = d.n1, n2 = d.n2, na = d.na, ne = d.ne;
+    T *rect = X + (size_t)seg * n1 * n2;
+    double nrm = 0.0;
+    double *zf = (u.nofe > 0 && !u.first) ? u.zfe[w] : nullptr;
+    int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
+    for (int ir = threadIdx.x; ir < n; ir += blockDim.x) {
+        int64_t i = off + ir;
+        int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
+        int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
+        double hv = u.H[i];
+        for (int q = 0; q < ne; q++) {
+            int s = u.vsrc[g * ne + q];
+            if (s < 0) continue;
+            int es = d.blk_elec[s];
+            double v = d.vvv[((((size_t)(et - 1) * ne + (es - 1)) * na) + a) * d.npt + ir];
+            hv += u.pk[d.foff[(size_t)s * na + a] + ir] * v;
+        }
+        double nv;
+        double pk = u.pk[i];
+        if (u.first) {
+            nv = (hv - u.emindlt * pk) / u.delta2;
+        } else {
+            double fab = u.absfr1[(size_t)w * n1 + ir1] * u.absfr2[(size_t)w * n2 + ir2];
+            double rhn = (hv - u.emindlt * pk) / u.delta2;
+            nv = (2.0 * rhn - fab * u.pkm1[i]) * fab;
+        }
+        u.out[i] = nv;
+        rect[(size_t)ir1 * n2 + ir2] = (T)nv;
+        nrm += nv * nv;
+        if (zf) {
+            for (int e = 0; e < u.nofe; e++) {
+                const double *ck = u.zcke + ((size_t)w * u.nofe + e) * 2;
+                double *zz = zf + ((size_t)e * wlen + (i - wst)) * 2;
+                zz[0] += ck[0] * nv;
+                zz[1] += ck[1] * nv;
+            }
+        }
+    }
+    // block reduction of the norm partial in a fixed order (deterministic)
+    __shared__ double red[256];
+    red[threadIdx.x] = nrm;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) u.normpart[seg] = red[0];
+}
+
+// V psi alone, for mw3_hphi: H(t) += sum_s V(e_s, e_t) psi(s) over same-Omega blocks
+// (difs V part, mod_Hphi_01y2.f:838-853)
+__global__ void k_addv(DevGrid d, const double *__restrict__ psi, double *__restrict__ H, const int *__restrict__ vsrc,
+                       int seg0)
+{
+    int seg = seg0 + blockIdx.x;
+    int g = seg / d.na, a = seg % d.na;
+    int et = d.blk_elec[g];
+    int64_t off = d.foff[seg];
+    int n = d.npunreal[a];
+    for (int ir = threadIdx.x; ir < n; ir += blockDim.x) {
+        double hv = H[off + ir];
+        for (int q = 0; q < d.ne; q++) {
+            int s = vsrc[g * d.ne + q];
+            if (s < 0) continue;
+            int es = d.blk_elec[s];
+            double v = d.vvv[((((size_t)(et - 1) * d.ne + (es - 1)) * d.na) + a) * d.npt + ir];
+            hv += psi[d.foff[(size_t)s * d.na + a] + ir] * v;
+        }
+        H[off + ir] = hv;
+    }
+}
+
+// check (main_madwave3.f:431-442): sum the norm partials of each wave
+__global__ void k_norms(const double *__restrict__ part, const int *__restrict__ wseg0, const int *__restrict__ wseg1,
+                        double *const *norms_out, const int64_t *__restrict__ cap, int64_t slot)
+{
+    int w = blockIdx.x;
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = wseg0[w] + threadIdx.x; i < wseg1[w]; i += blockDim.x) s += part[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && slot >= 0 && slot < cap[w]) norms_out[w][slot] = red[0];
+}
+
+// ---------------------------------------------------------------------------
+// accumulators
+// ---------------------------------------------------------------------------
+// CoefEcheby (main_madwave3.f:462-490): C_k(E) = d hbar/Delta e^{-ik acos Es}/sqrt(1-Es^2)
+__global__ void k_coefecheby(const double *__restrict__ etot, int netot, double emindlt, double delta2,
+                             double hbr, int64_t k, double *__restrict__ zck)
+{
+    int ie = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ie >= netot) return;
+    double dd = (k == 0) ? 1.0 : 2.0;
+    double zf = dd * hbr / delta2;
+    double Es = (etot[ie] - emindlt) / delta2;
+    double expo = -(double)k * acos(Es);
+    double deno = sqrt(1.0 - Es * Es);
+    double s, c;
+    sincos(expo, &s, &c);
+    zck[2 * ie] = zf * c / deno;
+    zck[2 * ie + 1] = zf * s / deno;
+}
+
+// totalflux_k (mod_flux_01y2.f:585-660): derivative at the flux line, rank-1 updates
+__global__ void __launch_bounds__(256) k_flux(const double *__restrict__ psi, const int64_t *__restrict__ fidx,
+                                              const int *__restrict__ dptr, const int64_t *__restrict__ didx,
+                                              const int *__restrict__ dir1, const double *__restrict__ zar,
+                                              const double *__restrict__ poti, const double *__restrict__ etot,
+                                              const double *__restrict__ zck, int netot, int gate_zero,
+                                              double *__restrict__ zcr, double *__restrict__ zcdr)
+{
+    int f = blockIdx.x;
+    __shared__ double dr, di, pf;
+    if (threadIdx.x == 0) {
+        double sr = 0.0, si = 0.0;
+        for (int q = dptr[f]; q < dptr[f + 1]; q++) {
+            double p = psi[didx[q]];
+            int ir1 = dir1[q];
+            sr = sr + (zar[2 * ir1] * p - zar[2 * ir1 + 1] * 0.0);
+            si = si + (zar[2 * ir1] * 0.0 + zar[2 * ir1 + 1] * p);
+        }
+        dr = sr;
+        di = si;
+        pf = psi[fidx[f]];
+    }
+    __syncthreads();
+    if (gate_zero) return;
+    double p = poti[f];
+    for (int ie = threadIdx.x; ie < netot; ie += blockDim.x) {
+        if (!(etot[ie] > p)) continue;
+        double cr = zck[2 * ie], ci = zck[2 * ie + 1];
+        size_t o = ((size_t)f * netot + ie) * 2;
+        zcr[o] += cr * pf;
+        zcr[o + 1] += ci * pf;
+        zcdr[o] += cr * dr - ci * di;
+        zcdr[o + 1] += cr * di + ci * dr;
+    }
+}
+
+// Cvjflux_k (mod_flux_01y2.f:663-775) for one block: projection at R(ir2abs) on
+// Djmmp x fd, then zS2 += Cvj C_k
+struct CvjArgs {
+    const double *psi;
+    const int *r2abs_map;        // [na][n1]
+    const double *djmmp;         // wave's Djmmp
+    const double *fd;            // [nelec][nj][nv][n1]
+    const int *nobc;             // [nelec][nj]
+    const double *zck;
+    double *zs2, *cvj;
+    int nangu2, jini, jmax, nvini, nvmax, inc, j00, ielec, iom, nj, nv, netot;
+    int skip_ref;                // ifail for the reference channel this iteration
+    int jref, nvref;
+    double sah2;
+    int blk;                     // block index within the wave
+    int64_t foff_row;            // index into foff for (g, angle 0)
+};
+
+__global__ void __launch_bounds__(256) k_cvj(DevGrid d, CvjArgs c)
+{
+    extern __shared__ double xjs[];            // [n1][nj]
+    int na = d.na, n1 = d.n1, ne = d.ne;
+    int nj = c.nj, nv = c.nv;
+    for (int e = threadIdx.x; e < n1 * nj; e += blockDim.x) {
+        int ir1 = e / nj, jj = e % nj;
+        int j = c.jini + jj;
+        double xj = 0.0;
+        if (j >= c.j00 && ((j - c.j00) % c.inc) == 0) {
+            for (int ia = 0; ia < na; ia++) {
+                int a = na - 1 - ia;            // angle order of the flat vector
+                int ir = c.r2abs_map[(size_t)a * n1 + ir1];
+                double rori = (ir >= 0) ? c.psi[d.foff[c.foff_row + a] + ir] / c.sah2 : 0.0;
+                double dj = c.djmmp[(((size_t)c.iom * ne + (c.ielec - 1)) * (c.nangu2 + 1) + j) * na + a];
+                xj = xj + rori * dj;
+            }
+        }
+        xjs[ir1 * nj + jj] = xj;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nj * nv; e += blockDim.x) {
+        int jj = e / nv, iv = e % nv;
+        int j = c.jini + jj;
+        int nob = c.nobc[(size_t)(c.ielec - 1) * nj + jj];
+        int maxnv = c.nvmax < nob ? c.nvmax : nob;
+        double r = 0.0;
+        bool on = (j >= c.j00 && ((j - c.j00) % c.inc) == 0 && c.nvini + iv <= maxnv);
+        if (on) {
+            const double *f = c.fd + (((size_t)(c.ielec - 1) * nj + jj) * nv + iv) * n1;
+            for (int ir1 = 0; ir1 < n1; ir1++) r = r + xjs[ir1 * nj + jj] * f[ir1];
+        }
+        c.cvj[((size_t)c.blk * nj + jj) * nv + iv] = on ? r : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nj * nv * c.netot; e += blockDim.x) {
+        int ie = e % c.netot, jv = e / c.netot;
+        int jj = jv / nv, iv = jv % nv;
+        int j = c.jini + jj;
+        int nob = c.nobc[(size_t)(c.ielec - 1) * nj + jj];
+        int maxnv = c.nvmax < nob ? c.nvmax : nob;
+        if (!(j >= c.j00 && ((j - c.j00) % c.inc) == 0 && c.nvini + iv <= maxnv)) continue;
+        if (c.skip_ref && j == c.jref && c.nvini + iv == c.nvref) continue;
+        double z = c.cvj[((size_t)c.blk * nj + jj) * nv + iv];
+        size_t o = ((((size_t)c.blk * nj + jj) * nv + iv) * c.netot + ie) * 2;
+        c.zs2[o] += z * c.zck[2 * ie];
+        c.zs2[o + 1] += z * c.zck[2 * ie + 1];
+    }
+}
+
+// totalflux (mod_flux_01y2.f:778-816)
+__global__ void k_totalflux(const double *__restrict__ zcr, const double *__restrict__ zcdr,
+                            const int *__restrict__ fblock, const int *__restrict__ nelebas, int nflux, int netot,
+                            int nelec, const double *__restrict__ reacfct, double ah1, double *__restrict__ out,
+                            double *__restrict__ outelec)
+{
+    int ie = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ie >= netot) return;
+    double s = 0.0;
+    double se[8];
+    for (int e = 0; e < 8; e++) se[e] = 0.0;
+    for (int f = 0; f < nflux; f++) {
+        size_t o = ((size_t)f * netot + ie) * 2;
+        double im = zcr[o] * zcdr[o + 1] + (-zcr[o + 1]) * zcdr[o];
+        s = s + im;
+        int el = nelebas[fblock[f]] - 1;
+        if (el < 8) se[el] = se[el] + im;
+    }
+    out[ie] = s * reacfct[ie] / ah1;
+    if (outelec)
+        for (int e = 0; e < nelec && e < 8; e++) outelec[(size_t)e * netot + ie] = se[e] * reacfct[ie] / ah1;
+}
+
+// ---------------------------------------------------------------------------
+// set-up: explicit angle x angle kinetic matrices from Djmmp and the scalars
+// (angkinj2 :255-272 and bfgridl2mat :419-468 assembled on the device)
+// ---------------------------------------------------------------------------
+struct KinBuildArgs {
+    int na, n1, n2, ne;
+    const int *blk_wave, *blk_elec, *blk_om, *blk_local;
+    const int *wnojb;            // [G] nojbas
+    const int *wjbas;            // [G][na]
+    const double *yj2;           // [G][n1][na]
+    const double *djmmp;         // all waves concatenated
+    const int64_t *djoff;        // [W]
+    const int *wnangu2, *wj0, *winc, *wiommin, *wiommax, *wnom, *wnj2;   // [W]
+    const double *l2tab;         // all waves
+    const int64_t *l2off;        // [W]
+    const char *l2used;
+    const int64_t *l2uoff;       // [W]
+};
+
+__device__ inline double djget(const KinBuildArgs &k, int w, int iom, int ielec, int j, int a)
+{
+    return k.djmmp[k.djoff[w] + (((size_t)iom * k.ne + (ielec - 1)) * (k.wnangu2[w] + 1) + j) * k.na + a];
+}
+
+template <typename T>
+__global__ void k_build_xj2(KinBuildArgs k, T *__restrict__ xj2, int g)
+{
+    int na = k.na;
+    int ir1 = blockIdx.x;
+    int w = k.blk_wave[g], e = k.blk_elec[g], om = k.blk_om[g];
+    const double *yy = k.yj2 + ((size_t)g * k.n1 + ir1) * na;
+    for (int ij = threadIdx.x; ij < na * na; ij += blockDim.x) {
+        int i = ij / na, j = ij % na;
+        double acc = 0.0;
+        for (int q = 0; q < k.wnojb[g]; q++) {
+            int jb = k.wjbas[(size_t)g * na + q];
+            double x1 = djget(k, w, om, e, jb, i), x2 = djget(k, w, om, e, jb, j);
+            acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(yy[q], x1), x2));
+        }
+        xj2[((size_t)g * k.n1 + ir1) * na * na + ij] = (T)acc;
+    }
+}
+
+template <typename T>
+__global__ void k_build_xl2p(KinBuildArgs k, T *__restrict__ xl2p, int s, int slot)
+{
+    int na = k.na;
+    int ir2 = blockIdx.x;
+    int w = k.blk_wave[s], e = k.blk_elec[s], oms = k.blk_om[s];
+    int q = slot - 1;
+    int omt = oms - q;
+    int iommin = k.wiommin[w], iommax = k.wiommax[w], nom = k.wnom[w], nj2 = k.wnj2[w];
+    T *out = xl2p + (((size_t)s * 3 + slot) * k.n2 + ir2) * na * na;
+    bool ok = (omt >= iommin && omt <= iommax);
+    for (int ij = threadIdx.x; ij < na * na; ij += blockDim.x) {
+        int i = ij / na, j = ij % na;
+        double acc = 0.0;
+        if (ok)
+            for (int jidx = 0; jidx < nj2; jidx++) {
+                int jv = k.wj0[w] + jidx * k.winc[w];
+                if (jv > (na - 1) * k.winc[w]) break;
+                size_t u = (((size_t)(e - 1) * nj2 + jidx) * nom + (omt - iommin)) * nom + (oms - iommin);
+                if (!k.l2used[k.l2uoff[w] + u]) continue;
+                double yyy = k.l2tab[k.l2off[w] + ((((size_t)(e - 1) * nj2 + jidx) * k.n2 + ir2) * nom + (omt - iommin)) * nom + (oms - iommin)];
+                double x11 = djget(k, w, omt, e, jv, i), x22 = djget(k, w, oms, e, jv, j);
+                acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(x11, x22), yyy));
+            }
+        out[ij] = (T)acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename T>
+void launch_scatter(Ctx &c, const double *psi, int g_begin, int g_end)
+{
+    int nseg = (g_end - g_begin) * c.na;
+    if (nseg <= 0) return;
+    k_scatter<T><<<nseg, 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, g_begin * c.na);
+    LAUNCH_CHECK(c);
+}
+
+static size_t col_smem(Ctx &c, size_t tsz) { return tsz * (size_t)c.n1 * (COL_W + COL_KC); }
+static size_t angj_smem(Ctx &c, size_t tsz) { return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1)); }
+static size_t angl_smem(Ctx &c, size_t tsz)
+{
+    return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1));
+}
+
+template <typename T>
+void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
+{
+    int ng = g_end - g_begin;
+    if (ng <= 0) return;
+    DevGrid d = devgrid(c);
+    constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
+    int64_t row0 = (int64_t)g_begin * c.na * c.n1;
+    int64_t nrows = (int64_t)ng * c.na * c.n1;
+    dim3 gr((c.n2 + BN - 1) / BN, (unsigned)((nrows + BM - 1) / BM));
+    // 1. DST along R
+    k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_S2, (T *)c.d_Y, nullptr,
+                                                    c.d_nopr1, row0, nrows);
+    LAUNCH_CHECK(c);
+    // 2. DST along r, k-space scaling, DST along r
+    dim3 gc((c.n2 + COL_W - 1) / COL_W, ng * c.na);
+    k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, (T *)c.d_Y, (const T *)c.d_S1, c.d_S1off,
+                                                                  c.d_nopr1, c.d_p2r1, c.d_p2r2, c.grid.radcutmax,
+                                                                  g_begin * c.na);
+    LAUNCH_CHECK(c);
+    // 3. DST along R, gathered into H at the stored points; points beyond the DST
+    k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_Y, (const T *)c.d_S2, nullptr, c.d_h,
+                                                   c.d_nopr1, row0, nrows);
+    LAUNCH_CHECK(c);
+    k_quirk<<<ng * c.na, 128, 0, c.stream>>>(d, psi, c.d_h, c.d_quirk_ptr, c.d_quirk, g_begin * c.na);
+    LAUNCH_CHECK(c);
+    // 4. angular kinetic terms
+    if (c.na > 1) {
+        dim3 gj(c.ncj, c.n1, ng);
+        k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_xj2, c.d_h,
+                                                                    c.d_tj_ptr, c.d_tj, c.ncj, g_begin);
+        LAUNCH_CHECK(c);
+        dim3 gl(c.ncl, c.n2, ng);
+        k_ang_l<T><<<gl, 256, angl_smem(c, sizeof(T)), c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_xl2p, c.d_h,
+                                                                    c.d_tl_ptr, c.d_tl, c.d_cpl, c.ncl, g_begin);
+        LAUNCH_CHECK(c);
+    }
+}
+
+template <typename T>
+void launch_update(Ctx &c, int first)
+{
+    UpdArgs u;
+    u.H = c.d_h;
+    u.pk = c.d_pk;
+    u.pkm1 = c.d_pkm1;
+    u.out = c.d_pkm1;
+    u.vsrc = c.d_vsrc;
+    u.absfr1 = c.d_absfr1;
+    u.absfr2 = c.d_absfr2;
+    u.emindlt = c.grid.emindlt;
+    u.delta2 = c.grid.delta2;
+    u.first = first;
+    u.normpart = c.d_normpart;
+    u.nofe = c.nofemax;
+    u.zcke = c.d_zcke;
+    u.zfe = c.d_zfe_ptrs;
+    u.wflat0 = c.d_wflat0;
+    k_update<T><<<c.nseg, 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+    LAUNCH_CHECK(c);
+}
+
+template <typename T>
+void launch_build_kinetic(Ctx &c)
+{
+    KinBuildArgs k;
+    k.na = c.na; k.n1 = c.n1; k.n2 = c.n2; k.ne = c.ne;
+    k.blk_wave = c.d_blk_wave; k.blk_elec = c.d_blk_elec; k.blk_om = c.d_blk_om; k.blk_local = nullptr;
+    k.wnojb = c.d_blk_nojb; k.wjbas = c.d_blk_jbas; k.yj2 = c.d_blk_yj2;
+    k.djmmp = c.d_djall; k.djoff = c.d_djoff;
+    k.wnangu2 = c.d_wnangu2; k.wj0 = c.d_wj0; k.winc = c.d_winc; k.wiommin = c.d_wiommin;
+    k.wiommax = c.d_wiommax; k.wnom = c.d_wnom; k.wnj2 = c.d_wnj2;
+    k.l2tab = c.d_l2all; k.l2off = c.d_l2off; k.l2used = c.d_l2used; k.l2uoff = c.d_l2uoff;
+    for (int g = 0; g < c.G; g++) {
+        k_build_xj2<T><<<c.n1, 256, 0, c.stream>>>(k, (T *)c.d_xj2, g);
+        LAUNCH_CHECK(c);
+        for (int slot = 0; slot < 3; slot++) {
+            if (!c.h_slot_used[(size_t)g * 3 + slot]) continue;
+            k_build_xl2p<T><<<c.n2, 256, 0, c.stream>>>(k, (T *)c.d_xl2p, g, slot);
+            LAUNCH_CHECK(c);
+        }
+    }
+}
+
+void set_kernel_attributes(Ctx &c)
+{
+    cudaFuncSetAttribute(k_dst_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem(c, 8));
+    cudaFuncSetAttribute(k_dst_cols<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem(c, 4));
+    cudaFuncSetAttribute(k_ang_j<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angj_smem(c, 8));
+    cudaFuncSetAttribute(k_ang_j<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angj_smem(c, 4));
+    cudaFuncSetAttribute(k_ang_l<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 8));
+    cudaFuncSetAttribute(k_ang_l<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 4));
+    cudaFuncSetAttribute(k_cvj, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+size_t max_smem_needed(Ctx &c)
+{
+    size_t m = col_smem(c, 8);
+    if (angj_smem(c, 8) > m) m = angj_smem(c, 8);
+    if (angl_smem(c, 8) > m) m = angl_smem(c, 8);
+    return m;
+}
+
+// accumulators of iteration it for every wave (CoefEcheby, totalflux_k, Cvjflux_k, funE coefficients)
+void launch_accumulators(Ctx &c, int64_t it)
+{
+    DevGrid d = devgrid(c);
+    double ah2 = (c.grid.rfin2 - c.grid.rmis2) / (double)(c.n2 - 1);
+    for (size_t w = 0; w < c.waves.size(); w++) {
+        WaveTables &t = c.waves[w];
+        WaveDev &wd = c.wdev[w];
+        k_coefecheby<<<(t.netot + 127) / 128, 128, 0, c.stream>>>(wd.etot, t.netot, c.grid.emindlt, c.grid.delta2,
+                                                                  c.grid.hbr, it, wd.zck);
+        LAUNCH_CHECK(c);
+        if (t.nofe > 0) {
+            k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(wd.efe, t.nofe, c.grid.emindlt, c.grid.delta2, c.grid.hbr, it,
+                                                  c.d_zcke + (size_t)w * c.nofemax * 2);
+            LAUNCH_CHECK(c);
+        }
+        if (c.n1 > 1 && t.nflux > 0) {
+            int gate = (t.iphoto == 0 && t.iprod == 1 && it < t.kminelastic) ? 1 : 0;
+            k_flux<<<t.nflux, 128, 0, c.stream>>>(c.d_pk + t.flat0, wd.fl_idx, wd.fl_dptr, wd.fl_didx, wd.fl_dir1, wd.zar1flux,
+                                                  wd.potiflux, wd.etot, wd.zck, t.netot, gate, wd.zcr, wd.zcdr);
+            LAUNCH_CHECK(c);
+        }
+        if (c.n2 > 1) {
+            for (int b = 0; b < t.ncan; b++) {
+                CvjArgs a;
+                a.psi = c.d_pk;
+                a.r2abs_map = wd.r2abs_map;
+                a.djmmp = wd.djmmp;
+                a.fd = wd.fd;
+                a.nobc = wd.nobc;
+                a.zck = wd.zck;
+                a.zs2 = wd.zs2;
+                a.cvj = wd.cvj;
+                a.nangu2 = t.nangu2; a.jini = t.jini; a.jmax = t.jmax; a.nvini = t.nvini; a.nvmax = t.nvmax;
+                a.inc = t.inc; a.j00 = t.j00[b]; a.ielec = t.nelebas[b]; a.iom = t.iombas[b];
+                a.nj = t.nj; a.nv = t.nv; a.netot = t.netot;
+                bool gate = (t.iprod != 1 && t.iphoto == 0 && it < t.kminelastic);
+                a.skip_ref = gate && (t.iomref < 0 || b == t.icanref);
+                a.jref = t.jref; a.nvref = t.nvref;
+                a.sah2 = sqrt(ah2);
+                a.blk = b;
+                a.foff_row = (int64_t)(t.g0 + b) * c.na;
+                size_t sm = sizeof(double) * (size_t)c.n1 * t.nj;
+                k_cvj<<<1, 256, sm, c.stream>>>(d, a);
+                LAUNCH_CHECK(c);
+            }
+        }
+    }
+}
+
+void launch_addv(Ctx &c, const double *psi, int g0, int g1)
+{
+    if (g1 <= g0) return;
+    k_addv<<<(g1 - g0) * c.na, 256, 0, c.stream>>>(devgrid(c), psi, c.d_h, c.d_vsrc, g0 * c.na);
+    LAUNCH_CHECK(c);
+}
+
+void launch_norms(Ctx &c, int64_t slot)
+{
+    k_norms<<<(int)c.waves.size(), 256, 0, c.stream>>>(c.d_normpart, c.d_wseg0, c.d_wseg1, c.d_norm_ptrs,
+                                                       c.d_norm_cap, slot);
+    LAUNCH_CHECK(c);
+}
+
+void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec)
+{
+    WaveTables &t = c.waves[w];
+    WaveDev &wd = c.wdev[w];
+    double ah1 = (c.grid.rfin1 - c.grid.rmis1) / (double)(c.n1 - 1);
+    k_totalflux<<<(t.netot + 127) / 128, 128, 0, c.stream>>>(wd.zcr, wd.zcdr, wd.fl_block, wd.nelebas, t.nflux,
+                                                             t.netot, c.ne, wd.reacfct, ah1, d_out, d_outelec);
+    LAUNCH_CHECK(c);
+}
+
+template void launch_scatter<double>(Ctx &, const double *, int, int);
+template void launch_scatter<float>(Ctx &, const double *, int, int);
+template void launch_hphi<double>(Ctx &, const double *, int, int);
+template void launch_hphi<float>(Ctx &, const double *, int, int);
+template void launch_update<double>(Ctx &, int);
+template void launch_update<float>(Ctx &, int);
+template void launch_build_kinetic<double>(Ctx &);
+template void launch_build_kinetic<float>(Ctx &);
+
+}  // namespace mw3

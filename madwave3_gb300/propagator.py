@@ -1,0 +1,306 @@
+"""Python host side over the C-ABI of libmw3gpu (include/mw3gpu.h).
+
+Mirrors the reference's module interface for the hot path: ``difs`` becomes
+:meth:`Propagator.hphi`, the time loop of main_madwave3.f (:308-368) becomes
+:meth:`Propagator.start` + :meth:`Propagator.run`, ``totalflux`` becomes
+:meth:`Propagator.totalflux`, and the accumulators ``zCR``/``zCdR``/``zS2``/
+``Cvj``/``zfE`` are read back with :meth:`Propagator.accumulators`.  Error
+behaviour follows the reference's convention of stopping on bad input: every
+non-zero status raises :class:`Mw3Error` with the library's message.
+
+The compute path is the CUDA library only; there is no CPU fallback.  Loading
+fails loudly when the library is missing or no CUDA device is present.
+"""
+import ctypes as ct
+import os
+
+import numpy as np
+
+from .host import constants as C
+
+I32P = ct.POINTER(ct.c_int32)
+F64P = ct.POINTER(ct.c_double)
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+
+class Mw3Error(RuntimeError):
+    pass
+
+
+class Grid(ct.Structure):
+    _fields_ = [
+        ("npun1", ct.c_int32), ("npun2", ct.c_int32), ("nangu", ct.c_int32), ("nelec", ct.c_int32),
+        ("npun1min", ct.c_int32), ("npuntot", ct.c_int32),
+        ("rmis1", ct.c_double), ("rfin1", ct.c_double), ("rmis2", ct.c_double), ("rfin2", ct.c_double),
+        ("hbr", ct.c_double), ("xm1red", ct.c_double), ("xm2red", ct.c_double),
+        ("radcutmax", ct.c_double), ("rotcutmax", ct.c_double),
+        ("emindlt", ct.c_double), ("delta2", ct.c_double),
+        ("precision", ct.c_int32),
+    ]
+
+
+class Wave(ct.Structure):
+    _fields_ = [
+        ("Jtot", ct.c_int32), ("iparity", ct.c_int32), ("inc", ct.c_int32), ("j0", ct.c_int32),
+        ("iommin", ct.c_int32), ("iommax", ct.c_int32), ("ncan", ct.c_int32),
+        ("iombas", I32P), ("nelebas", I32P), ("nojbas", I32P), ("j00", I32P), ("jbas", I32P),
+        ("iomdiat", I32P), ("iomatom", I32P), ("sigdiat", F64P), ("sigatom", F64P),
+        ("nangu2", ct.c_int32), ("djmmp", F64P), ("proj_j2_up", ct.c_int32),
+        ("absr1", ct.c_double), ("absalp1", ct.c_double), ("absr2", ct.c_double), ("absalp2", ct.c_double),
+        ("n1expo", ct.c_int32), ("ninterv1", ct.c_int32), ("n2expo", ct.c_int32), ("ninterv2", ct.c_int32),
+        ("r1flux_ang", ct.c_double), ("ekinmin", ct.c_double), ("ekinmax", ct.c_double),
+        ("netot", ct.c_int32), ("kminelastic", ct.c_int32), ("iphoto", ct.c_int32), ("iprod", ct.c_int32),
+        ("nvini", ct.c_int32), ("nvmax", ct.c_int32), ("jini", ct.c_int32), ("jmax", ct.c_int32),
+        ("nvref", ct.c_int32), ("jref", ct.c_int32), ("iomref", ct.c_int32), ("ielecref", ct.c_int32),
+        ("nobc", I32P), ("ediat", F64P), ("fd", F64P),
+        ("xm1reac", ct.c_double), ("xm2reac", ct.c_double),
+        ("rcolini", ct.c_double), ("alpha0", ct.c_double), ("xk0", ct.c_double), ("factor0", ct.c_double),
+        ("xmasa0", ct.c_double), ("il0", ct.c_int32),
+        ("nofe", ct.c_int32), ("efe", F64P),
+    ]
+
+
+HEADER_FUNCS = [
+    "mw3_create", "mw3_add_wave", "mw3_wave_size", "mw3_hphi", "mw3_start", "mw3_upload_state",
+    "mw3_run", "mw3_sync", "mw3_download_state", "mw3_norms", "mw3_totalflux", "mw3_flux_count",
+    "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_last_error", "mw3_destroy",
+]
+
+_lib = None
+
+
+def library_path():
+    from . import build as _b
+    return _b.LIB
+
+
+def load_library(build_if_missing=True):
+    """Load libmw3gpu.so from the package's build folder (building it if asked)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise Mw3Error("libmw3gpu.so is not built (run madwave3_gb300.build.build())")
+        from . import build as _b
+        _b.build()
+    L = ct.CDLL(path)
+    vp = ct.c_void_p
+    L.mw3_create.argtypes = [ct.POINTER(vp), ct.POINTER(Grid), I32P, I32P, I32P, F64P]
+    L.mw3_add_wave.argtypes = [vp, ct.POINTER(Wave), I32P]
+    L.mw3_wave_size.argtypes = [vp, ct.c_int32, ct.POINTER(ct.c_int64)]
+    L.mw3_hphi.argtypes = [vp, ct.c_int32, F64P, F64P]
+    L.mw3_start.argtypes = [vp, ct.POINTER(F64P)]
+    L.mw3_upload_state.argtypes = [vp, ct.c_int32, F64P, F64P, ct.c_int64]
+    L.mw3_run.argtypes = [vp, ct.c_int64]
+    L.mw3_sync.argtypes = [vp]
+    L.mw3_download_state.argtypes = [vp, ct.c_int32, F64P, F64P, ct.POINTER(ct.c_int64)]
+    L.mw3_norms.argtypes = [vp, ct.c_int32, F64P, ct.POINTER(ct.c_int64)]
+    L.mw3_totalflux.argtypes = [vp, ct.c_int32, F64P, F64P]
+    L.mw3_flux_count.argtypes = [vp, ct.c_int32, I32P]
+    L.mw3_download_accumulators.argtypes = [vp, ct.c_int32, F64P, F64P, F64P, F64P, F64P]
+    L.mw3_tables.argtypes = [vp, ct.c_int32, I32P, F64P, F64P, F64P, F64P, F64P]
+    L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
+    L.mw3_last_error.argtypes = [vp]
+    L.mw3_last_error.restype = ct.c_char_p
+    L.mw3_destroy.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _p(a, typ=ct.c_double):
+    return a.ctypes.data_as(ct.POINTER(typ))
+
+
+class Propagator:
+    """Every partial wave of a batch, propagated together on one GPU.
+
+    ``runs`` are host set-ups (:func:`madwave3_gb300.host.setup.load`) that
+    share one grid and potential; ``precision`` is "fp64" (the reference's
+    arithmetic) or "mixed" (FP32 transforms, FP64 recursion/accumulators).
+    """
+
+    def __init__(self, runs, precision="fp64"):
+        if not isinstance(runs, (list, tuple)):
+            runs = [runs]
+        self.L = load_library()
+        self.runs = list(runs)
+        r0 = runs[0]
+        i = r0.inp
+        self._keep = []
+        g = Grid()
+        g.npun1, g.npun2, g.nangu, g.nelec = i.npun1, i.npun2, i.nangu, r0.nelec
+        g.npun1min, g.npuntot = i.npun1min, r0.npuntot
+        g.rmis1, g.rfin1, g.rmis2, g.rfin2 = i.rmis1, i.rfin1, i.rmis2, i.rfin2
+        g.hbr, g.xm1red, g.xm2red = C.hbr, r0.xm1red, r0.xm2red
+        g.radcutmax, g.rotcutmax = r0.radcutmax, r0.rotcutmax
+        g.emindlt, g.delta2 = r0.emindlt, r0.delta2
+        g.precision = PREC_FP64 if precision == "fp64" else PREC_MIXED
+        self.precision = precision
+        npunreal = self._k(r0.npunreal, np.int32)
+        indr1 = self._k(r0.indr1, np.int32)
+        indr2 = self._k(r0.indr2, np.int32)
+        vvv = self._k(r0.vvv, np.float64)
+        h = ct.c_void_p()
+        rc = self.L.mw3_create(ct.byref(h), ct.byref(g), _p(npunreal, ct.c_int32), _p(indr1, ct.c_int32),
+                               _p(indr2, ct.c_int32), _p(vvv))
+        if rc != 0:
+            raise Mw3Error("mw3_create failed with status %d" % rc)
+        self.h = h
+        self.ntot = []
+        for r in self.runs:
+            self._add_wave(r)
+
+    def _k(self, a, dt):
+        a = np.ascontiguousarray(a, dt)
+        self._keep.append(a)
+        return a
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.L.mw3_last_error(self.h)
+            raise Mw3Error("%s failed with status %d: %s" % (what, rc, msg.decode() if msg else ""))
+
+    def _add_wave(self, r):
+        i = r.inp
+        w = Wave()
+        w.Jtot, w.iparity, w.inc, w.j0 = i.Jtot, i.iparity, i.inc, i.j0
+        w.iommin, w.iommax, w.ncan = i.iommin, i.iommax, r.ncan
+        w.iombas = _p(self._k(r.iombas, np.int32), ct.c_int32)
+        w.nelebas = _p(self._k(r.nelebas, np.int32), ct.c_int32)
+        w.nojbas = _p(self._k(r.nojbas, np.int32), ct.c_int32)
+        w.j00 = _p(self._k(r.j00, np.int32), ct.c_int32)
+        w.jbas = _p(self._k(r.jbas, np.int32), ct.c_int32)
+        w.iomdiat = _p(self._k(r.iomdiat, np.int32), ct.c_int32)
+        w.iomatom = _p(self._k(r.iomatom, np.int32), ct.c_int32)
+        w.sigdiat = _p(self._k(r.sigdiat, np.float64))
+        w.sigatom = _p(self._k(r.sigatom, np.float64))
+        w.nangu2 = r.nangu2
+        w.djmmp = _p(self._k(r.djmmp, np.float64))
+        w.proj_j2_up = i.proj_j2_up
+        w.absr1, w.absalp1, w.absr2, w.absalp2 = i.absr1, i.absalp1, i.absr2, i.absalp2
+        w.n1expo, w.ninterv1, w.n2expo, w.ninterv2 = i.n1expo, i.ninterv1, i.n2expo, i.ninterv2
+        w.r1flux_ang = i.r1flux_ang
+        w.ekinmin = i.ekinmin_ev * C.eV2cm * C.conve1
+        w.ekinmax = i.ekinmax_ev * C.eV2cm * C.conve1
+        w.netot, w.kminelastic, w.iphoto, w.iprod = i.netot, i.kminelastic, i.iphoto, i.iprod
+        w.nvini, w.nvmax, w.jini, w.jmax = i.nvini, i.nvmax, i.jini, i.jmax
+        w.nvref, w.jref, w.iomref, w.ielecref = i.nvref, i.jref, i.iomref, i.ielecref
+        w.nobc = _p(self._k(r.nobc, np.int32), ct.c_int32)
+        w.ediat = _p(self._k(r.ediat, np.float64))
+        w.fd = _p(self._k(r.fd, np.float64))
+        w.xm1reac, w.xm2reac = r.xm1reac, r.xm2reac
+        w.rcolini, w.alpha0, w.xk0, w.factor0 = r.rcolini, r.alpha0, r.xk0, r.factor0
+        w.xmasa0, w.il0 = r.xmasa0, r.il0
+        efe = getattr(r, "efe_zot", None)
+        if efe is not None and len(efe):
+            w.nofe = len(efe)
+            w.efe = _p(self._k(np.asarray(efe, np.float64), np.float64))
+        else:
+            w.nofe = 0
+            w.efe = _p(self._k(np.zeros(1), np.float64))
+        wid = ct.c_int32()
+        self._check(self.L.mw3_add_wave(self.h, ct.byref(w), ct.byref(wid)), "mw3_add_wave")
+        n = ct.c_int64()
+        self._check(self.L.mw3_wave_size(self.h, wid.value, ct.byref(n)), "mw3_wave_size")
+        if n.value != r.ntot:
+            raise Mw3Error("wave size mismatch: library %d, host %d" % (n.value, r.ntot))
+        self.ntot.append(n.value)
+
+    # ---- the reference's operations -------------------------------------
+    def hphi(self, psi, wave=0):
+        """difs: H psi for one wave (host arrays in and out)."""
+        psi = np.ascontiguousarray(psi, np.float64)
+        out = np.empty(self.ntot[wave])
+        self._check(self.L.mw3_hphi(self.h, wave, _p(psi), _p(out)), "mw3_hphi")
+        return out
+
+    def start(self, psi0s=None):
+        """Fresh start from each wave's initial packet (default: the host's psi0)."""
+        if psi0s is None:
+            psi0s = [r.psi0 for r in self.runs]
+        arrs = [np.ascontiguousarray(p, np.float64) for p in psi0s]
+        ptrs = (F64P * len(arrs))(*[_p(a) for a in arrs])
+        self._check(self.L.mw3_start(self.h, ptrs), "mw3_start")
+
+    def upload_state(self, wave, psi_km1, psi_k, it):
+        a = np.ascontiguousarray(psi_km1, np.float64)
+        b = np.ascontiguousarray(psi_k, np.float64)
+        self._check(self.L.mw3_upload_state(self.h, wave, _p(a), _p(b), it), "mw3_upload_state")
+
+    def run(self, n):
+        self._check(self.L.mw3_run(self.h, n), "mw3_run")
+
+    def sync(self):
+        self._check(self.L.mw3_sync(self.h), "mw3_sync")
+
+    def state(self, wave=0):
+        a, b = np.empty(self.ntot[wave]), np.empty(self.ntot[wave])
+        it = ct.c_int64()
+        self._check(self.L.mw3_download_state(self.h, wave, _p(a), _p(b), ct.byref(it)), "mw3_download_state")
+        return a, b, it.value
+
+    def norms(self, wave=0, cap=1 << 22):
+        buf = np.empty(cap)
+        n = ct.c_int64(cap)
+        self._check(self.L.mw3_norms(self.h, wave, _p(buf), ct.byref(n)), "mw3_norms")
+        return buf[: n.value].copy()
+
+    def totalflux(self, wave=0):
+        r = self.runs[wave]
+        netot = r.inp.netot
+        tot = np.empty(netot)
+        el = np.empty((r.nelec, netot))
+        self._check(self.L.mw3_totalflux(self.h, wave, _p(tot), _p(el)), "mw3_totalflux")
+        return tot, el
+
+    def nflux(self, wave=0):
+        n = ct.c_int32()
+        self._check(self.L.mw3_flux_count(self.h, wave, ct.byref(n)), "mw3_flux_count")
+        return n.value
+
+    def accumulators(self, wave=0):
+        r = self.runs[wave]
+        i = r.inp
+        netot = i.netot
+        nj, nv = i.jmax - i.jini + 1, i.nvmax - i.nvini + 1
+        nf = self.nflux(wave)
+        zcr = np.empty((nf, netot, 2))
+        zcdr = np.empty((nf, netot, 2))
+        zs2 = np.empty((r.ncan, nj, nv, netot, 2))
+        cvj = np.empty((r.ncan, nj, nv))
+        self._check(self.L.mw3_download_accumulators(self.h, wave, _p(zcr), _p(zcdr), _p(zs2), _p(cvj), None),
+                    "mw3_download_accumulators")
+        cx = lambda a: a[..., 0] + 1j * a[..., 1]
+        return dict(zcr=cx(zcr), zcdr=cx(zcdr), zs2=cx(zs2), cvj=cvj)
+
+    def tables(self, wave=0):
+        r = self.runs[wave]
+        i = r.inp
+        nj, nv = i.jmax - i.jini + 1, i.nvmax - i.nvini + 1
+        nopr1 = np.empty(i.nangu, np.int32)
+        etot, reac = np.empty(i.netot), np.empty(i.netot)
+        s2f = np.empty((r.nelec, nj, nv, i.netot))
+        a1, a2 = np.empty(i.npun1), np.empty(i.npun2)
+        self._check(self.L.mw3_tables(self.h, wave, _p(nopr1, ct.c_int32), _p(etot), _p(reac), _p(s2f), _p(a1),
+                                      _p(a2)), "mw3_tables")
+        return dict(nopr1=nopr1, etot=etot, reacfct=reac, s2factor=s2f, absfr1=a1, absfr2=a2)
+
+    def kernel_launches(self):
+        n = ct.c_int64()
+        self._check(self.L.mw3_kernel_launches(self.h, ct.byref(n)), "mw3_kernel_launches")
+        return n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mw3_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,108 @@
+"""GPU path against the CPU oracle, through the C-ABI (libmw3gpu.so).
+
+Bars: FP64 path <= 1e-12 relative on H psi, <= 1e-10 on the norm trace, the
+recursion vectors, P(E) and the state-resolved accumulators after 150
+iterations; mixed path |Delta P(E)| <= 1e-4 against the FP64 path, scaled by
+max|P| because these small grids are not converged after 150 iterations and
+their partial P(E) sums exceed 1.
+"""
+import numpy as np
+import pytest
+
+from madwave3_gb300 import Propagator
+from oracle.mw3ref import Oracle
+
+pytestmark = pytest.mark.gpu
+CASES = ["tiny_j0", "tiny_j3", "tiny_e2"]
+NIT = 150
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_hphi_fp64(runs, case):
+    run = runs[case]
+    prop = Propagator(run, "fp64")
+    ref = Oracle(run)
+    rng = np.random.default_rng(20261203)
+    for _ in range(3):
+        psi = rng.uniform(-1, 1, run.ntot)
+        assert rel(prop.hphi(psi), ref.hphi(psi)) < 1e-12
+    prop.close()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_tables(runs, case):
+    run = runs[case]
+    prop = Propagator(run, "fp64")
+    ref = Oracle(run)
+    t, r, f = prop.tables(), ref.tables(), ref.flux_tables()
+    assert np.array_equal(t["nopr1"], r["nopr1"])
+    assert np.array_equal(t["absfr1"], r["absfr1"]) and np.array_equal(t["absfr2"], r["absfr2"])
+    assert np.array_equal(t["etot"], f["etot"])
+    assert rel(t["reacfct"], f["reacfct"]) < 1e-13
+    assert prop.nflux() == ref.nflux()
+    prop.close()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_propagation_fp64(runs, case):
+    run = runs[case]
+    prop = Propagator(run, "fp64")
+    ref = Oracle(run)
+    prop.start()
+    ref.start(run.psi0)
+    prop.run(NIT)
+    n_ref = ref.run_iters(NIT)
+    n_gpu = prop.norms()
+    assert len(n_gpu) == NIT + 1
+    assert rel(n_gpu[1:], n_ref) < 1e-10
+    km1, k, it = prop.state()
+    rkm1, rk, rit = ref.state()
+    assert it == rit == NIT + 1
+    assert rel(k, rk) < 1e-10 and rel(km1, rkm1) < 1e-10
+    p, pe = prop.totalflux()
+    rp, rpe = ref.totalflux()
+    assert rel(p, rp) < 1e-10
+    assert rel(pe, rpe) < 1e-10
+    acc = prop.accumulators()
+    zcr, zcdr = ref.flux()
+    assert rel(acc["zcr"], zcr) < 1e-10 and rel(acc["zcdr"], zcdr) < 1e-10
+    zs2, cvj = ref.s2()
+    assert rel(acc["zs2"], zs2) < 1e-10
+    assert rel(acc["cvj"], cvj) < 1e-10
+    prop.close()
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mixed_vs_fp64(runs, case):
+    run = runs[case]
+    p64 = Propagator(run, "fp64")
+    pmx = Propagator(run, "mixed")
+    for p in (p64, pmx):
+        p.start()
+        p.run(NIT)
+    a, _ = p64.totalflux()
+    b, _ = pmx.totalflux()
+    assert np.abs(a - b).max() <= 1e-4 * max(1.0, np.abs(a).max())
+    assert rel(pmx.hphi(run.psi0), p64.hphi(run.psi0)) < 1e-6
+    p64.close()
+    pmx.close()
+
+
+def test_batched_waves(runs):
+    """Two partial waves in one context give the same results as separate runs."""
+    r0, r3 = runs["tiny_j0"], runs["tiny_j3"]
+    both = Propagator([r0, r3], "fp64")
+    both.start()
+    both.run(60)
+    for w, r in enumerate((r0, r3)):
+        one = Propagator(r, "fp64")
+        one.start()
+        one.run(60)
+        assert rel(both.state(w)[1], one.state()[1]) < 1e-13
+        assert rel(both.totalflux(w)[0], one.totalflux()[0]) < 1e-13
+        one.close()
+    both.close()
