@@ -1,0 +1,344 @@
+#!/usr/bin/env python
+"""Benchmark of the Chebyshev propagation step on GB300.
+
+A step is one Chebyshev iteration of every partial wave of the workload: H psi
+(difs), the damped three-term update, CoefEcheby and the flux/Cvj/norm
+accumulators (SRC/main_madwave3.f:324-352).  The metric is stored grid
+points x iterations per second, a stored point being one entry of the
+reference's compressed state vector (one Omega/electronic block at one grid
+point kept below Vcut).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+                  [--workload NAME] [--precision mixed|fp64]
+
+--impl reference times the CPU restatement of the same step (oracle/, all host
+threads) on the same workload.  With --gpus N > 1 (torchrun) the partial waves
+are independent, so each rank propagates its own replica of the workload
+("replicas only": the path has no exchange step on one node).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+L2_BYTES = 129 * 1024 * 1024
+
+WORKLOADS = {
+    # J=0, one Omega block, one state: 256 R x 128 r x 60 angles (synthetic LEPS)
+    "j0_256x128x60": dict(case="j0_256x128x60", waves=[dict()]),
+}
+
+
+def metric_name():
+    return "Chebyshev Hψ grid-pt·iter/s, mixed/batched vs FP64 plain at |ΔP(E)|≤1e-4"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), p.get("bf16_tflops", 1900.0), "of measured"
+    except Exception:
+        return 6800.0, 1900.0, "of fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def case_runs(workload, rank):
+    from madwave3_gb300.host import generator, setup
+    w = WORKLOADS[workload]
+    base = os.environ.get("MW3_CASES", os.path.join(tempfile.gettempdir(), "mw3_cases_r%d" % rank))
+    d = os.path.join(base, w["case"])
+    if not os.path.exists(os.path.join(d, "pot", "cont.pot")):
+        generator.write_case(d, **generator.CASES[w["case"]])
+    return [setup.load(os.path.join(d, "input.dat"))]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.path = os.path.join(tempfile.gettempdir(), "mw3_clocks_%d_%d.csv" % (os.getpid(), gpu_index))
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def stage_model(runs, prop):
+    """Algorithmic work of each stage of one iteration (flops or bytes)."""
+    r0 = runs[0]
+    i = r0.inp
+    n1, n2, na = i.npun1, i.npun2, i.nangu
+    tsz = 8 if prop.precision == "fp64" else 4
+    rows = 0
+    rows_sq = 0
+    nsto = 0
+    for w, r in enumerate(runs):
+        nopr1 = prop.tables(w)["nopr1"].astype(np.int64)
+        rows += r.ncan * int(nopr1.sum())
+        rows_sq += r.ncan * int((nopr1 ** 2).sum())
+        nsto += r.ntot
+    ne = r0.nelec
+    return {
+        "dst_R": ("flop", 2.0 * rows * n2 * n2),
+        "dst_r_pair": ("flop", 4.0 * rows_sq * n2),
+        "dst_R_gather": ("flop", 2.0 * rows * n2 * n2),
+        "ang_j2": ("flop", 2.0 * na * nsto),
+        "ang_l2": ("flop", 2.0 * na * nsto * 3),
+        # psi_k, psi_k-1, H read, psi_k+1 written, V row, rectangle store, two grid indices
+        "update": ("byte", nsto * (8 * 4 + 8 * ne + tsz + 8)),
+        "accumulators": ("byte", sum(prop.nflux(w) * r.inp.netot * 2 * 2 * 16 for w, r in enumerate(runs))),
+    }
+
+
+def run_gpu(args, rank, world, local):
+    import torch
+    from madwave3_gb300 import Propagator
+
+    torch.cuda.set_device(local)
+    runs = case_runs(args.workload, rank)
+    nsto = sum(r.ntot for r in runs)
+    prop = Propagator(runs, args.precision)
+    prop.start()
+    for _ in range(args.warmup):
+        prop.run(1)
+    prop.sync()
+    stream = torch.cuda.ExternalStream(prop.stream())
+    working_set = nsto * 8 * 4
+    flush = working_set < 2 * L2_BYTES
+    fbuf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda") if flush else None
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = prop.kernel_launches()
+    prop.profile(True)
+    clocks = ClockSampler(local)
+    evs = []
+    for _ in range(args.steps):
+        if flush:
+            with torch.cuda.stream(stream):
+                fbuf.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        prop.run(1)
+        e1.record(stream)
+        evs.append((e0, e1))
+    prop.sync()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = prop.kernel_launches() - launches0
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    stages, nrec = prop.stage_times()
+    prop.profile(False)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+    ms_max = float(t.item())
+    ms_step = ms_max / args.steps
+    value = world * nsto * args.steps / (ms_max * 1e-3)
+
+    # end to end through the C-ABI: host state in pinned memory, uploaded every
+    # step, one iteration, psi_k read back
+    e2e_steps = max(1, min(args.steps, 10))
+    pins = []
+    for w, r in enumerate(runs):
+        km1, k, it = prop.state(w)
+        a = torch.from_numpy(km1).pin_memory()
+        b = torch.from_numpy(k).pin_memory()
+        pins.append((a, b, it))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(e2e_steps):
+        for w, (a, b, it) in enumerate(pins):
+            prop.upload_state(w, a.numpy(), b.numpy(), it + s)
+        prop.run(1)
+        for w, (a, b, it) in enumerate(pins):
+            prop.state(w, out_km1=a.numpy(), out_k=b.numpy())   # the host keeps the state
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_value = world * nsto / (e2e_ms * 1e-3)
+
+    # roofline of the dominant stage
+    hbm, tf, src = load_peaks()
+    model = stage_model(runs, prop)
+    dom = max(stages, key=lambda k: stages[k])
+    kind, work = model[dom]
+    t_launch = stages[dom] / max(nrec, 1) * 1e-3
+    if kind == "flop":
+        achieved = work / t_launch / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": tf, "unit": "TFLOP/s",
+                "frac": achieved / tf, "traffic": None, "kernel": dom, "peak_source": src}
+    else:
+        achieved = work / t_launch / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "kernel": dom, "peak_source": src}
+    out = {
+        "metric": metric_name(), "value": value, "unit": "grid-pt*iter/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 recursion, f32 transforms" if args.precision == "mixed" else "f64",
+        "data": "synthetic LEPS surface, generated on the fly",
+        "config": {"workload": args.workload, "precision": args.precision,
+                   "stored_points": nsto, "waves": len(runs), "blocks": sum(r.ncan for r in runs),
+                   "grid": [runs[0].inp.npun2, runs[0].inp.npun1, runs[0].inp.nangu],
+                   "netot": runs[0].inp.netot,
+                   "l2": "flushed before every timed step" if flush else "working set larger than L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "grid-pt*iter/s",
+                "h2d_bytes_per_step": int(sum(2 * 8 * r.ntot for r in runs)),
+                "d2h_bytes_per_step": int(sum(2 * 8 * r.ntot for r in runs))},
+        "gpu_launches": launches,
+        "stages_ms_per_step": {k: v / max(nrec, 1) for k, v in stages.items()},
+        "roofline": roof,
+        "clocks": clk,
+    }
+    prop.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(runs, budget_s=args.cpu_seconds)
+    return out
+
+
+def cpu_baseline(runs, budget_s=15.0):
+    """The oracle (CPU restatement of the same step), all host threads, bounded sample."""
+    from oracle.mw3ref import Oracle
+    cores = os.cpu_count() or 1
+    total_pts, total_t, its_done = 0, 0.0, 0
+    per_wave = budget_s / len(runs)
+    for r in runs:
+        o = Oracle(r, threads=cores)
+        o.start(r.psi0)
+        t = time.time()
+        o.run_iters(1)
+        t1 = time.time() - t
+        n = max(1, min(200, int(per_wave / max(t1, 1e-6))))
+        t = time.time()
+        o.run_iters(n)
+        dt = time.time() - t
+        total_pts += r.ntot * n
+        total_t += dt
+        its_done += n
+        del o
+    return {"value": total_pts / total_t, "unit": "grid-pt*iter/s", "cores": cores, "kind": "port",
+            "sample": "%d Chebyshev iterations of the same workload after one warm-up iteration" % its_done}
+
+
+def run_reference(args, rank, world, local):
+    if rank != 0:
+        return None
+    from oracle.mw3ref import Oracle
+    runs = case_runs(args.workload, rank)
+    cores = os.cpu_count() or 1
+    oracles = []
+    for r in runs:
+        o = Oracle(r, threads=cores)
+        o.start(r.psi0)
+        oracles.append(o)
+    for _ in range(args.warmup):
+        for o in oracles:
+            o.run_iters(1)
+    t = time.time()
+    for _ in range(args.steps):
+        for o in oracles:
+            o.run_iters(1)
+    dt = time.time() - t
+    nsto = sum(r.ntot for r in runs)
+    value = nsto * args.steps / dt
+    return {
+        "impl": "reference", "metric": metric_name(), "value": value, "unit": "grid-pt*iter/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic LEPS surface, generated on the fly",
+        "config": {"workload": args.workload, "stored_points": nsto, "waves": len(runs)},
+        "cpu_baseline": {"value": value, "unit": "grid-pt*iter/s", "cores": cores, "kind": "port",
+                         "sample": "%d timed Chebyshev iterations after %d warm-up" % (args.steps, args.warmup)},
+        "e2e": {"value": value, "unit": "grid-pt*iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="j0_256x128x60", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        torch.distributed.init_process_group(backend=backend)
+    if args.impl == "reference":
+        out = run_reference(args, rank, world, local)
+    else:
+        out = run_gpu(args, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -152,6 +152,18 @@ int mw3_tables(mw3_ctx *ctx, int32_t wave_id, int32_t *nopr1, double *etot, doub
 /* Number of CUDA kernels this context has launched so far. */
 int mw3_kernel_launches(mw3_ctx *ctx, int64_t *count);
 
+/* The CUDA stream (cudaStream_t) all device work of the context runs on, for
+ * callers that order their own work or timing events against it. */
+int mw3_get_stream(mw3_ctx *ctx, void **stream);
+
+/* Per-stage timing: while enabled, mw3_run records CUDA events around each
+ * stage of every iteration.  mw3_stage_times waits for the stream and returns
+ * the accumulated milliseconds of MW3_NSTAGES stages and the number of
+ * iterations recorded, then clears the record. */
+#define MW3_NSTAGES 7   /* R-DST, r-DST pair, R-DST+gather, j^2, l^2, update, accumulators */
+int mw3_profile(mw3_ctx *ctx, int enable);
+int mw3_stage_times(mw3_ctx *ctx, double *ms, int64_t *iterations);
+
 const char *mw3_last_error(const mw3_ctx *ctx);
 int mw3_destroy(mw3_ctx *ctx);
 

@@ -460,6 +460,14 @@ int reset_accumulators(Ctx &c)
 
 }  // namespace
 
+namespace mw3 {
+void stage_mark(Ctx &c, int stage)
+{
+    if (!c.prof || c.prof_n >= c.prof_cap) return;
+    cudaEventRecord(c.prof_ev[(size_t)c.prof_n * (MW3_NSTAGES + 1) + stage], c.stream);
+}
+}  // namespace mw3
+
 // ===========================================================================
 // C-ABI
 // ===========================================================================
@@ -639,6 +647,13 @@ int mw3_run(mw3_ctx *h, int64_t n)
     }
     int rc = grow_norms(c, c.norm_slot + n);
     if (rc) return rc;
+    if (c.prof && c.prof_n + n > c.prof_cap) {
+        int64_t need = c.prof_n + n;
+        size_t old = c.prof_ev.size();
+        c.prof_ev.resize((size_t)need * (MW3_NSTAGES + 1));
+        for (size_t i = old; i < c.prof_ev.size(); i++) MW3_CUDA_TRY(cudaEventCreate(&c.prof_ev[i]));
+        c.prof_cap = need;
+    }
     for (int64_t s = 0; s < n; s++) {
         int64_t it = c.it + 1;
         hphi_all(c, c.d_pk, 0, c.G);
@@ -646,6 +661,10 @@ int mw3_run(mw3_ctx *h, int64_t n)
         std::swap(c.d_pk, c.d_pkm1);
         mw3::launch_accumulators(c, it);
         mw3::launch_norms(c, c.norm_slot);
+        if (c.prof && c.prof_n < c.prof_cap) {
+            mw3::stage_mark(c, MW3_NSTAGES);
+            c.prof_n++;
+        }
         c.it = it;
         c.norm_slot++;
     }
@@ -759,6 +778,41 @@ int mw3_kernel_launches(mw3_ctx *h, int64_t *count)
     return MW3_OK;
 }
 
+int mw3_get_stream(mw3_ctx *h, void **stream)
+{
+    if (!h || !stream) return MW3_ERR_ARG;
+    *stream = (void *)h->c.stream;
+    return MW3_OK;
+}
+
+int mw3_profile(mw3_ctx *h, int enable)
+{
+    if (!h) return MW3_ERR_ARG;
+    h->c.prof = enable != 0;
+    h->c.prof_n = 0;
+    return MW3_OK;
+}
+
+int mw3_stage_times(mw3_ctx *h, double *ms, int64_t *iterations)
+{
+    if (!h || !ms) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    for (int s = 0; s < MW3_NSTAGES; s++) ms[s] = 0.0;
+    for (int64_t i = 0; i < c.prof_n; i++) {
+        cudaEvent_t *e = &c.prof_ev[(size_t)i * (MW3_NSTAGES + 1)];
+        // stages without their own start mark (no angular kernels) fold into the next one
+        for (int s = 0; s < MW3_NSTAGES; s++) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, e[s], e[s + 1]) == cudaSuccess) ms[s] += t;
+        }
+    }
+    cudaGetLastError();
+    if (iterations) *iterations = c.prof_n;
+    c.prof_n = 0;
+    return MW3_OK;
+}
+
 const char *mw3_last_error(const mw3_ctx *h)
 {
     if (!h) return "null context";
@@ -770,6 +824,7 @@ int mw3_destroy(mw3_ctx *h)
     if (!h) return MW3_OK;
     Ctx &c = h->c;
     if (c.stream) cudaStreamSynchronize(c.stream);
+    for (cudaEvent_t e : c.prof_ev) cudaEventDestroy(e);
     free_device(c);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;

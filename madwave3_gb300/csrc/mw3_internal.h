@@ -162,6 +162,10 @@ struct Ctx {
     double *d_tmp = nullptr;
     int64_t tmp_cap = 0;
     int nseg = 0;                    // G*na segments, block-major
+    // optional per-stage event timing (mw3_profile)
+    bool prof = false;
+    std::vector<cudaEvent_t> prof_ev;    // (MW3_NSTAGES+1) events per recorded iteration
+    int64_t prof_n = 0, prof_cap = 0;
     std::vector<void *> allocs;      // everything allocated for the wave set
 };
 
@@ -179,6 +183,8 @@ template <typename T>
 void launch_scatter(Ctx &c, const double *psi, int g_begin, int g_end);
 template <typename T>
 void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end);
+// records the boundary event of a stage when per-stage timing is on
+void stage_mark(Ctx &c, int stage);
 template <typename T>
 void launch_update(Ctx &c, int first);
 template <typename T>

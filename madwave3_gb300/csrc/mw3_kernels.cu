@@ -699,27 +699,32 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     int64_t nrows = (int64_t)ng * c.na * c.n1;
     dim3 gr((c.n2 + BN - 1) / BN, (unsigned)((nrows + BM - 1) / BM));
     // 1. DST along R
+    stage_mark(c, 0);
     k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_S2, (T *)c.d_Y, nullptr,
                                                     c.d_nopr1, row0, nrows);
     LAUNCH_CHECK(c);
     // 2. DST along r, k-space scaling, DST along r
+    stage_mark(c, 1);
     dim3 gc((c.n2 + COL_W - 1) / COL_W, ng * c.na);
     k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, (T *)c.d_Y, (const T *)c.d_S1, c.d_S1off,
                                                                   c.d_nopr1, c.d_p2r1, c.d_p2r2, c.grid.radcutmax,
                                                                   g_begin * c.na);
     LAUNCH_CHECK(c);
     // 3. DST along R, gathered into H at the stored points; points beyond the DST
+    stage_mark(c, 2);
     k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_Y, (const T *)c.d_S2, nullptr, c.d_h,
                                                    c.d_nopr1, row0, nrows);
     LAUNCH_CHECK(c);
     k_quirk<<<ng * c.na, 128, 0, c.stream>>>(d, psi, c.d_h, c.d_quirk_ptr, c.d_quirk, g_begin * c.na);
     LAUNCH_CHECK(c);
     // 4. angular kinetic terms
+    stage_mark(c, 3);
     if (c.na > 1) {
         dim3 gj(c.ncj, c.n1, ng);
         k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_xj2, c.d_h,
                                                                     c.d_tj_ptr, c.d_tj, c.ncj, g_begin);
         LAUNCH_CHECK(c);
+        stage_mark(c, 4);
         dim3 gl(c.ncl, c.n2, ng);
         k_ang_l<T><<<gl, 256, angl_smem(c, sizeof(T)), c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_xl2p, c.d_h,
                                                                     c.d_tl_ptr, c.d_tl, c.d_cpl, c.ncl, g_begin);
@@ -746,6 +751,7 @@ void launch_update(Ctx &c, int first)
     u.zcke = c.d_zcke;
     u.zfe = c.d_zfe_ptrs;
     u.wflat0 = c.d_wflat0;
+    stage_mark(c, 5);
     k_update<T><<<c.nseg, 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
     LAUNCH_CHECK(c);
 }
@@ -794,6 +800,7 @@ size_t max_smem_needed(Ctx &c)
 // accumulators of iteration it for every wave (CoefEcheby, totalflux_k, Cvjflux_k, funE coefficients)
 void launch_accumulators(Ctx &c, int64_t it)
 {
+    stage_mark(c, 6);
     DevGrid d = devgrid(c);
     double ah2 = (c.grid.rfin2 - c.grid.rmis2) / (double)(c.n2 - 1);
     for (size_t w = 0; w < c.waves.size(); w++) {

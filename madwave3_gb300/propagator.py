@@ -65,8 +65,10 @@ class Wave(ct.Structure):
 HEADER_FUNCS = [
     "mw3_create", "mw3_add_wave", "mw3_wave_size", "mw3_hphi", "mw3_start", "mw3_upload_state",
     "mw3_run", "mw3_sync", "mw3_download_state", "mw3_norms", "mw3_totalflux", "mw3_flux_count",
-    "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_last_error", "mw3_destroy",
+    "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_get_stream", "mw3_profile",
+    "mw3_stage_times", "mw3_last_error", "mw3_destroy",
 ]
+STAGES = ["dst_R", "dst_r_pair", "dst_R_gather", "ang_j2", "ang_l2", "update", "accumulators"]
 
 _lib = None
 
@@ -104,6 +106,9 @@ def load_library(build_if_missing=True):
     L.mw3_download_accumulators.argtypes = [vp, ct.c_int32, F64P, F64P, F64P, F64P, F64P]
     L.mw3_tables.argtypes = [vp, ct.c_int32, I32P, F64P, F64P, F64P, F64P, F64P]
     L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
+    L.mw3_get_stream.argtypes = [vp, ct.POINTER(ct.c_void_p)]
+    L.mw3_profile.argtypes = [vp, ct.c_int]
+    L.mw3_stage_times.argtypes = [vp, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_last_error.argtypes = [vp]
     L.mw3_last_error.restype = ct.c_char_p
     L.mw3_destroy.argtypes = [vp]
@@ -237,8 +242,9 @@ class Propagator:
     def sync(self):
         self._check(self.L.mw3_sync(self.h), "mw3_sync")
 
-    def state(self, wave=0):
-        a, b = np.empty(self.ntot[wave]), np.empty(self.ntot[wave])
+    def state(self, wave=0, out_km1=None, out_k=None):
+        a = np.empty(self.ntot[wave]) if out_km1 is None else out_km1
+        b = np.empty(self.ntot[wave]) if out_k is None else out_k
         it = ct.c_int64()
         self._check(self.L.mw3_download_state(self.h, wave, _p(a), _p(b), ct.byref(it)), "mw3_download_state")
         return a, b, it.value
@@ -293,6 +299,22 @@ class Propagator:
         n = ct.c_int64()
         self._check(self.L.mw3_kernel_launches(self.h, ct.byref(n)), "mw3_kernel_launches")
         return n.value
+
+    def stream(self):
+        """cudaStream_t of the context, as an integer handle."""
+        s = ct.c_void_p()
+        self._check(self.L.mw3_get_stream(self.h, ct.byref(s)), "mw3_get_stream")
+        return s.value or 0
+
+    def profile(self, enable=True):
+        self._check(self.L.mw3_profile(self.h, 1 if enable else 0), "mw3_profile")
+
+    def stage_times(self):
+        """Accumulated per-stage milliseconds since profiling was enabled."""
+        ms = np.zeros(len(STAGES))
+        n = ct.c_int64()
+        self._check(self.L.mw3_stage_times(self.h, _p(ms), ct.byref(n)), "mw3_stage_times")
+        return dict(zip(STAGES, ms)), n.value
 
     def close(self):
         if getattr(self, "h", None):
