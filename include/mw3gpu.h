@@ -164,6 +164,27 @@ int mw3_get_stream(mw3_ctx *ctx, void **stream);
 int mw3_profile(mw3_ctx *ctx, int enable);
 int mw3_stage_times(mw3_ctx *ctx, double *ms, int64_t *iterations);
 
+/* H psi for one wave without allocating anything.
+ *
+ * No counterpart in the reference: it exists for callers that can allocate
+ * GPU memory only while they start up, not inside their time loop -- for
+ * example a host whose device memory is owned by another allocator that
+ * holds the whole GPU, or a loop where the implicit device synchronisation
+ * of cudaMalloc/cudaFree would stall every iteration.  psi and hpsi are
+ * DEVICE pointers to the wave's state vector layout (mw3_wave_size doubles).
+ * The transform scratch lives in one file-scope device array of
+ * MW3_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit; waves whose scratch (two rectangles of ncan*nangu*npun1*npun2
+ * elements, 8 bytes each in FP64, 4 in mixed) exceeds it are rejected with
+ * MW3_ERR_UNSUPPORTED.  The context's device tables must already exist (any
+ * earlier mw3_hphi, mw3_start or mw3_upload_state builds them).  The first
+ * call on a device looks up the array's device address once; make that
+ * first call before any stream capture.  All calls share the array, so calls
+ * that overlap on the GPU (other threads or contexts on the same device) race.
+ * Returns after the result is in hpsi. */
+#define MW3_NOALLOC_SCRATCH_BYTES (64u << 20)
+int mw3_hphi_noalloc(mw3_ctx *ctx, int32_t wave_id, const double *psi, double *hpsi);
+
 const char *mw3_last_error(const mw3_ctx *ctx);
 int mw3_destroy(mw3_ctx *ctx);
 

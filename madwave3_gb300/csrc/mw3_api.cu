@@ -15,10 +15,6 @@ using mw3::Ctx;
 using mw3::WaveDev;
 using mw3::WaveTables;
 
-struct mw3_ctx {
-    Ctx c;
-};
-
 namespace {
 
 constexpr int kAngCW = 64;   // column chunk of the angular kernels (must match mw3_kernels.cu)

@@ -198,6 +198,11 @@ size_t max_smem_needed(Ctx &c);
 
 }  // namespace mw3
 
+// the opaque handle of the C-ABI
+struct mw3_ctx {
+    mw3::Ctx c;
+};
+
 #define MW3_CUDA_TRY(expr)                                                            \
     do {                                                                              \
         cudaError_t e_ = (expr);                                                      \

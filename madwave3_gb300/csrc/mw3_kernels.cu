@@ -872,6 +872,108 @@ void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec)
     LAUNCH_CHECK(c);
 }
 
+// ---------------------------------------------------------------------------
+// H psi without allocation (mw3_hphi_noalloc): the same kernels as launch_hphi,
+// with the two scratch rectangles taken from one static device array.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MW3_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+static void *s_noalloc_ptr[kMaxDevices];   // device address of g_noalloc_scratch, per device
+
+template <typename T>
+static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, const double *psi, double *hpsi)
+{
+    int na = c.na, n1 = c.n1, n2 = c.n2;
+    int g0 = t.g0, g1 = t.g0 + t.ncan, ng = t.ncan;
+    size_t rect = (size_t)n1 * n2;
+    // kernels index rectangles and vectors by context-wide block and flat
+    // offsets: shift the bases so the wave's first entry lands at the buffer start
+    T *X = reinterpret_cast<T *>(scratch) - (size_t)g0 * na * rect;
+    T *Y = reinterpret_cast<T *>(scratch) + (size_t)ng * na * rect - (size_t)g0 * na * rect;
+    const double *P = psi - t.flat0;
+    double *H = hpsi - t.flat0;
+    DevGrid d = devgrid(c);
+    k_scatter<T><<<ng * na, 256, 0, c.stream>>>(d, X, P, g0 * na);
+    LAUNCH_CHECK(c);
+    constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
+    int64_t row0 = (int64_t)g0 * na * n1, nrows = (int64_t)ng * na * n1;
+    dim3 gr((n2 + BN - 1) / BN, (unsigned)((nrows + BM - 1) / BM));
+    k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, X, (const T *)c.d_S2, Y, nullptr, c.d_nopr1, row0, nrows);
+    LAUNCH_CHECK(c);
+    dim3 gc((n2 + COL_W - 1) / COL_W, ng * na);
+    k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, Y, (const T *)c.d_S1, c.d_S1off, c.d_nopr1,
+                                                                  c.d_p2r1, c.d_p2r2, c.grid.radcutmax, g0 * na);
+    LAUNCH_CHECK(c);
+    k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, Y, (const T *)c.d_S2, nullptr, H, c.d_nopr1, row0, nrows);
+    LAUNCH_CHECK(c);
+    k_quirk<<<ng * na, 128, 0, c.stream>>>(d, P, H, c.d_quirk_ptr, c.d_quirk, g0 * na);
+    LAUNCH_CHECK(c);
+    if (na > 1) {
+        dim3 gj(c.ncj, n1, ng);
+        k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, X, (const T *)c.d_xj2, H, c.d_tj_ptr, c.d_tj,
+                                                                    c.ncj, g0);
+        LAUNCH_CHECK(c);
+        dim3 gl(c.ncl, n2, ng);
+        k_ang_l<T><<<gl, 256, angl_smem(c, sizeof(T)), c.stream>>>(d, X, (const T *)c.d_xl2p, H, c.d_tl_ptr, c.d_tl,
+                                                                    c.d_cpl, c.ncl, g0);
+        LAUNCH_CHECK(c);
+    }
+    k_addv<<<ng * na, 256, 0, c.stream>>>(d, P, H, c.d_vsrc, g0 * na);
+    LAUNCH_CHECK(c);
+    (void)g1;
+}
+
+}  // namespace mw3
+
+extern "C" int mw3_hphi_noalloc(mw3_ctx *h, int32_t wave_id, const double *psi, double *hpsi)
+{
+    using namespace mw3;
+    if (!h || !psi || !hpsi) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (wave_id < 0 || wave_id >= (int)c.waves.size()) {
+        c.err = "mw3_hphi_noalloc: no such wave";
+        return MW3_ERR_ARG;
+    }
+    if (!c.built) {
+        c.err = "mw3_hphi_noalloc: device tables not built yet (call mw3_hphi, mw3_start or mw3_upload_state once)";
+        return MW3_ERR_STATE;
+    }
+    const WaveTables &t = c.waves[wave_id];
+    size_t tsz = c.fp64 ? sizeof(double) : sizeof(float);
+    size_t rect_bytes = (size_t)t.ncan * c.na * c.n1 * c.n2 * tsz;
+    if (rect_bytes > MW3_NOALLOC_SCRATCH_BYTES / 2) {
+        c.err = "mw3_hphi_noalloc: the wave needs " + std::to_string(2 * rect_bytes) +
+                " bytes of scratch, more than the static array's " + std::to_string((size_t)MW3_NOALLOC_SCRATCH_BYTES);
+        return MW3_ERR_UNSUPPORTED;
+    }
+    int dev = 0;
+    MW3_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        c.err = "mw3_hphi_noalloc: device index out of range";
+        return MW3_ERR_UNSUPPORTED;
+    }
+    if (!s_noalloc_ptr[dev]) {
+        // once per device, with that device current: the device address of the array
+        void *p = nullptr;
+        MW3_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        s_noalloc_ptr[dev] = p;
+    }
+    unsigned char *scratch = static_cast<unsigned char *>(s_noalloc_ptr[dev]);
+    // the array keeps the previous call's contents; the psi rectangle must be
+    // zero outside the stored points
+    MW3_CUDA_TRY(cudaMemsetAsync(scratch, 0, rect_bytes, c.stream));
+    if (c.fp64)
+        noalloc_hphi<double>(c, t, scratch, psi, hpsi);
+    else
+        noalloc_hphi<float>(c, t, scratch, psi, hpsi);
+    MW3_CUDA_TRY(cudaGetLastError());
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return MW3_OK;
+}
+
+namespace mw3 {
+
 template void launch_scatter<double>(Ctx &, const double *, int, int);
 template void launch_scatter<float>(Ctx &, const double *, int, int);
 template void launch_hphi<double>(Ctx &, const double *, int, int);

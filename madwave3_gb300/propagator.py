@@ -66,7 +66,7 @@ HEADER_FUNCS = [
     "mw3_create", "mw3_add_wave", "mw3_wave_size", "mw3_hphi", "mw3_start", "mw3_upload_state",
     "mw3_run", "mw3_sync", "mw3_download_state", "mw3_norms", "mw3_totalflux", "mw3_flux_count",
     "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_get_stream", "mw3_profile",
-    "mw3_stage_times", "mw3_last_error", "mw3_destroy",
+    "mw3_stage_times", "mw3_hphi_noalloc", "mw3_last_error", "mw3_destroy",
 ]
 STAGES = ["dst_R", "dst_r_pair", "dst_R_gather", "ang_j2", "ang_l2", "update", "accumulators"]
 
