@@ -1264,3 +1264,74 @@ int mw3ref_xl2p(const mw3ref *r, double *xl2p)
     memcpy(xl2p, r->xl2p, sizeof(double) * 3 * (size_t)r->nc * r->na * r->na * r->n2);
     return 0;
 }
+
+/* ---------------------------------------------------------------------- */
+/* stand-alone restatements for the known-answer tests                    */
+/* ---------------------------------------------------------------------- */
+int mw3ref_noptfft(int nin, int ntot) { return noptfft(nin, ntot); }
+
+void mw3ref_sinmom_p2(double box, int npun, double xmred, double hbr, double *p2r)
+{
+    sinmom(box, npun, npun, xmred, hbr, NULL, p2r);
+}
+
+/* one direction of ini_absorcion (mod_absorcion_01y2.f:72-100) */
+void mw3ref_absorption(int npun, double rmis, double ah, double absr, double absalp, int nexpo,
+                       int ninterv, double *f, int32_t *irabs)
+{
+    *irabs = npun;
+    for (int ir = 1; ir <= npun; ir++) {
+        double r = (double)(ir - 1) * ah + rmis;
+        double v = 1.0;
+        if (r >= absr) {
+            if (ir < *irabs) *irabs = ir;
+            double delta = (r - absr) / (double)ninterv;
+            v = exp(-(absalp * powi(delta, nexpo)));
+        }
+        f[ir - 1] = v;
+    }
+}
+
+/* Smatini_col (mod_flux_01y2.f:392-524), energy part */
+double mw3ref_smatini_col(int netot, double ekinmin, double ekinmax, double rmis2, double rfin2,
+                          double rcolini, double xk0, double alpha0, double factor0, double xmasa0,
+                          double xm1reac, int il0, double hbr, double *etot, double *apaqini,
+                          double *reacfct)
+{
+    double estep = (ekinmax - ekinmin) / (double)(netot - 1);
+    const int npunt = 1000;
+    double rg[1000];
+    double ahgauss = (rfin2 - rmis2) / (double)(npunt - 1);
+    for (int ir2 = 1; ir2 <= npunt; ir2++) {
+        double r2 = rmis2 + (double)(ir2 - 1) * ahgauss;
+        double g = cos((r2 - rcolini) * xk0) * sqrt(2.0);
+        rg[ir2 - 1] = g * factor0 * exp(-(r2 - rcolini) * (r2 - rcolini) / alpha0 / alpha0) / sqrt(2.0);
+    }
+    double pepe = (double)(il0 * (il0 + 1));
+    double rr = rcolini + 1.0;
+    double erot = hbr * hbr * pepe * 0.5 / (rr * rr * xmasa0);
+    double xnorm = 0.0;
+    for (int ie = 0; ie < netot; ie++) {
+        double e = ekinmin + (double)ie * estep;
+        double paqini = 0.0, pini = 0.0;
+        if (e > 0.0 && e > erot) {
+            pini = sqrt(e * xmasa0 * 2.0 / hbr / hbr);
+            double zr = 0.0, zi = 0.0;
+            for (int ir2 = 1; ir2 <= npunt; ir2++) {
+                double rx = rmis2 + (double)(ir2 - 1) * ahgauss;
+                double fb, gb;
+                mw3ref_riccati(il0, rx * pini, &fb, &gb);
+                if (fabs(fb) > 1e-20) { zr += rg[ir2 - 1] * (-gb); zi += rg[ir2 - 1] * fb; }
+            }
+            zr = zr * ahgauss / 2.0 / MW3_PI;
+            zi = zi * ahgauss / 2.0 / MW3_PI;
+            paqini = zr * zr + zi * zi;
+        }
+        if (etot) etot[ie] = e;
+        if (apaqini) apaqini[ie] = paqini;
+        xnorm = xnorm + paqini;
+        if (reacfct)
+            reacfct[ie] = (paqini < 1e-10) ? 0.0 : hbr * hbr * pini / paqini / xmasa0 / xm1reac / 4.0 / MW3_PI / MW3_PI;
+    }
+    return xnorm * estep;
+}

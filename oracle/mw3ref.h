@@ -109,6 +109,18 @@ int mw3ref_flux_tables(const mw3ref *r, double *etot, double *reacfct, double *a
                        double *zar1flux, int32_t *ir4flux);
 int mw3ref_xj2(const mw3ref *r, double *xj2);    /* [ncan][nangu(jang)][nangu(iang)][npun1] */
 int mw3ref_xl2p(const mw3ref *r, double *xl2p);  /* [3][ncan][nangu][nangu][npun2] */
+/* Stand-alone restatements used by the known-answer tests against the
+   reference's golden log (EXAMPLES/HD+H_collision/J000-check/sal.000). */
+int mw3ref_noptfft(int nin, int ntot);
+void mw3ref_sinmom_p2(double box, int npun, double xmred, double hbr, double *p2r);
+void mw3ref_absorption(int npun, double rmis, double ah, double absr, double absalp, int nexpo,
+                       int ninterv, double *f, int32_t *irabs);
+/* Smatini_col energy grid and packet projection; returns sum(apaqini)*estep,
+   the "Norm ini. wvp in energy" line of the log */
+double mw3ref_smatini_col(int netot, double ekinmin, double ekinmax, double rmis2, double rfin2,
+                          double rcolini, double xk0, double alpha0, double factor0, double xmasa0,
+                          double xm1reac, int il0, double hbr, double *etot, double *apaqini,
+                          double *reacfct);
 /* DST-I of one line (RODFT00), exposed for the known-answer tests */
 void mw3ref_dst1(int n, const double *x, double *y, int mode);
 void mw3ref_riccati(int l, double x, double *f, double *g);

@@ -89,6 +89,12 @@ def lib():
         L.mw3ref_xl2p.argtypes = [ct.c_void_p, F64P]
         L.mw3ref_dst1.argtypes = [ct.c_int, F64P, F64P, ct.c_int]
         L.mw3ref_riccati.argtypes = [ct.c_int, ct.c_double, F64P, F64P]
+        L.mw3ref_noptfft.argtypes = [ct.c_int, ct.c_int]
+        L.mw3ref_sinmom_p2.argtypes = [ct.c_double, ct.c_int, ct.c_double, ct.c_double, F64P]
+        L.mw3ref_absorption.argtypes = [ct.c_int, ct.c_double, ct.c_double, ct.c_double, ct.c_double, ct.c_int,
+                                        ct.c_int, F64P, I32P]
+        L.mw3ref_smatini_col.restype = ct.c_double
+        L.mw3ref_smatini_col.argtypes = [ct.c_int] + [ct.c_double] * 10 + [ct.c_int, ct.c_double, F64P, F64P, F64P]
         _lib = L
     return _lib
 
@@ -102,6 +108,30 @@ def dst1(x, mode=0):
     y = np.zeros_like(x)
     lib().mw3ref_dst1(len(x), _p(x, ct.c_double), _p(y, ct.c_double), mode)
     return y
+
+
+def noptfft(nin, ntot):
+    return lib().mw3ref_noptfft(nin, ntot)
+
+
+def sinmom_p2(box, npun, xmred, hbr):
+    out = np.zeros(npun)
+    lib().mw3ref_sinmom_p2(box, npun, xmred, hbr, _p(out, ct.c_double))
+    return out
+
+
+def absorption(npun, rmis, ah, absr, absalp, nexpo, ninterv):
+    f = np.zeros(npun)
+    ir = ct.c_int32()
+    lib().mw3ref_absorption(npun, rmis, ah, absr, absalp, nexpo, ninterv, _p(f, ct.c_double), ct.byref(ir))
+    return f, ir.value
+
+
+def smatini_col(netot, ekinmin, ekinmax, rmis2, rfin2, rcolini, xk0, alpha0, factor0, xmasa0, xm1reac, il0, hbr):
+    et, ap, rf = np.zeros(netot), np.zeros(netot), np.zeros(netot)
+    xn = lib().mw3ref_smatini_col(netot, ekinmin, ekinmax, rmis2, rfin2, rcolini, xk0, alpha0, factor0, xmasa0,
+                                  xm1reac, il0, hbr, _p(et, ct.c_double), _p(ap, ct.c_double), _p(rf, ct.c_double))
+    return xn, et, ap, rf
 
 
 def riccati(l, x):
