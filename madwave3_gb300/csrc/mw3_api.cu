@@ -309,45 +309,104 @@ int build_device(Ctx &c)
     TRY(dalloc(c, &c.d_h, NT));
     TRY(dalloc(c, &c.d_tmp, NT));
     c.tmp_cap = NT;
-    TRY(dalloc(c, &c.d_normpart, (size_t)c.nseg));
-    // ---- per-wave accumulators ----
+    c.nchunk = (c.npt + 1023) / 1024;
+    TRY(dalloc(c, &c.d_normpart, (size_t)c.nseg * c.nchunk));
+    // ---- accumulators: context-wide arrays, each wave a slice ----
+    {
+        const WaveTables &t0 = c.waves[0];
+        for (auto &t : c.waves)
+            if (t.netot != t0.netot || t.ekinmin != t0.ekinmin || t.ekinmax != t0.ekinmax || t.jini != t0.jini ||
+                t.jmax != t0.jmax || t.nvini != t0.nvini || t.nvmax != t0.nvmax || t.kminelastic != t0.kminelastic ||
+                t.iprod != t0.iprod || t.iphoto != t0.iphoto || t.jref != t0.jref || t.nvref != t0.nvref ||
+                t.r1flux_ang != t0.r1flux_ang || t.fd != t0.fd || t.nobc != t0.nobc) {
+                c.err = "the partial waves of one context must share the energy grid, j/v ranges, flux line and "
+                        "diatomic functions";
+                return MW3_ERR_ARG;
+            }
+        c.netot = t0.netot;
+        c.nj = t0.nj;
+        c.nv = t0.nv;
+        c.jini = t0.jini; c.jmax = t0.jmax; c.nvini = t0.nvini; c.nvmax = t0.nvmax;
+        c.kminelastic = t0.kminelastic; c.jref = t0.jref; c.nvref = t0.nvref;
+        c.gate_elastic = (t0.iphoto == 0) ? 1 : 0;
+        double ah2 = (c.grid.rfin2 - c.grid.rmis2) / (double)(n2 - 1);
+        c.sah2 = sqrt(ah2);
+        std::vector<int64_t> fidx, fdidx;
+        std::vector<int> fdptr, fdir1, bj00(G), binc(G), bref(G), r2abs((size_t)W * na * n1);
+        std::vector<double> fpoti;
+        int64_t nf = 0;
+        for (int w = 0; w < W; w++) {
+            WaveTables &t = c.waves[w];
+            for (int f = 0; f < t.nflux; f++) {
+                fidx.push_back(t.flat0 + t.fl_idx[f]);
+                fpoti.push_back(t.potiflux[f]);
+                fdptr.push_back((int)fdidx.size());
+                for (int q = t.fl_dptr[f]; q < t.fl_dptr[f + 1]; q++) {
+                    fdidx.push_back(t.flat0 + t.fl_didx[q]);
+                    fdir1.push_back(t.fl_dir1[q]);
+                }
+            }
+            nf += t.nflux;
+            for (int b = 0; b < t.ncan; b++) {
+                bj00[t.g0 + b] = t.j00[b];
+                binc[t.g0 + b] = t.inc;
+                bref[t.g0 + b] = (t.iomref < 0 || b == t.icanref) ? 1 : 0;
+            }
+            std::copy(t.r2abs_map.begin(), t.r2abs_map.end(), r2abs.begin() + (size_t)w * na * n1);
+        }
+        fdptr.push_back((int)fdidx.size());
+        c.NF = (int)nf;
+        TRY(dupload(c, &c.d_fl_idx, fidx));
+        TRY(dupload(c, &c.d_fl_poti, fpoti));
+        TRY(dupload(c, &c.d_fl_dptr, fdptr));
+        TRY(dupload(c, &c.d_fl_didx, fdidx));
+        TRY(dupload(c, &c.d_fl_dir1, fdir1));
+        TRY(dupload(c, &c.d_zar, t0.zar1flux));
+        TRY(dupload(c, &c.d_etot, t0.etot));
+        TRY(dalloc(c, &c.d_zck, (size_t)c.netot * 2));
+        TRY(dalloc(c, &c.d_fpsi, (size_t)std::max<int64_t>(nf, 1) * 4));
+        TRY(dalloc(c, &c.d_zcr, (size_t)std::max<int64_t>(nf, 1) * c.netot * 2));
+        TRY(dalloc(c, &c.d_zcdr, (size_t)std::max<int64_t>(nf, 1) * c.netot * 2));
+        TRY(dalloc(c, &c.d_xj, (size_t)G * n1 * c.nj));
+        TRY(dalloc(c, &c.d_cvj, (size_t)G * c.nj * c.nv));
+        TRY(dalloc(c, &c.d_zs2, (size_t)G * c.nj * c.nv * c.netot * 2));
+        TRY(dupload(c, &c.d_blk_j00, bj00));
+        TRY(dupload(c, &c.d_blk_inc, binc));
+        TRY(dupload(c, &c.d_blk_isref, bref));
+        TRY(dupload(c, &c.d_r2abs, r2abs));
+        TRY(dupload(c, &c.d_fd, t0.fd));
+        TRY(dupload(c, &c.d_nobc, t0.nobc));
+    }
     c.wdev.assign(W, WaveDev());
     c.nofemax = 0;
     for (auto &t : c.waves) c.nofemax = std::max(c.nofemax, t.nofe);
     TRY(dalloc(c, &c.d_zcke, (size_t)W * std::max(c.nofemax, 1) * 2));
     std::vector<double *> zfeptr(W, nullptr), normptr(W, nullptr);
     std::vector<int64_t> normcap(W, 0);
-    for (int w = 0; w < W; w++) {
-        WaveTables &t = c.waves[w];
-        WaveDev &d = c.wdev[w];
-        TRY(dalloc(c, &d.zck, (size_t)t.netot * 2));
-        TRY(dupload(c, &d.etot, t.etot));
-        TRY(dupload(c, &d.reacfct, t.reacfct));
-        TRY(dupload(c, &d.nelebas, t.nelebas));
-        TRY(dupload(c, &d.zar1flux, t.zar1flux));
-        TRY(dupload(c, &d.potiflux, t.potiflux));
-        TRY(dupload(c, &d.fl_idx, t.fl_idx));
-        TRY(dupload(c, &d.fl_block, t.fl_block));
-        TRY(dupload(c, &d.fl_dptr, t.fl_dptr));
-        TRY(dupload(c, &d.fl_didx, t.fl_didx));
-        TRY(dupload(c, &d.fl_dir1, t.fl_dir1));
-        TRY(dalloc(c, &d.zcr, (size_t)t.nflux * t.netot * 2));
-        TRY(dalloc(c, &d.zcdr, (size_t)t.nflux * t.netot * 2));
-        TRY(dalloc(c, &d.zs2, (size_t)t.ncan * t.nj * t.nv * t.netot * 2));
-        TRY(dalloc(c, &d.cvj, (size_t)t.ncan * t.nj * t.nv));
-        TRY(dupload(c, &d.fd, t.fd));
-        TRY(dupload(c, &d.nobc, t.nobc));
-        TRY(dupload(c, &d.r2abs_map, t.r2abs_map));
-        d.djmmp = c.d_djall + djoff[w];
-        if (t.nofe > 0) {
-            TRY(dupload(c, &d.efe, t.efe));
-            TRY(dalloc(c, &d.zfe, (size_t)t.nofe * t.ntot * 2));
-            zfeptr[w] = d.zfe;
+    {
+        int64_t foff = 0;
+        for (int w = 0; w < W; w++) {
+            WaveTables &t = c.waves[w];
+            WaveDev &d = c.wdev[w];
+            TRY(dupload(c, &d.reacfct, t.reacfct));
+            TRY(dupload(c, &d.nelebas, t.nelebas));
+            TRY(dupload(c, &d.fl_block, t.fl_block));
+            d.zcr = c.d_zcr + (size_t)foff * c.netot * 2;
+            d.zcdr = c.d_zcdr + (size_t)foff * c.netot * 2;
+            d.zs2 = c.d_zs2 + (size_t)t.g0 * c.nj * c.nv * c.netot * 2;
+            d.cvj = c.d_cvj + (size_t)t.g0 * c.nj * c.nv;
+            foff += t.nflux;
+            d.djmmp = c.d_djall + djoff[w];
+            if (t.nofe > 0) {
+                TRY(dupload(c, &d.efe, t.efe));
+                TRY(dalloc(c, &d.zfe, (size_t)t.nofe * t.ntot * 2));
+                zfeptr[w] = d.zfe;
+            }
+            d.norms_cap = 1024;
+            TRY(dalloc(c, &d.norms, (size_t)d.norms_cap));
+            normptr[w] = d.norms;
+            normcap[w] = d.norms_cap;
         }
-        d.norms_cap = 1024;
-        TRY(dalloc(c, &d.norms, (size_t)d.norms_cap));
-        normptr[w] = d.norms;
-        normcap[w] = d.norms_cap;
     }
     TRY(dupload(c, &c.d_zfe_ptrs, zfeptr));
     TRY(dupload(c, &c.d_norm_ptrs, normptr));
@@ -440,15 +499,14 @@ int check_launch(Ctx &c, const char *where)
 
 int reset_accumulators(Ctx &c)
 {
+    size_t nf = (size_t)std::max(c.NF, 1) * c.netot * 2;
+    MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcr, 0, sizeof(double) * nf, c.stream));
+    MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcdr, 0, sizeof(double) * nf, c.stream));
+    MW3_CUDA_TRY(cudaMemsetAsync(c.d_zs2, 0, sizeof(double) * 2 * (size_t)c.G * c.nj * c.nv * c.netot, c.stream));
+    MW3_CUDA_TRY(cudaMemsetAsync(c.d_cvj, 0, sizeof(double) * (size_t)c.G * c.nj * c.nv, c.stream));
     for (size_t w = 0; w < c.waves.size(); w++) {
         WaveTables &t = c.waves[w];
         WaveDev &d = c.wdev[w];
-        MW3_CUDA_TRY(cudaMemsetAsync(d.zcr, 0, sizeof(double) * 2 * std::max<size_t>((size_t)t.nflux * t.netot, 1),
-                                     c.stream));
-        MW3_CUDA_TRY(cudaMemsetAsync(d.zcdr, 0, sizeof(double) * 2 * std::max<size_t>((size_t)t.nflux * t.netot, 1),
-                                     c.stream));
-        MW3_CUDA_TRY(cudaMemsetAsync(d.zs2, 0, sizeof(double) * 2 * (size_t)t.ncan * t.nj * t.nv * t.netot,
-                                     c.stream));
         if (d.zfe) MW3_CUDA_TRY(cudaMemsetAsync(d.zfe, 0, sizeof(double) * 2 * (size_t)t.nofe * t.ntot, c.stream));
     }
     return MW3_OK;

@@ -162,6 +162,23 @@ struct Ctx {
     double *d_tmp = nullptr;
     int64_t tmp_cap = 0;
     int nseg = 0;                    // G*na segments, block-major
+    int nchunk = 1;                  // point chunks per segment (kPointChunk points each)
+    // context-wide accumulators (all waves share netot, the energy grid, j/v ranges)
+    int NF = 0, netot = 0, nj = 0, nv = 0;
+    int64_t *d_fl_idx = nullptr, *d_fl_didx = nullptr;
+    int *d_fl_dptr = nullptr, *d_fl_dir1 = nullptr;
+    double *d_fl_poti = nullptr, *d_zar = nullptr, *d_etot = nullptr, *d_zck = nullptr;
+    double *d_fpsi = nullptr;        // [NF][4]: psi, dpsi (re, im)
+    double *d_zcr = nullptr, *d_zcdr = nullptr;          // [NF][netot][2]
+    double *d_xj = nullptr;          // [G][n1][nj] angular projection at ir2abs
+    double *d_cvj = nullptr;         // [G][nj][nv]
+    double *d_zs2 = nullptr;         // [G][nj][nv][netot][2]
+    int *d_blk_j00 = nullptr, *d_blk_inc = nullptr, *d_blk_isref = nullptr;
+    int *d_r2abs = nullptr;          // [W][na][n1]
+    double *d_fd = nullptr;          // [nelec][nj][nv][n1] (shared by the waves)
+    int *d_nobc = nullptr;           // [nelec][nj]
+    double sah2 = 1.0;
+    int jini = 0, jmax = 0, nvini = 0, nvmax = 0, kminelastic = 0, gate_elastic = 0, jref = 0, nvref = 0;
     // optional per-stage event timing (mw3_profile)
     bool prof = false;
     std::vector<cudaEvent_t> prof_ev;    // (MW3_NSTAGES+1) events per recorded iteration

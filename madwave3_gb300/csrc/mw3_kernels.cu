@@ -45,20 +45,22 @@ static DevGrid devgrid(Ctx &c)
 // ---------------------------------------------------------------------------
 // scatter: compressed psi -> rectangle X[g][a][ir1][ir2]
 // ---------------------------------------------------------------------------
+constexpr int kPointChunk = 1024;   // stored points per CTA in the point kernels
+
 template <typename T>
 __global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict__ psi, int seg0)
 {
     int seg = seg0 + blockIdx.x;
-    int g = seg / d.na, a = seg % d.na;
+    int a = seg % d.na;
     int64_t off = d.foff[seg];
     int n = d.npunreal[a];
+    int i0 = blockIdx.y * kPointChunk, i1 = min(n, i0 + kPointChunk);
     T *base = X + (size_t)seg * d.n1 * d.n2;
-    for (int ir = threadIdx.x; ir < n; ir += blockDim.x) {
+    for (int ir = i0 + threadIdx.x; ir < i1; ir += blockDim.x) {
         int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
         int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
         base[(size_t)ir1 * d.n2 + ir2] = (T)psi[off + ir];
     }
-    (void)g;
 }
 
 // ---------------------------------------------------------------------------
@@ -361,13 +363,13 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
     int w = d.blk_wave[g];
     int et = d.blk_elec[g];
     int64_t off = d.foff[seg];
-    int n = d.npunreal[a];
+    int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
     int n1 = d.n1, n2 = d.n2, na = d.na, ne = d.ne;
     T *rect = X + (size_t)seg * n1 * n2;
     double nrm = 0.0;
     double *zf = (u.nofe > 0 && !u.first) ? u.zfe[w] : nullptr;
     int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
-    for (int ir = threadIdx.x; ir < n; ir += blockDim.x) {
+    for (int ir = blockIdx.y * kPointChunk + threadIdx.x; ir < n; ir += blockDim.x) {
         int64_t i = off + ir;
         int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
         int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
         if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) u.normpart[seg] = red[0];
+    if (threadIdx.x == 0) u.normpart[(size_t)seg * gridDim.y + blockIdx.y] = red[0];
 }
 
 // V psi alone, for mw3_hphi: H(t) += sum_s V(e_s, e_t) psi(s) over same-Omega blocks
@@ -420,8 +422,8 @@ __global__ void k_addv(DevGrid d, const double *__restrict__ psi, double *__rest
     int g = seg / d.na, a = seg % d.na;
     int et = d.blk_elec[g];
     int64_t off = d.foff[seg];
-    int n = d.npunreal[a];
-    for (int ir = threadIdx.x; ir < n; ir += blockDim.x) {
+    int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
+    for (int ir = blockIdx.y * kPointChunk + threadIdx.x; ir < n; ir += blockDim.x) {
         double hv = H[off + ir];
         for (int q = 0; q < d.ne; q++) {
             int s = vsrc[g * d.ne + q];
@@ -436,12 +438,13 @@ __global__ void k_addv(DevGrid d, const double *__restrict__ psi, double *__rest
 
 // check (main_madwave3.f:431-442): sum the norm partials of each wave
 __global__ void k_norms(const double *__restrict__ part, const int *__restrict__ wseg0, const int *__restrict__ wseg1,
-                        double *const *norms_out, const int64_t *__restrict__ cap, int64_t slot)
+                        int nchunk, double *const *norms_out, const int64_t *__restrict__ cap, int64_t slot)
 {
     int w = blockIdx.x;
     __shared__ double red[256];
     double s = 0.0;
-    for (int i = wseg0[w] + threadIdx.x; i < wseg1[w]; i += blockDim.x) s += part[i];
+    for (int64_t i = (int64_t)wseg0[w] * nchunk + threadIdx.x; i < (int64_t)wseg1[w] * nchunk; i += blockDim.x)
+        s += part[i];
     red[threadIdx.x] = s;
     __syncthreads();
     for (int k = blockDim.x / 2; k > 0; k >>= 1) {
@@ -471,111 +474,147 @@ __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double 
     zck[2 * ie + 1] = zf * s / deno;
 }
 
-// totalflux_k (mod_flux_01y2.f:585-660): derivative at the flux line, rank-1 updates
-__global__ void __launch_bounds__(256) k_flux(const double *__restrict__ psi, const int64_t *__restrict__ fidx,
-                                              const int *__restrict__ dptr, const int64_t *__restrict__ didx,
-                                              const int *__restrict__ dir1, const double *__restrict__ zar,
-                                              const double *__restrict__ poti, const double *__restrict__ etot,
-                                              const double *__restrict__ zck, int netot, int gate_zero,
-                                              double *__restrict__ zcr, double *__restrict__ zcdr)
+// totalflux_k (mod_flux_01y2.f:585-660), first half: psi and d psi/d r1 at every
+// flux point of every wave; one warp per flux point, lanes stride over the
+// stored points of its (block, angle, R) line, butterfly reduction
+__global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ psi, const int64_t *__restrict__ fidx,
+                                                    const int *__restrict__ dptr, const int64_t *__restrict__ didx,
+                                                    const int *__restrict__ dir1, const double *__restrict__ zar,
+                                                    int NF, double *__restrict__ fpsi)
 {
-    int f = blockIdx.x;
-    __shared__ double dr, di, pf;
-    if (threadIdx.x == 0) {
-        double sr = 0.0, si = 0.0;
-        for (int q = dptr[f]; q < dptr[f + 1]; q++) {
-            double p = psi[didx[q]];
-            int ir1 = dir1[q];
-            sr = sr + (zar[2 * ir1] * p - zar[2 * ir1 + 1] * 0.0);
-            si = si + (zar[2 * ir1] * 0.0 + zar[2 * ir1 + 1] * p);
-        }
-        dr = sr;
-        di = si;
-        pf = psi[fidx[f]];
+    int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (f >= NF) return;
+    double sr = 0.0, si = 0.0;
+    for (int q = dptr[f] + lane; q < dptr[f + 1]; q += 32) {
+        double p = psi[didx[q]];
+        int ir1 = dir1[q];
+        sr += zar[2 * ir1] * p;
+        si += zar[2 * ir1 + 1] * p;
     }
-    __syncthreads();
-    if (gate_zero) return;
-    double p = poti[f];
-    for (int ie = threadIdx.x; ie < netot; ie += blockDim.x) {
-        if (!(etot[ie] > p)) continue;
-        double cr = zck[2 * ie], ci = zck[2 * ie + 1];
-        size_t o = ((size_t)f * netot + ie) * 2;
-        zcr[o] += cr * pf;
-        zcr[o + 1] += ci * pf;
-        zcdr[o] += cr * dr - ci * di;
-        zcdr[o + 1] += cr * di + ci * dr;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) {
+        fpsi[4 * (size_t)f] = psi[fidx[f]];
+        fpsi[4 * (size_t)f + 1] = sr;
+        fpsi[4 * (size_t)f + 2] = si;
     }
 }
 
-// Cvjflux_k (mod_flux_01y2.f:663-775) for one block: projection at R(ir2abs) on
-// Djmmp x fd, then zS2 += Cvj C_k
+// second half: zCR(E,f) += C_k(E) psi(f), zCdR(E,f) += C_k(E) dpsi(f) for E > V(f)
+constexpr int kFluxPerBlock = 8;
+__global__ void __launch_bounds__(128) k_flux_acc(const double *__restrict__ fpsi, const double *__restrict__ poti,
+                                                  const double *__restrict__ etot, const double *__restrict__ zck,
+                                                  int netot, int NF, double *__restrict__ zcr, double *__restrict__ zcdr)
+{
+    int ie = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ie >= netot) return;
+    double e = etot[ie], cr = zck[2 * ie], ci = zck[2 * ie + 1];
+    int f0 = blockIdx.y * kFluxPerBlock, f1 = min(NF, f0 + kFluxPerBlock);
+    for (int f = f0; f < f1; f++) {
+        if (!(e > poti[f])) continue;
+        double pf = fpsi[4 * (size_t)f], dr = fpsi[4 * (size_t)f + 1], di = fpsi[4 * (size_t)f + 2];
+        size_t o = ((size_t)f * netot + ie) * 2;
+        double2 a = *reinterpret_cast<double2 *>(zcr + o);
+        double2 b = *reinterpret_cast<double2 *>(zcdr + o);
+        a.x += cr * pf;
+        a.y += ci * pf;
+        b.x += cr * dr - ci * di;
+        b.y += cr * di + ci * dr;
+        *reinterpret_cast<double2 *>(zcr + o) = a;
+        *reinterpret_cast<double2 *>(zcdr + o) = b;
+    }
+}
+
+// Cvjflux_k (mod_flux_01y2.f:663-775) in three parallel passes over every block
+// 1. xj(g, r1, j) = sum_gamma psi(g, gamma, r1, R(ir2abs)) / sqrt(ah2) Djmmp(gamma, j)
 struct CvjArgs {
     const double *psi;
-    const int *r2abs_map;        // [na][n1]
-    const double *djmmp;         // wave's Djmmp
-    const double *fd;            // [nelec][nj][nv][n1]
-    const int *nobc;             // [nelec][nj]
+    const int *r2abs;             // [W][na][n1]
+    const double *djall;
+    const int64_t *djoff;         // [W]
+    const int *wnangu2;           // [W]
+    const int *blk_j00, *blk_inc, *blk_isref;
+    const double *fd;             // [nelec][nj][nv][n1]
+    const int *nobc;              // [nelec][nj]
+    double *xj, *cvj, *zs2;
     const double *zck;
-    double *zs2, *cvj;
-    int nangu2, jini, jmax, nvini, nvmax, inc, j00, ielec, iom, nj, nv, netot;
-    int skip_ref;                // ifail for the reference channel this iteration
-    int jref, nvref;
+    int jini, jmax, nvini, nvmax, nj, nv, netot, jref, nvref, gate;
     double sah2;
-    int blk;                     // block index within the wave
-    int64_t foff_row;            // index into foff for (g, angle 0)
 };
 
-__global__ void __launch_bounds__(256) k_cvj(DevGrid d, CvjArgs c)
+__device__ inline bool cvj_on(const CvjArgs &c, int g, int j) { return j >= c.blk_j00[g] && ((j - c.blk_j00[g]) % c.blk_inc[g]) == 0; }
+
+__global__ void __launch_bounds__(256) k_cvj_proj(DevGrid d, CvjArgs c)
 {
-    extern __shared__ double xjs[];            // [n1][nj]
-    int na = d.na, n1 = d.n1, ne = d.ne;
-    int nj = c.nj, nv = c.nv;
-    for (int e = threadIdx.x; e < n1 * nj; e += blockDim.x) {
-        int ir1 = e / nj, jj = e % nj;
-        int j = c.jini + jj;
-        double xj = 0.0;
-        if (j >= c.j00 && ((j - c.j00) % c.inc) == 0) {
-            for (int ia = 0; ia < na; ia++) {
-                int a = na - 1 - ia;            // angle order of the flat vector
-                int ir = c.r2abs_map[(size_t)a * n1 + ir1];
-                double rori = (ir >= 0) ? c.psi[d.foff[c.foff_row + a] + ir] / c.sah2 : 0.0;
-                double dj = c.djmmp[(((size_t)c.iom * ne + (c.ielec - 1)) * (c.nangu2 + 1) + j) * na + a];
-                xj = xj + rori * dj;
-            }
+    int g = blockIdx.y;
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    int n1 = d.n1, na = d.na, nj = c.nj;
+    if (e >= n1 * nj) return;
+    int ir1 = e / nj, jj = e % nj;
+    int j = c.jini + jj;
+    int w = d.blk_wave[g], el = d.blk_elec[g], om = d.blk_om[g];
+    double xj = 0.0;
+    if (cvj_on(c, g, j)) {
+        const double *D = c.djall + c.djoff[w] + (((size_t)om * d.ne + (el - 1)) * (c.wnangu2[w] + 1) + j) * na;
+        const int *m = c.r2abs + (size_t)w * na * n1;
+        for (int ia = 0; ia < na; ia++) {
+            int a = na - 1 - ia;                      // angle order of the flat vector
+            int ir = m[(size_t)a * n1 + ir1];
+            double rori = (ir >= 0) ? c.psi[d.foff[(size_t)g * na + a] + ir] / c.sah2 : 0.0;
+            xj = xj + rori * D[a];
         }
-        xjs[ir1 * nj + jj] = xj;
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nj * nv; e += blockDim.x) {
-        int jj = e / nv, iv = e % nv;
-        int j = c.jini + jj;
-        int nob = c.nobc[(size_t)(c.ielec - 1) * nj + jj];
-        int maxnv = c.nvmax < nob ? c.nvmax : nob;
-        double r = 0.0;
-        bool on = (j >= c.j00 && ((j - c.j00) % c.inc) == 0 && c.nvini + iv <= maxnv);
-        if (on) {
-            const double *f = c.fd + (((size_t)(c.ielec - 1) * nj + jj) * nv + iv) * n1;
-            for (int ir1 = 0; ir1 < n1; ir1++) r = r + xjs[ir1 * nj + jj] * f[ir1];
-        }
-        c.cvj[((size_t)c.blk * nj + jj) * nv + iv] = on ? r : 0.0;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nj * nv * c.netot; e += blockDim.x) {
-        int ie = e % c.netot, jv = e / c.netot;
-        int jj = jv / nv, iv = jv % nv;
-        int j = c.jini + jj;
-        int nob = c.nobc[(size_t)(c.ielec - 1) * nj + jj];
-        int maxnv = c.nvmax < nob ? c.nvmax : nob;
-        if (!(j >= c.j00 && ((j - c.j00) % c.inc) == 0 && c.nvini + iv <= maxnv)) continue;
-        if (c.skip_ref && j == c.jref && c.nvini + iv == c.nvref) continue;
-        double z = c.cvj[((size_t)c.blk * nj + jj) * nv + iv];
-        size_t o = ((((size_t)c.blk * nj + jj) * nv + iv) * c.netot + ie) * 2;
-        c.zs2[o] += z * c.zck[2 * ie];
-        c.zs2[o + 1] += z * c.zck[2 * ie + 1];
-    }
+    c.xj[((size_t)g * n1 + ir1) * nj + jj] = xj;
 }
 
-// totalflux (mod_flux_01y2.f:778-816)
+// 2. Cvj(g, j, v) = sum_r1 xj(g, r1, j) fd(r1, v, j); one warp per (g, j, v)
+__global__ void __launch_bounds__(256) k_cvj_fd(DevGrid d, CvjArgs c)
+{
+    int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    int nj = c.nj, nv = c.nv, n1 = d.n1;
+    if (wid >= d.G * nj * nv) return;
+    int g = wid / (nj * nv), jv = wid % (nj * nv), jj = jv / nv, iv = jv % nv;
+    int j = c.jini + jj, el = d.blk_elec[g];
+    int nob = c.nobc[(size_t)(el - 1) * nj + jj];
+    int maxnv = c.nvmax < nob ? c.nvmax : nob;
+    bool on = cvj_on(c, g, j) && c.nvini + iv <= maxnv;
+    double r = 0.0;
+    if (on) {
+        const double *f = c.fd + (((size_t)(el - 1) * nj + jj) * nv + iv) * n1;
+        const double *x = c.xj + (size_t)g * n1 * nj + jj;
+        for (int ir1 = lane; ir1 < n1; ir1 += 32) r += x[(size_t)ir1 * nj] * f[ir1];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane == 0) c.cvj[((size_t)g * nj + jj) * nv + iv] = on ? r : 0.0;
+}
+
+// 3. zS2(E, v, j, g) += Cvj C_k(E), the elastic reference channel gated below kminelastic
+__global__ void __launch_bounds__(256) k_cvj_acc(DevGrid d, CvjArgs c)
+{
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int nj = c.nj, nv = c.nv, netot = c.netot;
+    if (e >= (int64_t)d.G * nj * nv * netot) return;
+    int ie = (int)(e % netot);
+    int64_t r = e / netot;
+    int iv = (int)(r % nv);
+    int jj = (int)((r / nv) % nj);
+    int g = (int)(r / ((int64_t)nv * nj));
+    int j = c.jini + jj, el = d.blk_elec[g];
+    int nob = c.nobc[(size_t)(el - 1) * nj + jj];
+    int maxnv = c.nvmax < nob ? c.nvmax : nob;
+    if (!(cvj_on(c, g, j) && c.nvini + iv <= maxnv)) return;
+    if (c.gate && c.blk_isref[g] && j == c.jref && c.nvini + iv == c.nvref) return;
+    double z = c.cvj[r];
+    c.zs2[2 * e] += z * c.zck[2 * ie];
+    c.zs2[2 * e + 1] += z * c.zck[2 * ie + 1];
+}
+
+// totalflux (mod_flux_01y2.f:778-816) for one wave's flux points
 __global__ void k_totalflux(const double *__restrict__ zcr, const double *__restrict__ zcdr,
                             const int *__restrict__ fblock, const int *__restrict__ nelebas, int nflux, int netot,
                             int nelec, const double *__restrict__ reacfct, double ah1, double *__restrict__ out,
@@ -677,7 +716,7 @@ void launch_scatter(Ctx &c, const double *psi, int g_begin, int g_end)
 {
     int nseg = (g_end - g_begin) * c.na;
     if (nseg <= 0) return;
-    k_scatter<T><<<nseg, 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, g_begin * c.na);
+    k_scatter<T><<<dim3(nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, g_begin * c.na);
     LAUNCH_CHECK(c);
 }
 
@@ -752,7 +791,7 @@ void launch_update(Ctx &c, int first)
     u.zfe = c.d_zfe_ptrs;
     u.wflat0 = c.d_wflat0;
     stage_mark(c, 5);
-    k_update<T><<<c.nseg, 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+    k_update<T><<<dim3(c.nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
     LAUNCH_CHECK(c);
 }
 
@@ -786,7 +825,6 @@ void set_kernel_attributes(Ctx &c)
     cudaFuncSetAttribute(k_ang_j<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angj_smem(c, 4));
     cudaFuncSetAttribute(k_ang_l<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 8));
     cudaFuncSetAttribute(k_ang_l<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 4));
-    cudaFuncSetAttribute(k_cvj, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 size_t max_smem_needed(Ctx &c)
@@ -802,63 +840,69 @@ void launch_accumulators(Ctx &c, int64_t it)
 {
     stage_mark(c, 6);
     DevGrid d = devgrid(c);
-    double ah2 = (c.grid.rfin2 - c.grid.rmis2) / (double)(c.n2 - 1);
+    k_coefecheby<<<(c.netot + 127) / 128, 128, 0, c.stream>>>(c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2,
+                                                              c.grid.hbr, it, c.d_zck);
+    LAUNCH_CHECK(c);
     for (size_t w = 0; w < c.waves.size(); w++) {
         WaveTables &t = c.waves[w];
-        WaveDev &wd = c.wdev[w];
-        k_coefecheby<<<(t.netot + 127) / 128, 128, 0, c.stream>>>(wd.etot, t.netot, c.grid.emindlt, c.grid.delta2,
-                                                                  c.grid.hbr, it, wd.zck);
-        LAUNCH_CHECK(c);
         if (t.nofe > 0) {
-            k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(wd.efe, t.nofe, c.grid.emindlt, c.grid.delta2, c.grid.hbr, it,
-                                                  c.d_zcke + (size_t)w * c.nofemax * 2);
+            k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(c.wdev[w].efe, t.nofe, c.grid.emindlt,
+                                                                     c.grid.delta2, c.grid.hbr, it,
+                                                                     c.d_zcke + (size_t)w * c.nofemax * 2);
             LAUNCH_CHECK(c);
         }
-        if (c.n1 > 1 && t.nflux > 0) {
-            int gate = (t.iphoto == 0 && t.iprod == 1 && it < t.kminelastic) ? 1 : 0;
-            k_flux<<<t.nflux, 128, 0, c.stream>>>(c.d_pk + t.flat0, wd.fl_idx, wd.fl_dptr, wd.fl_didx, wd.fl_dir1, wd.zar1flux,
-                                                  wd.potiflux, wd.etot, wd.zck, t.netot, gate, wd.zcr, wd.zcdr);
-            LAUNCH_CHECK(c);
-        }
-        if (c.n2 > 1) {
-            for (int b = 0; b < t.ncan; b++) {
-                CvjArgs a;
-                a.psi = c.d_pk;
-                a.r2abs_map = wd.r2abs_map;
-                a.djmmp = wd.djmmp;
-                a.fd = wd.fd;
-                a.nobc = wd.nobc;
-                a.zck = wd.zck;
-                a.zs2 = wd.zs2;
-                a.cvj = wd.cvj;
-                a.nangu2 = t.nangu2; a.jini = t.jini; a.jmax = t.jmax; a.nvini = t.nvini; a.nvmax = t.nvmax;
-                a.inc = t.inc; a.j00 = t.j00[b]; a.ielec = t.nelebas[b]; a.iom = t.iombas[b];
-                a.nj = t.nj; a.nv = t.nv; a.netot = t.netot;
-                bool gate = (t.iprod != 1 && t.iphoto == 0 && it < t.kminelastic);
-                a.skip_ref = gate && (t.iomref < 0 || b == t.icanref);
-                a.jref = t.jref; a.nvref = t.nvref;
-                a.sah2 = sqrt(ah2);
-                a.blk = b;
-                a.foff_row = (int64_t)(t.g0 + b) * c.na;
-                size_t sm = sizeof(double) * (size_t)c.n1 * t.nj;
-                k_cvj<<<1, 256, sm, c.stream>>>(d, a);
-                LAUNCH_CHECK(c);
-            }
-        }
+    }
+    bool gate = c.gate_elastic && it < c.kminelastic;
+    if (c.NF > 0 && !(gate && c.waves[0].iprod == 1)) {
+        k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx,
+                                                                     c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi);
+        LAUNCH_CHECK(c);
+        dim3 g((c.netot + 127) / 128, (c.NF + kFluxPerBlock - 1) / kFluxPerBlock);
+        k_flux_acc<<<g, 128, 0, c.stream>>>(c.d_fpsi, c.d_fl_poti, c.d_etot, c.d_zck, c.netot, c.NF, c.d_zcr,
+                                            c.d_zcdr);
+        LAUNCH_CHECK(c);
+    }
+    if (c.n2 > 1) {
+        CvjArgs a;
+        a.psi = c.d_pk;
+        a.r2abs = c.d_r2abs;
+        a.djall = c.d_djall;
+        a.djoff = c.d_djoff;
+        a.wnangu2 = c.d_wnangu2;
+        a.blk_j00 = c.d_blk_j00;
+        a.blk_inc = c.d_blk_inc;
+        a.blk_isref = c.d_blk_isref;
+        a.fd = c.d_fd;
+        a.nobc = c.d_nobc;
+        a.xj = c.d_xj;
+        a.cvj = c.d_cvj;
+        a.zs2 = c.d_zs2;
+        a.zck = c.d_zck;
+        a.jini = c.jini; a.jmax = c.jmax; a.nvini = c.nvini; a.nvmax = c.nvmax;
+        a.nj = c.nj; a.nv = c.nv; a.netot = c.netot; a.jref = c.jref; a.nvref = c.nvref;
+        a.gate = gate ? 1 : 0;
+        a.sah2 = c.sah2;
+        k_cvj_proj<<<dim3((c.n1 * c.nj + 255) / 256, c.G), 256, 0, c.stream>>>(d, a);
+        LAUNCH_CHECK(c);
+        k_cvj_fd<<<(c.G * c.nj * c.nv * 32 + 255) / 256, 256, 0, c.stream>>>(d, a);
+        LAUNCH_CHECK(c);
+        int64_t tot = (int64_t)c.G * c.nj * c.nv * c.netot;
+        k_cvj_acc<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(d, a);
+        LAUNCH_CHECK(c);
     }
 }
 
 void launch_addv(Ctx &c, const double *psi, int g0, int g1)
 {
     if (g1 <= g0) return;
-    k_addv<<<(g1 - g0) * c.na, 256, 0, c.stream>>>(devgrid(c), psi, c.d_h, c.d_vsrc, g0 * c.na);
+    k_addv<<<dim3((g1 - g0) * c.na, c.nchunk), 256, 0, c.stream>>>(devgrid(c), psi, c.d_h, c.d_vsrc, g0 * c.na);
     LAUNCH_CHECK(c);
 }
 
 void launch_norms(Ctx &c, int64_t slot)
 {
-    k_norms<<<(int)c.waves.size(), 256, 0, c.stream>>>(c.d_normpart, c.d_wseg0, c.d_wseg1, c.d_norm_ptrs,
-                                                       c.d_norm_cap, slot);
+    k_norms<<<(int)c.waves.size(), 256, 0, c.stream>>>(c.d_normpart, c.d_wseg0, c.d_wseg1, c.nchunk,
+                                                       c.d_norm_ptrs, c.d_norm_cap, slot);
     LAUNCH_CHECK(c);
 }
 
@@ -894,7 +938,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     const double *P = psi - t.flat0;
     double *H = hpsi - t.flat0;
     DevGrid d = devgrid(c);
-    k_scatter<T><<<ng * na, 256, 0, c.stream>>>(d, X, P, g0 * na);
+    k_scatter<T><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, X, P, g0 * na);
     LAUNCH_CHECK(c);
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g0 * na * n1, nrows = (int64_t)ng * na * n1;
@@ -919,7 +963,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
                                                                     c.d_cpl, c.ncl, g0);
         LAUNCH_CHECK(c);
     }
-    k_addv<<<ng * na, 256, 0, c.stream>>>(d, P, H, c.d_vsrc, g0 * na);
+    k_addv<<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, P, H, c.d_vsrc, g0 * na);
     LAUNCH_CHECK(c);
     (void)g1;
 }
