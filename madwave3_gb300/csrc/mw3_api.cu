@@ -164,6 +164,12 @@ int build_device(Ctx &c)
                 map[((size_t)a * n1 + ir1) * n2 + ir2] = ir;
             }
         TRY(dupload(c, &c.d_map, map));
+        std::vector<int> mapT((size_t)na * n1 * n2);
+        for (int a = 0; a < na; a++)
+            for (int i1 = 0; i1 < n1; i1++)
+                for (int i2 = 0; i2 < n2; i2++)
+                    mapT[((size_t)a * n2 + i2) * n1 + i1] = map[((size_t)a * n1 + i1) * n2 + i2];
+        TRY(dupload(c, &c.d_mapT, mapT));
     }
     // ---- layout of the wave set ----
     int G = 0;
@@ -309,6 +315,7 @@ int build_device(Ctx &c)
     TRY(dalloc(c, &c.d_h, NT));
     TRY(dalloc(c, &c.d_tmp, NT));
     c.tmp_cap = NT;
+    TRY(dalloc(c, &c.d_tc_err, 1));
     c.nchunk = (c.npt + 1023) / 1024;
     TRY(dalloc(c, &c.d_normpart, (size_t)c.nseg * c.nchunk));
     // ---- accumulators: context-wide arrays, each wave a slice ----
@@ -497,6 +504,19 @@ int check_launch(Ctx &c, const char *where)
     return MW3_OK;
 }
 
+// after a synchronisation: did a tensor-core kernel give up waiting for its MMAs?
+int check_device_flags(Ctx &c, const char *where)
+{
+    if (!c.d_tc_err) return MW3_OK;
+    int h = 0;
+    MW3_CUDA_TRY(cudaMemcpy(&h, c.d_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        c.err = std::string(where) + ": a tensor-core kernel timed out waiting for its MMAs";
+        return MW3_ERR_CUDA;
+    }
+    return MW3_OK;
+}
+
 int reset_accumulators(Ctx &c)
 {
     size_t nf = (size_t)std::max(c.NF, 1) * c.netot * 2;
@@ -632,7 +652,7 @@ int mw3_hphi(mw3_ctx *h, int32_t w, const double *psi, double *hpsi)
     rc = check_launch(c, "mw3_hphi");
     if (rc) return rc;
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    return MW3_OK;
+    return check_device_flags(c, "mw3_hphi");
 }
 
 int mw3_start(mw3_ctx *h, const double *const *psi0s)
@@ -730,7 +750,9 @@ int mw3_sync(mw3_ctx *h)
     if (!h) return MW3_ERR_ARG;
     Ctx &c = h->c;
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    return check_launch(c, "mw3_sync");
+    int rc = check_launch(c, "mw3_sync");
+    if (rc) return rc;
+    return check_device_flags(c, "mw3_sync");
 }
 
 int mw3_download_state(mw3_ctx *h, int32_t w, double *km1, double *k, int64_t *it)
@@ -747,7 +769,7 @@ int mw3_download_state(mw3_ctx *h, int32_t w, double *km1, double *k, int64_t *i
                                      c.stream));
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
     if (it) *it = c.it;
-    return MW3_OK;
+    return check_device_flags(c, "mw3_download_state");
 }
 
 int mw3_norms(mw3_ctx *h, int32_t w, double *norms, int64_t *n)

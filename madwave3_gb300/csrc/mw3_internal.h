@@ -113,6 +113,7 @@ struct Ctx {
     int *d_indr1 = nullptr, *d_indr2 = nullptr, *d_npunreal = nullptr;
     double *d_vvv = nullptr;
     int *d_map = nullptr;            // [na][n1][n2] local point index, -1 = not stored
+    int *d_mapT = nullptr;           // [na][n2][n1] the same, r1 fastest (stored points are r1-major runs)
     // block tables
     int *d_blk_wave = nullptr, *d_blk_elec = nullptr, *d_blk_om = nullptr;
     int64_t *d_foff = nullptr;       // [G][na] context-wide flat start of (block, angle)
@@ -179,12 +180,39 @@ struct Ctx {
     int *d_nobc = nullptr;           // [nelec][nj]
     double sah2 = 1.0;
     int jini = 0, jmax = 0, nvini = 0, nvmax = 0, kminelastic = 0, gate_elastic = 0, jref = 0, nvref = 0;
+    bool use_tc = true;              // mixed path: radial DSTs on the tensor cores when the shape allows
+    int *d_tc_err = nullptr;         // set by a tensor-core kernel whose mbarrier wait ran out
     // optional per-stage event timing (mw3_profile)
     bool prof = false;
     std::vector<cudaEvent_t> prof_ev;    // (MW3_NSTAGES+1) events per recorded iteration
     int64_t prof_n = 0, prof_cap = 0;
     std::vector<void *> allocs;      // everything allocated for the wave set
 };
+
+// device-side view of the shared grid and block tables (passed by value)
+struct DevGrid {
+    int n1, n2, na, ne, npt, G;
+    const int *indr1, *indr2, *npunreal;
+    const double *vvv;
+    const int *map;
+    const int *mapT;
+    const int64_t *foff;
+    const int *blk_wave, *blk_elec, *blk_om;
+};
+
+inline DevGrid devgrid(Ctx &c)
+{
+    DevGrid d;
+    d.n1 = c.n1; d.n2 = c.n2; d.na = c.na; d.ne = c.ne; d.npt = c.npt; d.G = c.G;
+    d.indr1 = c.d_indr1; d.indr2 = c.d_indr2; d.npunreal = c.d_npunreal; d.vvv = c.d_vvv;
+    d.map = c.d_map; d.mapT = c.d_mapT; d.foff = c.d_foff;
+    d.blk_wave = c.d_blk_wave; d.blk_elec = c.d_blk_elec; d.blk_om = c.d_blk_om;
+    return d;
+}
+
+// tensor-core radial DSTs of the mixed path (mw3_tc.cu); false = shape not supported
+bool tc_dst_supported(Ctx &c);
+void launch_tc_dst(Ctx &c, const float *X, float *Y, double *H, int g_begin, int g_end, int stage_base);
 
 // ---------------------------------------------------------------------------
 // setup (mw3_setup.cu)

@@ -20,26 +20,6 @@
 
 namespace mw3 {
 
-// device-side views of the context (passed by value)
-struct DevGrid {
-    int n1, n2, na, ne, npt, G;
-    const int *indr1, *indr2, *npunreal;
-    const double *vvv;
-    const int *map;
-    const int64_t *foff;
-    const int *blk_wave, *blk_elec, *blk_om;
-};
-
-static DevGrid devgrid(Ctx &c)
-{
-    DevGrid d;
-    d.n1 = c.n1; d.n2 = c.n2; d.na = c.na; d.ne = c.ne; d.npt = c.npt; d.G = c.G;
-    d.indr1 = c.d_indr1; d.indr2 = c.d_indr2; d.npunreal = c.d_npunreal; d.vvv = c.d_vvv;
-    d.map = c.d_map; d.foff = c.d_foff;
-    d.blk_wave = c.d_blk_wave; d.blk_elec = c.d_blk_elec; d.blk_om = c.d_blk_om;
-    return d;
-}
-
 #define LAUNCH_CHECK(c) do { (c).launches++; } while (0)
 
 // ---------------------------------------------------------------------------
@@ -258,6 +238,39 @@ __global__ void k_quirk(DevGrid d, const double *__restrict__ psi, double *__res
 // ---------------------------------------------------------------------------
 constexpr int ANG_CW = 64;
 
+// Target descriptors of one angular CTA: angle, column inside the chunk and
+// output index, with eight independent loads in flight per thread.
+__device__ __forceinline__ void stage_targets(const DevGrid &d, const int *__restrict__ tl, int nt,
+                                              const int *__restrict__ ind, int c0, size_t frow, int *t_a, int *t_c,
+                                              long long *t_o)
+{
+    constexpr int U = 8;
+    for (int q0 = threadIdx.x; q0 < nt; q0 += U * blockDim.x) {
+        int ent[U], col[U];
+        long long off[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int q = q0 + u * blockDim.x;
+            ent[u] = q < nt ? __ldg(tl + q) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int a = ent[u] >> 20, ir = ent[u] & 0xFFFFF;
+            col[u] = __ldg(ind + (size_t)a * d.npt + ir) - 1 - c0;
+            off[u] = __ldg(d.foff + frow + a) + ir;
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            int q = q0 + u * blockDim.x;
+            if (q < nt) {
+                t_a[q] = ent[u] >> 20;
+                t_c[q] = col[u];
+                t_o[q] = off[u];
+            }
+        }
+    }
+}
+
 // j^2: H(g, a, r1, r2) += sum_j' X(g, j', r1, r2) xj2(g, r1, a, j')
 template <typename T>
 __global__ void __launch_bounds__(256) k_ang_j(DevGrid d, const T *__restrict__ X, const T *__restrict__ xj2,
@@ -271,6 +284,11 @@ __global__ void __launch_bounds__(256) k_ang_j(DevGrid d, const T *__restrict__ 
     int na = d.na, n1 = d.n1, n2 = d.n2;
     T *Xs = reinterpret_cast<T *>(smraw);       // [na][ANG_CW]
     T *xs = Xs + (size_t)na * ANG_CW;           // [na][na+1]
+    // target descriptors (angle, column, output index), loaded with all loads in flight
+    int *t_a = reinterpret_cast<int *>(xs + (size_t)na * (na + 1));
+    int *t_c = t_a + na * ANG_CW;
+    long long *t_o = reinterpret_cast<long long *>(t_c + na * ANG_CW);
+    stage_targets(d, tlist + b, e - b, d.indr2, chunk * ANG_CW, (size_t)g * na, t_a, t_c, t_o);
     int c0 = chunk * ANG_CW;
     for (int i = threadIdx.x; i < na * ANG_CW; i += blockDim.x) {
         int j = i / ANG_CW, cc = i % ANG_CW;
@@ -279,14 +297,12 @@ __global__ void __launch_bounds__(256) k_ang_j(DevGrid d, const T *__restrict__ 
     const T *xm = xj2 + ((size_t)g * n1 + ir1) * na * na;
     for (int i = threadIdx.x; i < na * na; i += blockDim.x) xs[(i / na) * (na + 1) + (i % na)] = xm[i];
     __syncthreads();
-    for (int q = b + threadIdx.x; q < e; q += blockDim.x) {
-        int ent = tlist[q];
-        int a = ent >> 20, ir = ent & 0xFFFFF;
-        int col = d.indr2[(size_t)a * d.npt + ir] - 1 - c0;
+    for (int q = threadIdx.x; q < e - b; q += blockDim.x) {
+        int col = t_c[q];
         T acc = (T)0;
-        const T *row = xs + (size_t)a * (na + 1);
+        const T *row = xs + (size_t)t_a[q] * (na + 1);
         for (int j = 0; j < na; j++) acc += Xs[j * ANG_CW + col] * row[j];
-        H[d.foff[(size_t)g * na + a] + ir] += (double)acc;
+        H[t_o[q]] += (double)acc;
     }
 }
 
@@ -305,9 +321,13 @@ __global__ void __launch_bounds__(256) k_ang_l(DevGrid d, const T *__restrict__ 
     T *acc = reinterpret_cast<T *>(smraw);                     // [e-b]
     T *Xs = reinterpret_cast<T *>(acc + (na * ANG_CW));         // [na][ANG_CW]
     T *xs = Xs + (size_t)na * ANG_CW;                           // [na][na+1]
+    int *t_a = reinterpret_cast<int *>(xs + (size_t)na * (na + 1));
+    int *t_c = t_a + na * ANG_CW;
+    long long *t_o = reinterpret_cast<long long *>(t_c + na * ANG_CW);
     int c0 = chunk * ANG_CW;
     int nt = e - b;
     for (int q = threadIdx.x; q < nt; q += blockDim.x) acc[q] = (T)0;
+    stage_targets(d, tlist + b, nt, d.indr1, c0, (size_t)t * na, t_a, t_c, t_o);
     for (int slot = 0; slot < 3; slot++) {
         int s = cpl[(t * 3 + slot) * 2], qq = cpl[(t * 3 + slot) * 2 + 1];
         if (s < 0) continue;
@@ -320,21 +340,15 @@ __global__ void __launch_bounds__(256) k_ang_l(DevGrid d, const T *__restrict__ 
         for (int i = threadIdx.x; i < na * na; i += blockDim.x) xs[(i / na) * (na + 1) + (i % na)] = xm[i];
         __syncthreads();
         for (int q = threadIdx.x; q < nt; q += blockDim.x) {
-            int ent = tlist[b + q];
-            int a = ent >> 20, ir = ent & 0xFFFFF;
-            int col = d.indr1[(size_t)a * d.npt + ir] - 1 - c0;
+            int col = t_c[q];
             T s_ = (T)0;
-            const T *row = xs + (size_t)a * (na + 1);
+            const T *row = xs + (size_t)t_a[q] * (na + 1);
             for (int j = 0; j < na; j++) s_ += Xs[j * ANG_CW + col] * row[j];
             acc[q] += s_;
         }
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < nt; q += blockDim.x) {
-        int ent = tlist[b + q];
-        int a = ent >> 20, ir = ent & 0xFFFFF;
-        H[d.foff[(size_t)t * na + a] + ir] += (double)acc[q];
-    }
+    for (int q = threadIdx.x; q < nt; q += blockDim.x) H[t_o[q]] += (double)acc[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -548,27 +562,43 @@ struct CvjArgs {
 
 __device__ inline bool cvj_on(const CvjArgs &c, int g, int j) { return j >= c.blk_j00[g] && ((j - c.blk_j00[g]) % c.blk_inc[g]) == 0; }
 
+constexpr int kCvjR1 = 8;   // r1 points per CTA of the Cvj projection
+
 __global__ void __launch_bounds__(256) k_cvj_proj(DevGrid d, CvjArgs c)
 {
-    int g = blockIdx.y;
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    // one CTA per block: gather psi on the line R = R(ir2abs) for every angle and
+    // the block's Djmmp columns into shared memory, then contract over angles
+    extern __shared__ double cvsm[];
+    int g = blockIdx.x;
     int n1 = d.n1, na = d.na, nj = c.nj;
-    if (e >= n1 * nj) return;
-    int ir1 = e / nj, jj = e % nj;
-    int j = c.jini + jj;
+    int r1a = blockIdx.y * kCvjR1, r1b = min(n1, r1a + kCvjR1);     // this CTA's r1 chunk
     int w = d.blk_wave[g], el = d.blk_elec[g], om = d.blk_om[g];
-    double xj = 0.0;
-    if (cvj_on(c, g, j)) {
-        const double *D = c.djall + c.djoff[w] + (((size_t)om * d.ne + (el - 1)) * (c.wnangu2[w] + 1) + j) * na;
-        const int *m = c.r2abs + (size_t)w * na * n1;
-        for (int ia = 0; ia < na; ia++) {
-            int a = na - 1 - ia;                      // angle order of the flat vector
-            int ir = m[(size_t)a * n1 + ir1];
-            double rori = (ir >= 0) ? c.psi[d.foff[(size_t)g * na + a] + ir] / c.sah2 : 0.0;
-            xj = xj + rori * D[a];
-        }
+    double *fr = cvsm;                       // [na][n1] psi / sqrt(ah2) (chunk columns used)
+    double *dj = cvsm + (size_t)na * n1;     // [nj][na]
+    const int *m = c.r2abs + (size_t)w * na * n1;
+    int cw = r1b - r1a;
+    for (int e = threadIdx.x; e < na * cw; e += blockDim.x) {
+        int a = e / cw, ir1 = r1a + e % cw;
+        int ir = m[(size_t)a * n1 + ir1];
+        fr[(size_t)a * n1 + ir1] = (ir >= 0) ? c.psi[d.foff[(size_t)g * na + a] + ir] / c.sah2 : 0.0;
     }
-    c.xj[((size_t)g * n1 + ir1) * nj + jj] = xj;
+    for (int e = threadIdx.x; e < nj * na; e += blockDim.x) {
+        int jj = e / na, a = e % na;
+        int j = c.jini + jj;
+        dj[e] = cvj_on(c, g, j)
+                    ? c.djall[c.djoff[w] + (((size_t)om * d.ne + (el - 1)) * (c.wnangu2[w] + 1) + j) * na + a]
+                    : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < cw * nj; e += blockDim.x) {
+        int ir1 = r1a + e / nj, jj = e % nj;
+        double xj = 0.0;
+        for (int ia = 0; ia < na; ia++) {
+            int a = na - 1 - ia;                  // angle order of the flat vector
+            xj = xj + fr[(size_t)a * n1 + ir1] * dj[(size_t)jj * na + a];
+        }
+        c.xj[((size_t)g * n1 + ir1) * nj + jj] = xj;
+    }
 }
 
 // 2. Cvj(g, j, v) = sum_r1 xj(g, r1, j) fd(r1, v, j); one warp per (g, j, v)
@@ -721,10 +751,14 @@ void launch_scatter(Ctx &c, const double *psi, int g_begin, int g_end)
 }
 
 static size_t col_smem(Ctx &c, size_t tsz) { return tsz * (size_t)c.n1 * (COL_W + COL_KC); }
-static size_t angj_smem(Ctx &c, size_t tsz) { return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1)); }
+static size_t ang_desc(Ctx &c) { return (size_t)c.na * ANG_CW * 16 + 16; }
+static size_t angj_smem(Ctx &c, size_t tsz)
+{
+    return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1)) + ang_desc(c);
+}
 static size_t angl_smem(Ctx &c, size_t tsz)
 {
-    return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1));
+    return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1)) + ang_desc(c);
 }
 
 template <typename T>
@@ -737,23 +771,29 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     int64_t row0 = (int64_t)g_begin * c.na * c.n1;
     int64_t nrows = (int64_t)ng * c.na * c.n1;
     dim3 gr((c.n2 + BN - 1) / BN, (unsigned)((nrows + BM - 1) / BM));
-    // 1. DST along R
-    stage_mark(c, 0);
-    k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_S2, (T *)c.d_Y, nullptr,
-                                                    c.d_nopr1, row0, nrows);
-    LAUNCH_CHECK(c);
-    // 2. DST along r, k-space scaling, DST along r
-    stage_mark(c, 1);
-    dim3 gc((c.n2 + COL_W - 1) / COL_W, ng * c.na);
-    k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, (T *)c.d_Y, (const T *)c.d_S1, c.d_S1off,
-                                                                  c.d_nopr1, c.d_p2r1, c.d_p2r2, c.grid.radcutmax,
-                                                                  g_begin * c.na);
-    LAUNCH_CHECK(c);
-    // 3. DST along R, gathered into H at the stored points; points beyond the DST
-    stage_mark(c, 2);
-    k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_Y, (const T *)c.d_S2, nullptr, c.d_h,
-                                                   c.d_nopr1, row0, nrows);
-    LAUNCH_CHECK(c);
+    if (sizeof(T) == 4 && tc_dst_supported(c)) {
+        // mixed path: the three DST passes on the tensor cores
+        launch_tc_dst(c, (const float *)c.d_X, (float *)c.d_Y, c.d_h, g_begin, g_end, 0);
+    } else {
+        // 1. DST along R
+        stage_mark(c, 0);
+        k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_S2, (T *)c.d_Y, nullptr,
+                                                        c.d_nopr1, row0, nrows);
+        LAUNCH_CHECK(c);
+        // 2. DST along r, k-space scaling, DST along r
+        stage_mark(c, 1);
+        dim3 gc((c.n2 + COL_W - 1) / COL_W, ng * c.na);
+        k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, (T *)c.d_Y, (const T *)c.d_S1, c.d_S1off,
+                                                                      c.d_nopr1, c.d_p2r1, c.d_p2r2, c.grid.radcutmax,
+                                                                      g_begin * c.na);
+        LAUNCH_CHECK(c);
+        // 3. DST along R, gathered into H at the stored points
+        stage_mark(c, 2);
+        k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_Y, (const T *)c.d_S2, nullptr, c.d_h,
+                                                       c.d_nopr1, row0, nrows);
+        LAUNCH_CHECK(c);
+    }
+    // points beyond the r1 DST length keep psi
     k_quirk<<<ng * c.na, 128, 0, c.stream>>>(d, psi, c.d_h, c.d_quirk_ptr, c.d_quirk, g_begin * c.na);
     LAUNCH_CHECK(c);
     // 4. angular kinetic terms
@@ -819,6 +859,7 @@ void launch_build_kinetic(Ctx &c)
 
 void set_kernel_attributes(Ctx &c)
 {
+    cudaFuncSetAttribute(k_cvj_proj, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_dst_cols<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem(c, 8));
     cudaFuncSetAttribute(k_dst_cols<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem(c, 4));
     cudaFuncSetAttribute(k_ang_j<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angj_smem(c, 8));
@@ -882,7 +923,8 @@ void launch_accumulators(Ctx &c, int64_t it)
         a.nj = c.nj; a.nv = c.nv; a.netot = c.netot; a.jref = c.jref; a.nvref = c.nvref;
         a.gate = gate ? 1 : 0;
         a.sah2 = c.sah2;
-        k_cvj_proj<<<dim3((c.n1 * c.nj + 255) / 256, c.G), 256, 0, c.stream>>>(d, a);
+        size_t smp = sizeof(double) * ((size_t)c.na * c.n1 + (size_t)c.nj * c.na);
+        k_cvj_proj<<<dim3(c.G, (c.n1 + kCvjR1 - 1) / kCvjR1), 256, smp, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
         k_cvj_fd<<<(c.G * c.nj * c.nv * 32 + 255) / 256, 256, 0, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
