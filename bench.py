@@ -32,9 +32,14 @@ sys.path.insert(0, HERE)
 L2_BYTES = 129 * 1024 * 1024
 
 WORKLOADS = {
+    # partial-wave sweep J=0..40, Omega=0..min(J,6): 266 blocks on 256 R x 128 r x 60 angles
+    "jsweep0-40_256x128x60": dict(case="j0_256x128x60", sweep=list(range(0, 41))),
     # J=0, one Omega block, one state: 256 R x 128 r x 60 angles (synthetic LEPS)
-    "j0_256x128x60": dict(case="j0_256x128x60", waves=[dict()]),
+    "j0_256x128x60": dict(case="j0_256x128x60", sweep=None),
+    # J=0 at 512 R x 256 r x 120 angles
+    "j0_512x256x120": dict(case="j0_512x256x120", sweep=None),
 }
+DEFAULT_WORKLOAD = "jsweep0-40_256x128x60"
 
 
 def metric_name():
@@ -64,7 +69,17 @@ def case_runs(workload, rank):
     d = os.path.join(base, w["case"])
     if not os.path.exists(os.path.join(d, "pot", "cont.pot")):
         generator.write_case(d, **generator.CASES[w["case"]])
-    return [setup.load(os.path.join(d, "input.dat"))]
+    if w["sweep"] is None:
+        return [setup.load(os.path.join(d, "input.dat"))]
+    return setup.load_sweep(os.path.join(d, "input.dat"), w["sweep"], generator.jsweep_inputs)
+
+
+def sample_waves(runs, n=5):
+    """Waves spread over a sweep (first, last and evenly between) for CPU samples."""
+    if len(runs) <= n:
+        return list(runs)
+    idx = sorted(set(int(round(x)) for x in np.linspace(0, len(runs) - 1, n)))
+    return [runs[i] for i in idx]
 
 
 class ClockSampler:
@@ -113,8 +128,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def stage_model(runs, prop):
-    """Algorithmic work of each stage of one iteration (flops or bytes)."""
+def stage_model(runs, prop, stages=None):
+    """Algorithmic work of each stage of one iteration (flops or bytes).
+
+    The angular stage is counted as bytes when the mixed path runs it as the
+    fused tensor-core contraction (the l^2 stage then measures ~0): psi read at
+    every stored point in FP32 and H read and written in FP64, 20 bytes per
+    stored point.  The explicit form is counted in flops."""
     r0 = runs[0]
     i = r0.inp
     n1, n2, na = i.npun1, i.npun2, i.nangu
@@ -128,12 +148,13 @@ def stage_model(runs, prop):
         rows_sq += r.ncan * int((nopr1 ** 2).sum())
         nsto += r.ntot
     ne = r0.nelec
+    fused = bool(stages) and stages.get("angular_l2", 0.0) < 0.01 * max(stages.get("angular", 0.0), 1e-30)
     return {
         "dst_R": ("flop", 2.0 * rows * n2 * n2),
         "dst_r_pair": ("flop", 4.0 * rows_sq * n2),
         "dst_R_gather": ("flop", 2.0 * rows * n2 * n2),
-        "ang_j2": ("flop", 2.0 * na * nsto),
-        "ang_l2": ("flop", 2.0 * na * nsto * 3),
+        "angular": (("byte", 20.0 * nsto) if fused else ("flop", 2.0 * na * nsto)),
+        "angular_l2": ("flop", 2.0 * na * nsto * 3),
         # psi_k, psi_k-1, H read, psi_k+1 written, V row, rectangle store, two grid indices
         "update": ("byte", nsto * (8 * 4 + 8 * ne + tsz + 8)),
         "accumulators": ("byte", sum(prop.nflux(w) * r.inp.netot * 2 * 2 * 16 for w, r in enumerate(runs))),
@@ -214,7 +235,7 @@ def run_gpu(args, rank, world, local):
 
     # roofline of the dominant stage
     hbm, tf, src = load_peaks()
-    model = stage_model(runs, prop)
+    model = stage_model(runs, prop, stages)
     dom = max(stages, key=lambda k: stages[k])
     kind, work = model[dom]
     t_launch = stages[dom] / max(nrec, 1) * 1e-3
@@ -246,10 +267,39 @@ def run_gpu(args, rank, world, local):
         "roofline": roof,
         "clocks": clk,
     }
+    out["config"]["kernels"] = prop.path()
     prop.close()
+    del prop
+    if args.precision == "mixed" and args.fp64_steps > 0:
+        out["fp64_plain"] = fp64_plain(runs, args.fp64_steps, stream_world=world)
+        out["fp64_plain"]["speedup_mixed_over_fp64"] = value / out["fp64_plain"]["value"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(runs, budget_s=args.cpu_seconds)
+        out["cpu_baseline"] = cpu_baseline(sample_waves(runs), budget_s=args.cpu_seconds)
     return out
+
+
+def fp64_plain(runs, steps, stream_world=1, warmup=3):
+    """The plain FP64 path on the same workload, for the mixed/FP64 ratio."""
+    import torch
+    from madwave3_gb300 import Propagator
+    prop = Propagator(runs, "fp64")
+    prop.start()
+    for _ in range(warmup):
+        prop.run(1)
+    prop.sync()
+    stream = torch.cuda.ExternalStream(prop.stream())
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    prop.run(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    prop.close()
+    nsto = sum(r.ntot for r in runs)
+    return {"value": stream_world * nsto * steps / (ms * 1e-3), "unit": "grid-pt*iter/s",
+            "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
 
 
 def cpu_baseline(runs, budget_s=15.0):
@@ -273,14 +323,15 @@ def cpu_baseline(runs, budget_s=15.0):
         its_done += n
         del o
     return {"value": total_pts / total_t, "unit": "grid-pt*iter/s", "cores": cores, "kind": "port",
-            "sample": "%d Chebyshev iterations of the same workload after one warm-up iteration" % its_done}
+            "sample": "%d Chebyshev iterations in total, after one warm-up iteration each, over the waves J=%s "
+                      "of the workload" % (its_done, ",".join(str(r.inp.Jtot) for r in runs))}
 
 
 def run_reference(args, rank, world, local):
     if rank != 0:
         return None
     from oracle.mw3ref import Oracle
-    runs = case_runs(args.workload, rank)
+    runs = sample_waves(case_runs(args.workload, rank))
     cores = os.cpu_count() or 1
     oracles = []
     for r in runs:
@@ -302,9 +353,10 @@ def run_reference(args, rank, world, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic LEPS surface, generated on the fly",
-        "config": {"workload": args.workload, "stored_points": nsto, "waves": len(runs)},
+        "config": {"workload": args.workload, "stored_points_per_step": nsto, "waves_per_step": len(runs)},
         "cpu_baseline": {"value": value, "unit": "grid-pt*iter/s", "cores": cores, "kind": "port",
-                         "sample": "%d timed Chebyshev iterations after %d warm-up" % (args.steps, args.warmup)},
+                         "sample": "%d timed Chebyshev iterations after %d warm-up, each over the waves J=%s"
+                                   % (args.steps, args.warmup, ",".join(str(r.inp.Jtot) for r in runs))},
         "e2e": {"value": value, "unit": "grid-pt*iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -315,10 +367,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--workload", default="j0_256x128x60", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=3,
+                    help="timed steps of the plain FP64 path on the same workload (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

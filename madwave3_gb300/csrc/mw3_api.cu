@@ -131,7 +131,9 @@ int build_typed(Ctx &c)
     TRY(dalloc(c, &y, rect));
     c.d_X = x;
     c.d_Y = y;
-    // explicit angular matrices
+    // explicit angular matrices (not needed when the factorised contraction runs)
+    c.d_xj2 = c.d_xl2p = nullptr;
+    if (c.use_tc_ang) return MW3_OK;
     T *xj2, *xl2p;
     TRY(dalloc(c, &xj2, (size_t)c.G * n1 * na * na));
     TRY(dalloc(c, &xl2p, (size_t)c.G * 3 * n2 * na * na));
@@ -420,6 +422,7 @@ int build_device(Ctx &c)
     TRY(dupload(c, &c.d_norm_cap, normcap));
     // ---- typed tables ----
     mw3::set_kernel_attributes(c);
+    TRY(mw3::build_tc_ang(c));
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;
     cudaError_t e = cudaStreamSynchronize(c.stream);
@@ -851,6 +854,18 @@ int mw3_kernel_launches(mw3_ctx *h, int64_t *count)
 {
     if (!h || !count) return MW3_ERR_ARG;
     *count = h->c.launches;
+    return MW3_OK;
+}
+
+int mw3_path_flags(mw3_ctx *h, int32_t *flags)
+{
+    if (!h || !flags) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (!c.built) {
+        c.err = "mw3_path_flags before the device tables were built";
+        return MW3_ERR_STATE;
+    }
+    *flags = (mw3::tc_dst_supported(c) ? MW3_PATH_TC_DST : 0) | (c.use_tc_ang ? MW3_PATH_TC_ANG : 0);
     return MW3_OK;
 }
 

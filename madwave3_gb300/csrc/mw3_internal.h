@@ -181,6 +181,15 @@ struct Ctx {
     double sah2 = 1.0;
     int jini = 0, jmax = 0, nvini = 0, nvmax = 0, kminelastic = 0, gate_elastic = 0, jref = 0, nvref = 0;
     bool use_tc = true;              // mixed path: radial DSTs on the tensor cores when the shape allows
+    // mixed path: factorised angular contraction on the tensor cores (mw3_tc_ang.cu)
+    bool use_tc_ang = false;
+    float *d_ang_dfw = nullptr, *d_ang_dbk = nullptr;   // [G][2][64*64] Djmmp hi/lo planes, both layouts
+    float *d_ang_yj = nullptr;                          // [G][n1][64] yyy(j, r1) by ladder slot
+    float *d_ang_l2 = nullptr;                          // [G][3][n2][64] xl2mat_j(Om, Om+q; R)
+    int *d_ang_chain_ptr = nullptr, *d_ang_chain = nullptr;   // blocks per (wave, electronic state), Omega ascending
+    int *d_ang_tiles = nullptr;                         // 16 r1 x 8 R tiles holding stored points
+    int ang_ntiles = 0;
+    std::vector<int> ang_wchain;                        // [W+1] first chain of each wave
     int *d_tc_err = nullptr;         // set by a tensor-core kernel whose mbarrier wait ran out
     // optional per-stage event timing (mw3_profile)
     bool prof = false;
@@ -213,6 +222,9 @@ inline DevGrid devgrid(Ctx &c)
 // tensor-core radial DSTs of the mixed path (mw3_tc.cu); false = shape not supported
 bool tc_dst_supported(Ctx &c);
 void launch_tc_dst(Ctx &c, const float *X, float *Y, double *H, int g_begin, int g_end, int stage_base);
+// tensor-core angular terms of the mixed path (mw3_tc_ang.cu); sets c.use_tc_ang
+int build_tc_ang(Ctx &c);
+void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end);
 
 // ---------------------------------------------------------------------------
 // setup (mw3_setup.cu)

@@ -63,8 +63,8 @@ __global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN];
     const int n1 = d.n1, n2 = d.n2, na = d.na;
-    int64_t rbase = row0 + (int64_t)blockIdx.y * BM;
-    int cbase = blockIdx.x * BN;
+    int64_t rbase = row0 + (int64_t)blockIdx.x * BM;     // row tiles on x: no 65535 limit
+    int cbase = blockIdx.y * BN;
     int tid = threadIdx.x;
     // skip tiles whose rows all lie beyond the DST length of their angle
     __shared__ int any;
@@ -155,13 +155,13 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
     extern __shared__ unsigned char smraw[];
     T *Yt = reinterpret_cast<T *>(smraw);                 // [n1][COL_W]
     T *Sc = Yt + (size_t)d.n1 * COL_W;                    // [n1][COL_KC]
-    int seg = seg0 + blockIdx.y;
+    int seg = seg0 + blockIdx.x;
     int g = seg / d.na, a = seg % d.na;
     int w = d.blk_wave[g];
     int nn = nopr1[w * d.na + a];
     const T *S1 = S1all + s1off[w * d.na + a];
     int n1 = d.n1, n2 = d.n2;
-    int c0 = blockIdx.x * COL_W;
+    int c0 = blockIdx.y * COL_W;
     int tx = threadIdx.x % COL_W, ty = threadIdx.x / COL_W;   // 8 row groups
     T *base = Y + (size_t)seg * n1 * n2;
     for (int e = threadIdx.x; e < nn * COL_W; e += 256) {
@@ -372,42 +372,84 @@ struct UpdArgs {
 template <typename T>
 __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
 {
-    int seg = blockIdx.x;
-    int g = seg / d.na, a = seg % d.na;
-    int w = d.blk_wave[g];
-    int et = d.blk_elec[g];
-    int64_t off = d.foff[seg];
-    int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
-    int n1 = d.n1, n2 = d.n2, na = d.na, ne = d.ne;
-    T *rect = X + (size_t)seg * n1 * n2;
+    const int seg = blockIdx.x;
+    const int g = seg / d.na, a = seg % d.na;
+    const int w = d.blk_wave[g];
+    const int64_t off = d.foff[seg];
+    const int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
+    const int n1 = d.n1, n2 = d.n2, ne = d.ne;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // same-Omega sources of V psi for this segment: potential row and psi_k row
+    __shared__ const double *s_vrow[8];
+    __shared__ const double *s_prow[8];
+    __shared__ int s_nsrc;
+    __shared__ double s_wsum[8];
+    if (threadIdx.x == 0) {
+        int et = d.blk_elec[g], ns = 0;
+        for (int q = 0; q < ne; q++) {
+            int sb = u.vsrc[g * ne + q];
+            if (sb < 0) continue;
+            int es = d.blk_elec[sb];
+            s_vrow[ns] = d.vvv + ((((size_t)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
+            s_prow[ns] = u.pk + d.foff[(size_t)sb * d.na + a];
+            ns++;
+        }
+        s_nsrc = ns;
+    }
+    __syncthreads();
+    const int nsrc = s_nsrc;
+    const double *__restrict__ Hp = u.H + off;
+    const double *__restrict__ pkp = u.pk + off;
+    const double *__restrict__ pm1 = u.pkm1 + off;
+    double *__restrict__ outp = u.out + off;
+    const int *__restrict__ i1p = d.indr1 + (size_t)a * d.npt;
+    const int *__restrict__ i2p = d.indr2 + (size_t)a * d.npt;
+    const double *__restrict__ ab1 = u.absfr1 + (size_t)w * n1;
+    const double *__restrict__ ab2 = u.absfr2 + (size_t)w * n2;
+    T *__restrict__ rect = X + (size_t)seg * n1 * n2;
+    const double emin = u.emindlt;
     double nrm = 0.0;
     double *zf = (u.nofe > 0 && !u.first) ? u.zfe[w] : nullptr;
     int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
-    for (int ir = blockIdx.y * kPointChunk + threadIdx.x; ir < n; ir += blockDim.x) {
-        int64_t i = off + ir;
-        int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
-        int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
-        double hv = u.H[i];
-        for (int q = 0; q < ne; q++) {
-            int s = u.vsrc[g * ne + q];
-            if (s < 0) continue;
-            int es = d.blk_elec[s];
-            double v = d.vvv[((((size_t)(et - 1) * ne + (es - 1)) * na) + a) * d.npt + ir];
-            hv += u.pk[d.foff[(size_t)s * na + a] + ir] * v;
+    constexpr int U = kPointChunk / 256;        // points per thread, loads issued together
+    const int ir0 = blockIdx.y * kPointChunk + threadIdx.x;
+    int r1[U], r2[U];
+    double hv[U], pk[U], p1[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+        int ir = ir0 + k * 256;
+        bool on = ir < n;
+        r1[k] = on ? i1p[ir] - 1 : 0;
+        r2[k] = on ? i2p[ir] - 1 : 0;
+        hv[k] = on ? Hp[ir] : 0.0;
+        pk[k] = on ? pkp[ir] : 0.0;
+        p1[k] = on && !u.first ? pm1[ir] : 0.0;
+    }
+    for (int q = 0; q < nsrc; q++) {
+        const double *vr = s_vrow[q], *pr = s_prow[q];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            int ir = ir0 + k * 256;
+            if (ir < n) hv[k] += pr[ir] * vr[ir];
         }
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+        int ir = ir0 + k * 256;
+        if (ir >= n) continue;
         double nv;
-        double pk = u.pk[i];
         if (u.first) {
-            nv = (hv - u.emindlt * pk) / u.delta2;
+            nv = (hv[k] - emin * pk[k]) / u.delta2;
         } else {
-            double fab = u.absfr1[(size_t)w * n1 + ir1] * u.absfr2[(size_t)w * n2 + ir2];
-            double rhn = (hv - u.emindlt * pk) / u.delta2;
-            nv = (2.0 * rhn - fab * u.pkm1[i]) * fab;
+            double fab = ab1[r1[k]] * ab2[r2[k]];
+            double rhn = (hv[k] - emin * pk[k]) / u.delta2;
+            nv = (2.0 * rhn - fab * p1[k]) * fab;
         }
-        u.out[i] = nv;
-        rect[(size_t)ir1 * n2 + ir2] = (T)nv;
+        outp[ir] = nv;
+        rect[(size_t)r1[k] * n2 + r2[k]] = (T)nv;
         nrm += nv * nv;
         if (zf) {
+            int64_t i = off + ir;
             for (int e = 0; e < u.nofe; e++) {
                 const double *ck = u.zcke + ((size_t)w * u.nofe + e) * 2;
                 double *zz = zf + ((size_t)e * wlen + (i - wst)) * 2;
@@ -416,15 +458,16 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             }
         }
     }
-    // block reduction of the norm partial in a fixed order (deterministic)
-    __shared__ double red[256];
-    red[threadIdx.x] = nrm;
+    // norm partial: fixed shuffle tree per warp, then the warps in order (deterministic)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, o);
+    if (lane == 0) s_wsum[warp] = nrm;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += s_wsum[i];
+        u.normpart[(size_t)seg * gridDim.y + blockIdx.y] = t;
     }
-    if (threadIdx.x == 0) u.normpart[(size_t)seg * gridDim.y + blockIdx.y] = red[0];
 }
 
 // V psi alone, for mw3_hphi: H(t) += sum_s V(e_s, e_t) psi(s) over same-Omega blocks
@@ -524,10 +567,10 @@ __global__ void __launch_bounds__(128) k_flux_acc(const double *__restrict__ fps
                                                   const double *__restrict__ etot, const double *__restrict__ zck,
                                                   int netot, int NF, double *__restrict__ zcr, double *__restrict__ zcdr)
 {
-    int ie = blockIdx.x * blockDim.x + threadIdx.x;
+    int ie = blockIdx.y * blockDim.x + threadIdx.x;      // flux groups on x: no 65535 limit
     if (ie >= netot) return;
     double e = etot[ie], cr = zck[2 * ie], ci = zck[2 * ie + 1];
-    int f0 = blockIdx.y * kFluxPerBlock, f1 = min(NF, f0 + kFluxPerBlock);
+    int f0 = blockIdx.x * kFluxPerBlock, f1 = min(NF, f0 + kFluxPerBlock);
     for (int f = f0; f < f1; f++) {
         if (!(e > poti[f])) continue;
         double pf = fpsi[4 * (size_t)f], dr = fpsi[4 * (size_t)f + 1], di = fpsi[4 * (size_t)f + 2];
@@ -770,7 +813,7 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g_begin * c.na * c.n1;
     int64_t nrows = (int64_t)ng * c.na * c.n1;
-    dim3 gr((c.n2 + BN - 1) / BN, (unsigned)((nrows + BM - 1) / BM));
+    dim3 gr((unsigned)((nrows + BM - 1) / BM), (c.n2 + BN - 1) / BN);
     if (sizeof(T) == 4 && tc_dst_supported(c)) {
         // mixed path: the three DST passes on the tensor cores
         launch_tc_dst(c, (const float *)c.d_X, (float *)c.d_Y, c.d_h, g_begin, g_end, 0);
@@ -782,7 +825,7 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
         LAUNCH_CHECK(c);
         // 2. DST along r, k-space scaling, DST along r
         stage_mark(c, 1);
-        dim3 gc((c.n2 + COL_W - 1) / COL_W, ng * c.na);
+        dim3 gc(ng * c.na, (c.n2 + COL_W - 1) / COL_W);
         k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, (T *)c.d_Y, (const T *)c.d_S1, c.d_S1off,
                                                                       c.d_nopr1, c.d_p2r1, c.d_p2r2, c.grid.radcutmax,
                                                                       g_begin * c.na);
@@ -798,7 +841,11 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     LAUNCH_CHECK(c);
     // 4. angular kinetic terms
     stage_mark(c, 3);
-    if (c.na > 1) {
+    if (sizeof(T) == 4 && c.use_tc_ang) {
+        // mixed path: j^2 + l^2 + Coriolis in one factorised tensor-core contraction
+        launch_tc_ang(c, (const float *)c.d_X, c.d_h, g_begin, g_end);
+        stage_mark(c, 4);
+    } else if (c.na > 1) {
         dim3 gj(c.ncj, c.n1, ng);
         k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_xj2, c.d_h,
                                                                     c.d_tj_ptr, c.d_tj, c.ncj, g_begin);
@@ -898,7 +945,7 @@ void launch_accumulators(Ctx &c, int64_t it)
         k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx,
                                                                      c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi);
         LAUNCH_CHECK(c);
-        dim3 g((c.netot + 127) / 128, (c.NF + kFluxPerBlock - 1) / kFluxPerBlock);
+        dim3 g((c.NF + kFluxPerBlock - 1) / kFluxPerBlock, (c.netot + 127) / 128);
         k_flux_acc<<<g, 128, 0, c.stream>>>(c.d_fpsi, c.d_fl_poti, c.d_etot, c.d_zck, c.netot, c.NF, c.d_zcr,
                                             c.d_zcdr);
         LAUNCH_CHECK(c);
@@ -984,10 +1031,10 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     LAUNCH_CHECK(c);
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g0 * na * n1, nrows = (int64_t)ng * na * n1;
-    dim3 gr((n2 + BN - 1) / BN, (unsigned)((nrows + BM - 1) / BM));
+    dim3 gr((unsigned)((nrows + BM - 1) / BM), (n2 + BN - 1) / BN);
     k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, X, (const T *)c.d_S2, Y, nullptr, c.d_nopr1, row0, nrows);
     LAUNCH_CHECK(c);
-    dim3 gc((n2 + COL_W - 1) / COL_W, ng * na);
+    dim3 gc(ng * na, (n2 + COL_W - 1) / COL_W);
     k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, Y, (const T *)c.d_S1, c.d_S1off, c.d_nopr1,
                                                                   c.d_p2r1, c.d_p2r2, c.grid.radcutmax, g0 * na);
     LAUNCH_CHECK(c);
@@ -995,7 +1042,9 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     LAUNCH_CHECK(c);
     k_quirk<<<ng * na, 128, 0, c.stream>>>(d, P, H, c.d_quirk_ptr, c.d_quirk, g0 * na);
     LAUNCH_CHECK(c);
-    if (na > 1) {
+    if (sizeof(T) == 4 && c.use_tc_ang) {
+        launch_tc_ang(c, (const float *)X, H, g0, g1);
+    } else if (na > 1) {
         dim3 gj(c.ncj, n1, ng);
         k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, X, (const T *)c.d_xj2, H, c.d_tj_ptr, c.d_tj,
                                                                     c.ncj, g0);

@@ -24,7 +24,7 @@ import numpy as np
 
 from . import constants as C
 from . import namelist
-from .wigner import dwigner, gauleg
+from .wigner import dwigner, dwigner_vec, gauleg
 
 
 def _get(d, key, default):
@@ -341,12 +341,13 @@ def angular_functions(run):
             if i.nangu == 1:
                 D[iom, ielec, jprin:lmax + 1, 0] = 1.0
                 continue
-            for iang in range(i.nangu):
-                gamma = math.acos(run._cgamprod[iang])
-                pm = dwigner(jmax2, m2, mp2, gamma)
-                for j in range(jprin, lmax + 1):
-                    xn = math.sqrt((2.0 * j + 1.0) * 0.5)
-                    D[iom, ielec, j, iang] = pm[2 * j] * xn * math.sqrt(run.wreal[iang])
+            if iom > i.iommax + 1:
+                continue          # only Omega <= iommax (+1 for the coupling bounds) is ever read
+            gam = np.arccos(run._cgamprod[: i.nangu])
+            pm = dwigner_vec(jmax2, m2, mp2, gam)
+            for j in range(jprin, lmax + 1):
+                xn = math.sqrt((2.0 * j + 1.0) * 0.5)
+                D[iom, ielec, j, :] = pm[:, 2 * j] * xn * np.sqrt(run.wreal[: i.nangu])
     run.djmmp = D
 
 
@@ -478,14 +479,43 @@ def set_colini(run):
             else:
                 angpart = ((-1.0) ** iom) * run.djmmp[iom, ielec - 1, jref, iang - 1] if iom <= jref else 0.0
             o = run.offs[iang - 1, b]
-            for ir in range(n):
-                ir1 = run.indr1[iang - 1, ir]
-                ir2 = run.indr2[iang - 1, ir]
-                rg = i.rmis2 + (ir2 - 1) * run.ah2
-                fdi = 1.0 if i.npun1 == 1 else run.fd[i.ielecref - 1, jref - i.jini, i.nvref - i.nvini, ir1 - 1]
-                xr2 = rgauscolini(rg, run.rcolini, run.alpha0, run.xk0, run.factor0)
-                psi[o + ir] = -xr2 * angpart * 1.0 * fdi * math.sqrt(run.ah2)
+            ir1 = run.indr1[iang - 1, :n]
+            ir2 = run.indr2[iang - 1, :n]
+            rg = i.rmis2 + (ir2 - 1) * run.ah2
+            fdi = np.ones(n) if i.npun1 == 1 else run.fd[i.ielecref - 1, jref - i.jini, i.nvref - i.nvini, ir1 - 1]
+            g = np.cos((rg - run.rcolini) * run.xk0) * math.sqrt(2.0)
+            xr2 = g * run.factor0 * np.exp(-(rg - run.rcolini) * (rg - run.rcolini) / run.alpha0 / run.alpha0)
+            psi[o:o + n] = -xr2 * angpart * 1.0 * fdi * math.sqrt(run.ah2)
     run.psi0 = psi
+
+
+def load_sweep(inputfile, Js, overrides):
+    """Partial waves that share one grid, potential and diatomic functions:
+    the files are read once; ``overrides(J)`` gives the per-J namelist values
+    (Jtot, iparity, iommin, iommax, iomref)."""
+    import copy
+    base = load(inputfile)
+    runs = []
+    for J in Js:
+        inp = copy.copy(base.inp)
+        for k, v in overrides(J).items():
+            setattr(inp, k, v)
+        r = copy.copy(base)
+        r.inp = inp
+        basis(r)
+        angular_functions(r)
+        # flat layout depends on the number of blocks
+        r.offs = np.zeros((inp.nangu, r.ncan), np.int64)
+        cnt = 0
+        for iang in r.angle_order():
+            for b in range(r.ncan):
+                r.offs[iang - 1, b] = cnt
+                cnt += int(r.npunreal[iang - 1])
+        r.ntot = cnt
+        if inp.iphoto == 0:
+            set_colini(r)
+        runs.append(r)
+    return runs
 
 
 def load(inputfile, potdir=None, funcdir=None, inputs=None):

@@ -125,3 +125,65 @@ def dwigner(jmax2, m2, mp2, beta, ndim=None):
             facjm = math.sqrt(fac1jm * fac2jm) / facden
             dj[indp] = factot * (facj * dj[ind] - facjm * dj[indm])
     return dj
+
+
+def dwigner_vec(jmax2, m2, mp2, beta):
+    """dwigner for an array of angles at once: returns [len(beta), jmax2+1]."""
+    beta = np.asarray(beta, dtype=np.float64)
+    nb = beta.shape[0]
+    dj = np.zeros((nb, jmax2 + 1))
+    jmin2 = max(abs(m2), abs(mp2))
+    y = np.cos(beta)
+    if jmin2 == 0:
+        dj[:, 0] = 1.0
+        if jmax2 >= 2:
+            dj[:, 2] = y
+        for ind in range(4, jmax2 + 1, 2):
+            xj = ind * 0.5
+            dj[:, ind] = (y * (2.0 * xj - 1.0) * dj[:, ind - 2] - (xj - 1.0) * dj[:, ind - 4]) / xj
+        return dj
+    facnum = sum(math.log(float(i)) for i in range(1, jmin2 + 1))
+    mreal2 = mp2 if jmin2 == abs(m2) else m2
+    facden1 = sum(math.log(i * 0.5) for i in range(2, jmin2 + mreal2 + 1, 2)) if jmin2 + mreal2 > 0 else 0.0
+    facden2 = sum(math.log(i * 0.5) for i in range(2, jmin2 - mreal2 + 1, 2)) if jmin2 - mreal2 > 0 else 0.0
+    fact = math.exp(0.5 * (facnum - facden1 - facden2))
+    sign = 1.0
+    xsin = np.sin(beta * 0.5)
+    xcos = np.cos(beta * 0.5)
+    if jmin2 == abs(m2):
+        if jmin2 == m2:
+            if (jmin2 - mp2) % 2 != 0:
+                raise ValueError("dwigner: complex phase")
+            sign = float((-1) ** int((jmin2 - mp2) * 0.5 + 0.5))
+            a = xsin ** ((jmin2 - mp2) * 0.5)
+            b = xcos ** ((jmin2 + mp2) * 0.5)
+        else:
+            a = xsin ** ((jmin2 + mp2) * 0.5)
+            b = xcos ** ((jmin2 - mp2) * 0.5)
+    else:
+        if jmin2 == mp2:
+            a = xsin ** ((jmin2 - m2) * 0.5)
+            b = xcos ** ((jmin2 + m2) * 0.5)
+        else:
+            if (jmin2 + m2) % 2 != 0:
+                raise ValueError("dwigner: complex phase")
+            sign = float((-1) ** int((jmin2 + m2) * 0.5 + 0.5))
+            a = xsin ** ((jmin2 + m2) * 0.5)
+            b = xcos ** ((jmin2 - m2) * 0.5)
+    dj[:, jmin2] = fact * sign * a * b
+    xj = jmin2 * 0.5
+    xm = m2 * 0.5
+    xmp = mp2 * 0.5
+    xjp = xj + 1.0
+    factot = xjp * (2.0 * xj + 1.0) / math.sqrt((xjp * xjp - xm * xm) * (xjp * xjp - xmp * xmp))
+    facj = y - xm * xmp / (xj * (xj + 1.0))
+    if jmin2 + 2 <= jmax2:
+        dj[:, jmin2 + 2] = factot * facj * dj[:, jmin2]
+        for indp in range(jmin2 + 4, jmax2 + 1, 2):
+            xjp = indp * 0.5
+            xj = xjp - 1.0
+            factot = xjp * (2.0 * xj + 1.0) / math.sqrt((xjp * xjp - xm * xm) * (xjp * xjp - xmp * xmp))
+            facj = y - xm * xmp / (xj * (xj + 1.0))
+            facjm = math.sqrt((xj * xj - xm * xm) * (xj * xj - xmp * xmp)) / (xj * (2.0 * xj + 1.0))
+            dj[:, indp] = factot * (facj * dj[:, indp - 2] - facjm * dj[:, indp - 4])
+    return dj

@@ -65,10 +65,13 @@ class Wave(ct.Structure):
 HEADER_FUNCS = [
     "mw3_create", "mw3_add_wave", "mw3_wave_size", "mw3_hphi", "mw3_start", "mw3_upload_state",
     "mw3_run", "mw3_sync", "mw3_download_state", "mw3_norms", "mw3_totalflux", "mw3_flux_count",
-    "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_get_stream", "mw3_profile",
+    "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_path_flags", "mw3_get_stream",
+    "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_last_error", "mw3_destroy",
 ]
-STAGES = ["dst_R", "dst_r_pair", "dst_R_gather", "ang_j2", "ang_l2", "update", "accumulators"]
+# stage 3 is the whole angular part when the mixed path runs it as one fused
+# tensor-core contraction (stage 4 is then empty); the explicit form splits j^2 and l^2
+STAGES = ["dst_R", "dst_r_pair", "dst_R_gather", "angular", "angular_l2", "update", "accumulators"]
 
 _lib = None
 
@@ -106,6 +109,7 @@ def load_library(build_if_missing=True):
     L.mw3_download_accumulators.argtypes = [vp, ct.c_int32, F64P, F64P, F64P, F64P, F64P]
     L.mw3_tables.argtypes = [vp, ct.c_int32, I32P, F64P, F64P, F64P, F64P, F64P]
     L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
+    L.mw3_path_flags.argtypes = [vp, ct.POINTER(ct.c_int32)]
     L.mw3_get_stream.argtypes = [vp, ct.POINTER(ct.c_void_p)]
     L.mw3_profile.argtypes = [vp, ct.c_int]
     L.mw3_stage_times.argtypes = [vp, F64P, ct.POINTER(ct.c_int64)]
@@ -299,6 +303,12 @@ class Propagator:
         n = ct.c_int64()
         self._check(self.L.mw3_kernel_launches(self.h, ct.byref(n)), "mw3_kernel_launches")
         return n.value
+
+    def path(self):
+        """Kernels in use: {"tc_dst": bool, "tc_angular": bool} (after start)."""
+        f = ct.c_int32()
+        self._check(self.L.mw3_path_flags(self.h, ct.byref(f)), "mw3_path_flags")
+        return {"tc_dst": bool(f.value & 1), "tc_angular": bool(f.value & 2)}
 
     def stream(self):
         """cudaStream_t of the context, as an integer handle."""

@@ -1,5 +1,6 @@
-"""tcgen05 tensor-core tile (3xTF32 split, FP32 accumulation in tensor memory)
-against an FP64 product, through the library's self-test hook."""
+"""tcgen05 tensor-core kernels of the mixed path: the 3xTF32 GEMM tile against
+an FP64 product (through the library's self-test hook), and the factorised
+angular contraction against the FP64 path and against separate runs."""
 import ctypes as ct
 
 import numpy as np
@@ -28,3 +29,43 @@ def test_tc_gemm_tile(M, N, K, bn):
     ref = A.astype(np.float64) @ Bt.astype(np.float64).T
     err = np.abs(C - ref).max() / np.abs(ref).max()
     assert err < 5e-6, err          # FP32 accumulation over K <= 256
+
+
+@pytest.mark.parametrize("case", ["tiny_j0", "tiny_j3", "tiny_e2"])
+def test_fused_angular_runs_and_matches_fp64(runs, case):
+    """The mixed path takes the tensor-core DSTs and the factorised tensor-core
+    angular contraction, and its H psi agrees with FP64."""
+    from madwave3_gb300 import Propagator
+
+    run = runs[case]
+    pmx = Propagator(run, "mixed")
+    p64 = Propagator(run, "fp64")
+    pmx.start()
+    p64.start()
+    assert pmx.path() == {"tc_dst": True, "tc_angular": True}
+    assert p64.path() == {"tc_dst": False, "tc_angular": False}
+    rng = np.random.default_rng(7)
+    psi = rng.uniform(-1.0, 1.0, run.ntot)
+    a, b = pmx.hphi(psi), p64.hphi(psi)
+    assert np.abs(a - b).max() / np.abs(b).max() < 1e-6
+    pmx.close()
+    p64.close()
+
+
+def test_batched_waves_mixed(runs):
+    """Waves with different block chains in one mixed context reproduce their
+    separate mixed runs (every tile and chain is computed the same way)."""
+    from madwave3_gb300 import Propagator
+
+    r0, r3 = runs["tiny_j0"], runs["tiny_j3"]
+    both = Propagator([r0, r3], "mixed")
+    both.start()
+    both.run(60)
+    for w, r in enumerate((r0, r3)):
+        one = Propagator(r, "mixed")
+        one.start()
+        one.run(60)
+        x, y = both.state(w)[1], one.state()[1]
+        assert np.abs(x - y).max() / np.abs(y).max() < 1e-12
+        one.close()
+    both.close()

@@ -21,7 +21,7 @@ def _rel(a, b):
 
 
 # tolerances as in the parity tests: FP64 1e-12; mixed 1e-6 (FP32 transforms, and
-# mw3_hphi may take its radial DSTs on the tensor cores where this entry point does not)
+# mw3_hphi takes its radial DSTs on the tensor cores where this entry point does not)
 @pytest.mark.parametrize("case,precision,tol", [("tiny_j3", "fp64", 1e-12), ("tiny_e2", "mixed", 1e-6)])
 def test_hphi_noalloc_matches_hphi(runs, case, precision, tol):
     torch = pytest.importorskip("torch")
