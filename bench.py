@@ -34,6 +34,8 @@ L2_BYTES = 129 * 1024 * 1024
 WORKLOADS = {
     # partial-wave sweep J=0..40, Omega=0..min(J,6): 266 blocks on 256 R x 128 r x 60 angles
     "jsweep0-40_256x128x60": dict(case="j0_256x128x60", sweep=list(range(0, 41))),
+    # the first five partial waves of that sweep (15 blocks): a profiling-sized case
+    "jsweep0-4_256x128x60": dict(case="j0_256x128x60", sweep=list(range(0, 5))),
     # J=0, one Omega block, one state: 256 R x 128 r x 60 angles (synthetic LEPS)
     "j0_256x128x60": dict(case="j0_256x128x60", sweep=None),
     # J=0 at 512 R x 256 r x 120 angles

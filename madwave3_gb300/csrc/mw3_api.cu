@@ -376,6 +376,13 @@ int build_device(Ctx &c)
         TRY(dalloc(c, &c.d_fpsi, (size_t)std::max<int64_t>(nf, 1) * 4));
         TRY(dalloc(c, &c.d_zcr, (size_t)std::max<int64_t>(nf, 1) * c.netot * 2));
         TRY(dalloc(c, &c.d_zcdr, (size_t)std::max<int64_t>(nf, 1) * c.netot * 2));
+        c.d_fring = nullptr;
+        c.d_cring = nullptr;
+        c.fring_n = 0;
+        if (!c.fp64 && nf > 0) {
+            TRY(dalloc(c, &c.d_fring, (size_t)mw3::kFluxRing * nf * 3, false));
+            TRY(dalloc(c, &c.d_cring, (size_t)mw3::kFluxRing * c.netot * 2, false));
+        }
         TRY(dalloc(c, &c.d_xj, (size_t)G * n1 * c.nj));
         TRY(dalloc(c, &c.d_cvj, (size_t)G * c.nj * c.nv));
         TRY(dalloc(c, &c.d_zs2, (size_t)G * c.nj * c.nv * c.netot * 2));
@@ -523,6 +530,7 @@ int check_device_flags(Ctx &c, const char *where)
 int reset_accumulators(Ctx &c)
 {
     size_t nf = (size_t)std::max(c.NF, 1) * c.netot * 2;
+    c.fring_n = 0;
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcr, 0, sizeof(double) * nf, c.stream));
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcdr, 0, sizeof(double) * nf, c.stream));
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zs2, 0, sizeof(double) * 2 * (size_t)c.G * c.nj * c.nv * c.netot, c.stream));
@@ -795,6 +803,7 @@ int mw3_totalflux(mw3_ctx *h, int32_t w, double *tot, double *elec)
     if (w < 0 || w >= (int)c.waves.size() || !c.built) return MW3_ERR_STATE;
     WaveTables &t = c.waves[w];
     double *d = nullptr;
+    mw3::flush_flux(c);
     MW3_CUDA_TRY(cudaMallocAsync(&d, sizeof(double) * (size_t)t.netot * (1 + c.ne), c.stream));
     mw3::launch_totalflux(c, w, d, d + t.netot);
     MW3_CUDA_TRY(cudaMemcpyAsync(tot, d, sizeof(double) * t.netot, cudaMemcpyDeviceToHost, c.stream));
@@ -823,6 +832,7 @@ int mw3_download_accumulators(mw3_ctx *h, int32_t w, double *zcr, double *zcdr, 
     WaveDev &d = c.wdev[w];
     size_t nf = (size_t)t.nflux * t.netot * 2;
     size_t ns = (size_t)t.ncan * t.nj * t.nv;
+    mw3::flush_flux(c);
     if (zcr && nf) MW3_CUDA_TRY(cudaMemcpyAsync(zcr, d.zcr, sizeof(double) * nf, cudaMemcpyDeviceToHost, c.stream));
     if (zcdr && nf)
         MW3_CUDA_TRY(cudaMemcpyAsync(zcdr, d.zcdr, sizeof(double) * nf, cudaMemcpyDeviceToHost, c.stream));

@@ -170,6 +170,11 @@ struct Ctx {
     int *d_fl_dptr = nullptr, *d_fl_dir1 = nullptr;
     double *d_fl_poti = nullptr, *d_zar = nullptr, *d_etot = nullptr, *d_zck = nullptr;
     double *d_fpsi = nullptr;        // [NF][4]: psi, dpsi (re, im)
+    // mixed path: the last iterations' flux samples and C_k(E), FP32, flushed
+    // into zCR/zCdR every kFluxRing iterations and before every read
+    float *d_fring = nullptr;        // [kFluxRing][NF][3]
+    float *d_cring = nullptr;        // [kFluxRing][netot][2]
+    int fring_n = 0;                 // slots filled since the last flush
     double *d_zcr = nullptr, *d_zcdr = nullptr;          // [NF][netot][2]
     double *d_xj = nullptr;          // [G][n1][nj] angular projection at ir2abs
     double *d_cvj = nullptr;         // [G][nj][nv]
@@ -247,6 +252,9 @@ void launch_update(Ctx &c, int first);
 template <typename T>
 void launch_build_kinetic(Ctx &c);
 void launch_accumulators(Ctx &c, int64_t it);
+// mixed path: add the pending ring slots to the FP64 flux accumulators
+void flush_flux(Ctx &c);
+constexpr int kFluxRing = 32;
 void launch_norms(Ctx &c, int64_t slot);
 void launch_addv(Ctx &c, const double *psi, int g0, int g1);
 void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec);

@@ -361,6 +361,7 @@ struct UpdArgs {
     const int *vsrc;               // [G][ne]
     const double *absfr1, *absfr2; // [W][n1], [W][n2]
     double emindlt, delta2;
+    double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
     int first;
     double *normpart;              // [G*na]
     int nofe;                      // max over waves; 0 = funE off
@@ -368,6 +369,24 @@ struct UpdArgs {
     double *const *zfe;            // per wave [nofe][ntot_w][2] (null when the wave has none)
     const int64_t *wflat0;         // [W+1]
 };
+
+// double -> float, round to nearest even, with integer instructions only (the
+// F2F conversion issues on the FP64 pipe); magnitudes below FLT_MIN go to a
+// signed zero, above FLT_MAX to infinity
+__device__ __forceinline__ float f64_to_f32_int(double x)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    unsigned int m = (unsigned int)((b >> 29) & 0x7FFFFFu);
+    unsigned int rest = (unsigned int)(b & 0x1FFFFFFFu);
+    unsigned int r = ((unsigned int)e << 23) | m;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) r += 1u;   // carry may round into the exponent
+    if (r >= 0x7F800000u) r = 0x7F800000u;
+    return __uint_as_float(sign | r);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
@@ -433,21 +452,45 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             if (ir < n) hv[k] += pr[ir] * vr[ir];
         }
     }
+    float nrmf = 0.f;
 #pragma unroll
     for (int k = 0; k < U; k++) {
         int ir = ir0 + k * 256;
         if (ir >= n) continue;
         double nv;
-        if (u.first) {
-            nv = (hv[k] - emin * pk[k]) / u.delta2;
+        if (sizeof(T) == 8) {
+            // FP64 path: the reference's operations in its order
+            if (u.first) {
+                nv = (hv[k] - emin * pk[k]) / u.delta2;
+            } else {
+                double fab = ab1[r1[k]] * ab2[r2[k]];
+                double rhn = (hv[k] - emin * pk[k]) / u.delta2;
+                nv = (2.0 * rhn - fab * p1[k]) * fab;
+            }
+            rect[(size_t)r1[k] * n2 + r2[k]] = (T)nv;
+            nrm += nv * nv;
         } else {
-            double fab = ab1[r1[k]] * ab2[r2[k]];
-            double rhn = (hv[k] - emin * pk[k]) / u.delta2;
-            nv = (2.0 * rhn - fab * p1[k]) * fab;
+            // mixed path, few FP64 instructions (GB300 runs FP64 at 1/64 of FP32):
+            // reciprocal multiplies, damping only inside the absorbers, the FP32
+            // copy rounded with integer operations, the norm partial in FP32
+            if (u.first) {
+                nv = (hv[k] - emin * pk[k]) * u.rdelta;
+            } else {
+                double a1 = ab1[r1[k]], a2 = ab2[r2[k]];
+                double rhn2 = (hv[k] - emin * pk[k]) * u.r2delta;
+                if (__double_as_longlong(a1) == 0x3FF0000000000000LL &&
+                    __double_as_longlong(a2) == 0x3FF0000000000000LL) {
+                    nv = rhn2 - p1[k];
+                } else {
+                    double fab = a1 * a2;
+                    nv = (rhn2 - fab * p1[k]) * fab;
+                }
+            }
+            float nf = f64_to_f32_int(nv);
+            rect[(size_t)r1[k] * n2 + r2[k]] = (T)nf;
+            nrmf = fmaf(nf, nf, nrmf);
         }
         outp[ir] = nv;
-        rect[(size_t)r1[k] * n2 + r2[k]] = (T)nv;
-        nrm += nv * nv;
         if (zf) {
             int64_t i = off + ir;
             for (int e = 0; e < u.nofe; e++) {
@@ -458,6 +501,7 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             }
         }
     }
+    if (sizeof(T) == 4) nrm = (double)nrmf;
     // norm partial: fixed shuffle tree per warp, then the warps in order (deterministic)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, o);
@@ -516,7 +560,7 @@ __global__ void k_norms(const double *__restrict__ part, const int *__restrict__
 // ---------------------------------------------------------------------------
 // CoefEcheby (main_madwave3.f:462-490): C_k(E) = d hbar/Delta e^{-ik acos Es}/sqrt(1-Es^2)
 __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double emindlt, double delta2,
-                             double hbr, int64_t k, double *__restrict__ zck)
+                             double hbr, int64_t k, double *__restrict__ zck, float *__restrict__ cring)
 {
     int ie = blockIdx.x * blockDim.x + threadIdx.x;
     if (ie >= netot) return;
@@ -529,6 +573,10 @@ __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double 
     sincos(expo, &s, &c);
     zck[2 * ie] = zf * c / deno;
     zck[2 * ie + 1] = zf * s / deno;
+    if (cring) {                    // mixed path: this iteration's slot of the flux ring
+        cring[2 * ie] = (float)(zf * c / deno);
+        cring[2 * ie + 1] = (float)(zf * s / deno);
+    }
 }
 
 // totalflux_k (mod_flux_01y2.f:585-660), first half: psi and d psi/d r1 at every
@@ -537,7 +585,7 @@ __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double 
 __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ psi, const int64_t *__restrict__ fidx,
                                                     const int *__restrict__ dptr, const int64_t *__restrict__ didx,
                                                     const int *__restrict__ dir1, const double *__restrict__ zar,
-                                                    int NF, double *__restrict__ fpsi)
+                                                    int NF, double *__restrict__ fpsi, float *__restrict__ fring)
 {
     int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -555,9 +603,16 @@ __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ p
         si += __shfl_xor_sync(0xffffffffu, si, o);
     }
     if (lane == 0) {
-        fpsi[4 * (size_t)f] = psi[fidx[f]];
-        fpsi[4 * (size_t)f + 1] = sr;
-        fpsi[4 * (size_t)f + 2] = si;
+        double p0 = psi[fidx[f]];
+        if (fring) {                // mixed path: ring slot [f][3] in FP32
+            fring[3 * (size_t)f] = (float)p0;
+            fring[3 * (size_t)f + 1] = (float)sr;
+            fring[3 * (size_t)f + 2] = (float)si;
+        } else {
+            fpsi[4 * (size_t)f] = p0;
+            fpsi[4 * (size_t)f + 1] = sr;
+            fpsi[4 * (size_t)f + 2] = si;
+        }
     }
 }
 
@@ -583,6 +638,83 @@ __global__ void __launch_bounds__(128) k_flux_acc(const double *__restrict__ fps
         b.y += cr * di + ci * dr;
         *reinterpret_cast<double2 *>(zcr + o) = a;
         *reinterpret_cast<double2 *>(zcdr + o) = b;
+    }
+}
+
+// Mixed path: the flux accumulation of up to kFluxRing iterations at once.
+// zCR(E,f) += sum_s C_s(E) psi_s(f) and zCdR(E,f) += sum_s C_s(E) dpsi_s(f) for
+// E > V(f): the products and the sum over the ring slots in FP32 (a 64 x 64
+// (E, f) tile per CTA, 4 x 4 per thread), added once to the FP64 accumulators,
+// so each accumulator is read and written once per flush instead of once per
+// iteration.
+constexpr int kFlushE = 64, kFlushF = 64;
+__global__ void __launch_bounds__(256) k_flux_flush(const float *__restrict__ fring, const float *__restrict__ cring,
+                                                    int nslots, const double *__restrict__ poti,
+                                                    const double *__restrict__ etot, int netot, int NF,
+                                                    double *__restrict__ zcr, double *__restrict__ zcdr)
+{
+    __shared__ float sc[kFluxRing][kFlushE][2];
+    __shared__ float sp[kFluxRing][kFlushF][3];
+    const int f0 = blockIdx.x * kFlushF, e0 = blockIdx.y * kFlushE;
+    for (int i = threadIdx.x; i < nslots * kFlushE * 2; i += blockDim.x) {
+        int s = i / (kFlushE * 2), r = i % (kFlushE * 2);
+        int e = e0 + r / 2;
+        sc[s][r / 2][r & 1] = e < netot ? cring[((size_t)s * netot + e) * 2 + (r & 1)] : 0.f;
+    }
+    for (int i = threadIdx.x; i < nslots * kFlushF * 3; i += blockDim.x) {
+        int s = i / (kFlushF * 3), r = i % (kFlushF * 3);
+        int f = f0 + r / 3;
+        sp[s][r / 3][r % 3] = f < NF ? fring[((size_t)s * NF + f) * 3 + r % 3] : 0.f;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // E = e0 + tx + 16 i, f = f0 + ty + 16 j
+    float ar[4][4], ai[4][4], br[4][4], bi[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) ar[i][j] = ai[i][j] = br[i][j] = bi[i][j] = 0.f;
+    for (int s = 0; s < nslots; s++) {
+        float cr[4], ci[4], p[4], dr[4], di[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            cr[i] = sc[s][tx + 16 * i][0];
+            ci[i] = sc[s][tx + 16 * i][1];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            p[j] = sp[s][ty + 16 * j][0];
+            dr[j] = sp[s][ty + 16 * j][1];
+            di[j] = sp[s][ty + 16 * j][2];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                ar[i][j] = fmaf(cr[i], p[j], ar[i][j]);
+                ai[i][j] = fmaf(ci[i], p[j], ai[i][j]);
+                br[i][j] = fmaf(cr[i], dr[j], fmaf(-ci[i], di[j], br[i][j]));
+                bi[i][j] = fmaf(cr[i], di[j], fmaf(ci[i], dr[j], bi[i][j]));
+            }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        int f = f0 + ty + 16 * j;
+        if (f >= NF) continue;
+        double v = poti[f];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            int e = e0 + tx + 16 * i;
+            if (e >= netot || !(etot[e] > v)) continue;
+            size_t o = ((size_t)f * netot + e) * 2;
+            double2 a = *reinterpret_cast<double2 *>(zcr + o);
+            double2 b = *reinterpret_cast<double2 *>(zcdr + o);
+            a.x += (double)ar[i][j];
+            a.y += (double)ai[i][j];
+            b.x += (double)br[i][j];
+            b.y += (double)bi[i][j];
+            *reinterpret_cast<double2 *>(zcr + o) = a;
+            *reinterpret_cast<double2 *>(zcdr + o) = b;
+        }
     }
 }
 
@@ -871,6 +1003,8 @@ void launch_update(Ctx &c, int first)
     u.absfr2 = c.d_absfr2;
     u.emindlt = c.grid.emindlt;
     u.delta2 = c.grid.delta2;
+    u.rdelta = 1.0 / c.grid.delta2;
+    u.r2delta = 2.0 / c.grid.delta2;
     u.first = first;
     u.normpart = c.d_normpart;
     u.nofe = c.nofemax;
@@ -928,27 +1062,34 @@ void launch_accumulators(Ctx &c, int64_t it)
 {
     stage_mark(c, 6);
     DevGrid d = devgrid(c);
-    k_coefecheby<<<(c.netot + 127) / 128, 128, 0, c.stream>>>(c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2,
-                                                              c.grid.hbr, it, c.d_zck);
+    const bool ring = c.d_fring != nullptr;
+    k_coefecheby<<<(c.netot + 127) / 128, 128, 0, c.stream>>>(
+        c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2, c.grid.hbr, it, c.d_zck,
+        ring ? c.d_cring + (size_t)c.fring_n * c.netot * 2 : nullptr);
     LAUNCH_CHECK(c);
     for (size_t w = 0; w < c.waves.size(); w++) {
         WaveTables &t = c.waves[w];
         if (t.nofe > 0) {
             k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(c.wdev[w].efe, t.nofe, c.grid.emindlt,
                                                                      c.grid.delta2, c.grid.hbr, it,
-                                                                     c.d_zcke + (size_t)w * c.nofemax * 2);
+                                                                     c.d_zcke + (size_t)w * c.nofemax * 2, nullptr);
             LAUNCH_CHECK(c);
         }
     }
     bool gate = c.gate_elastic && it < c.kminelastic;
     if (c.NF > 0 && !(gate && c.waves[0].iprod == 1)) {
-        k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx,
-                                                                     c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi);
+        k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(
+            c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx, c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi,
+            ring ? c.d_fring + (size_t)c.fring_n * c.NF * 3 : nullptr);
         LAUNCH_CHECK(c);
-        dim3 g((c.NF + kFluxPerBlock - 1) / kFluxPerBlock, (c.netot + 127) / 128);
-        k_flux_acc<<<g, 128, 0, c.stream>>>(c.d_fpsi, c.d_fl_poti, c.d_etot, c.d_zck, c.netot, c.NF, c.d_zcr,
-                                            c.d_zcdr);
-        LAUNCH_CHECK(c);
+        if (ring) {
+            if (++c.fring_n == kFluxRing) flush_flux(c);
+        } else {
+            dim3 g((c.NF + kFluxPerBlock - 1) / kFluxPerBlock, (c.netot + 127) / 128);
+            k_flux_acc<<<g, 128, 0, c.stream>>>(c.d_fpsi, c.d_fl_poti, c.d_etot, c.d_zck, c.netot, c.NF, c.d_zcr,
+                                                c.d_zcdr);
+            LAUNCH_CHECK(c);
+        }
     }
     if (c.n2 > 1) {
         CvjArgs a;
@@ -979,6 +1120,16 @@ void launch_accumulators(Ctx &c, int64_t it)
         k_cvj_acc<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
     }
+}
+
+void flush_flux(Ctx &c)
+{
+    if (!c.d_fring || c.fring_n == 0) return;
+    dim3 g((c.NF + kFlushF - 1) / kFlushF, (c.netot + kFlushE - 1) / kFlushE);
+    k_flux_flush<<<g, 256, 0, c.stream>>>(c.d_fring, c.d_cring, c.fring_n, c.d_fl_poti, c.d_etot, c.netot, c.NF,
+                                          c.d_zcr, c.d_zcdr);
+    LAUNCH_CHECK(c);
+    c.fring_n = 0;
 }
 
 void launch_addv(Ctx &c, const double *psi, int g0, int g1)
