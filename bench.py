@@ -151,8 +151,11 @@ def stage_model(runs, prop, stages=None):
         nsto += r.ntot
     ne = r0.nelec
     fused = bool(stages) and stages.get("angular_l2", 0.0) < 0.01 * max(stages.get("angular", 0.0), 1e-30)
+    kin = prop.path()
     return {
-        "dst_R": ("flop", 2.0 * rows * n2 * n2),
+        # the fused radial kernel does all four DST products in stage 0
+        "dst_R": ("flop", 4.0 * rows * n2 * n2 + 4.0 * rows_sq * n2) if kin["tc_dst_fused"]
+        else ("flop", 2.0 * rows * n2 * n2),
         "dst_r_pair": ("flop", 4.0 * rows_sq * n2),
         "dst_R_gather": ("flop", 2.0 * rows * n2 * n2),
         "angular": (("byte", 20.0 * nsto) if fused else ("flop", 2.0 * na * nsto)),

@@ -154,11 +154,13 @@ int mw3_kernel_launches(mw3_ctx *ctx, int64_t *count);
 
 /* Which kernels the context runs, valid once its device tables exist (after
  * mw3_start, mw3_upload_state or mw3_hphi): MW3_PATH_TC_DST when the radial
- * DSTs run on the tensor cores, MW3_PATH_TC_ANG when the angular terms run as
- * the factorised tensor-core contraction (both mixed precision only).  No
+ * DSTs run on the tensor cores (with MW3_PATH_TC_DST_FUSED when as one fused
+ * kernel), MW3_PATH_TC_ANG when the angular terms run as the factorised
+ * tensor-core contraction (all mixed precision only).  No
  * reference counterpart: the reference has a single code path. */
 #define MW3_PATH_TC_DST 1
 #define MW3_PATH_TC_ANG 2
+#define MW3_PATH_TC_DST_FUSED 4   /* the whole radial DST chain in one kernel per (block, angle) */
 int mw3_path_flags(mw3_ctx *ctx, int32_t *flags);
 
 /* The CUDA stream (cudaStream_t) all device work of the context runs on, for
@@ -169,7 +171,7 @@ int mw3_get_stream(mw3_ctx *ctx, void **stream);
  * stage of every iteration.  mw3_stage_times waits for the stream and returns
  * the accumulated milliseconds of MW3_NSTAGES stages and the number of
  * iterations recorded, then clears the record. */
-#define MW3_NSTAGES 7   /* R-DST, r-DST pair, R-DST+gather, angular (j^2, or j^2+l^2 fused), l^2, update, accumulators */
+#define MW3_NSTAGES 7   /* R-DST (or the fused DST chain), r-DST pair, R-DST+gather, angular (j^2, or j^2+l^2 fused), l^2, update, accumulators */
 int mw3_profile(mw3_ctx *ctx, int enable);
 int mw3_stage_times(mw3_ctx *ctx, double *ms, int64_t *iterations);
 

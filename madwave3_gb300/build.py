@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmw3gpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["mw3_api.cu", "mw3_kernels.cu", "mw3_setup.cu", "mw3_tc.cu", "mw3_tc_ang.cu"]
+SOURCES = ["mw3_api.cu", "mw3_kernels.cu", "mw3_setup.cu", "mw3_tc.cu", "mw3_tc_ang.cu", "mw3_tc_dst2d.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code without FMA contraction: the reference's x86-64 build never contracts,
 # and set-up tables (absorber start, flux line) must not depend on the host CPU

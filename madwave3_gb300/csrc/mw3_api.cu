@@ -74,6 +74,9 @@ void free_device(Ctx &c)
         if (rc_) return rc_;   \
     } while (0)
 
+}  // namespace
+
+namespace mw3 {
 // DST-I matrix of length n, the unnormalised RODFT00 of FFTW: S[i][k] = 2 sin(pi (i+1)(k+1)/(n+1))
 std::vector<double> dst_matrix(int n)
 {
@@ -86,6 +89,10 @@ std::vector<double> dst_matrix(int n)
         }
     return s;
 }
+}  // namespace mw3
+
+namespace {
+using mw3::dst_matrix;
 
 template <typename T>
 std::vector<T> cast(const std::vector<double> &v)
@@ -430,6 +437,7 @@ int build_device(Ctx &c)
     // ---- typed tables ----
     mw3::set_kernel_attributes(c);
     TRY(mw3::build_tc_ang(c));
+    TRY(mw3::build_tc_dst2d(c));
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;
     cudaError_t e = cudaStreamSynchronize(c.stream);
@@ -875,7 +883,8 @@ int mw3_path_flags(mw3_ctx *h, int32_t *flags)
         c.err = "mw3_path_flags before the device tables were built";
         return MW3_ERR_STATE;
     }
-    *flags = (mw3::tc_dst_supported(c) ? MW3_PATH_TC_DST : 0) | (c.use_tc_ang ? MW3_PATH_TC_ANG : 0);
+    *flags = ((mw3::tc_dst_supported(c) || c.use_tc_dst2d) ? MW3_PATH_TC_DST : 0) |
+             (c.use_tc_dst2d ? MW3_PATH_TC_DST_FUSED : 0) | (c.use_tc_ang ? MW3_PATH_TC_ANG : 0);
     return MW3_OK;
 }
 

@@ -946,7 +946,13 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     int64_t row0 = (int64_t)g_begin * c.na * c.n1;
     int64_t nrows = (int64_t)ng * c.na * c.n1;
     dim3 gr((unsigned)((nrows + BM - 1) / BM), (c.n2 + BN - 1) / BN);
-    if (sizeof(T) == 4 && tc_dst_supported(c)) {
+    if (sizeof(T) == 4 && c.use_tc_dst2d) {
+        // mixed path: the whole DST chain of each slab in one tensor-core kernel
+        stage_mark(c, 0);
+        launch_tc_dst2d(c, (const float *)c.d_X, c.d_h, g_begin, g_end);
+        stage_mark(c, 1);
+        stage_mark(c, 2);
+    } else if (sizeof(T) == 4 && tc_dst_supported(c)) {
         // mixed path: the three DST passes on the tensor cores
         launch_tc_dst(c, (const float *)c.d_X, (float *)c.d_Y, c.d_h, g_begin, g_end, 0);
     } else {

@@ -69,8 +69,9 @@ HEADER_FUNCS = [
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_last_error", "mw3_destroy",
 ]
-# stage 3 is the whole angular part when the mixed path runs it as one fused
-# tensor-core contraction (stage 4 is then empty); the explicit form splits j^2 and l^2
+# stage 0 holds the whole radial DST chain when the mixed path runs it as one
+# fused kernel (stages 1 and 2 are then empty); stage 3 is the whole angular
+# part when it runs as one fused tensor-core contraction (stage 4 then empty)
 STAGES = ["dst_R", "dst_r_pair", "dst_R_gather", "angular", "angular_l2", "update", "accumulators"]
 
 _lib = None
@@ -305,10 +306,11 @@ class Propagator:
         return n.value
 
     def path(self):
-        """Kernels in use: {"tc_dst": bool, "tc_angular": bool} (after start)."""
+        """Kernels in use (after start): tensor-core radial DSTs, fused into one
+        kernel per slab or not, and the tensor-core angular contraction."""
         f = ct.c_int32()
         self._check(self.L.mw3_path_flags(self.h, ct.byref(f)), "mw3_path_flags")
-        return {"tc_dst": bool(f.value & 1), "tc_angular": bool(f.value & 2)}
+        return {"tc_dst": bool(f.value & 1), "tc_dst_fused": bool(f.value & 4), "tc_angular": bool(f.value & 2)}
 
     def stream(self):
         """cudaStream_t of the context, as an integer handle."""
