@@ -438,6 +438,23 @@ int build_device(Ctx &c)
     mw3::set_kernel_attributes(c);
     TRY(mw3::build_tc_ang(c));
     TRY(mw3::build_tc_dst2d(c));
+    c.h32 = c.use_tc_dst2d && c.use_tc_ang;
+    c.d_h32 = nullptr;
+    c.d_vr = nullptr;
+    if (c.use_tc_dst2d) TRY(dalloc(c, &c.d_h32, (size_t)c.NT));
+    if (!c.fp64) {
+        // potential pre-scaled for the mixed update: V 2/delta2, minus emindlt 2/delta2 on the diagonal
+        const double r2d = 2.0 / c.grid.delta2;
+        std::vector<double> vr(c.vvv.size());
+        const size_t per = (size_t)c.na * c.npt;
+        for (int et = 0; et < c.ne; et++)
+            for (int es = 0; es < c.ne; es++) {
+                size_t b = ((size_t)et * c.ne + es) * per;
+                for (size_t i = 0; i < per; i++)
+                    vr[b + i] = c.vvv[b + i] * r2d - (et == es ? c.grid.emindlt * r2d : 0.0);
+            }
+        TRY(dupload(c, &c.d_vr, vr));
+    }
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;
     cudaError_t e = cudaStreamSynchronize(c.stream);

@@ -200,6 +200,11 @@ struct Ctx {
     float *d_dst_planes = nullptr;   // S2, then S1 of every length: 128 x 128 TF32 hi/lo chunk planes
     int64_t *d_dst_s1off = nullptr;  // [W][na] float offset of the slab's S1
     float *d_p2r1f = nullptr, *d_p2r2f = nullptr;      // FP32 copies of the momenta tables
+    // mixed path with the fused DSTs: H psi (without V) kept in FP32, and the
+    // potential pre-scaled for the update: vr = V 2/delta2 - [same state] emindlt 2/delta2
+    bool h32 = false;
+    float *d_h32 = nullptr;          // [NT]
+    double *d_vr = nullptr;          // like vvv
     int *d_tc_err = nullptr;         // set by a tensor-core kernel whose mbarrier wait ran out
     // optional per-stage event timing (mw3_profile)
     bool prof = false;
@@ -235,9 +240,10 @@ void launch_tc_dst(Ctx &c, const float *X, float *Y, double *H, int g_begin, int
 // tensor-core angular terms of the mixed path (mw3_tc_ang.cu); sets c.use_tc_ang
 int build_tc_ang(Ctx &c);
 void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end);
+void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end);
 // fused tensor-core radial DSTs of the mixed path (mw3_tc_dst2d.cu); sets c.use_tc_dst2d
 int build_tc_dst2d(Ctx &c);
-void launch_tc_dst2d(Ctx &c, const float *X, double *H, int g_begin, int g_end);
+void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end);
 std::vector<double> dst_matrix(int n);
 
 // ---------------------------------------------------------------------------

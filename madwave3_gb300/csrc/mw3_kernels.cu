@@ -218,8 +218,55 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
         }
 }
 
+// double -> float, round to nearest even, with integer instructions only (the
+// F2F conversion issues on the FP64 pipe); magnitudes below FLT_MIN go to a
+// signed zero, above FLT_MAX to infinity
+__device__ __forceinline__ float f64_to_f32_int(double x)
+{
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    unsigned int m = (unsigned int)((b >> 29) & 0x7FFFFFu);
+    unsigned int rest = (unsigned int)(b & 0x1FFFFFFFu);
+    unsigned int r = ((unsigned int)e << 23) | m;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) r += 1u;   // carry may round into the exponent
+    if (r >= 0x7F800000u) r = 0x7F800000u;
+    return __uint_as_float(sign | r);
+}
+
+// exact float -> double with integer instructions (the F2F conversion issues
+// on the FP64 pipe); subnormal inputs become a signed zero
+__device__ __forceinline__ double f32_to_f64_int(float f)
+{
+    unsigned int u = __float_as_uint(f);
+    unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    unsigned int e = (u >> 23) & 0xFFu, mt = u & 0x7FFFFFu;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    unsigned long long ex = (e == 255) ? 0x7FFull : (unsigned long long)(e - 127 + 1023);
+    return __longlong_as_double((long long)(sign | (ex << 52) | ((unsigned long long)mt << 29)));
+}
+
+__device__ __forceinline__ double h_load(const double *H, int64_t i) { return H[i]; }
+__device__ __forceinline__ double h_load(const float *H, int64_t i) { return f32_to_f64_int(H[i]); }
+__device__ __forceinline__ void h_store(double *H, int64_t i, double v) { H[i] = v; }
+__device__ __forceinline__ void h_store(float *H, int64_t i, double v) { H[i] = f64_to_f32_int(v); }
+
+// H (FP64) = H32 at every stored point of the segments, for the explicit
+// angular kernels that accumulate in FP64
+__global__ void k_h32_to_h(DevGrid d, const float *__restrict__ h32, double *__restrict__ H, int seg0)
+{
+    int seg = seg0 + blockIdx.x;
+    int a = seg % d.na;
+    int64_t off = d.foff[seg];
+    int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
+    for (int ir = blockIdx.y * kPointChunk + threadIdx.x; ir < n; ir += blockDim.x) H[off + ir] = f32_to_f64_int(h32[off + ir]);
+}
+
 // stored points with ir1 beyond the DST length keep psi as their "kinetic" term
-__global__ void k_quirk(DevGrid d, const double *__restrict__ psi, double *__restrict__ H,
+template <typename HT>
+__global__ void k_quirk(DevGrid d, const double *__restrict__ psi, HT *__restrict__ H,
                         const int *__restrict__ qptr, const int *__restrict__ qlist, int seg0)
 {
     int seg = seg0 + blockIdx.x;
@@ -229,7 +276,7 @@ __global__ void k_quirk(DevGrid d, const double *__restrict__ psi, double *__res
     int64_t off = d.foff[seg];
     for (int q = b + threadIdx.x; q < e; q += blockDim.x) {
         int ir = qlist[q];
-        H[off + ir] = psi[off + ir];
+        h_store(H, off + ir, psi[off + ir]);
     }
 }
 
@@ -356,12 +403,14 @@ __global__ void __launch_bounds__(256) k_ang_l(DevGrid d, const T *__restrict__ 
 // :245-248), next rectangle, norm partials and funE (mod_PsiE_01y2.f:108-120)
 // ---------------------------------------------------------------------------
 struct UpdArgs {
-    const double *H, *pk, *pkm1;
+    const void *H;                 // double, or float when the mixed path keeps H psi in FP32
+    const double *pk, *pkm1;
     double *out;
     const int *vsrc;               // [G][ne]
     const double *absfr1, *absfr2; // [W][n1], [W][n2]
     double emindlt, delta2;
     double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
+    const double *vr;              // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
     int first;
     double *normpart;              // [G*na]
     int nofe;                      // max over waves; 0 = funE off
@@ -370,25 +419,7 @@ struct UpdArgs {
     const int64_t *wflat0;         // [W+1]
 };
 
-// double -> float, round to nearest even, with integer instructions only (the
-// F2F conversion issues on the FP64 pipe); magnitudes below FLT_MIN go to a
-// signed zero, above FLT_MAX to infinity
-__device__ __forceinline__ float f64_to_f32_int(double x)
-{
-    unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-    int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
-    if (e <= 0) return __uint_as_float(sign);
-    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
-    unsigned int m = (unsigned int)((b >> 29) & 0x7FFFFFu);
-    unsigned int rest = (unsigned int)(b & 0x1FFFFFFFu);
-    unsigned int r = ((unsigned int)e << 23) | m;
-    if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) r += 1u;   // carry may round into the exponent
-    if (r >= 0x7F800000u) r = 0x7F800000u;
-    return __uint_as_float(sign | r);
-}
-
-template <typename T>
+template <typename T, typename HT>
 __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
 {
     const int seg = blockIdx.x;
@@ -409,7 +440,7 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             int sb = u.vsrc[g * ne + q];
             if (sb < 0) continue;
             int es = d.blk_elec[sb];
-            s_vrow[ns] = d.vvv + ((((size_t)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
+            s_vrow[ns] = (sizeof(T) == 4 ? u.vr : d.vvv) + ((((size_t)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
             s_prow[ns] = u.pk + d.foff[(size_t)sb * d.na + a];
             ns++;
         }
@@ -417,7 +448,7 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
     }
     __syncthreads();
     const int nsrc = s_nsrc;
-    const double *__restrict__ Hp = u.H + off;
+    const HT *__restrict__ Hp = reinterpret_cast<const HT *>(u.H) + off;
     const double *__restrict__ pkp = u.pk + off;
     const double *__restrict__ pm1 = u.pkm1 + off;
     double *__restrict__ outp = u.out + off;
@@ -440,16 +471,18 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
         bool on = ir < n;
         r1[k] = on ? i1p[ir] - 1 : 0;
         r2[k] = on ? i2p[ir] - 1 : 0;
-        hv[k] = on ? Hp[ir] : 0.0;
+        hv[k] = on ? h_load(Hp, ir) : 0.0;
         pk[k] = on ? pkp[ir] : 0.0;
         p1[k] = on && !u.first ? pm1[ir] : 0.0;
     }
-    for (int q = 0; q < nsrc; q++) {
-        const double *vr = s_vrow[q], *pr = s_prow[q];
+    if (sizeof(T) == 8) {
+        for (int q = 0; q < nsrc; q++) {
+            const double *vr = s_vrow[q], *pr = s_prow[q];
 #pragma unroll
-        for (int k = 0; k < U; k++) {
-            int ir = ir0 + k * 256;
-            if (ir < n) hv[k] += pr[ir] * vr[ir];
+            for (int k = 0; k < U; k++) {
+                int ir = ir0 + k * 256;
+                if (ir < n) hv[k] += pr[ir] * vr[ir];
+            }
         }
     }
     float nrmf = 0.f;
@@ -471,20 +504,21 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             nrm += nv * nv;
         } else {
             // mixed path, few FP64 instructions (GB300 runs FP64 at 1/64 of FP32):
-            // reciprocal multiplies, damping only inside the absorbers, the FP32
-            // copy rounded with integer operations, the norm partial in FP32
+            //   t = H 2/delta2 + sum_s vr_s psi_s = 2 (H psi - emindlt psi) / delta2
+            // with the potential pre-scaled, damping only inside the absorbers,
+            // the FP32 copy rounded with integer operations, the norm partial in FP32
+            const bool damp = !u.first && !(__double_as_longlong(ab1[r1[k]]) == 0x3FF0000000000000LL &&
+                                            __double_as_longlong(ab2[r2[k]]) == 0x3FF0000000000000LL);
+            double acc = (u.first || damp) ? 0.0 : -p1[k];
+            for (int q = 0; q < nsrc; q++) acc = fma(s_vrow[q][ir], s_prow[q][ir], acc);
+            double t = fma(hv[k], u.r2delta, acc);
             if (u.first) {
-                nv = (hv[k] - emin * pk[k]) * u.rdelta;
+                nv = 0.5 * t;
+            } else if (damp) {
+                double fab = ab1[r1[k]] * ab2[r2[k]];
+                nv = fma(-fab, p1[k], t) * fab;
             } else {
-                double a1 = ab1[r1[k]], a2 = ab2[r2[k]];
-                double rhn2 = (hv[k] - emin * pk[k]) * u.r2delta;
-                if (__double_as_longlong(a1) == 0x3FF0000000000000LL &&
-                    __double_as_longlong(a2) == 0x3FF0000000000000LL) {
-                    nv = rhn2 - p1[k];
-                } else {
-                    double fab = a1 * a2;
-                    nv = (rhn2 - fab * p1[k]) * fab;
-                }
+                nv = t;
             }
             float nf = f64_to_f32_int(nv);
             rect[(size_t)r1[k] * n2 + r2[k]] = (T)nf;
@@ -516,8 +550,9 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
 
 // V psi alone, for mw3_hphi: H(t) += sum_s V(e_s, e_t) psi(s) over same-Omega blocks
 // (difs V part, mod_Hphi_01y2.f:838-853)
-__global__ void k_addv(DevGrid d, const double *__restrict__ psi, double *__restrict__ H, const int *__restrict__ vsrc,
-                       int seg0)
+template <typename HT>
+__global__ void k_addv(DevGrid d, const double *__restrict__ psi, const HT *__restrict__ Hin, double *__restrict__ H,
+                       const int *__restrict__ vsrc, int seg0)
 {
     int seg = seg0 + blockIdx.x;
     int g = seg / d.na, a = seg % d.na;
@@ -525,7 +560,7 @@ __global__ void k_addv(DevGrid d, const double *__restrict__ psi, double *__rest
     int64_t off = d.foff[seg];
     int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
     for (int ir = blockIdx.y * kPointChunk + threadIdx.x; ir < n; ir += blockDim.x) {
-        double hv = H[off + ir];
+        double hv = h_load(Hin, off + ir);
         for (int q = 0; q < d.ne; q++) {
             int s = vsrc[g * d.ne + q];
             if (s < 0) continue;
@@ -947,11 +982,22 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     int64_t nrows = (int64_t)ng * c.na * c.n1;
     dim3 gr((unsigned)((nrows + BM - 1) / BM), (c.n2 + BN - 1) / BN);
     if (sizeof(T) == 4 && c.use_tc_dst2d) {
-        // mixed path: the whole DST chain of each slab in one tensor-core kernel
+        // mixed path: the whole DST chain of each slab in one tensor-core kernel, H in FP32
         stage_mark(c, 0);
-        launch_tc_dst2d(c, (const float *)c.d_X, c.d_h, g_begin, g_end);
+        launch_tc_dst2d(c, (const float *)c.d_X, c.d_h32, g_begin, g_end);
         stage_mark(c, 1);
         stage_mark(c, 2);
+        k_quirk<float><<<ng * c.na, 128, 0, c.stream>>>(d, psi, c.d_h32, c.d_quirk_ptr, c.d_quirk, g_begin * c.na);
+        LAUNCH_CHECK(c);
+        stage_mark(c, 3);
+        if (c.use_tc_ang) {
+            launch_tc_ang(c, (const float *)c.d_X, c.d_h32, g_begin, g_end);
+            stage_mark(c, 4);
+            return;
+        }
+        // the explicit angular kernels accumulate in FP64: widen H first
+        k_h32_to_h<<<dim3(ng * c.na, c.nchunk), 256, 0, c.stream>>>(d, c.d_h32, c.d_h, g_begin * c.na);
+        LAUNCH_CHECK(c);
     } else if (sizeof(T) == 4 && tc_dst_supported(c)) {
         // mixed path: the three DST passes on the tensor cores
         launch_tc_dst(c, (const float *)c.d_X, (float *)c.d_Y, c.d_h, g_begin, g_end, 0);
@@ -975,10 +1021,12 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
         LAUNCH_CHECK(c);
     }
     // points beyond the r1 DST length keep psi
-    k_quirk<<<ng * c.na, 128, 0, c.stream>>>(d, psi, c.d_h, c.d_quirk_ptr, c.d_quirk, g_begin * c.na);
-    LAUNCH_CHECK(c);
+    if (!(sizeof(T) == 4 && c.use_tc_dst2d)) {
+        k_quirk<double><<<ng * c.na, 128, 0, c.stream>>>(d, psi, c.d_h, c.d_quirk_ptr, c.d_quirk, g_begin * c.na);
+        LAUNCH_CHECK(c);
+        stage_mark(c, 3);
+    }
     // 4. angular kinetic terms
-    stage_mark(c, 3);
     if (sizeof(T) == 4 && c.use_tc_ang) {
         // mixed path: j^2 + l^2 + Coriolis in one factorised tensor-core contraction
         launch_tc_ang(c, (const float *)c.d_X, c.d_h, g_begin, g_end);
@@ -1011,6 +1059,7 @@ void launch_update(Ctx &c, int first)
     u.delta2 = c.grid.delta2;
     u.rdelta = 1.0 / c.grid.delta2;
     u.r2delta = 2.0 / c.grid.delta2;
+    u.vr = c.d_vr;
     u.first = first;
     u.normpart = c.d_normpart;
     u.nofe = c.nofemax;
@@ -1018,7 +1067,12 @@ void launch_update(Ctx &c, int first)
     u.zfe = c.d_zfe_ptrs;
     u.wflat0 = c.d_wflat0;
     stage_mark(c, 5);
-    k_update<T><<<dim3(c.nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+    if (c.h32) {
+        u.H = c.d_h32;
+        k_update<T, float><<<dim3(c.nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+    } else {
+        k_update<T, double><<<dim3(c.nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+    }
     LAUNCH_CHECK(c);
 }
 
@@ -1141,7 +1195,12 @@ void flush_flux(Ctx &c)
 void launch_addv(Ctx &c, const double *psi, int g0, int g1)
 {
     if (g1 <= g0) return;
-    k_addv<<<dim3((g1 - g0) * c.na, c.nchunk), 256, 0, c.stream>>>(devgrid(c), psi, c.d_h, c.d_vsrc, g0 * c.na);
+    if (c.h32)
+        k_addv<float><<<dim3((g1 - g0) * c.na, c.nchunk), 256, 0, c.stream>>>(devgrid(c), psi, c.d_h32, c.d_h,
+                                                                               c.d_vsrc, g0 * c.na);
+    else
+        k_addv<double><<<dim3((g1 - g0) * c.na, c.nchunk), 256, 0, c.stream>>>(devgrid(c), psi, c.d_h, c.d_h,
+                                                                                c.d_vsrc, g0 * c.na);
     LAUNCH_CHECK(c);
 }
 
@@ -1197,7 +1256,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     LAUNCH_CHECK(c);
     k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, Y, (const T *)c.d_S2, nullptr, H, c.d_nopr1, row0, nrows);
     LAUNCH_CHECK(c);
-    k_quirk<<<ng * na, 128, 0, c.stream>>>(d, P, H, c.d_quirk_ptr, c.d_quirk, g0 * na);
+    k_quirk<double><<<ng * na, 128, 0, c.stream>>>(d, P, H, c.d_quirk_ptr, c.d_quirk, g0 * na);
     LAUNCH_CHECK(c);
     if (sizeof(T) == 4 && c.use_tc_ang) {
         launch_tc_ang(c, (const float *)X, H, g0, g1);
@@ -1211,7 +1270,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
                                                                     c.d_cpl, c.ncl, g0);
         LAUNCH_CHECK(c);
     }
-    k_addv<<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, P, H, c.d_vsrc, g0 * na);
+    k_addv<double><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, P, H, H, c.d_vsrc, g0 * na);
     LAUNCH_CHECK(c);
     (void)g1;
 }

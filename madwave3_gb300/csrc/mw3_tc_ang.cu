@@ -38,9 +38,10 @@ constexpr uint32_t AG_BYTES = 2 * AG_APLANE + 2 * AG_DPLANE;   // 96 KB
 constexpr uint32_t AG_COLS = 256;                 // three ring slots + the output tile
 constexpr uint32_t AG_OUT = 192;                  // column of the output tile
 
+template <typename HT>
 struct AngArgs {
     const float *X;              // rectangle [G][na][n1][n2]
-    double *H;                   // flat H accumulator
+    HT *H;                       // flat H accumulator (FP32 when the mixed path keeps H in FP32)
     const float *dfw, *dbk;      // [G][2][64*64] hi/lo planes: (j, angle) and (angle, j), K-major
     const float *yj;             // [G][n1][64]   yyy(j, r1), 0 outside the block's j list
     const float *l2;             // [G][3][n2][64] xl2mat_j(Om, Om+q; R), slot q+1, 0 where absent
@@ -55,7 +56,8 @@ struct AngArgs {
 // X tile of block g: A operand rows m = (r1 offset)*8 + (R offset), K = angle.
 // A quarter warp takes 8 consecutive R of one r1 row: its global loads are one
 // 32-byte sector per angle and its shared stores one 128-byte core-matrix block.
-__device__ __forceinline__ void ang_stage_x(const AngArgs &p, int g, int r1_0, int r2_0, unsigned char *hi,
+template <typename HT>
+__device__ __forceinline__ void ang_stage_x(const AngArgs<HT> &p, int g, int r1_0, int r2_0, unsigned char *hi,
                                             unsigned char *lo)
 {
     const float *Xg = p.X + (size_t)g * p.na * p.n1 * p.n2;
@@ -100,7 +102,8 @@ __device__ __forceinline__ void ang_issue(uint32_t dcol, const unsigned char *a,
     }
 }
 
-__global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs p)
+template <typename HT>
+__global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
 {
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char *sm = smraw + ((1024 - (smem_u32(smraw) & 1023)) & 1023);
@@ -241,12 +244,12 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs p)
                         int a = a0 + h8 + i;
                         idx[i] = (inrow && a < na) ? __ldg(p.map + ((size_t)a * n1 + ir1) * n2 + ir2) : -1;
                     }
-                    double hv[8];
+                    HT hv[8];
 #pragma unroll
-                    for (int i = 0; i < 8; i++) hv[i] = idx[i] >= 0 ? p.H[fo[a0 + h8 + i] + idx[i]] : 0.0;
+                    for (int i = 0; i < 8; i++) hv[i] = idx[i] >= 0 ? p.H[fo[a0 + h8 + i] + idx[i]] : (HT)0;
 #pragma unroll
                     for (int i = 0; i < 8; i++)
-                        if (idx[i] >= 0) p.H[fo[a0 + h8 + i] + idx[i]] = hv[i] + (double)v[h8 + i];
+                        if (idx[i] >= 0) p.H[fo[a0 + h8 + i] + idx[i]] = hv[i] + (HT)v[h8 + i];
                 }
             }
         }
@@ -411,13 +414,14 @@ int build_tc_ang(Ctx &c)
 }
 
 // blocks [g_begin, g_end) must be whole waves
-void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end)
+template <typename HT>
+static void tc_ang_launch(Ctx &c, const float *X, HT *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
     const size_t smem = AG_BYTES + 64 + 1024;
     if (!attr) {
-        cudaFuncSetAttribute(k_tc_ang, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_tc_ang<HT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
     int w0 = c.waves.size(), w1 = 0;
@@ -431,15 +435,25 @@ void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end)
     if (w1 <= w0) return;
     int ch0 = c.ang_wchain[w0], nch = c.ang_wchain[w1] - ch0;
     if (nch <= 0) return;
-    AngArgs p;
+    AngArgs<HT> p;
     p.X = X; p.H = H;
     p.dfw = c.d_ang_dfw; p.dbk = c.d_ang_dbk; p.yj = c.d_ang_yj; p.l2 = c.d_ang_l2;
     p.chain_ptr = c.d_ang_chain_ptr; p.chain = c.d_ang_chain; p.tiles = c.d_ang_tiles;
     p.blk_om = c.d_blk_om; p.map = c.d_map; p.foff = c.d_foff;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.chain0 = ch0;
     p.err = c.d_tc_err;
-    k_tc_ang<<<dim3(c.ang_ntiles, nch), 256, smem, c.stream>>>(p);
+    k_tc_ang<HT><<<dim3(c.ang_ntiles, nch), 256, smem, c.stream>>>(p);
     c.launches++;
+}
+
+void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end)
+{
+    tc_ang_launch<double>(c, X, H, g_begin, g_end);
+}
+
+void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end)
+{
+    tc_ang_launch<float>(c, X, H, g_begin, g_end);
 }
 
 }  // namespace mw3

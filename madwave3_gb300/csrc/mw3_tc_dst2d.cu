@@ -41,7 +41,7 @@ constexpr uint32_t D2_BYTES = 2 * D2_STAGE;       // 192 KB
 
 struct Dst2Args {
     const float *X;               // rectangle [G][na][n1][n2]
-    double *H;
+    float *H;                     // H psi without V, FP32
     const float *planes;          // S2 (RB x RB) at 0, S1 of each length at s1off
     const int64_t *s1off;         // [W][na]
     const int *nopr1;             // [W][na]
@@ -53,18 +53,6 @@ struct Dst2Args {
     int na, n1, n2, seg0;
     int *err;
 };
-
-// exact float -> double with integer instructions (the F2F conversion issues
-// on the FP64 pipe); subnormal inputs become a signed zero
-__device__ __forceinline__ double f32_to_f64_int(float f)
-{
-    uint32_t u = __float_as_uint(f);
-    uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
-    uint32_t e = (u >> 23) & 0xFFu, mt = u & 0x7FFFFFu;
-    if (e == 0) return __longlong_as_double((long long)sign);
-    uint64_t ex = (e == 255) ? 0x7FFull : (uint64_t)(e - 127 + 1023);
-    return __longlong_as_double((long long)(sign | (ex << 52) | ((uint64_t)mt << 29)));
-}
 
 // four values of one row into the hi plane at off and the lo plane lo_off further
 __device__ __forceinline__ void d2_split4(unsigned char *hi, uint32_t lo_off, uint32_t off, float a, float b,
@@ -295,7 +283,7 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
             }
 #pragma unroll
             for (int i = 0; i < 16; i++)
-                if (idx[i] >= 0) p.H[fo + idx[i]] = f32_to_f64_int(v[i]);
+                if (idx[i] >= 0) p.H[fo + idx[i]] = v[i];
         }
     }
 done:
@@ -404,7 +392,7 @@ int build_tc_dst2d(Ctx &c)
     return MW3_OK;
 }
 
-void launch_tc_dst2d(Ctx &c, const float *X, double *H, int g_begin, int g_end)
+void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
