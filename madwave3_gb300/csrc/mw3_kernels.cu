@@ -535,10 +535,16 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             }
         }
     }
-    if (sizeof(T) == 4) nrm = (double)nrmf;
-    // norm partial: fixed shuffle tree per warp, then the warps in order (deterministic)
+    // norm partial: fixed shuffle tree per warp, then the warps in order (deterministic);
+    // the mixed path reduces its FP32 sums in FP32 up to the warp level
+    if (sizeof(T) == 4) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, o);
+        for (int o = 16; o > 0; o >>= 1) nrmf += __shfl_down_sync(0xffffffffu, nrmf, o);
+        nrm = f32_to_f64_int(nrmf);
+    } else {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, o);
+    }
     if (lane == 0) s_wsum[warp] = nrm;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -625,6 +631,28 @@ __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ p
     int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (f >= NF) return;
+    if (fring) {
+        // mixed path: FP32 products and sums (the ring holds FP32 anyway), so
+        // no FP64 instruction per term; zar rows read as FP32 from the FP64 table
+        float sr = 0.f, si = 0.f;
+        for (int q = dptr[f] + lane; q < dptr[f + 1]; q += 32) {
+            float p = f64_to_f32_int(psi[didx[q]]);
+            int ir1 = dir1[q];
+            sr = fmaf(f64_to_f32_int(zar[2 * ir1]), p, sr);
+            si = fmaf(f64_to_f32_int(zar[2 * ir1 + 1]), p, si);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0) {
+            fring[3 * (size_t)f] = f64_to_f32_int(psi[fidx[f]]);
+            fring[3 * (size_t)f + 1] = sr;
+            fring[3 * (size_t)f + 2] = si;
+        }
+        return;
+    }
     double sr = 0.0, si = 0.0;
     for (int q = dptr[f] + lane; q < dptr[f + 1]; q += 32) {
         double p = psi[didx[q]];
@@ -639,11 +667,7 @@ __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ p
     }
     if (lane == 0) {
         double p0 = psi[fidx[f]];
-        if (fring) {                // mixed path: ring slot [f][3] in FP32
-            fring[3 * (size_t)f] = (float)p0;
-            fring[3 * (size_t)f + 1] = (float)sr;
-            fring[3 * (size_t)f + 2] = (float)si;
-        } else {
+        {
             fpsi[4 * (size_t)f] = p0;
             fpsi[4 * (size_t)f + 1] = sr;
             fpsi[4 * (size_t)f + 2] = si;
