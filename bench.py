@@ -31,6 +31,12 @@ sys.path.insert(0, HERE)
 
 L2_BYTES = 129 * 1024 * 1024
 
+# DRAM bytes per stored point and launch of the mixed path's top kernels, from
+# one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the J=0..4
+# sweep; the per-block structure of the full sweep is the same, so the traffic
+# scales with the stored points (profiles/k_tc_dst2d_jsweep0-4_256x128x60_mixed.md)
+TRAFFIC_PER_POINT = {"dst_R": 14.0, "angular": 17.0, "update": 29.7}
+
 WORKLOADS = {
     # partial-wave sweep J=0..40, Omega=0..min(J,6): 266 blocks on 256 R x 128 r x 60 angles
     "jsweep0-40_256x128x60": dict(case="j0_256x128x60", sweep=list(range(0, 41))),
@@ -244,14 +250,20 @@ def run_gpu(args, rank, world, local):
     dom = max(stages, key=lambda k: stages[k])
     kind, work = model[dom]
     t_launch = stages[dom] / max(nrec, 1) * 1e-3
+    kin = out_kernels = prop.path()
+    traffic = None
+    if args.precision == "mixed" and kin["tc_dst_fused"] and kin["tc_angular"] and dom in TRAFFIC_PER_POINT:
+        traffic = TRAFFIC_PER_POINT[dom] * nsto
     if kind == "flop":
         achieved = work / t_launch / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": tf, "unit": "TFLOP/s",
-                "frac": achieved / tf, "traffic": None, "kernel": dom, "peak_source": src}
+                "frac": achieved / tf, "traffic": traffic, "kernel": dom, "peak_source": src,
+                "work": "algorithmic DST flops (4 nopr1 npun2^2 + 4 nopr1^2 npun2 per slab); the kernel issues "
+                        "3 TF32 products per flop (3xTF32), and the peak is the dense bf16 one"}
     else:
         achieved = work / t_launch / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "kernel": dom, "peak_source": src}
+                "frac": achieved / hbm, "traffic": traffic, "kernel": dom, "peak_source": src}
     out = {
         "metric": metric_name(), "value": value, "unit": "grid-pt*iter/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -272,7 +284,7 @@ def run_gpu(args, rank, world, local):
         "roofline": roof,
         "clocks": clk,
     }
-    out["config"]["kernels"] = prop.path()
+    out["config"]["kernels"] = out_kernels
     prop.close()
     del prop
     if args.precision == "mixed" and args.fp64_steps > 0:
