@@ -197,7 +197,8 @@ struct Ctx {
     std::vector<int> ang_wchain;                        // [W+1] first chain of each wave
     // mixed path: the whole radial DST chain in one tensor-core kernel per slab (mw3_tc_dst2d.cu)
     bool use_tc_dst2d = false;
-    float *d_dst_planes = nullptr;   // S2, then S1 of every length: 128 x 128 TF32 hi/lo chunk planes
+    float *d_dst_planes = nullptr;   // S1 of every length: 128 x 128 TF32 hi/lo chunk planes
+    float *d_dst_s2fold = nullptr;   // S2 split by column parity (DST-I symmetry), hi/lo chunk planes
     int64_t *d_dst_s1off = nullptr;  // [W][na] float offset of the slab's S1
     float *d_p2r1f = nullptr, *d_p2r2f = nullptr;      // FP32 copies of the momenta tables
     // mixed path with the fused DSTs: H psi (without V) kept in FP32, and the

@@ -9,10 +9,10 @@
 // Four 128 x 128 tensor-core GEMMs, oriented so that each result can be read
 // out of tensor memory row by row (a thread owns one lane) and written back as
 // the next GEMM's K-major operand without a transpose:
-//   D1[R][r1] = S2 Xs^T            A = S2 (bulk copy)      B = Xs rows (global)
+//   D1[R][r1] = S2 Xs^T            A = S2 (bulk copy)      B = Xs rows (global)      [R folded]
 //   D2[R][r1] = D1 S1^T            A = D1 (tensor memory)  B = S1 (bulk copy)
 //   D3[r1][R] = S1 (D2 o F^T)^T    A = S1 (bulk copy)      B = D2 o F^T (tensor memory)
-//   D4[r1][R] = D3 S2              A = D3 (tensor memory)  B = S2 (bulk copy)
+//   D4[r1][R] = D3 S2              A = D3 (tensor memory)  B = S2 (bulk copy)        [R folded]
 // so H[r1][R] = D4, written with lanes along r1 (stored points are r1-major runs).
 // K streams in chunks of 32 through two shared-memory stages; the DST matrices
 // are split on the host into TF32 hi/lo planes in the canonical K-major chunk
@@ -29,20 +29,29 @@
 namespace mw3 {
 namespace tc {
 
-// R (npun2) up to 256: one or two 128-row tiles.  Each stage has a "big" slot
-// for the operand that spans R (hi and lo planes of RB rows x 32 k, RB = 128
-// or 256) and a "small" slot for the 128-row operand.
+// The two products along R use the symmetry of DST-I,
+//   S[n-1-i][k] = (-1)^k S[i][k]:
+// with E_i = sum_{k even} S[i][k] x_k and O_i = sum_{k odd} S[i][k] x_k for
+// i < h = ceil(n/2), y_i = E_i + O_i and y_{n-1-i} = E_i - O_i, so each is a
+// pair of 128 x 128 products over the even and the odd half of K instead of a
+// 256 x 256 one.  The products along r1 take N = nopr1 rounded up to 16.
+// Every tcgen05.ld below is executed by whole warps (its conditions depend on
+// the warp only); lane-dependent choices are made on the loaded values.
 constexpr int D2_KC = 32;
 constexpr uint32_t D2_SBO = (D2_KC / 4) * 128;    // 1 KB between 8-row groups
 constexpr uint32_t D2_SMALL = 2 * 128 * 128;      // 32 KB: hi + lo, 128 rows x 32 k
+constexpr uint32_t D2_SMALL_LO = D2_SMALL / 2;    // lo plane of a 128-row operand
 constexpr uint32_t D2_BIGMAX = 2 * 256 * 128;     // 64 KB: hi + lo, 256 rows x 32 k
 constexpr uint32_t D2_STAGE = D2_BIGMAX + D2_SMALL;
 constexpr uint32_t D2_BYTES = 2 * D2_STAGE;       // 192 KB
+constexpr int D2_NKH = 4;                         // K chunks of one parity half (j < 128)
+constexpr size_t D2_CHUNK = D2_SMALL / 4;         // floats of one 128-row chunk (hi + lo)
 
 struct Dst2Args {
     const float *X;               // rectangle [G][na][n1][n2]
     float *H;                     // H psi without V, FP32
-    const float *planes;          // S2 (RB x RB) at 0, S1 of each length at s1off
+    const float *s2fold;          // [parity][D2_NKH][hi, lo]: S2[i][2j+parity], i < 128, j chunk of 32
+    const float *s1planes;        // S1 of each length, 4 chunks of 32 columns
     const int64_t *s1off;         // [W][na]
     const int *nopr1;             // [W][na]
     const float *p2r1f, *p2r2f;   // [W][na][n1], [W][na][n2]
@@ -64,51 +73,62 @@ __device__ __forceinline__ void d2_split4(unsigned char *hi, uint32_t lo_off, ui
     *reinterpret_cast<float4 *>(hi + lo_off + off) = l;
 }
 
-// rows r < nn of the slab, K columns [32c, 32c+32): four float4 per thread;
+// X rows r < nn, columns 2j + parity for j in [32 jc, 32 jc + 32): each thread
+// takes four (row, 4 j) groups, reading the 8 consecutive columns that hold them;
 // a quarter warp covers 8 rows of one 16-byte column group (one core matrix)
 struct XStage {
-    float4 v[4];
+    float4 v[4][2];
     __device__ __forceinline__ static void idx(int e, int &r, int &kg)
     {
         int rest = e >> 3;
         kg = rest & 7;
         r = (rest >> 3) * 8 + (e & 7);
     }
-    __device__ __forceinline__ void load(const float *Xs, int n2, int nn, int c)
+    __device__ __forceinline__ void load(const float *Xs, int n2, int nn, int jc)
     {
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             int r, kg;
             idx(threadIdx.x + 256 * i, r, kg);
-            int k = c * D2_KC + kg * 4;
-            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+            int k = 2 * (jc * D2_KC + kg * 4);          // first of the 8 columns
+            float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0;
             if (r < nn) {
                 const float *q = Xs + (size_t)r * n2 + k;
-                if (k + 3 < n2 && (n2 & 3) == 0) {
-                    x = __ldg(reinterpret_cast<const float4 *>(q));
+                if (k + 7 < n2 && (n2 & 3) == 0) {
+                    x0 = __ldg(reinterpret_cast<const float4 *>(q));
+                    x1 = __ldg(reinterpret_cast<const float4 *>(q + 4));
                 } else {
-                    if (k < n2) x.x = __ldg(q);
-                    if (k + 1 < n2) x.y = __ldg(q + 1);
-                    if (k + 2 < n2) x.z = __ldg(q + 2);
-                    if (k + 3 < n2) x.w = __ldg(q + 3);
+                    float t[8];
+#pragma unroll
+                    for (int u = 0; u < 8; u++) t[u] = (k + u < n2) ? __ldg(q + u) : 0.f;
+                    x0 = make_float4(t[0], t[1], t[2], t[3]);
+                    x1 = make_float4(t[4], t[5], t[6], t[7]);
                 }
             }
-            v[i] = x;
+            v[i][0] = x0;
+            v[i][1] = x1;
         }
     }
-    __device__ __forceinline__ void store(unsigned char *dst) const
+    __device__ __forceinline__ void store(unsigned char *dst, int parity) const
     {
 #pragma unroll
         for (int i = 0; i < 4; i++) {
             int r, kg;
             idx(threadIdx.x + 256 * i, r, kg);
-            d2_split4(dst, D2_SMALL / 2, kmaj_off(r, kg * 4, D2_KC), v[i].x, v[i].y, v[i].z, v[i].w);
+            const float4 &a = v[i][0], &b = v[i][1];
+            if (parity == 0)
+                d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.x, a.z, b.x, b.z);
+            else
+                d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.y, a.w, b.y, b.w);
         }
     }
 };
 
-// Tensor memory (512 columns): D1 and D3 at [0, 256), D2 and D4 at [256, 512);
-// D1/D2 hold R tile t at +128 t.
+// Tensor memory (512 columns):
+//   D1 = S2 Xs^T folded: E at [0,128), O at [128,256)   (lane i < h, column r1)
+//   D2 = D1 S1^T:        R tile t at [256 + 128 t)       (lane R, column r1)
+//   D3 = S1 (D2 o F^T)^T at [0, 256)                     (lane r1, column R)
+//   D4 = D3 S2 folded:   E at [256,384), O at [384,512)  (lane r1, column i < h)
 __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
 {
     extern __shared__ __align__(1024) unsigned char smraw[];
@@ -126,21 +146,23 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
     fence_after_sync();
     const uint32_t tb = *slot;
     const int na = p.na, n1 = p.n1, n2 = p.n2;
-    const int NT = (n2 + 127) / 128;                    // R tiles
+    const int h = (n2 + 1) >> 1;                        // rows i < h: E + O; row n2-1-i: E - O
+    const int nkh = (h + D2_KC - 1) / D2_KC;            // K chunks of one parity half
+    const int NT = (n2 + 127) / 128;                    // R tiles of D2 and of the D3 columns
     const int RB = 128 * NT;
-    const uint32_t big_lo = (uint32_t)RB * 128;         // lo plane offset in the big slot
+    const uint32_t big_lo = (uint32_t)RB * 128;         // lo plane of an RB-row operand
     const int seg = p.seg0 + blockIdx.x;
     const int g = seg / na, a = seg % na, w = p.blk_wave[g];
     const int nn = p.nopr1[w * na + a];
-    const float *S2p = p.planes;
-    const float *S1p = p.planes + p.s1off[w * na + a];
+    const int nnp = (nn + 15) & ~15;                    // N of the products along r1
+    const float *S1p = p.s1planes + p.s1off[w * na + a];
     const float *Xs = p.X + (size_t)seg * n1 * n2;
     const int q4 = warp & 3, half = warp >> 2;
     const int m = q4 * 32 + lane;                       // the tensor-memory lane this thread reads
     const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
     const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
     const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
-    const int rR = 128 * half + m;                      // the R row this thread fills in GEMM 2 and 3
+    const int rR = 128 * half + m;                      // the R row this thread fills in the third product
     const float e2 = (half < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
     uint32_t ph_m[2] = {0u, 0u}, ph_c[2] = {0u, 0u};
     bool pend[2] = {false, false};
@@ -149,12 +171,9 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
     XStage xs;
 
     for (int gi = 0; gi < 4; gi++) {
-        const bool s2 = (gi == 0 || gi == 3);
-        const int nk = s2 ? (n2 + D2_KC - 1) / D2_KC : (nn + D2_KC - 1) / D2_KC;
-        // bulk operand: S2 chunk (RB rows) into the big slot, or S1 chunk into the small slot
-        const size_t bulk_floats = s2 ? (size_t)2 * RB * D2_KC : (size_t)D2_SMALL / 4;
-        const float *Sp = s2 ? S2p : S1p;
-        if (gi > 0) {                                   // the previous GEMM must be complete
+        const bool alongR = (gi == 0 || gi == 3);
+        const int nk = alongR ? 2 * nkh : (nn + D2_KC - 1) / D2_KC;
+        if (gi > 0) {                                   // the previous product must be complete
             for (int s = 0; s < 2; s++)
                 if (pend[s]) {
                     if (!mbar_wait(&bars[s], ph_m[s])) bad = true;
@@ -167,6 +186,7 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
         }
         for (int c = 0; c < nk; c++, q++) {
             const int s = q & 1;
+            const int par = alongR ? c / nkh : 0, jc = alongR ? c % nkh : c;
             unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
             if (pend[s]) {                              // stage s is free once its MMAs are done
                 if (!mbar_wait(&bars[s], ph_m[s])) bad = true;
@@ -175,31 +195,54 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
                 fence_after_sync();
             }
             if (threadIdx.x == 0) {
-                mbar_expect_tx(&bars[2 + s], (uint32_t)(bulk_floats * 4));
-                bulk_g2s(s2 ? big : small, Sp + (size_t)c * bulk_floats, (uint32_t)(bulk_floats * 4), &bars[2 + s]);
+                // the DST operand: folded S2 into the big slot (products 1, 4), S1 into the small slot
+                const float *src = alongR ? p.s2fold + ((size_t)par * D2_NKH + jc) * D2_CHUNK
+                                          : S1p + (size_t)c * D2_CHUNK;
+                mbar_expect_tx(&bars[2 + s], D2_SMALL);
+                bulk_g2s(alongR ? big : small, src, D2_SMALL, &bars[2 + s]);
                 copy_out[s] = true;
             }
             if (gi == 0) {
-                // B = Xs rows (r1) into the small slot
-                xs.store(small);
-                if (c + 1 < nk) xs.load(Xs, n2, nn, c + 1);
-            } else if (gi == 1 || gi == 2) {
-                // A = D1 (gi 1) or B = D2 o F^T (gi 2): RB rows (R) into the big slot; warp half = R tile
+                // B = Xs columns of this parity (rows r1) into the small slot
+                xs.store(small, par);
+                if (c + 1 < nk) xs.load(Xs, n2, nn, (c + 1) % nkh);
+            } else if (gi == 1) {
+                // A = D1 rows R into the big slot: half 0 the sum rows R = i, half 1 the
+                // difference rows R = n2-1-i, from the E and O columns of lane i (all lanes
+                // load; lanes without a row store nothing)
+                float e[32], o[32];
+                tmem_ld32(lrow + (uint32_t)(c * D2_KC), e);
+                tmem_ld32(lrow + 128u + (uint32_t)(c * D2_KC), o);
+                const bool on = half == 0 ? (m < h) : (m < n2 - h);
+                if (on) {
+                    const int R = half == 0 ? m : n2 - 1 - m;
+                    const float sg = half == 0 ? 1.f : -1.f;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        float t[4];
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            int k = c * D2_KC + 4 * j + u;
+                            t[u] = k < nn ? e[4 * j + u] + sg * o[4 * j + u] : 0.f;
+                        }
+                        d2_split4(big, big_lo, kmaj_off(R, 4 * j, D2_KC), t[0], t[1], t[2], t[3]);
+                    }
+                }
+            } else if (gi == 2) {
+                // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
                 if (half < NT) {
                     float v[32];
-                    const uint32_t src = (gi == 1 ? 0u : 256u) + 128u * half + (uint32_t)(c * D2_KC);
-                    tmem_ld32(lrow + src, v);
-                    if (gi == 2) {
+                    tmem_ld32(lrow + 256u + 128u * half + (uint32_t)(c * D2_KC), v);
 #pragma unroll
-                        for (int i = 0; i < 32; i++) {
-                            int k = c * D2_KC + i;
-                            float ek = 0.f;
-                            if (k < nn && rR < n2) {
-                                ek = __ldg(p1f + k) + e2;
-                                if (ek > p.radcut) ek = p.radcut;
-                            }
-                            v[i] = v[i] * ek * divi;
+                    for (int i = 0; i < 32; i++) {
+                        int k = c * D2_KC + i;
+                        float x = 0.f;
+                        if (k < nn && rR < n2) {
+                            float ek = __ldg(p1f + k) + e2;
+                            if (ek > p.radcut) ek = p.radcut;
+                            x = v[i] * ek * divi;
                         }
+                        v[i] = x;
                     }
 #pragma unroll
                     for (int j = 0; j < 8; j++)
@@ -207,14 +250,22 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
                                   v[4 * j + 3]);
                 }
             } else {
-                // A = D3 rows (r1) into the small slot, the two warp halves 16 columns each
-                float v[16];
-                const int k0 = c * D2_KC + 16 * half;
-                tmem_ld16(lrow + (uint32_t)k0, v);
+                // A = D3 columns 2j + parity (rows r1) into the small slot; each warp half
+                // reads 32 consecutive columns and keeps the 16 of this parity
+                float v[32];
+                const int col0 = 2 * (jc * D2_KC) + 32 * half;
+                tmem_ld32(lrow + (uint32_t)col0, v);
 #pragma unroll
-                for (int j = 0; j < 4; j++)
-                    d2_split4(small, D2_SMALL / 2, kmaj_off(m, 16 * half + 4 * j, D2_KC), v[4 * j], v[4 * j + 1],
-                              v[4 * j + 2], v[4 * j + 3]);
+                for (int j = 0; j < 4; j++) {
+                    float t[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        int cc = 2 * (4 * j + u);          // register index fixed at compile time
+                        float x = par == 0 ? v[cc] : v[cc + 1];
+                        t[u] = (col0 + cc + par < n2) ? x : 0.f;
+                    }
+                    d2_split4(small, D2_SMALL_LO, kmaj_off(m, 16 * half + 4 * j, D2_KC), t[0], t[1], t[2], t[3]);
+                }
             }
             fence_async_smem();
             fence_before_sync();
@@ -228,25 +279,42 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
 #pragma unroll
                     for (int ks = 0; ks < D2_KC / 8; ks++) {
                         const uint32_t o = ks * 256;
-                        const int acc0 = (c > 0 || ks > 0) ? 1 : 0;
-                        if (gi <= 1) {
-                            // M = 128 per R tile, N = 128 (r1): A = big (R rows), B = small
-                            const uint32_t idesc = idesc_tf32(128, 128);
-                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL / 2 + o, 128, D2_SBO);
+                        const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
+                        if (gi == 0) {
+                            // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
+                            const uint32_t idesc = idesc_tf32(128, nnp);
+                            uint64_t dah = sdesc(bg + o, 128, D2_SBO), dal = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint32_t d = tb + 128u * par;
+                            mma_tf32(d, dah, dbh, idesc, acc0);
+                            mma_tf32(d, dah, dbl, idesc, 1);
+                            mma_tf32(d, dal, dbh, idesc, 1);
+                        } else if (gi == 1) {
+                            // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
+                            const uint32_t idesc = idesc_tf32(128, nnp);
+                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
                             for (int t = 0; t < NT; t++) {
                                 uint32_t at = bg + (uint32_t)t * 16 * D2_SBO;
                                 uint64_t dah = sdesc(at + o, 128, D2_SBO), dal = sdesc(at + big_lo + o, 128, D2_SBO);
-                                uint32_t d = tb + (gi == 0 ? 0u : 256u) + 128u * t;
+                                uint32_t d = tb + 256u + 128u * t;
                                 mma_tf32(d, dah, dbh, idesc, acc0);
                                 mma_tf32(d, dah, dbl, idesc, 1);
                                 mma_tf32(d, dal, dbh, idesc, 1);
                             }
-                        } else {
-                            // M = 128 (r1), N = RB (R): A = small, B = big
+                        } else if (gi == 2) {
+                            // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
                             const uint32_t idesc = idesc_tf32(128, RB);
-                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL / 2 + o, 128, D2_SBO);
+                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
                             uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + big_lo + o, 128, D2_SBO);
-                            uint32_t d = tb + (gi == 2 ? 0u : 256u);
+                            mma_tf32(tb, dah, dbh, idesc, acc0);
+                            mma_tf32(tb, dah, dbl, idesc, 1);
+                            mma_tf32(tb, dal, dbh, idesc, 1);
+                        } else {
+                            // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
+                            const uint32_t idesc = idesc_tf32(128, 128);
+                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint32_t d = tb + 256u + 128u * par;
                             mma_tf32(d, dah, dbh, idesc, acc0);
                             mma_tf32(d, dah, dbl, idesc, 1);
                             mma_tf32(d, dal, dbh, idesc, 1);
@@ -267,23 +335,28 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
         }
     fence_after_sync();
     if (__syncthreads_or(bad)) goto done;
-    // ---- H at the stored points: D4 lane = r1, column = R ----
+    // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
     {
         const int *mT = p.mapT + (size_t)a * n2 * n1;
         const int64_t fo = p.foff[seg];
-        for (int cc = 0; cc < RB / 32; cc++) {
-            const int c0 = (RB / 2) * half + 16 * cc;
-            float v[16];
-            tmem_ld16(lrow + 256u + (uint32_t)c0, v);
-            int idx[16];
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-                int r2 = c0 + i;
-                idx[i] = (m < nn && r2 < n2) ? __ldg(mT + (size_t)r2 * n1 + m) : -1;
+        for (int cc = 0; cc < 4; cc++) {
+            const int i0 = 64 * half + 16 * cc;
+            float e[16], o[16];
+            tmem_ld16(lrow + 256u + (uint32_t)i0, e);
+            tmem_ld16(lrow + 384u + (uint32_t)i0, o);
+            int is[16], id[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                int i = i0 + u;
+                is[u] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
+                id[u] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
             }
 #pragma unroll
-            for (int i = 0; i < 16; i++)
-                if (idx[i] >= 0) p.H[fo + idx[i]] = v[i];
+            for (int u = 0; u < 16; u++) {
+                if (is[u] >= 0) p.H[fo + is[u]] = e[u] + o[u];
+                if (id[u] >= 0) p.H[fo + id[u]] = e[u] - o[u];
+            }
         }
     }
 done:
@@ -314,13 +387,13 @@ float tf32_round_nearest(float x)
     return r;
 }
 
-// one n x n DST-I matrix as K-chunks of 32: each chunk [hi plane][lo plane] of
-// rows x 32 k in the canonical K-major layout, zero padded to rows x rows
-void append_planes(std::vector<float> &out, const std::vector<double> &S, int n, int rows)
+// one n x n DST-I matrix (n <= 128) as 4 K-chunks of 32: each chunk [hi plane]
+// [lo plane] of 128 rows x 32 k in the canonical K-major layout, zero padded
+void append_planes(std::vector<float> &out, const std::vector<double> &S, int n)
 {
     size_t base = out.size();
-    const size_t plane = (size_t)rows * tc::D2_KC;
-    out.resize(base + (size_t)(rows / tc::D2_KC) * 2 * plane, 0.f);
+    const size_t plane = (size_t)128 * tc::D2_KC;
+    out.resize(base + 4 * 2 * plane, 0.f);
     for (int r = 0; r < n; r++)
         for (int k = 0; k < n; k++) {
             float x = (float)S[(size_t)r * n + k], h = tf32_round_nearest(x), l = x - h;
@@ -329,6 +402,26 @@ void append_planes(std::vector<float> &out, const std::vector<double> &S, int n,
             out[base + (size_t)c * 2 * plane + o] = h;
             out[base + (size_t)c * 2 * plane + plane + o] = l;
         }
+}
+
+// S2 (n <= 256) folded by parity: [parity][chunk][hi, lo] with element
+// (i, j) = S2[i][2j + parity] for i < ceil(n/2), zero padded to 128 x 128
+std::vector<float> s2_fold_planes(const std::vector<double> &S, int n)
+{
+    const size_t plane = (size_t)128 * tc::D2_KC;
+    std::vector<float> out((size_t)2 * tc::D2_NKH * 2 * plane, 0.f);
+    const int h = (n + 1) / 2;
+    for (int par = 0; par < 2; par++)
+        for (int i = 0; i < h; i++)
+            for (int j = 0; 2 * j + par < n; j++) {
+                float x = (float)S[(size_t)i * n + 2 * j + par], hi = tf32_round_nearest(x), lo = x - hi;
+                int c = j / tc::D2_KC, kk = j % tc::D2_KC;
+                size_t o = (size_t)((i & 7) * 16 + (i >> 3) * tc::D2_SBO + (kk & 3) * 4 + (kk >> 2) * 128) / 4;
+                size_t base = ((size_t)par * tc::D2_NKH + c) * 2 * plane;
+                out[base + o] = hi;
+                out[base + plane + o] = lo;
+            }
+    return out;
 }
 
 template <typename V>
@@ -363,8 +456,8 @@ int build_tc_dst2d(Ctx &c)
     for (auto &t : c.waves)
         for (int a = 0; a < na; a++)
             if (t.nopr1[a] > 128 || t.nopr1[a] < 1) return MW3_OK;
+    std::vector<float> fold = s2_fold_planes(dst_matrix(c.n2), c.n2);
     std::vector<float> planes;
-    append_planes(planes, dst_matrix(c.n2), c.n2, 128 * ((c.n2 + 127) / 128));
     std::map<int, int64_t> off;
     std::vector<int64_t> s1off((size_t)W * na);
     std::vector<float> p1f((size_t)W * na * c.n1), p2f((size_t)W * na * c.n2);
@@ -375,7 +468,7 @@ int build_tc_dst2d(Ctx &c)
             auto it = off.find(nn);
             if (it == off.end()) {
                 int64_t o = (int64_t)planes.size();
-                append_planes(planes, dst_matrix(nn), nn, 128);
+                append_planes(planes, dst_matrix(nn), nn);
                 it = off.emplace(nn, o).first;
             }
             s1off[(size_t)w * na + a] = it->second;
@@ -385,6 +478,7 @@ int build_tc_dst2d(Ctx &c)
     }
     int rc;
     if ((rc = upload_vec(c, &c.d_dst_planes, planes))) return rc;
+    if ((rc = upload_vec(c, &c.d_dst_s2fold, fold))) return rc;
     if ((rc = upload_vec(c, &c.d_dst_s1off, s1off))) return rc;
     if ((rc = upload_vec(c, &c.d_p2r1f, p1f))) return rc;
     if ((rc = upload_vec(c, &c.d_p2r2f, p2f))) return rc;
@@ -405,7 +499,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     if (nseg <= 0) return;
     Dst2Args p;
     p.X = X; p.H = H;
-    p.planes = c.d_dst_planes; p.s1off = c.d_dst_s1off; p.nopr1 = c.d_nopr1;
+    p.s2fold = c.d_dst_s2fold; p.s1planes = c.d_dst_planes; p.s1off = c.d_dst_s1off; p.nopr1 = c.d_nopr1;
     p.p2r1f = c.d_p2r1f; p.p2r2f = c.d_p2r2f; p.radcut = (float)c.grid.radcutmax;
     p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
