@@ -14,7 +14,7 @@
 //   D3[r1][R] = S1 (D2 o F^T)^T    A = S1 (bulk copy)      B = D2 o F^T (tensor memory)
 //   D4[r1][R] = D3 S2              A = D3 (tensor memory)  B = S2 (bulk copy)        [R folded]
 // so H[r1][R] = D4, written with lanes along r1 (stored points are r1-major runs).
-// K streams in chunks of 32 through two shared-memory stages; the DST matrices
+// K streams in chunks of 16 through four shared-memory stages; the DST matrices
 // are split on the host into TF32 hi/lo planes in the canonical K-major chunk
 // layout and arrive by one bulk (TMA) copy per chunk.  3xTF32 products with
 // FP32 accumulation as the other tensor-core kernels of the mixed path.
@@ -35,23 +35,32 @@ namespace tc {
 // i < h = ceil(n/2), y_i = E_i + O_i and y_{n-1-i} = E_i - O_i, so each is a
 // pair of 128 x 128 products over the even and the odd half of K instead of a
 // 256 x 256 one.  The products along r1 take N = nopr1 rounded up to 16.
-// Every tcgen05.ld below is executed by whole warps (its conditions depend on
-// the warp only); lane-dependent choices are made on the loaded values.
-constexpr int D2_KC = 32;
-constexpr uint32_t D2_SBO = (D2_KC / 4) * 128;    // 1 KB between 8-row groups
-constexpr uint32_t D2_SMALL = 2 * 128 * 128;      // 32 KB: hi + lo, 128 rows x 32 k
-constexpr uint32_t D2_SMALL_LO = D2_SMALL / 2;    // lo plane of a 128-row operand
-constexpr uint32_t D2_BIGMAX = 2 * 256 * 128;     // 64 KB: hi + lo, 256 rows x 32 k
-constexpr uint32_t D2_STAGE = D2_BIGMAX + D2_SMALL;
-constexpr uint32_t D2_BYTES = 2 * D2_STAGE;       // 192 KB
-constexpr int D2_NKH = 4;                         // K chunks of one parity half (j < 128)
-constexpr size_t D2_CHUNK = D2_SMALL / 4;         // floats of one 128-row chunk (hi + lo)
+//
+// Pipeline: the four products form one sequence of K chunks of 16 per slab,
+// streamed through four shared-memory stages.  The thread that issues the
+// MMAs also issues the bulk copy of each chunk's DST-matrix operand two chunks
+// ahead (across product boundaries too), so its L2 latency overlaps the fills
+// and MMAs of the chunks before it; every thread fills the register-built
+// operand of the current chunk once the MMAs that last read its stage are done.
+// Every tcgen05.ld is executed by whole warps (its conditions depend on the
+// warp only); lane-dependent choices are made on the loaded values.
+constexpr int D2_KC = 16;
+constexpr int D2_NS = 4;                                // stages
+constexpr int D2_LEAD = 2;                              // chunks a DST-matrix copy runs ahead
+constexpr uint32_t D2_SBO = (D2_KC / 4) * 128;          // 512 B between 8-row groups
+constexpr uint32_t D2_SMALL = 2 * 128 * D2_KC * 4;      // 16 KB: hi + lo, 128 rows x 16 k
+constexpr uint32_t D2_SMALL_LO = D2_SMALL / 2;          // lo plane of a 128-row operand
+constexpr uint32_t D2_BIGMAX = 2 * 256 * D2_KC * 4;     // 32 KB: hi + lo, 256 rows x 16 k
+constexpr uint32_t D2_STAGE = D2_BIGMAX + D2_SMALL;     // 48 KB
+constexpr uint32_t D2_BYTES = D2_NS * D2_STAGE;         // 192 KB
+constexpr int D2_NKH = 128 / D2_KC;                     // K chunks of a 128-wide operand
+constexpr size_t D2_CHUNK = D2_SMALL / 4;               // floats of one 128-row chunk (hi + lo)
 
 struct Dst2Args {
     const float *X;               // rectangle [G][na][n1][n2]
     float *H;                     // H psi without V, FP32
-    const float *s2fold;          // [parity][D2_NKH][hi, lo]: S2[i][2j+parity], i < 128, j chunk of 32
-    const float *s1planes;        // S1 of each length, 4 chunks of 32 columns
+    const float *s2fold;          // [parity][D2_NKH][hi, lo]: S2[i][2j+parity], i < 128, j chunk of 16
+    const float *s1planes;        // S1 of each length, D2_NKH chunks of 16 columns
     const int64_t *s1off;         // [W][na]
     const int *nopr1;             // [W][na]
     const float *p2r1f, *p2r2f;   // [W][na][n1], [W][na][n2]
@@ -73,21 +82,21 @@ __device__ __forceinline__ void d2_split4(unsigned char *hi, uint32_t lo_off, ui
     *reinterpret_cast<float4 *>(hi + lo_off + off) = l;
 }
 
-// X rows r < nn, columns 2j + parity for j in [32 jc, 32 jc + 32): each thread
-// takes four (row, 4 j) groups, reading the 8 consecutive columns that hold them;
+// X rows r < nn, columns 2j + parity for j in [16 jc, 16 jc + 16): each thread
+// takes two (row, 4 j) groups, reading the 8 consecutive columns that hold them;
 // a quarter warp covers 8 rows of one 16-byte column group (one core matrix)
 struct XStage {
-    float4 v[4][2];
+    float4 v[2][2];
     __device__ __forceinline__ static void idx(int e, int &r, int &kg)
     {
         int rest = e >> 3;
-        kg = rest & 7;
-        r = (rest >> 3) * 8 + (e & 7);
+        kg = rest & 3;
+        r = (rest >> 2) * 8 + (e & 7);
     }
     __device__ __forceinline__ void load(const float *Xs, int n2, int nn, int jc)
     {
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < 2; i++) {
             int r, kg;
             idx(threadIdx.x + 256 * i, r, kg);
             int k = 2 * (jc * D2_KC + kg * 4);          // first of the 8 columns
@@ -112,7 +121,7 @@ struct XStage {
     __device__ __forceinline__ void store(unsigned char *dst, int parity) const
     {
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < 2; i++) {
             int r, kg;
             idx(threadIdx.x + 256 * i, r, kg);
             const float4 &a = v[i][0], &b = v[i][1];
@@ -124,6 +133,18 @@ struct XStage {
     }
 };
 
+// position of chunk t of a slab's sequence: product gi and chunk c inside it
+__device__ __forceinline__ void d2_chunk(int t, int nkh, int nkr, int &gi, int &c)
+{
+    if (t < 2 * nkh) { gi = 0; c = t; return; }
+    t -= 2 * nkh;
+    if (t < nkr) { gi = 1; c = t; return; }
+    t -= nkr;
+    if (t < nkr) { gi = 2; c = t; return; }
+    gi = 3;
+    c = t - nkr;
+}
+
 // Tensor memory (512 columns):
 //   D1 = S2 Xs^T folded: E at [0,128), O at [128,256)   (lane i < h, column r1)
 //   D2 = D1 S1^T:        R tile t at [256 + 128 t)       (lane R, column r1)
@@ -133,12 +154,12 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
 {
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char *sm = smraw + ((1024 - (smem_u32(smraw) & 1023)) & 1023);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + D2_BYTES);   // [s] MMA of stage s, [2+s] its bulk copy
-    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 4);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + D2_BYTES);   // [s] MMAs of stage s, [NS+s] its bulk copy
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2 * D2_NS);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) tmem_alloc(slot, 512);
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 4; i++) mbar_init(&bars[i], 1);
+        for (int i = 0; i < 2 * D2_NS; i++) mbar_init(&bars[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before_sync();
@@ -150,11 +171,13 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
     const int nkh = (h + D2_KC - 1) / D2_KC;            // K chunks of one parity half
     const int NT = (n2 + 127) / 128;                    // R tiles of D2 and of the D3 columns
     const int RB = 128 * NT;
-    const uint32_t big_lo = (uint32_t)RB * 128;         // lo plane of an RB-row operand
+    const uint32_t big_lo = (uint32_t)RB * D2_KC * 4;   // lo plane of an RB-row operand
     const int seg = p.seg0 + blockIdx.x;
     const int g = seg / na, a = seg % na, w = p.blk_wave[g];
     const int nn = p.nopr1[w * na + a];
     const int nnp = (nn + 15) & ~15;                    // N of the products along r1
+    const int nkr = (nn + D2_KC - 1) / D2_KC;           // K chunks of the products along r1
+    const int total = 4 * nkh + 2 * nkr;
     const float *S1p = p.s1planes + p.s1off[w * na + a];
     const float *Xs = p.X + (size_t)seg * n1 * n2;
     const int q4 = warp & 3, half = warp >> 2;
@@ -164,175 +187,175 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
     const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
     const int rR = 128 * half + m;                      // the R row this thread fills in the third product
     const float e2 = (half < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
-    uint32_t ph_m[2] = {0u, 0u}, ph_c[2] = {0u, 0u};
-    bool pend[2] = {false, false};
-    bool bad = false, copy_out[2] = {false, false};
-    int q = 0;
+    // commits on each stage's MMA barrier and copies into each stage (thread 0 counts
+    // the copies; every thread counts the commits at the same program points)
+    uint32_t ncm[D2_NS] = {0u, 0u, 0u, 0u}, ncp[D2_NS] = {0u, 0u, 0u, 0u}, nwc[D2_NS] = {0u, 0u, 0u, 0u};
+    bool bad = false;
     XStage xs;
 
-    for (int gi = 0; gi < 4; gi++) {
+    // bulk copy of chunk t's DST-matrix operand (thread 0), once its stage is free
+    auto issue_copy = [&](int t) {
+        int gi, c;
+        d2_chunk(t, nkh, nkr, gi, c);
+        const int s = t % D2_NS;
+        if (ncm[s] > 0 && !mbar_wait(&bars[s], (ncm[s] - 1) & 1u)) bad = true;
+        unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
         const bool alongR = (gi == 0 || gi == 3);
-        const int nk = alongR ? 2 * nkh : (nn + D2_KC - 1) / D2_KC;
-        if (gi > 0) {                                   // the previous product must be complete
-            for (int s = 0; s < 2; s++)
-                if (pend[s]) {
-                    if (!mbar_wait(&bars[s], ph_m[s])) bad = true;
-                    ph_m[s] ^= 1u;
-                    pend[s] = false;
-                }
+        const float *src = alongR ? p.s2fold + ((size_t)(c / nkh) * D2_NKH + (c % nkh)) * D2_CHUNK
+                                  : S1p + (size_t)c * D2_CHUNK;
+        mbar_expect_tx(&bars[D2_NS + s], D2_SMALL);
+        bulk_g2s(alongR ? big : small, src, D2_SMALL, &bars[D2_NS + s]);
+        ncp[s]++;
+    };
+    if (threadIdx.x == 0)
+        for (int t = 0; t < D2_LEAD && t < total; t++) issue_copy(t);
+    xs.load(Xs, n2, nn, 0);
+
+    for (int t = 0; t < total; t++) {
+        int gi, c;
+        d2_chunk(t, nkh, nkr, gi, c);
+        const int s = t % D2_NS;
+        const int par = (gi == 0 || gi == 3) ? c / nkh : 0, jc = (gi == 0 || gi == 3) ? c % nkh : c;
+        unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
+        if (c == 0 && gi > 0) {
+            // the previous product's result is read from tensor memory: its last chunk
+            // (the latest commit overall) must be complete
+            const int sp = (t - 1) % D2_NS;
+            if (!mbar_wait(&bars[sp], (ncm[sp] - 1) & 1u)) bad = true;
             fence_after_sync();
-        } else {
-            xs.load(Xs, n2, nn, 0);
         }
-        for (int c = 0; c < nk; c++, q++) {
-            const int s = q & 1;
-            const int par = alongR ? c / nkh : 0, jc = alongR ? c % nkh : c;
-            unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
-            if (pend[s]) {                              // stage s is free once its MMAs are done
-                if (!mbar_wait(&bars[s], ph_m[s])) bad = true;
-                ph_m[s] ^= 1u;
-                pend[s] = false;
-                fence_after_sync();
-            }
-            if (threadIdx.x == 0) {
-                // the DST operand: folded S2 into the big slot (products 1, 4), S1 into the small slot
-                const float *src = alongR ? p.s2fold + ((size_t)par * D2_NKH + jc) * D2_CHUNK
-                                          : S1p + (size_t)c * D2_CHUNK;
-                mbar_expect_tx(&bars[2 + s], D2_SMALL);
-                bulk_g2s(alongR ? big : small, src, D2_SMALL, &bars[2 + s]);
-                copy_out[s] = true;
-            }
-            if (gi == 0) {
-                // B = Xs columns of this parity (rows r1) into the small slot
-                xs.store(small, par);
-                if (c + 1 < nk) xs.load(Xs, n2, nn, (c + 1) % nkh);
-            } else if (gi == 1) {
-                // A = D1 rows R into the big slot: half 0 the sum rows R = i, half 1 the
-                // difference rows R = n2-1-i, from the E and O columns of lane i (all lanes
-                // load; lanes without a row store nothing)
-                float e[32], o[32];
-                tmem_ld32(lrow + (uint32_t)(c * D2_KC), e);
-                tmem_ld32(lrow + 128u + (uint32_t)(c * D2_KC), o);
-                const bool on = half == 0 ? (m < h) : (m < n2 - h);
-                if (on) {
-                    const int R = half == 0 ? m : n2 - 1 - m;
-                    const float sg = half == 0 ? 1.f : -1.f;
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        float t[4];
-#pragma unroll
-                        for (int u = 0; u < 4; u++) {
-                            int k = c * D2_KC + 4 * j + u;
-                            t[u] = k < nn ? e[4 * j + u] + sg * o[4 * j + u] : 0.f;
-                        }
-                        d2_split4(big, big_lo, kmaj_off(R, 4 * j, D2_KC), t[0], t[1], t[2], t[3]);
-                    }
-                }
-            } else if (gi == 2) {
-                // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
-                if (half < NT) {
-                    float v[32];
-                    tmem_ld32(lrow + 256u + 128u * half + (uint32_t)(c * D2_KC), v);
-#pragma unroll
-                    for (int i = 0; i < 32; i++) {
-                        int k = c * D2_KC + i;
-                        float x = 0.f;
-                        if (k < nn && rR < n2) {
-                            float ek = __ldg(p1f + k) + e2;
-                            if (ek > p.radcut) ek = p.radcut;
-                            x = v[i] * ek * divi;
-                        }
-                        v[i] = x;
-                    }
-#pragma unroll
-                    for (int j = 0; j < 8; j++)
-                        d2_split4(big, big_lo, kmaj_off(rR, 4 * j, D2_KC), v[4 * j], v[4 * j + 1], v[4 * j + 2],
-                                  v[4 * j + 3]);
-                }
-            } else {
-                // A = D3 columns 2j + parity (rows r1) into the small slot; each warp half
-                // reads 32 consecutive columns and keeps the 16 of this parity
-                float v[32];
-                const int col0 = 2 * (jc * D2_KC) + 32 * half;
-                tmem_ld32(lrow + (uint32_t)col0, v);
+        if (ncm[s] > 0) {                               // the MMAs of chunk t - NS read this stage
+            if (!mbar_wait(&bars[s], (ncm[s] - 1) & 1u)) bad = true;
+            fence_after_sync();
+        }
+        if (gi == 0) {
+            // B = Xs columns of this parity (rows r1) into the small slot
+            xs.store(small, par);
+            if (c + 1 < 2 * nkh) xs.load(Xs, n2, nn, (c + 1) % nkh);
+        } else if (gi == 1) {
+            // A = D1 rows R into the big slot: half 0 the sum rows R = i, half 1 the
+            // difference rows R = n2-1-i, from the E and O columns of lane i (all lanes
+            // load; lanes without a row store nothing)
+            float e[16], o[16];
+            tmem_ld16(lrow + (uint32_t)(c * D2_KC), e);
+            tmem_ld16(lrow + 128u + (uint32_t)(c * D2_KC), o);
+            const bool on = half == 0 ? (m < h) : (m < n2 - h);
+            if (on) {
+                const int R = half == 0 ? m : n2 - 1 - m;
+                const float sg = half == 0 ? 1.f : -1.f;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    float t[4];
+                    float tv[4];
 #pragma unroll
                     for (int u = 0; u < 4; u++) {
-                        int cc = 2 * (4 * j + u);          // register index fixed at compile time
-                        float x = par == 0 ? v[cc] : v[cc + 1];
-                        t[u] = (col0 + cc + par < n2) ? x : 0.f;
+                        int k = c * D2_KC + 4 * j + u;
+                        tv[u] = k < nn ? e[4 * j + u] + sg * o[4 * j + u] : 0.f;
                     }
-                    d2_split4(small, D2_SMALL_LO, kmaj_off(m, 16 * half + 4 * j, D2_KC), t[0], t[1], t[2], t[3]);
+                    d2_split4(big, big_lo, kmaj_off(R, 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
                 }
             }
-            fence_async_smem();
-            fence_before_sync();
-            if (__syncthreads_or(bad)) goto done;
-            if (threadIdx.x == 0) {
-                if (!mbar_wait(&bars[2 + s], ph_c[s])) bad = true;
-                copy_out[s] = false;
-                fence_after_sync();
-                if (!bad) {
-                    const uint32_t bg = smem_u32(big), sl = smem_u32(small);
+        } else if (gi == 2) {
+            // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
+            if (half < NT) {
+                float v[16];
+                tmem_ld16(lrow + 256u + 128u * half + (uint32_t)(c * D2_KC), v);
 #pragma unroll
-                    for (int ks = 0; ks < D2_KC / 8; ks++) {
-                        const uint32_t o = ks * 256;
-                        const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
-                        if (gi == 0) {
-                            // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
-                            const uint32_t idesc = idesc_tf32(128, nnp);
-                            uint64_t dah = sdesc(bg + o, 128, D2_SBO), dal = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint32_t d = tb + 128u * par;
-                            mma_tf32(d, dah, dbh, idesc, acc0);
-                            mma_tf32(d, dah, dbl, idesc, 1);
-                            mma_tf32(d, dal, dbh, idesc, 1);
-                        } else if (gi == 1) {
-                            // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
-                            const uint32_t idesc = idesc_tf32(128, nnp);
-                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                            for (int t = 0; t < NT; t++) {
-                                uint32_t at = bg + (uint32_t)t * 16 * D2_SBO;
-                                uint64_t dah = sdesc(at + o, 128, D2_SBO), dal = sdesc(at + big_lo + o, 128, D2_SBO);
-                                uint32_t d = tb + 256u + 128u * t;
-                                mma_tf32(d, dah, dbh, idesc, acc0);
-                                mma_tf32(d, dah, dbl, idesc, 1);
-                                mma_tf32(d, dal, dbh, idesc, 1);
-                            }
-                        } else if (gi == 2) {
-                            // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
-                            const uint32_t idesc = idesc_tf32(128, RB);
-                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + big_lo + o, 128, D2_SBO);
-                            mma_tf32(tb, dah, dbh, idesc, acc0);
-                            mma_tf32(tb, dah, dbl, idesc, 1);
-                            mma_tf32(tb, dal, dbh, idesc, 1);
-                        } else {
-                            // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
-                            const uint32_t idesc = idesc_tf32(128, 128);
-                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint32_t d = tb + 256u + 128u * par;
+                for (int i = 0; i < 16; i++) {
+                    int k = c * D2_KC + i;
+                    float x = 0.f;
+                    if (k < nn && rR < n2) {
+                        float ek = __ldg(p1f + k) + e2;
+                        if (ek > p.radcut) ek = p.radcut;
+                        x = v[i] * ek * divi;
+                    }
+                    v[i] = x;
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    d2_split4(big, big_lo, kmaj_off(rR, 4 * j, D2_KC), v[4 * j], v[4 * j + 1], v[4 * j + 2],
+                              v[4 * j + 3]);
+            }
+        } else {
+            // A = D3 columns 2j + parity (rows r1) into the small slot; each warp half
+            // reads 16 consecutive columns and keeps the 8 of this parity
+            float v[16];
+            const int col0 = 2 * (jc * D2_KC) + 16 * half;
+            tmem_ld16(lrow + (uint32_t)col0, v);
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                float tv[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    int cc = 2 * (4 * j + u);              // register index fixed at compile time
+                    float x = par == 0 ? v[cc] : v[cc + 1];
+                    tv[u] = (col0 + cc + par < n2) ? x : 0.f;
+                }
+                d2_split4(small, D2_SMALL_LO, kmaj_off(m, 8 * half + 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
+            }
+        }
+        fence_async_smem();
+        fence_before_sync();
+        if (__syncthreads_or(bad)) goto done;
+        if (threadIdx.x == 0) {
+            if (!mbar_wait(&bars[D2_NS + s], (ncp[s] - 1) & 1u)) bad = true;
+            nwc[s] = ncp[s];
+            fence_after_sync();
+            if (!bad) {
+                const uint32_t bg = smem_u32(big), sl = smem_u32(small);
+#pragma unroll
+                for (int ks = 0; ks < D2_KC / 8; ks++) {
+                    const uint32_t o = ks * 256;
+                    const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
+                    if (gi == 0) {
+                        // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
+                        const uint32_t idesc = idesc_tf32(128, nnp);
+                        uint64_t dah = sdesc(bg + o, 128, D2_SBO), dal = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
+                        uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                        uint32_t d = tb + 128u * par;
+                        mma_tf32(d, dah, dbh, idesc, acc0);
+                        mma_tf32(d, dah, dbl, idesc, 1);
+                        mma_tf32(d, dal, dbh, idesc, 1);
+                    } else if (gi == 1) {
+                        // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
+                        const uint32_t idesc = idesc_tf32(128, nnp);
+                        uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                        for (int tt = 0; tt < NT; tt++) {
+                            uint32_t at = bg + (uint32_t)tt * 16 * D2_SBO;
+                            uint64_t dah = sdesc(at + o, 128, D2_SBO), dal = sdesc(at + big_lo + o, 128, D2_SBO);
+                            uint32_t d = tb + 256u + 128u * tt;
                             mma_tf32(d, dah, dbh, idesc, acc0);
                             mma_tf32(d, dah, dbl, idesc, 1);
                             mma_tf32(d, dal, dbh, idesc, 1);
                         }
+                    } else if (gi == 2) {
+                        // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
+                        const uint32_t idesc = idesc_tf32(128, RB);
+                        uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                        uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + big_lo + o, 128, D2_SBO);
+                        mma_tf32(tb, dah, dbh, idesc, acc0);
+                        mma_tf32(tb, dah, dbl, idesc, 1);
+                        mma_tf32(tb, dal, dbh, idesc, 1);
+                    } else {
+                        // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
+                        const uint32_t idesc = idesc_tf32(128, 128);
+                        uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                        uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
+                        uint32_t d = tb + 256u + 128u * par;
+                        mma_tf32(d, dah, dbh, idesc, acc0);
+                        mma_tf32(d, dah, dbl, idesc, 1);
+                        mma_tf32(d, dal, dbh, idesc, 1);
                     }
                 }
-                mma_commit(&bars[s]);
             }
-            ph_c[s] ^= 1u;
-            pend[s] = true;
+            mma_commit(&bars[s]);
         }
+        ncm[s]++;
+        if (threadIdx.x == 0 && t + D2_LEAD < total) issue_copy(t + D2_LEAD);
     }
-    for (int s = 0; s < 2; s++)
-        if (pend[s]) {
-            if (!mbar_wait(&bars[s], ph_m[s])) bad = true;
-            ph_m[s] ^= 1u;
-            pend[s] = false;
-        }
+    {
+        const int sp = (total - 1) % D2_NS;             // the last commit tracks every MMA
+        if (!mbar_wait(&bars[sp], (ncm[sp] - 1) & 1u)) bad = true;
+    }
     fence_after_sync();
     if (__syncthreads_or(bad)) goto done;
     // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
@@ -362,12 +385,12 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
 done:
     if (bad && threadIdx.x == 0) atomicExch(p.err, 1);
     if (threadIdx.x == 0) {
-        // a bulk copy issued before a failed wait must land before the CTA exits
-        for (int s = 0; s < 2; s++)
-            if (copy_out[s]) mbar_wait(&bars[2 + s], ph_c[s]);
+        // bulk copies issued but not waited for must land before the CTA exits
+        for (int s = 0; s < D2_NS; s++)
+            if (ncp[s] > nwc[s]) mbar_wait(&bars[D2_NS + s], (ncp[s] - 1) & 1u);
     }
-    for (int s = 0; s < 2; s++)
-        if (pend[s]) mbar_wait(&bars[s], ph_m[s]);
+    for (int s = 0; s < D2_NS; s++)
+        if (ncm[s] > 0) mbar_wait(&bars[s], (ncm[s] - 1) & 1u);
     fence_before_sync();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tb, 512);
@@ -387,13 +410,13 @@ float tf32_round_nearest(float x)
     return r;
 }
 
-// one n x n DST-I matrix (n <= 128) as 4 K-chunks of 32: each chunk [hi plane]
-// [lo plane] of 128 rows x 32 k in the canonical K-major layout, zero padded
+// one n x n DST-I matrix (n <= 128) as K-chunks: each chunk [hi plane][lo plane]
+// of 128 rows x D2_KC k in the canonical K-major layout, zero padded
 void append_planes(std::vector<float> &out, const std::vector<double> &S, int n)
 {
     size_t base = out.size();
     const size_t plane = (size_t)128 * tc::D2_KC;
-    out.resize(base + 4 * 2 * plane, 0.f);
+    out.resize(base + (size_t)tc::D2_NKH * 2 * plane, 0.f);
     for (int r = 0; r < n; r++)
         for (int k = 0; k < n; k++) {
             float x = (float)S[(size_t)r * n + k], h = tf32_round_nearest(x), l = x - h;
@@ -490,7 +513,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    const size_t smem = D2_BYTES + 64 + 1024;
+    const size_t smem = D2_BYTES + 128 + 1024;
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
