@@ -475,36 +475,14 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
         pk[k] = on ? pkp[ir] : 0.0;
         p1[k] = on && !u.first ? pm1[ir] : 0.0;
     }
-    // mixed path: absorber factors and the V sum of every point of the thread
-    // before any store, so their loads are in flight together
-    double a1[U], a2[U], acc[U];
-    bool damp[U];
-    if (sizeof(T) == 4) {
+    if (sizeof(T) == 8) {
+        for (int q = 0; q < nsrc; q++) {
+            const double *vr = s_vrow[q], *pr = s_prow[q];
 #pragma unroll
-        for (int k = 0; k < U; k++) {
-            a1[k] = ab1[r1[k]];
-            a2[k] = ab2[r2[k]];
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            damp[k] = !u.first && !(__double_as_longlong(a1[k]) == 0x3FF0000000000000LL &&
-                                    __double_as_longlong(a2[k]) == 0x3FF0000000000000LL);
-            acc[k] = (u.first || damp[k]) ? 0.0 : -p1[k];
-        }
-    }
-    for (int q = 0; q < nsrc; q++) {
-        const double *vr = s_vrow[q], *pr = s_prow[q];
-        double vv[U], pp[U];
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            int ir = ir0 + k * 256;
-            vv[k] = ir < n ? vr[ir] : 0.0;
-            pp[k] = ir < n ? pr[ir] : 0.0;
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            if (sizeof(T) == 8) hv[k] += pp[k] * vv[k];
-            else acc[k] = fma(vv[k], pp[k], acc[k]);
+            for (int k = 0; k < U; k++) {
+                int ir = ir0 + k * 256;
+                if (ir < n) hv[k] += pr[ir] * vr[ir];
+            }
         }
     }
     float nrmf = 0.f;
@@ -529,11 +507,15 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             //   t = H 2/delta2 + sum_s vr_s psi_s = 2 (H psi - emindlt psi) / delta2
             // with the potential pre-scaled, damping only inside the absorbers,
             // the FP32 copy rounded with integer operations, the norm partial in FP32
-            double t = fma(hv[k], u.r2delta, acc[k]);
+            const bool damp = !u.first && !(__double_as_longlong(ab1[r1[k]]) == 0x3FF0000000000000LL &&
+                                            __double_as_longlong(ab2[r2[k]]) == 0x3FF0000000000000LL);
+            double acc = (u.first || damp) ? 0.0 : -p1[k];
+            for (int q = 0; q < nsrc; q++) acc = fma(s_vrow[q][ir], s_prow[q][ir], acc);
+            double t = fma(hv[k], u.r2delta, acc);
             if (u.first) {
                 nv = 0.5 * t;
-            } else if (damp[k]) {
-                double fab = a1[k] * a2[k];
+            } else if (damp) {
+                double fab = ab1[r1[k]] * ab2[r2[k]];
                 nv = fma(-fab, p1[k], t) * fab;
             } else {
                 nv = t;
