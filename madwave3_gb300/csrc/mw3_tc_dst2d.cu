@@ -37,16 +37,11 @@ namespace tc {
 // 256 x 256 one.  The products along r1 take N = nopr1 rounded up to 16.
 //
 // Pipeline: the four products form one sequence of K chunks of 16 per slab,
-// streamed through four shared-memory stages.  The thread that issues the
-// MMAs also issues the bulk copy of each chunk's DST-matrix operand two chunks
-// ahead (across product boundaries too), so its L2 latency overlaps the fills
-// and MMAs of the chunks before it; every thread fills the register-built
-// operand of the current chunk once the MMAs that last read its stage are done.
+// streamed through four shared-memory stages by three warp roles (below).
 // Every tcgen05.ld is executed by whole warps (its conditions depend on the
 // warp only); lane-dependent choices are made on the loaded values.
 constexpr int D2_KC = 16;
 constexpr int D2_NS = 4;                                // stages
-constexpr int D2_LEAD = 2;                              // chunks a DST-matrix copy runs ahead
 constexpr uint32_t D2_SBO = (D2_KC / 4) * 128;          // 512 B between 8-row groups
 constexpr uint32_t D2_SMALL = 2 * 128 * D2_KC * 4;      // 16 KB: hi + lo, 128 rows x 16 k
 constexpr uint32_t D2_SMALL_LO = D2_SMALL / 2;          // lo plane of a 128-row operand
@@ -150,16 +145,49 @@ __device__ __forceinline__ void d2_chunk(int t, int nkh, int nkr, int &gi, int &
 //   D2 = D1 S1^T:        R tile t at [256 + 128 t)       (lane R, column r1)
 //   D3 = S1 (D2 o F^T)^T at [0, 256)                     (lane r1, column R)
 //   D4 = D3 S2 folded:   E at [256,384), O at [384,512)  (lane r1, column i < h)
-__global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
+//
+// Warp roles (320 threads): warps 0-7 build the register-side operand of each
+// chunk (two warps per 32-lane quarter of tensor memory) and write H; warp 8
+// issues the MMAs; warp 9 issues the bulk copies of the DST-matrix operands.
+// They meet only at per-stage mbarriers: copy_full (bytes landed), fill_full
+// (8 fill-warp arrivals) and empty (the MMAs that read the stage completed).
+// Chunk t uses stage t % NS for the (t / NS)-th time, so every wait names the
+// phase parity (t / NS) & 1; no role can run a full phase ahead of a waiter.
+// After any wait runs out of time the CTA's shared failure flag makes every
+// later wait return at once, so a fault ends the kernel instead of hanging it.
+constexpr int D2_WARPS = 10;
+
+__device__ __forceinline__ void mbar_arrive1(uint64_t *mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" : : "r"(smem_u32(mbar)) : "memory");
+}
+
+__device__ __forceinline__ bool d2_wait(uint64_t *mbar, uint32_t parity, volatile int *fail)
+{
+    if (*fail) return false;
+    if (mbar_wait(mbar, parity)) return true;
+    *fail = 1;
+    return false;
+}
+
+__global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
 {
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char *sm = smraw + ((1024 - (smem_u32(smraw) & 1023)) & 1023);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + D2_BYTES);   // [s] MMAs of stage s, [NS+s] its bulk copy
-    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2 * D2_NS);
+    uint64_t *copy_full = reinterpret_cast<uint64_t *>(sm + D2_BYTES);
+    uint64_t *fill_full = copy_full + D2_NS;
+    uint64_t *empty = fill_full + D2_NS;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(empty + D2_NS);
+    volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) tmem_alloc(slot, 512);
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 2 * D2_NS; i++) mbar_init(&bars[i], 1);
+        for (int i = 0; i < D2_NS; i++) {
+            mbar_init(&copy_full[i], 1);
+            mbar_init(&fill_full[i], 8);
+            mbar_init(&empty[i], 1);
+        }
+        *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before_sync();
@@ -179,220 +207,220 @@ __global__ void __launch_bounds__(256, 1) k_tc_dst2d(Dst2Args p)
     const int nkr = (nn + D2_KC - 1) / D2_KC;           // K chunks of the products along r1
     const int total = 4 * nkh + 2 * nkr;
     const float *S1p = p.s1planes + p.s1off[w * na + a];
-    const float *Xs = p.X + (size_t)seg * n1 * n2;
-    const int q4 = warp & 3, half = warp >> 2;
-    const int m = q4 * 32 + lane;                       // the tensor-memory lane this thread reads
-    const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
-    const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
-    const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
-    const int rR = 128 * half + m;                      // the R row this thread fills in the third product
-    const float e2 = (half < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
-    // commits on each stage's MMA barrier and copies into each stage (thread 0 counts
-    // the copies; every thread counts the commits at the same program points)
-    uint32_t ncm[D2_NS] = {0u, 0u, 0u, 0u}, ncp[D2_NS] = {0u, 0u, 0u, 0u}, nwc[D2_NS] = {0u, 0u, 0u, 0u};
-    bool bad = false;
-    XStage xs;
 
-    // bulk copy of chunk t's DST-matrix operand (thread 0), once its stage is free
-    auto issue_copy = [&](int t) {
-        int gi, c;
-        d2_chunk(t, nkh, nkr, gi, c);
-        const int s = t % D2_NS;
-        if (ncm[s] > 0 && !mbar_wait(&bars[s], (ncm[s] - 1) & 1u)) bad = true;
-        unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
-        const bool alongR = (gi == 0 || gi == 3);
-        const float *src = alongR ? p.s2fold + ((size_t)(c / nkh) * D2_NKH + (c % nkh)) * D2_CHUNK
-                                  : S1p + (size_t)c * D2_CHUNK;
-        mbar_expect_tx(&bars[D2_NS + s], D2_SMALL);
-        bulk_g2s(alongR ? big : small, src, D2_SMALL, &bars[D2_NS + s]);
-        ncp[s]++;
-    };
-    if (threadIdx.x == 0)
-        for (int t = 0; t < D2_LEAD && t < total; t++) issue_copy(t);
-    xs.load(Xs, n2, nn, 0);
-
-    for (int t = 0; t < total; t++) {
-        int gi, c;
-        d2_chunk(t, nkh, nkr, gi, c);
-        const int s = t % D2_NS;
-        const int par = (gi == 0 || gi == 3) ? c / nkh : 0, jc = (gi == 0 || gi == 3) ? c % nkh : c;
-        unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
-        if (c == 0 && gi > 0) {
-            // the previous product's result is read from tensor memory: its last chunk
-            // (the latest commit overall) must be complete
-            const int sp = (t - 1) % D2_NS;
-            if (!mbar_wait(&bars[sp], (ncm[sp] - 1) & 1u)) bad = true;
-            fence_after_sync();
-        }
-        if (ncm[s] > 0) {                               // the MMAs of chunk t - NS read this stage
-            if (!mbar_wait(&bars[s], (ncm[s] - 1) & 1u)) bad = true;
-            fence_after_sync();
-        }
-        if (gi == 0) {
-            // B = Xs columns of this parity (rows r1) into the small slot
-            xs.store(small, par);
-            if (c + 1 < 2 * nkh) xs.load(Xs, n2, nn, (c + 1) % nkh);
-        } else if (gi == 1) {
-            // A = D1 rows R into the big slot: half 0 the sum rows R = i, half 1 the
-            // difference rows R = n2-1-i, from the E and O columns of lane i (all lanes
-            // load; lanes without a row store nothing)
-            float e[16], o[16];
-            tmem_ld16(lrow + (uint32_t)(c * D2_KC), e);
-            tmem_ld16(lrow + 128u + (uint32_t)(c * D2_KC), o);
-            const bool on = half == 0 ? (m < h) : (m < n2 - h);
-            if (on) {
-                const int R = half == 0 ? m : n2 - 1 - m;
-                const float sg = half == 0 ? 1.f : -1.f;
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    float tv[4];
-#pragma unroll
-                    for (int u = 0; u < 4; u++) {
-                        int k = c * D2_KC + 4 * j + u;
-                        tv[u] = k < nn ? e[4 * j + u] + sg * o[4 * j + u] : 0.f;
-                    }
-                    d2_split4(big, big_lo, kmaj_off(R, 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
-                }
+    int copies = 0;                                     // copies issued (warp 9, lane 0)
+    if (warp == 9) {
+        // ---- bulk copies of the DST-matrix operands ----
+        if (lane == 0)
+            for (int t = 0; t < total && !*fail; t++) {
+                const int s = t % D2_NS, u = t / D2_NS;
+                if (t >= D2_NS && !d2_wait(&empty[s], (u - 1) & 1, fail)) break;
+                int gi, c;
+                d2_chunk(t, nkh, nkr, gi, c);
+                unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
+                const bool alongR = (gi == 0 || gi == 3);
+                const float *src = alongR ? p.s2fold + ((size_t)(c / nkh) * D2_NKH + (c % nkh)) * D2_CHUNK
+                                          : S1p + (size_t)c * D2_CHUNK;
+                mbar_expect_tx(&copy_full[s], D2_SMALL);
+                bulk_g2s(alongR ? big : small, src, D2_SMALL, &copy_full[s]);
+                copies = t + 1;
             }
-        } else if (gi == 2) {
-            // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
-            if (half < NT) {
-                float v[16];
-                tmem_ld16(lrow + 256u + 128u * half + (uint32_t)(c * D2_KC), v);
+    } else if (warp == 8) {
+        // ---- MMA issue ----
+        if (lane == 0) {
+            for (int t = 0; t < total; t++) {
+                const int s = t % D2_NS, u = t / D2_NS;
+                d2_wait(&copy_full[s], u & 1, fail);
+                d2_wait(&fill_full[s], u & 1, fail);
+                fence_after_sync();
+                int gi, c;
+                d2_chunk(t, nkh, nkr, gi, c);
+                const int par = (gi == 0 || gi == 3) ? c / nkh : 0, jc = (gi == 0 || gi == 3) ? c % nkh : c;
+                unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
+                if (!*fail) {
+                    const uint32_t bg = smem_u32(big), sl = smem_u32(small);
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    int k = c * D2_KC + i;
-                    float x = 0.f;
-                    if (k < nn && rR < n2) {
-                        float ek = __ldg(p1f + k) + e2;
-                        if (ek > p.radcut) ek = p.radcut;
-                        x = v[i] * ek * divi;
-                    }
-                    v[i] = x;
-                }
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                    d2_split4(big, big_lo, kmaj_off(rR, 4 * j, D2_KC), v[4 * j], v[4 * j + 1], v[4 * j + 2],
-                              v[4 * j + 3]);
-            }
-        } else {
-            // A = D3 columns 2j + parity (rows r1) into the small slot; each warp half
-            // reads 16 consecutive columns and keeps the 8 of this parity
-            float v[16];
-            const int col0 = 2 * (jc * D2_KC) + 16 * half;
-            tmem_ld16(lrow + (uint32_t)col0, v);
-#pragma unroll
-            for (int j = 0; j < 2; j++) {
-                float tv[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    int cc = 2 * (4 * j + u);              // register index fixed at compile time
-                    float x = par == 0 ? v[cc] : v[cc + 1];
-                    tv[u] = (col0 + cc + par < n2) ? x : 0.f;
-                }
-                d2_split4(small, D2_SMALL_LO, kmaj_off(m, 8 * half + 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
-            }
-        }
-        fence_async_smem();
-        fence_before_sync();
-        if (__syncthreads_or(bad)) goto done;
-        if (threadIdx.x == 0) {
-            if (!mbar_wait(&bars[D2_NS + s], (ncp[s] - 1) & 1u)) bad = true;
-            nwc[s] = ncp[s];
-            fence_after_sync();
-            if (!bad) {
-                const uint32_t bg = smem_u32(big), sl = smem_u32(small);
-#pragma unroll
-                for (int ks = 0; ks < D2_KC / 8; ks++) {
-                    const uint32_t o = ks * 256;
-                    const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
-                    if (gi == 0) {
-                        // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
-                        const uint32_t idesc = idesc_tf32(128, nnp);
-                        uint64_t dah = sdesc(bg + o, 128, D2_SBO), dal = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
-                        uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                        uint32_t d = tb + 128u * par;
-                        mma_tf32(d, dah, dbh, idesc, acc0);
-                        mma_tf32(d, dah, dbl, idesc, 1);
-                        mma_tf32(d, dal, dbh, idesc, 1);
-                    } else if (gi == 1) {
-                        // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
-                        const uint32_t idesc = idesc_tf32(128, nnp);
-                        uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                        for (int tt = 0; tt < NT; tt++) {
-                            uint32_t at = bg + (uint32_t)tt * 16 * D2_SBO;
-                            uint64_t dah = sdesc(at + o, 128, D2_SBO), dal = sdesc(at + big_lo + o, 128, D2_SBO);
-                            uint32_t d = tb + 256u + 128u * tt;
+                    for (int ks = 0; ks < D2_KC / 8; ks++) {
+                        const uint32_t o = ks * 256;
+                        const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
+                        if (gi == 0) {
+                            // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
+                            const uint32_t idesc = idesc_tf32(128, nnp);
+                            uint64_t dah = sdesc(bg + o, 128, D2_SBO), dal = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint32_t d = tb + 128u * par;
+                            mma_tf32(d, dah, dbh, idesc, acc0);
+                            mma_tf32(d, dah, dbl, idesc, 1);
+                            mma_tf32(d, dal, dbh, idesc, 1);
+                        } else if (gi == 1) {
+                            // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
+                            const uint32_t idesc = idesc_tf32(128, nnp);
+                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                            for (int tt = 0; tt < NT; tt++) {
+                                uint32_t at = bg + (uint32_t)tt * 16 * D2_SBO;
+                                uint64_t dah = sdesc(at + o, 128, D2_SBO), dal = sdesc(at + big_lo + o, 128, D2_SBO);
+                                uint32_t d = tb + 256u + 128u * tt;
+                                mma_tf32(d, dah, dbh, idesc, acc0);
+                                mma_tf32(d, dah, dbl, idesc, 1);
+                                mma_tf32(d, dal, dbh, idesc, 1);
+                            }
+                        } else if (gi == 2) {
+                            // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
+                            const uint32_t idesc = idesc_tf32(128, RB);
+                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + big_lo + o, 128, D2_SBO);
+                            mma_tf32(tb, dah, dbh, idesc, acc0);
+                            mma_tf32(tb, dah, dbl, idesc, 1);
+                            mma_tf32(tb, dal, dbh, idesc, 1);
+                        } else {
+                            // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
+                            const uint32_t idesc = idesc_tf32(128, 128);
+                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
+                            uint32_t d = tb + 256u + 128u * par;
                             mma_tf32(d, dah, dbh, idesc, acc0);
                             mma_tf32(d, dah, dbl, idesc, 1);
                             mma_tf32(d, dal, dbh, idesc, 1);
                         }
-                    } else if (gi == 2) {
-                        // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
-                        const uint32_t idesc = idesc_tf32(128, RB);
-                        uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                        uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + big_lo + o, 128, D2_SBO);
-                        mma_tf32(tb, dah, dbh, idesc, acc0);
-                        mma_tf32(tb, dah, dbl, idesc, 1);
-                        mma_tf32(tb, dal, dbh, idesc, 1);
-                    } else {
-                        // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
-                        const uint32_t idesc = idesc_tf32(128, 128);
-                        uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                        uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
-                        uint32_t d = tb + 256u + 128u * par;
-                        mma_tf32(d, dah, dbh, idesc, acc0);
-                        mma_tf32(d, dah, dbl, idesc, 1);
-                        mma_tf32(d, dal, dbh, idesc, 1);
                     }
                 }
-            }
-            mma_commit(&bars[s]);
-        }
-        ncm[s]++;
-        if (threadIdx.x == 0 && t + D2_LEAD < total) issue_copy(t + D2_LEAD);
-    }
-    {
-        const int sp = (total - 1) % D2_NS;             // the last commit tracks every MMA
-        if (!mbar_wait(&bars[sp], (ncm[sp] - 1) & 1u)) bad = true;
-    }
-    fence_after_sync();
-    if (__syncthreads_or(bad)) goto done;
-    // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
-    {
-        const int *mT = p.mapT + (size_t)a * n2 * n1;
-        const int64_t fo = p.foff[seg];
-#pragma unroll
-        for (int cc = 0; cc < 4; cc++) {
-            const int i0 = 64 * half + 16 * cc;
-            float e[16], o[16];
-            tmem_ld16(lrow + 256u + (uint32_t)i0, e);
-            tmem_ld16(lrow + 384u + (uint32_t)i0, o);
-            int is[16], id[16];
-#pragma unroll
-            for (int u = 0; u < 16; u++) {
-                int i = i0 + u;
-                is[u] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
-                id[u] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
-            }
-#pragma unroll
-            for (int u = 0; u < 16; u++) {
-                if (is[u] >= 0) p.H[fo + is[u]] = e[u] + o[u];
-                if (id[u] >= 0) p.H[fo + id[u]] = e[u] - o[u];
+                mma_commit(&empty[s]);        // also after a failure, so no waiter is left behind
             }
         }
+    } else {
+        // ---- operand fills (warps 0-7) and the H epilogue ----
+        const float *Xs = p.X + (size_t)seg * n1 * n2;
+        const int q4 = warp & 3, half = warp >> 2;
+        const int m = q4 * 32 + lane;                   // the tensor-memory lane this thread reads
+        const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
+        const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
+        const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
+        const int rR = 128 * half + m;                  // the R row this thread fills in the third product
+        const float e2 = (half < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
+        XStage xs;
+        xs.load(Xs, n2, nn, 0);
+        for (int t = 0; t < total; t++) {
+            int gi, c;
+            d2_chunk(t, nkh, nkr, gi, c);
+            const int s = t % D2_NS, u = t / D2_NS;
+            const int par = (gi == 0 || gi == 3) ? c / nkh : 0, jc = (gi == 0 || gi == 3) ? c % nkh : c;
+            unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
+            if (c == 0 && gi > 0) {
+                // this product reads the previous one from tensor memory: its last chunk done
+                d2_wait(&empty[(t - 1) % D2_NS], ((t - 1) / D2_NS) & 1, fail);
+                fence_after_sync();
+            }
+            if (t >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
+            if (gi == 0) {
+                // B = Xs columns of this parity (rows r1) into the small slot
+                xs.store(small, par);
+                if (c + 1 < 2 * nkh) xs.load(Xs, n2, nn, (c + 1) % nkh);
+            } else if (gi == 1) {
+                // A = D1 rows R into the big slot: half 0 the sum rows R = i, half 1 the
+                // difference rows R = n2-1-i, from the E and O columns of lane i (all lanes
+                // load; lanes without a row store nothing)
+                float e[16], o[16];
+                tmem_ld16(lrow + (uint32_t)(c * D2_KC), e);
+                tmem_ld16(lrow + 128u + (uint32_t)(c * D2_KC), o);
+                const bool on = half == 0 ? (m < h) : (m < n2 - h);
+                if (on) {
+                    const int R = half == 0 ? m : n2 - 1 - m;
+                    const float sg = half == 0 ? 1.f : -1.f;
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        float tv[4];
+#pragma unroll
+                        for (int uu = 0; uu < 4; uu++) {
+                            int k = c * D2_KC + 4 * j + uu;
+                            tv[uu] = k < nn ? e[4 * j + uu] + sg * o[4 * j + uu] : 0.f;
+                        }
+                        d2_split4(big, big_lo, kmaj_off(R, 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
+                    }
+                }
+            } else if (gi == 2) {
+                // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
+                if (half < NT) {
+                    float v[16];
+                    tmem_ld16(lrow + 256u + 128u * half + (uint32_t)(c * D2_KC), v);
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        int k = c * D2_KC + i;
+                        float x = 0.f;
+                        if (k < nn && rR < n2) {
+                            float ek = __ldg(p1f + k) + e2;
+                            if (ek > p.radcut) ek = p.radcut;
+                            x = v[i] * ek * divi;
+                        }
+                        v[i] = x;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        d2_split4(big, big_lo, kmaj_off(rR, 4 * j, D2_KC), v[4 * j], v[4 * j + 1], v[4 * j + 2],
+                                  v[4 * j + 3]);
+                }
+            } else {
+                // A = D3 columns 2j + parity (rows r1) into the small slot; each warp half
+                // reads 16 consecutive columns and keeps the 8 of this parity
+                float v[16];
+                const int col0 = 2 * (jc * D2_KC) + 16 * half;
+                tmem_ld16(lrow + (uint32_t)col0, v);
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    float tv[4];
+#pragma unroll
+                    for (int uu = 0; uu < 4; uu++) {
+                        int cc = 2 * (4 * j + uu);             // register index fixed at compile time
+                        float x = par == 0 ? v[cc] : v[cc + 1];
+                        tv[uu] = (col0 + cc + par < n2) ? x : 0.f;
+                    }
+                    d2_split4(small, D2_SMALL_LO, kmaj_off(m, 8 * half + 4 * j, D2_KC), tv[0], tv[1], tv[2],
+                              tv[3]);
+                }
+            }
+            // make the generic shared-memory writes visible to the tensor cores, order the
+            // tensor-memory loads before the arrival, then one arrival per warp
+            fence_async_smem();
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&fill_full[s]);
+        }
+        // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
+        d2_wait(&empty[(total - 1) % D2_NS], ((total - 1) / D2_NS) & 1, fail);
+        fence_after_sync();
+        if (!*fail) {
+            const int *mT = p.mapT + (size_t)a * n2 * n1;
+            const int64_t fo = p.foff[seg];
+#pragma unroll
+            for (int cc = 0; cc < 4; cc++) {
+                const int i0 = 64 * half + 16 * cc;
+                float e[16], o[16];
+                tmem_ld16(lrow + 256u + (uint32_t)i0, e);
+                tmem_ld16(lrow + 384u + (uint32_t)i0, o);
+                int is[16], id[16];
+#pragma unroll
+                for (int uu = 0; uu < 16; uu++) {
+                    int i = i0 + uu;
+                    is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
+                    id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
+                }
+#pragma unroll
+                for (int uu = 0; uu < 16; uu++) {
+                    if (is[uu] >= 0) p.H[fo + is[uu]] = e[uu] + o[uu];
+                    if (id[uu] >= 0) p.H[fo + id[uu]] = e[uu] - o[uu];
+                }
+            }
+        }
     }
-done:
-    if (bad && threadIdx.x == 0) atomicExch(p.err, 1);
-    if (threadIdx.x == 0) {
-        // bulk copies issued but not waited for must land before the CTA exits
-        for (int s = 0; s < D2_NS; s++)
-            if (ncp[s] > nwc[s]) mbar_wait(&bars[D2_NS + s], (ncp[s] - 1) & 1u);
-    }
-    for (int s = 0; s < D2_NS; s++)
-        if (ncm[s] > 0) mbar_wait(&bars[s], (ncm[s] - 1) & 1u);
+    // before shared and tensor memory are released, the async work this CTA issued
+    // must be done: the copy warp waits for its last copy, the MMA warp for its
+    // last commit (which tracks all its MMAs); both phases were issued, so these
+    // bounded waits end at once in a normal run and soon after a failure
+    if (lane == 0 && warp == 9 && copies > 0)
+        mbar_wait(&copy_full[(copies - 1) % D2_NS], ((copies - 1) / D2_NS) & 1);
+    if (lane == 0 && warp == 8) mbar_wait(&empty[(total - 1) % D2_NS], ((total - 1) / D2_NS) & 1);
     fence_before_sync();
     __syncthreads();
+    if (threadIdx.x == 0 && *fail) atomicExch(p.err, 1);
     if (warp == 0) tmem_dealloc(tb, 512);
 }
 
@@ -527,7 +555,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
     p.err = c.d_tc_err;
-    k_tc_dst2d<<<nseg, 256, smem, c.stream>>>(p);
+    k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p);
     c.launches++;
 }
 
