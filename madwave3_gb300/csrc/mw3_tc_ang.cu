@@ -228,29 +228,29 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
         ph1 ^= 1u;
         fence_after_sync();
         if (__syncthreads_or(bad)) break;
-        // ---- H += result at the stored points of this block: 16 angles at a time,
-        // their map and flat-start loads in flight together, then their H loads;
-        // flat offsets fit 32 bits (checked at set-up) ----
+        // ---- H += result at the stored points of this block ----
         {
             const int64_t *fo = p.foff + (size_t)g * na;
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
-                const int a0 = half * 32 + 16 * cc;
-                int off[16];
-#pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    int a = a0 + i;
-                    int idx = (inrow && a < na) ? __ldg(p.map + ((size_t)a * n1 + ir1) * n2 + ir2) : -1;
-                    off[i] = idx >= 0 ? (int)__ldg(fo + a) + idx : -1;
-                }
-                HT hv[16];
-#pragma unroll
-                for (int i = 0; i < 16; i++) hv[i] = off[i] >= 0 ? p.H[off[i]] : (HT)0;
+                const int a0 = half * 32 + cc * 16;
                 float v[16];
                 tmem_ld16(lrow + AG_OUT + a0, v);
 #pragma unroll
-                for (int i = 0; i < 16; i++)
-                    if (off[i] >= 0) p.H[off[i]] = hv[i] + (HT)v[i];
+                for (int h8 = 0; h8 < 16; h8 += 8) {
+                    int idx[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        int a = a0 + h8 + i;
+                        idx[i] = (inrow && a < na) ? __ldg(p.map + ((size_t)a * n1 + ir1) * n2 + ir2) : -1;
+                    }
+                    HT hv[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) hv[i] = idx[i] >= 0 ? p.H[fo[a0 + h8 + i] + idx[i]] : (HT)0;
+#pragma unroll
+                    for (int i = 0; i < 8; i++)
+                        if (idx[i] >= 0) p.H[fo[a0 + h8 + i] + idx[i]] = hv[i] + (HT)v[h8 + i];
+                }
             }
         }
         fence_before_sync();
@@ -316,7 +316,6 @@ int build_tc_ang(Ctx &c)
     using tc::AG_K;
     c.use_tc_ang = false;
     if (c.fp64 || !c.use_tc || c.na < 2 || c.na > AG_K) return MW3_OK;
-    if (c.NT >= ((int64_t)1 << 31)) return MW3_OK;    // the kernel's flat offsets are 32-bit
     const int na = c.na, n1 = c.n1, n2 = c.n2, G = c.G;
     std::vector<float> dfw((size_t)G * 2 * 64 * AG_K, 0.f), dbk((size_t)G * 2 * 64 * AG_K, 0.f);
     std::vector<float> yj((size_t)G * n1 * AG_K, 0.f), l2((size_t)G * 3 * n2 * AG_K, 0.f);
