@@ -128,18 +128,6 @@ struct XStage {
     }
 };
 
-// position of chunk t of a slab's sequence: product gi and chunk c inside it
-__device__ __forceinline__ void d2_chunk(int t, int nkh, int nkr, int &gi, int &c)
-{
-    if (t < 2 * nkh) { gi = 0; c = t; return; }
-    t -= 2 * nkh;
-    if (t < nkr) { gi = 1; c = t; return; }
-    t -= nkr;
-    if (t < nkr) { gi = 2; c = t; return; }
-    gi = 3;
-    c = t - nkr;
-}
-
 // Tensor memory (512 columns):
 //   D1 = S2 Xs^T folded: E at [0,128), O at [128,256)   (lane i < h, column r1)
 //   D2 = D1 S1^T:        R tile t at [256 + 128 t)       (lane R, column r1)
@@ -153,8 +141,10 @@ __device__ __forceinline__ void d2_chunk(int t, int nkh, int nkr, int &gi, int &
 // (8 fill-warp arrivals) and empty (the MMAs that read the stage completed).
 // Chunk t uses stage t % NS for the (t / NS)-th time, so every wait names the
 // phase parity (t / NS) & 1; no role can run a full phase ahead of a waiter.
-// After any wait runs out of time the CTA's shared failure flag makes every
-// later wait return at once, so a fault ends the kernel instead of hanging it.
+// The three roles walk the same chunk sequence as nested loops (product, then
+// parity and K chunk), with no integer division per chunk.  After any wait
+// runs out of time the CTA's shared failure flag makes every later wait return
+// at once, so a fault ends the kernel instead of hanging it.
 constexpr int D2_WARPS = 10;
 
 __device__ __forceinline__ void mbar_arrive1(uint64_t *mbar)
@@ -168,6 +158,20 @@ __device__ __forceinline__ bool d2_wait(uint64_t *mbar, uint32_t parity, volatil
     if (mbar_wait(mbar, parity)) return true;
     *fail = 1;
     return false;
+}
+
+// the chunk sequence of one slab: product gi in 0..3, parity half par (products
+// along R) and K chunk jc; f(t, gi, par, jc) is called for t = 0, 1, ...
+template <typename F>
+__device__ __forceinline__ void d2_for_chunks(int nkh, int nkr, F &&f)
+{
+    int t = 0;
+    for (int par = 0; par < 2; par++)
+        for (int jc = 0; jc < nkh; jc++) f(t++, 0, par, jc);
+    for (int jc = 0; jc < nkr; jc++) f(t++, 1, 0, jc);
+    for (int jc = 0; jc < nkr; jc++) f(t++, 2, 0, jc);
+    for (int par = 0; par < 2; par++)
+        for (int jc = 0; jc < nkh; jc++) f(t++, 3, par, jc);
 }
 
 __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
@@ -207,85 +211,73 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     const int nkr = (nn + D2_KC - 1) / D2_KC;           // K chunks of the products along r1
     const int total = 4 * nkh + 2 * nkr;
     const float *S1p = p.s1planes + p.s1off[w * na + a];
-
     int copies = 0;                                     // copies issued (warp 9, lane 0)
+
     if (warp == 9) {
         // ---- bulk copies of the DST-matrix operands ----
         if (lane == 0)
-            for (int t = 0; t < total && !*fail; t++) {
-                const int s = t % D2_NS, u = t / D2_NS;
-                if (t >= D2_NS && !d2_wait(&empty[s], (u - 1) & 1, fail)) break;
-                int gi, c;
-                d2_chunk(t, nkh, nkr, gi, c);
+            d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
+                if (*fail) return;
+                const int s = t & (D2_NS - 1), u = t >> 2;
+                if (t >= D2_NS && !d2_wait(&empty[s], (u - 1) & 1, fail)) return;
                 unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
                 const bool alongR = (gi == 0 || gi == 3);
-                const float *src = alongR ? p.s2fold + ((size_t)(c / nkh) * D2_NKH + (c % nkh)) * D2_CHUNK
-                                          : S1p + (size_t)c * D2_CHUNK;
+                const float *src = alongR ? p.s2fold + (size_t)(par * D2_NKH + jc) * D2_CHUNK
+                                          : S1p + (size_t)jc * D2_CHUNK;
                 mbar_expect_tx(&copy_full[s], D2_SMALL);
                 bulk_g2s(alongR ? big : small, src, D2_SMALL, &copy_full[s]);
                 copies = t + 1;
-            }
+            });
     } else if (warp == 8) {
-        // ---- MMA issue ----
+        // ---- MMA issue: descriptors built once, advanced by 16-byte units ----
         if (lane == 0) {
-            for (int t = 0; t < total; t++) {
-                const int s = t % D2_NS, u = t / D2_NS;
+            const uint64_t k16 = 256 >> 4;                  // one K step of 8 (two core matrices)
+            const uint64_t d0 = sdesc(smem_u32(sm), 128, D2_SBO);
+            const uint64_t stage16 = D2_STAGE >> 4, small16 = D2_BIGMAX >> 4;
+            const uint64_t lo128 = D2_SMALL_LO >> 4, loRB = big_lo >> 4, tile16 = (16 * D2_SBO) >> 4;
+            const uint32_t id_nn = idesc_tf32(128, nnp), id_rb = idesc_tf32(128, RB), id_128 = idesc_tf32(128, 128);
+            d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
+                const int s = t & (D2_NS - 1), u = t >> 2;
                 d2_wait(&copy_full[s], u & 1, fail);
                 d2_wait(&fill_full[s], u & 1, fail);
                 fence_after_sync();
-                int gi, c;
-                d2_chunk(t, nkh, nkr, gi, c);
-                const int par = (gi == 0 || gi == 3) ? c / nkh : 0, jc = (gi == 0 || gi == 3) ? c % nkh : c;
-                unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
                 if (!*fail) {
-                    const uint32_t bg = smem_u32(big), sl = smem_u32(small);
+                    const uint64_t bg = d0 + (uint64_t)s * stage16, sl = bg + small16;
 #pragma unroll
                     for (int ks = 0; ks < D2_KC / 8; ks++) {
-                        const uint32_t o = ks * 256;
+                        const uint64_t o = ks * k16;
                         const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
                         if (gi == 0) {
                             // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
-                            const uint32_t idesc = idesc_tf32(128, nnp);
-                            uint64_t dah = sdesc(bg + o, 128, D2_SBO), dal = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint32_t d = tb + 128u * par;
-                            mma_tf32(d, dah, dbh, idesc, acc0);
-                            mma_tf32(d, dah, dbl, idesc, 1);
-                            mma_tf32(d, dal, dbh, idesc, 1);
+                            const uint32_t d = tb + 128u * par;
+                            mma_tf32(d, bg + o, sl + o, id_nn, acc0);
+                            mma_tf32(d, bg + o, sl + lo128 + o, id_nn, 1);
+                            mma_tf32(d, bg + lo128 + o, sl + o, id_nn, 1);
                         } else if (gi == 1) {
                             // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
-                            const uint32_t idesc = idesc_tf32(128, nnp);
-                            uint64_t dbh = sdesc(sl + o, 128, D2_SBO), dbl = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
                             for (int tt = 0; tt < NT; tt++) {
-                                uint32_t at = bg + (uint32_t)tt * 16 * D2_SBO;
-                                uint64_t dah = sdesc(at + o, 128, D2_SBO), dal = sdesc(at + big_lo + o, 128, D2_SBO);
-                                uint32_t d = tb + 256u + 128u * tt;
-                                mma_tf32(d, dah, dbh, idesc, acc0);
-                                mma_tf32(d, dah, dbl, idesc, 1);
-                                mma_tf32(d, dal, dbh, idesc, 1);
+                                const uint64_t at = bg + tt * tile16;
+                                const uint32_t d = tb + 256u + 128u * tt;
+                                mma_tf32(d, at + o, sl + o, id_nn, acc0);
+                                mma_tf32(d, at + o, sl + lo128 + o, id_nn, 1);
+                                mma_tf32(d, at + loRB + o, sl + o, id_nn, 1);
                             }
                         } else if (gi == 2) {
                             // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
-                            const uint32_t idesc = idesc_tf32(128, RB);
-                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + big_lo + o, 128, D2_SBO);
-                            mma_tf32(tb, dah, dbh, idesc, acc0);
-                            mma_tf32(tb, dah, dbl, idesc, 1);
-                            mma_tf32(tb, dal, dbh, idesc, 1);
+                            mma_tf32(tb, sl + o, bg + o, id_rb, acc0);
+                            mma_tf32(tb, sl + o, bg + loRB + o, id_rb, 1);
+                            mma_tf32(tb, sl + lo128 + o, bg + o, id_rb, 1);
                         } else {
                             // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
-                            const uint32_t idesc = idesc_tf32(128, 128);
-                            uint64_t dah = sdesc(sl + o, 128, D2_SBO), dal = sdesc(sl + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint64_t dbh = sdesc(bg + o, 128, D2_SBO), dbl = sdesc(bg + D2_SMALL_LO + o, 128, D2_SBO);
-                            uint32_t d = tb + 256u + 128u * par;
-                            mma_tf32(d, dah, dbh, idesc, acc0);
-                            mma_tf32(d, dah, dbl, idesc, 1);
-                            mma_tf32(d, dal, dbh, idesc, 1);
+                            const uint32_t d = tb + 256u + 128u * par;
+                            mma_tf32(d, sl + o, bg + o, id_128, acc0);
+                            mma_tf32(d, sl + o, bg + lo128 + o, id_128, 1);
+                            mma_tf32(d, sl + lo128 + o, bg + o, id_128, 1);
                         }
                     }
                 }
                 mma_commit(&empty[s]);        // also after a failure, so no waiter is left behind
-            }
+            });
         }
     } else {
         // ---- operand fills (warps 0-7) and the H epilogue ----
@@ -297,61 +289,64 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
         const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
         const int rR = 128 * half + m;                  // the R row this thread fills in the third product
         const float e2 = (half < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
+        const float radcut = p.radcut;
+        // G2 rows: half 0 the sum rows R = i, half 1 the difference rows R = n2-1-i
+        const bool on2 = half == 0 ? (m < h) : (m < n2 - h);
+        const int R2 = half == 0 ? m : n2 - 1 - m;
+        const float sg2 = half == 0 ? 1.f : -1.f;
         XStage xs;
         xs.load(Xs, n2, nn, 0);
-        for (int t = 0; t < total; t++) {
-            int gi, c;
-            d2_chunk(t, nkh, nkr, gi, c);
-            const int s = t % D2_NS, u = t / D2_NS;
-            const int par = (gi == 0 || gi == 3) ? c / nkh : 0, jc = (gi == 0 || gi == 3) ? c % nkh : c;
+        d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
+            const int s = t & (D2_NS - 1), u = t >> 2;
             unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
-            if (c == 0 && gi > 0) {
+            if (jc == 0 && par == 0 && gi > 0) {
                 // this product reads the previous one from tensor memory: its last chunk done
-                d2_wait(&empty[(t - 1) % D2_NS], ((t - 1) / D2_NS) & 1, fail);
+                d2_wait(&empty[(t - 1) & (D2_NS - 1)], ((t - 1) >> 2) & 1, fail);
                 fence_after_sync();
             }
             if (t >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
+            const int k0 = jc * D2_KC;
             if (gi == 0) {
                 // B = Xs columns of this parity (rows r1) into the small slot
                 xs.store(small, par);
-                if (c + 1 < 2 * nkh) xs.load(Xs, n2, nn, (c + 1) % nkh);
+                const int nj = jc + 1 < nkh ? jc + 1 : 0;
+                if (par == 0 || jc + 1 < nkh) xs.load(Xs, n2, nn, nj);
             } else if (gi == 1) {
-                // A = D1 rows R into the big slot: half 0 the sum rows R = i, half 1 the
-                // difference rows R = n2-1-i, from the E and O columns of lane i (all lanes
-                // load; lanes without a row store nothing)
+                // A = D1 rows R into the big slot from the E and O columns of lane i
+                // (all lanes load; lanes without a row store nothing)
                 float e[16], o[16];
-                tmem_ld16(lrow + (uint32_t)(c * D2_KC), e);
-                tmem_ld16(lrow + 128u + (uint32_t)(c * D2_KC), o);
-                const bool on = half == 0 ? (m < h) : (m < n2 - h);
-                if (on) {
-                    const int R = half == 0 ? m : n2 - 1 - m;
-                    const float sg = half == 0 ? 1.f : -1.f;
+                tmem_ld16(lrow + (uint32_t)k0, e);
+                tmem_ld16(lrow + 128u + (uint32_t)k0, o);
+                if (on2) {
+                    const bool full = k0 + D2_KC <= nn;
 #pragma unroll
                     for (int j = 0; j < 4; j++) {
                         float tv[4];
 #pragma unroll
                         for (int uu = 0; uu < 4; uu++) {
-                            int k = c * D2_KC + 4 * j + uu;
-                            tv[uu] = k < nn ? e[4 * j + uu] + sg * o[4 * j + uu] : 0.f;
+                            float x = e[4 * j + uu] + sg2 * o[4 * j + uu];
+                            tv[uu] = (full || k0 + 4 * j + uu < nn) ? x : 0.f;
                         }
-                        d2_split4(big, big_lo, kmaj_off(R, 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
+                        d2_split4(big, big_lo, kmaj_off(R2, 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
                     }
                 }
             } else if (gi == 2) {
                 // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
                 if (half < NT) {
                     float v[16];
-                    tmem_ld16(lrow + 256u + 128u * half + (uint32_t)(c * D2_KC), v);
+                    tmem_ld16(lrow + 256u + 128u * half + (uint32_t)k0, v);
+                    float pv[16];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        float4 q = __ldg(reinterpret_cast<const float4 *>(p1f + k0) + j);
+                        pv[4 * j] = q.x; pv[4 * j + 1] = q.y; pv[4 * j + 2] = q.z; pv[4 * j + 3] = q.w;
+                    }
+                    const bool full = k0 + D2_KC <= nn && rR < n2;
 #pragma unroll
                     for (int i = 0; i < 16; i++) {
-                        int k = c * D2_KC + i;
-                        float x = 0.f;
-                        if (k < nn && rR < n2) {
-                            float ek = __ldg(p1f + k) + e2;
-                            if (ek > p.radcut) ek = p.radcut;
-                            x = v[i] * ek * divi;
-                        }
-                        v[i] = x;
+                        float ek = fminf(pv[i] + e2, radcut);
+                        float x = v[i] * ek * divi;
+                        v[i] = (full || (k0 + i < nn && rR < n2)) ? x : 0.f;
                     }
 #pragma unroll
                     for (int j = 0; j < 4; j++)
@@ -362,8 +357,9 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                 // A = D3 columns 2j + parity (rows r1) into the small slot; each warp half
                 // reads 16 consecutive columns and keeps the 8 of this parity
                 float v[16];
-                const int col0 = 2 * (jc * D2_KC) + 16 * half;
+                const int col0 = 2 * k0 + 16 * half;
                 tmem_ld16(lrow + (uint32_t)col0, v);
+                const bool full = col0 + 16 <= n2;
 #pragma unroll
                 for (int j = 0; j < 2; j++) {
                     float tv[4];
@@ -371,7 +367,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                     for (int uu = 0; uu < 4; uu++) {
                         int cc = 2 * (4 * j + uu);             // register index fixed at compile time
                         float x = par == 0 ? v[cc] : v[cc + 1];
-                        tv[uu] = (col0 + cc + par < n2) ? x : 0.f;
+                        tv[uu] = (full || col0 + cc + par < n2) ? x : 0.f;
                     }
                     d2_split4(small, D2_SMALL_LO, kmaj_off(m, 8 * half + 4 * j, D2_KC), tv[0], tv[1], tv[2],
                               tv[3]);
@@ -383,9 +379,9 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             fence_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive1(&fill_full[s]);
-        }
+        });
         // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
-        d2_wait(&empty[(total - 1) % D2_NS], ((total - 1) / D2_NS) & 1, fail);
+        d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
         if (!*fail) {
             const int *mT = p.mapT + (size_t)a * n2 * n1;
@@ -416,8 +412,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     // last commit (which tracks all its MMAs); both phases were issued, so these
     // bounded waits end at once in a normal run and soon after a failure
     if (lane == 0 && warp == 9 && copies > 0)
-        mbar_wait(&copy_full[(copies - 1) % D2_NS], ((copies - 1) / D2_NS) & 1);
-    if (lane == 0 && warp == 8) mbar_wait(&empty[(total - 1) % D2_NS], ((total - 1) / D2_NS) & 1);
+        mbar_wait(&copy_full[(copies - 1) & (D2_NS - 1)], ((copies - 1) >> 2) & 1);
+    if (lane == 0 && warp == 8) mbar_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1);
     fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && *fail) atomicExch(p.err, 1);
@@ -502,7 +498,8 @@ std::vector<double> dst_matrix(int n);
 int build_tc_dst2d(Ctx &c)
 {
     c.use_tc_dst2d = false;
-    if (c.fp64 || !c.use_tc || c.n2 > 256) return MW3_OK;
+    // n1 a multiple of 4: the kernel reads the r1 momenta as float4
+    if (c.fp64 || !c.use_tc || c.n2 > 256 || (c.n1 & 3) != 0) return MW3_OK;
     const int na = c.na, W = (int)c.waves.size();
     for (auto &t : c.waves)
         for (int a = 0; a < na; a++)
@@ -511,7 +508,8 @@ int build_tc_dst2d(Ctx &c)
     std::vector<float> planes;
     std::map<int, int64_t> off;
     std::vector<int64_t> s1off((size_t)W * na);
-    std::vector<float> p1f((size_t)W * na * c.n1), p2f((size_t)W * na * c.n2);
+    // the r1 momenta padded by one chunk: the kernel reads them 16 at a time
+    std::vector<float> p1f((size_t)W * na * c.n1 + 16, 0.f), p2f((size_t)W * na * c.n2);
     for (int w = 0; w < W; w++) {
         const WaveTables &t = c.waves[w];
         for (int a = 0; a < na; a++) {
