@@ -441,9 +441,6 @@ int build_device(Ctx &c)
     c.h32 = c.use_tc_dst2d && c.use_tc_ang;
     c.d_h32 = nullptr;
     c.d_vr = nullptr;
-    c.d_roff = nullptr;
-    c.d_fab = nullptr;
-    c.d_fabw = nullptr;
     if (c.use_tc_dst2d) TRY(dalloc(c, &c.d_h32, (size_t)c.NT));
     if (!c.fp64) {
         // potential pre-scaled for the mixed update: V 2/delta2, minus emindlt 2/delta2 on the diagonal
@@ -457,37 +454,6 @@ int build_device(Ctx &c)
                     vr[b + i] = c.vvv[b + i] * r2d - (et == es ? c.grid.emindlt * r2d : 0.0);
             }
         TRY(dupload(c, &c.d_vr, vr));
-        std::vector<int> roff(per, 0);
-        for (int a = 0; a < c.na; a++)
-            for (int ir = 0; ir < c.npunreal[a]; ir++)
-                roff[(size_t)a * c.npt + ir] = (c.indr1[(size_t)a * c.npt + ir] - 1) * c.n2 +
-                                               (c.indr2[(size_t)a * c.npt + ir] - 1);
-        TRY(dupload(c, &c.d_roff, roff));
-        std::vector<int> fabw(W, 0);
-        std::vector<int> first_of;                     // wave that defines each table
-        std::vector<double> fab;
-        for (int w = 0; w < W; w++) {
-            const WaveTables &t = c.waves[w];
-            int found = -1;
-            for (size_t k = 0; k < first_of.size() && found < 0; k++) {
-                const WaveTables &o = c.waves[first_of[k]];
-                if (o.absfr1 == t.absfr1 && o.absfr2 == t.absfr2) found = (int)k;
-            }
-            if (found < 0) {
-                found = (int)first_of.size();
-                first_of.push_back(w);
-                size_t b = fab.size();
-                fab.resize(b + per, 1.0);
-                for (int a = 0; a < c.na; a++)
-                    for (int ir = 0; ir < c.npunreal[a]; ir++) {
-                        int i1 = c.indr1[(size_t)a * c.npt + ir] - 1, i2 = c.indr2[(size_t)a * c.npt + ir] - 1;
-                        fab[b + (size_t)a * c.npt + ir] = t.absfr1[i1] * t.absfr2[i2];
-                    }
-            }
-            fabw[w] = found;
-        }
-        TRY(dupload(c, &c.d_fab, fab));
-        TRY(dupload(c, &c.d_fabw, fabw));
     }
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;

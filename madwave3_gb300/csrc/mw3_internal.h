@@ -206,11 +206,6 @@ struct Ctx {
     bool h32 = false;
     float *d_h32 = nullptr;          // [NT]
     double *d_vr = nullptr;          // like vvv
-    // mixed update: per (angle, point) rectangle offset and absorber product
-    // absfr1(r1) absfr2(R); waves with equal absorbers share one table
-    int *d_roff = nullptr;           // [na][npt]
-    double *d_fab = nullptr;         // [tables][na][npt]
-    int *d_fabw = nullptr;           // [W] table of each wave
     int *d_tc_err = nullptr;         // set by a tensor-core kernel whose mbarrier wait ran out
     // optional per-stage event timing (mw3_profile)
     bool prof = false;

@@ -411,9 +411,6 @@ struct UpdArgs {
     double emindlt, delta2;
     double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
     const double *vr;              // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
-    const int *roff;               // mixed path: [na][npt] rectangle offset of each stored point
-    const double *fab;             // mixed path: [tables][na][npt] absfr1 * absfr2
-    const int *fabw;               // mixed path: [W] absorber table of each wave
     int first;
     double *normpart;              // [G*na]
     int nofe;                      // max over waves; 0 = funE off
@@ -549,115 +546,6 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
         for (int o = 16; o > 0; o >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, o);
     }
     if (lane == 0) s_wsum[warp] = nrm;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += s_wsum[i];
-        u.normpart[(size_t)seg * gridDim.y + blockIdx.y] = t;
-    }
-}
-
-// Mixed-path update: the same recursion as k_update's mixed branch, with the
-// rectangle offset and absorber product of each point read from per-(angle,
-// point) tables (no dependent loads through indr1/indr2), the same-block
-// potential term taking the psi_k already loaded, 512 threads of two points
-// each (few registers, all loads of a thread in flight together).
-template <typename HT>
-__global__ void __launch_bounds__(512) k_update_mx(DevGrid d, UpdArgs u, float *__restrict__ X)
-{
-    const int seg = blockIdx.x;
-    const int g = seg / d.na, a = seg % d.na;
-    const int w = d.blk_wave[g];
-    const int64_t off = d.foff[seg];
-    const int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
-    const int ne = d.ne;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __shared__ const double *s_vrow[8];
-    __shared__ const double *s_prow[8];
-    __shared__ int s_nsrc, s_self;
-    __shared__ double s_wsum[16];
-    if (threadIdx.x == 0) {
-        int et = d.blk_elec[g], ns = 0, self = -1;
-        for (int q = 0; q < ne; q++) {
-            int sb = u.vsrc[g * ne + q];
-            if (sb < 0) continue;
-            int es = d.blk_elec[sb];
-            s_vrow[ns] = u.vr + ((((size_t)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
-            s_prow[ns] = u.pk + d.foff[(size_t)sb * d.na + a];
-            if (sb == g) self = ns;
-            ns++;
-        }
-        s_nsrc = ns;
-        s_self = self;
-    }
-    __syncthreads();
-    const int nsrc = s_nsrc, self = s_self;
-    const HT *__restrict__ Hp = reinterpret_cast<const HT *>(u.H) + off;
-    const double *__restrict__ pkp = u.pk + off;
-    const double *__restrict__ pm1 = u.pkm1 + off;
-    double *__restrict__ outp = u.out + off;
-    const int *__restrict__ rop = u.roff + (size_t)a * d.npt;
-    const double *__restrict__ fap = u.fab + ((size_t)u.fabw[w] * d.na + a) * d.npt;
-    float *__restrict__ rect = X + (size_t)seg * d.n1 * d.n2;
-    constexpr int U = kPointChunk / 512;
-    const int ir0 = blockIdx.y * kPointChunk + threadIdx.x;
-    double hv[U], pk[U], p1[U], fb[U];
-    int ro[U];
-#pragma unroll
-    for (int k = 0; k < U; k++) {
-        int ir = ir0 + k * 512;
-        bool on = ir < n;
-        ro[k] = on ? rop[ir] : 0;
-        fb[k] = on ? fap[ir] : 1.0;
-        hv[k] = on ? h_load(Hp, ir) : 0.0;
-        pk[k] = on ? pkp[ir] : 0.0;
-        p1[k] = on && !u.first ? pm1[ir] : 0.0;
-    }
-    double acc[U];
-    bool damp[U];
-#pragma unroll
-    for (int k = 0; k < U; k++) {
-        damp[k] = !u.first && __double_as_longlong(fb[k]) != 0x3FF0000000000000LL;
-        acc[k] = (u.first || damp[k]) ? 0.0 : -p1[k];
-    }
-    for (int q = 0; q < nsrc; q++) {
-        const double *vr = s_vrow[q], *pr = s_prow[q];
-        double vv[U], pp[U];
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            int ir = ir0 + k * 512;
-            vv[k] = ir < n ? vr[ir] : 0.0;
-            pp[k] = q == self ? pk[k] : (ir < n ? pr[ir] : 0.0);
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) acc[k] = fma(vv[k], pp[k], acc[k]);
-    }
-    double *zf = (u.nofe > 0 && !u.first) ? u.zfe[w] : nullptr;
-    int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
-    float nrmf = 0.f;
-#pragma unroll
-    for (int k = 0; k < U; k++) {
-        int ir = ir0 + k * 512;
-        if (ir >= n) continue;
-        double t = fma(hv[k], u.r2delta, acc[k]);
-        double nv = u.first ? 0.5 * t : (damp[k] ? fma(-fb[k], p1[k], t) * fb[k] : t);
-        float nf = f64_to_f32_int(nv);
-        outp[ir] = nv;
-        rect[ro[k]] = nf;
-        nrmf = fmaf(nf, nf, nrmf);
-        if (zf) {
-            int64_t i = off + ir;
-            for (int e = 0; e < u.nofe; e++) {
-                const double *ck = u.zcke + ((size_t)w * u.nofe + e) * 2;
-                double *zz = zf + ((size_t)e * wlen + (i - wst)) * 2;
-                zz[0] += ck[0] * nv;
-                zz[1] += ck[1] * nv;
-            }
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) nrmf += __shfl_down_sync(0xffffffffu, nrmf, o);
-    if (lane == 0) s_wsum[warp] = f32_to_f64_int(nrmf);
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
@@ -1196,9 +1084,6 @@ void launch_update(Ctx &c, int first)
     u.rdelta = 1.0 / c.grid.delta2;
     u.r2delta = 2.0 / c.grid.delta2;
     u.vr = c.d_vr;
-    u.roff = c.d_roff;
-    u.fab = c.d_fab;
-    u.fabw = c.d_fabw;
     u.first = first;
     u.normpart = c.d_normpart;
     u.nofe = c.nofemax;
@@ -1206,14 +1091,7 @@ void launch_update(Ctx &c, int first)
     u.zfe = c.d_zfe_ptrs;
     u.wflat0 = c.d_wflat0;
     stage_mark(c, 5);
-    if (sizeof(T) == 4 && c.d_roff) {
-        if (c.h32) {
-            u.H = c.d_h32;
-            k_update_mx<float><<<dim3(c.nseg, c.nchunk), 512, 0, c.stream>>>(devgrid(c), u, (float *)c.d_X);
-        } else {
-            k_update_mx<double><<<dim3(c.nseg, c.nchunk), 512, 0, c.stream>>>(devgrid(c), u, (float *)c.d_X);
-        }
-    } else if (c.h32) {
+    if (c.h32) {
         u.H = c.d_h32;
         k_update<T, float><<<dim3(c.nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
     } else {
