@@ -63,7 +63,7 @@ struct Dst2Args {
     const int *mapT;              // [na][n2][n1]
     const int64_t *foff;
     const int *blk_wave;
-    int na, n1, n2, seg0, nseg;   // slabs seg0 .. seg0 + nseg - 1
+    int na, n1, n2, seg0;
     int *err;
 };
 
@@ -141,14 +141,10 @@ struct XStage {
 // (8 fill-warp arrivals) and empty (the MMAs that read the stage completed).
 // Chunk t uses stage t % NS for the (t / NS)-th time, so every wait names the
 // phase parity (t / NS) & 1; no role can run a full phase ahead of a waiter.
-//
-// The kernel is persistent: CTA b takes the slabs b, b + gridDim, ...  The
-// chunk sequence simply continues from slab to slab, and the fill warps write
-// a slab's H only after building the next slab's first product, whose MMAs
-// (tensor-memory columns 0-255) then overlap the epilogue (columns 256-511);
-// the MMA warp marks the end of each slab on slab_done.  After any wait runs
-// out of time the CTA's shared failure flag makes every later wait return at
-// once, so a fault ends the kernel instead of hanging it.
+// The three roles walk the same chunk sequence as nested loops (product, then
+// parity and K chunk), with no integer division per chunk.  After any wait
+// runs out of time the CTA's shared failure flag makes every later wait return
+// at once, so a fault ends the kernel instead of hanging it.
 constexpr int D2_WARPS = 10;
 
 __device__ __forceinline__ void mbar_arrive1(uint64_t *mbar)
@@ -164,36 +160,18 @@ __device__ __forceinline__ bool d2_wait(uint64_t *mbar, uint32_t parity, volatil
     return false;
 }
 
-// what a role needs to know about one slab
-struct D2Slab {
-    int seg, a, w, nn, nnp, nkr;
-    const float *S1p;
-};
-
-__device__ __forceinline__ D2Slab d2_slab(const Dst2Args &p, int sidx)
-{
-    D2Slab s;
-    s.seg = p.seg0 + sidx;
-    int g = s.seg / p.na;
-    s.a = s.seg - g * p.na;
-    s.w = p.blk_wave[g];
-    s.nn = p.nopr1[s.w * p.na + s.a];
-    s.nnp = (s.nn + 15) & ~15;
-    s.nkr = (s.nn + D2_KC - 1) / D2_KC;
-    s.S1p = p.s1planes + p.s1off[s.w * p.na + s.a];
-    return s;
-}
-
-// one product's chunks (gi 0..3) of a slab: f(t, par, jc) with the running chunk counter t
+// the chunk sequence of one slab: product gi in 0..3, parity half par (products
+// along R) and K chunk jc; f(t, gi, par, jc) is called for t = 0, 1, ...
 template <typename F>
-__device__ __forceinline__ void d2_for_product(int gi, int nkh, int nkr, int &t, F &&f)
+__device__ __forceinline__ void d2_for_chunks(int nkh, int nkr, F &&f)
 {
-    if (gi == 0 || gi == 3) {
-        for (int par = 0; par < 2; par++)
-            for (int jc = 0; jc < nkh; jc++) f(t++, par, jc);
-    } else {
-        for (int jc = 0; jc < nkr; jc++) f(t++, 0, jc);
-    }
+    int t = 0;
+    for (int par = 0; par < 2; par++)
+        for (int jc = 0; jc < nkh; jc++) f(t++, 0, par, jc);
+    for (int jc = 0; jc < nkr; jc++) f(t++, 1, 0, jc);
+    for (int jc = 0; jc < nkr; jc++) f(t++, 2, 0, jc);
+    for (int par = 0; par < 2; par++)
+        for (int jc = 0; jc < nkh; jc++) f(t++, 3, par, jc);
 }
 
 __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
@@ -203,8 +181,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     uint64_t *copy_full = reinterpret_cast<uint64_t *>(sm + D2_BYTES);
     uint64_t *fill_full = copy_full + D2_NS;
     uint64_t *empty = fill_full + D2_NS;
-    uint64_t *slab_done = empty + D2_NS;
-    uint32_t *slot = reinterpret_cast<uint32_t *>(slab_done + 1);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(empty + D2_NS);
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) tmem_alloc(slot, 512);
@@ -214,7 +191,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             mbar_init(&fill_full[i], 8);
             mbar_init(&empty[i], 1);
         }
-        mbar_init(slab_done, 1);
         *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -222,35 +198,36 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     __syncthreads();
     fence_after_sync();
     const uint32_t tb = *slot;
-    const int n1 = p.n1, n2 = p.n2;
+    const int na = p.na, n1 = p.n1, n2 = p.n2;
     const int h = (n2 + 1) >> 1;                        // rows i < h: E + O; row n2-1-i: E - O
     const int nkh = (h + D2_KC - 1) / D2_KC;            // K chunks of one parity half
     const int NT = (n2 + 127) / 128;                    // R tiles of D2 and of the D3 columns
     const int RB = 128 * NT;
     const uint32_t big_lo = (uint32_t)RB * D2_KC * 4;   // lo plane of an RB-row operand
-    int copies = 0, commits = 0;                        // issued by warp 9 / warp 8 (lane 0)
+    const int seg = p.seg0 + blockIdx.x;
+    const int g = seg / na, a = seg % na, w = p.blk_wave[g];
+    const int nn = p.nopr1[w * na + a];
+    const int nnp = (nn + 15) & ~15;                    // N of the products along r1
+    const int nkr = (nn + D2_KC - 1) / D2_KC;           // K chunks of the products along r1
+    const int total = 4 * nkh + 2 * nkr;
+    const float *S1p = p.s1planes + p.s1off[w * na + a];
+    int copies = 0;                                     // copies issued (warp 9, lane 0)
 
     if (warp == 9) {
         // ---- bulk copies of the DST-matrix operands ----
-        if (lane == 0) {
-            int t = 0;
-            for (int sidx = blockIdx.x; sidx < p.nseg && !*fail; sidx += gridDim.x) {
-                const D2Slab sl = d2_slab(p, sidx);
-                for (int gi = 0; gi < 4; gi++)
-                    d2_for_product(gi, nkh, sl.nkr, t, [&](int tt, int par, int jc) {
-                        if (*fail) return;
-                        const int s = tt & (D2_NS - 1), u = tt >> 2;
-                        if (tt >= D2_NS && !d2_wait(&empty[s], (u - 1) & 1, fail)) return;
-                        unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
-                        const bool alongR = (gi == 0 || gi == 3);
-                        const float *src = alongR ? p.s2fold + (size_t)(par * D2_NKH + jc) * D2_CHUNK
-                                                  : sl.S1p + (size_t)jc * D2_CHUNK;
-                        mbar_expect_tx(&copy_full[s], D2_SMALL);
-                        bulk_g2s(alongR ? big : small, src, D2_SMALL, &copy_full[s]);
-                        copies = tt + 1;
-                    });
-            }
-        }
+        if (lane == 0)
+            d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
+                if (*fail) return;
+                const int s = t & (D2_NS - 1), u = t >> 2;
+                if (t >= D2_NS && !d2_wait(&empty[s], (u - 1) & 1, fail)) return;
+                unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
+                const bool alongR = (gi == 0 || gi == 3);
+                const float *src = alongR ? p.s2fold + (size_t)(par * D2_NKH + jc) * D2_CHUNK
+                                          : S1p + (size_t)jc * D2_CHUNK;
+                mbar_expect_tx(&copy_full[s], D2_SMALL);
+                bulk_g2s(alongR ? big : small, src, D2_SMALL, &copy_full[s]);
+                copies = t + 1;
+            });
     } else if (warp == 8) {
         // ---- MMA issue: descriptors built once, advanced by 16-byte units ----
         if (lane == 0) {
@@ -258,89 +235,82 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             const uint64_t d0 = sdesc(smem_u32(sm), 128, D2_SBO);
             const uint64_t stage16 = D2_STAGE >> 4, small16 = D2_BIGMAX >> 4;
             const uint64_t lo128 = D2_SMALL_LO >> 4, loRB = big_lo >> 4, tile16 = (16 * D2_SBO) >> 4;
-            const uint32_t id_rb = idesc_tf32(128, RB), id_128 = idesc_tf32(128, 128);
-            int t = 0;
-            for (int sidx = blockIdx.x; sidx < p.nseg; sidx += gridDim.x) {
-                const D2Slab sl = d2_slab(p, sidx);
-                const uint32_t id_nn = idesc_tf32(128, sl.nnp);
-                for (int gi = 0; gi < 4; gi++)
-                    d2_for_product(gi, nkh, sl.nkr, t, [&](int tt, int par, int jc) {
-                        const int s = tt & (D2_NS - 1), u = tt >> 2;
-                        d2_wait(&copy_full[s], u & 1, fail);
-                        d2_wait(&fill_full[s], u & 1, fail);
-                        fence_after_sync();
-                        if (!*fail) {
-                            const uint64_t bg = d0 + (uint64_t)s * stage16, smd = bg + small16;
+            const uint32_t id_nn = idesc_tf32(128, nnp), id_rb = idesc_tf32(128, RB), id_128 = idesc_tf32(128, 128);
+            d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
+                const int s = t & (D2_NS - 1), u = t >> 2;
+                d2_wait(&copy_full[s], u & 1, fail);
+                d2_wait(&fill_full[s], u & 1, fail);
+                fence_after_sync();
+                if (!*fail) {
+                    const uint64_t bg = d0 + (uint64_t)s * stage16, sl = bg + small16;
 #pragma unroll
-                            for (int ks = 0; ks < D2_KC / 8; ks++) {
-                                const uint64_t o = ks * k16;
-                                const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
-                                if (gi == 0) {
-                                    // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
-                                    const uint32_t d = tb + 128u * par;
-                                    mma_tf32(d, bg + o, smd + o, id_nn, acc0);
-                                    mma_tf32(d, bg + o, smd + lo128 + o, id_nn, 1);
-                                    mma_tf32(d, bg + lo128 + o, smd + o, id_nn, 1);
-                                } else if (gi == 1) {
-                                    // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
-                                    for (int r = 0; r < NT; r++) {
-                                        const uint64_t at = bg + r * tile16;
-                                        const uint32_t d = tb + 256u + 128u * r;
-                                        mma_tf32(d, at + o, smd + o, id_nn, acc0);
-                                        mma_tf32(d, at + o, smd + lo128 + o, id_nn, 1);
-                                        mma_tf32(d, at + loRB + o, smd + o, id_nn, 1);
-                                    }
-                                } else if (gi == 2) {
-                                    // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
-                                    mma_tf32(tb, smd + o, bg + o, id_rb, acc0);
-                                    mma_tf32(tb, smd + o, bg + loRB + o, id_rb, 1);
-                                    mma_tf32(tb, smd + lo128 + o, bg + o, id_rb, 1);
-                                } else {
-                                    // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
-                                    const uint32_t d = tb + 256u + 128u * par;
-                                    mma_tf32(d, smd + o, bg + o, id_128, acc0);
-                                    mma_tf32(d, smd + o, bg + lo128 + o, id_128, 1);
-                                    mma_tf32(d, smd + lo128 + o, bg + o, id_128, 1);
-                                }
+                    for (int ks = 0; ks < D2_KC / 8; ks++) {
+                        const uint64_t o = ks * k16;
+                        const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
+                        if (gi == 0) {
+                            // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
+                            const uint32_t d = tb + 128u * par;
+                            mma_tf32(d, bg + o, sl + o, id_nn, acc0);
+                            mma_tf32(d, bg + o, sl + lo128 + o, id_nn, 1);
+                            mma_tf32(d, bg + lo128 + o, sl + o, id_nn, 1);
+                        } else if (gi == 1) {
+                            // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
+                            for (int tt = 0; tt < NT; tt++) {
+                                const uint64_t at = bg + tt * tile16;
+                                const uint32_t d = tb + 256u + 128u * tt;
+                                mma_tf32(d, at + o, sl + o, id_nn, acc0);
+                                mma_tf32(d, at + o, sl + lo128 + o, id_nn, 1);
+                                mma_tf32(d, at + loRB + o, sl + o, id_nn, 1);
                             }
+                        } else if (gi == 2) {
+                            // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
+                            mma_tf32(tb, sl + o, bg + o, id_rb, acc0);
+                            mma_tf32(tb, sl + o, bg + loRB + o, id_rb, 1);
+                            mma_tf32(tb, sl + lo128 + o, bg + o, id_rb, 1);
+                        } else {
+                            // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
+                            const uint32_t d = tb + 256u + 128u * par;
+                            mma_tf32(d, sl + o, bg + o, id_128, acc0);
+                            mma_tf32(d, sl + o, bg + lo128 + o, id_128, 1);
+                            mma_tf32(d, sl + lo128 + o, bg + o, id_128, 1);
                         }
-                        mma_commit(&empty[s]);   // also after a failure, so no waiter is left behind
-                        commits = tt + 1;
-                    });
-                mma_commit(slab_done);           // tracks every MMA of this slab
-            }
+                    }
+                }
+                mma_commit(&empty[s]);        // also after a failure, so no waiter is left behind
+            });
         }
     } else {
         // ---- operand fills (warps 0-7) and the H epilogue ----
+        const float *Xs = p.X + (size_t)seg * n1 * n2;
         const int q4 = warp & 3, half = warp >> 2;
         const int m = q4 * 32 + lane;                   // the tensor-memory lane this thread reads
         const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
+        const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
+        const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
         const int rR = 128 * half + m;                  // the R row this thread fills in the third product
+        const float e2 = (half < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
         const float radcut = p.radcut;
-        // second product rows: half 0 the sum rows R = i, half 1 the difference rows R = n2-1-i
+        // G2 rows: half 0 the sum rows R = i, half 1 the difference rows R = n2-1-i
         const bool on2 = half == 0 ? (m < h) : (m < n2 - h);
         const int R2 = half == 0 ? m : n2 - 1 - m;
         const float sg2 = half == 0 ? 1.f : -1.f;
         XStage xs;
-        int t = 0;
-
-        // one chunk of product gi of slab sl
-        auto fill = [&](const D2Slab &sl, int gi, int tt, int par, int jc) {
-            const int s = tt & (D2_NS - 1), u = tt >> 2;
+        xs.load(Xs, n2, nn, 0);
+        d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
+            const int s = t & (D2_NS - 1), u = t >> 2;
             unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
             if (jc == 0 && par == 0 && gi > 0) {
                 // this product reads the previous one from tensor memory: its last chunk done
-                d2_wait(&empty[(tt - 1) & (D2_NS - 1)], ((tt - 1) >> 2) & 1, fail);
+                d2_wait(&empty[(t - 1) & (D2_NS - 1)], ((t - 1) >> 2) & 1, fail);
                 fence_after_sync();
             }
-            if (tt >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk tt - NS read this stage
+            if (t >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
             const int k0 = jc * D2_KC;
-            const int nn = sl.nn;
             if (gi == 0) {
                 // B = Xs columns of this parity (rows r1) into the small slot
                 xs.store(small, par);
                 const int nj = jc + 1 < nkh ? jc + 1 : 0;
-                if (par == 0 || jc + 1 < nkh) xs.load(p.X + (size_t)sl.seg * n1 * n2, n2, nn, nj);
+                if (par == 0 || jc + 1 < nkh) xs.load(Xs, n2, nn, nj);
             } else if (gi == 1) {
                 // A = D1 rows R into the big slot from the E and O columns of lane i
                 // (all lanes load; lanes without a row store nothing)
@@ -363,9 +333,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             } else if (gi == 2) {
                 // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
                 if (half < NT) {
-                    const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
-                    const float *p1f = p.p2r1f + ((size_t)sl.w * p.na + sl.a) * n1;
-                    const float e2 = rR < n2 ? __ldg(p.p2r2f + ((size_t)sl.w * p.na + sl.a) * n2 + rR) : 0.f;
                     float v[16];
                     tmem_ld16(lrow + 256u + 128u * half + (uint32_t)k0, v);
                     float pv[16];
@@ -412,16 +379,13 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             fence_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive1(&fill_full[s]);
-        };
-
-        // H at the stored points of a finished slab: lane r1; R = i takes E + O, R = n2-1-i takes E - O
-        auto epilogue = [&](const D2Slab &sl, int slab_no) {
-            d2_wait(slab_done, slab_no & 1, fail);
-            fence_after_sync();
-            if (*fail) return;
-            const int *mT = p.mapT + (size_t)sl.a * n2 * n1;
-            const int64_t fo = p.foff[sl.seg];
-            const int nn = sl.nn;
+        });
+        // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
+        d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
+        fence_after_sync();
+        if (!*fail) {
+            const int *mT = p.mapT + (size_t)a * n2 * n1;
+            const int64_t fo = p.foff[seg];
 #pragma unroll
             for (int cc = 0; cc < 4; cc++) {
                 const int i0 = 64 * half + 16 * cc;
@@ -441,28 +405,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                     if (id[uu] >= 0) p.H[fo + id[uu]] = e[uu] - o[uu];
                 }
             }
-            // the next slab's second product overwrites these columns once all warps arrive
-            fence_before_sync();
-        };
-
-        if (blockIdx.x < p.nseg) {
-            D2Slab cur = d2_slab(p, blockIdx.x);
-            xs.load(p.X + (size_t)cur.seg * n1 * n2, n2, cur.nn, 0);
-            d2_for_product(0, nkh, cur.nkr, t, [&](int tt, int par, int jc) { fill(cur, 0, tt, par, jc); });
-            int slab_no = 0;
-            for (int sidx = blockIdx.x; sidx < p.nseg; sidx += gridDim.x, slab_no++) {
-                for (int gi = 1; gi < 4; gi++)
-                    d2_for_product(gi, nkh, cur.nkr, t, [&](int tt, int par, int jc) { fill(cur, gi, tt, par, jc); });
-                const int nidx = sidx + gridDim.x;
-                D2Slab nxt = cur;
-                if (nidx < p.nseg) {
-                    nxt = d2_slab(p, nidx);
-                    xs.load(p.X + (size_t)nxt.seg * n1 * n2, n2, nxt.nn, 0);
-                    d2_for_product(0, nkh, nxt.nkr, t, [&](int tt, int par, int jc) { fill(nxt, 0, tt, par, jc); });
-                }
-                epilogue(cur, slab_no);
-                cur = nxt;
-            }
         }
     }
     // before shared and tensor memory are released, the async work this CTA issued
@@ -471,8 +413,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     // bounded waits end at once in a normal run and soon after a failure
     if (lane == 0 && warp == 9 && copies > 0)
         mbar_wait(&copy_full[(copies - 1) & (D2_NS - 1)], ((copies - 1) >> 2) & 1);
-    if (lane == 0 && warp == 8 && commits > 0)
-        mbar_wait(&empty[(commits - 1) & (D2_NS - 1)], ((commits - 1) >> 2) & 1);
+    if (lane == 0 && warp == 8) mbar_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1);
     fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && *fail) atomicExch(p.err, 1);
@@ -598,7 +539,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    const size_t smem = D2_BYTES + 256 + 1024;
+    const size_t smem = D2_BYTES + 128 + 1024;
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
@@ -610,17 +551,9 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.s2fold = c.d_dst_s2fold; p.s1planes = c.d_dst_planes; p.s1off = c.d_dst_s1off; p.nopr1 = c.d_nopr1;
     p.p2r1f = c.d_p2r1f; p.p2r2f = c.d_p2r2f; p.radcut = (float)c.grid.radcutmax;
     p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
-    p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na; p.nseg = nseg;
+    p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
     p.err = c.d_tc_err;
-    // persistent: one CTA per SM (the kernel takes all of shared and tensor memory)
-    static int nsm = 0;
-    if (nsm == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (nsm <= 0) nsm = 1;
-    }
-    k_tc_dst2d<<<std::min(nseg, nsm), D2_WARPS * 32, smem, c.stream>>>(p);
+    k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p);
     c.launches++;
 }
 
