@@ -2,6 +2,11 @@
 FP64 path after a full propagation of a workload.
 
     python -m madwave3_gb300.gate --case j0_256x128x60 --iterations 2000 [--out FILE]
+    python -m madwave3_gb300.gate --case j0_256x128x60 --sweep 0,10,20,30,40 --iterations 3000
+
+With --sweep the partial waves J (Omega_max = min(J, 6), parity (-1)^J, the
+J = 0..40 sweep's settings) run batched in one context per precision, and the
+line reports max |Delta P(E)| for every J.
 
 Both runs start from the same packet and take the same number of Chebyshev
 iterations; P(E) is the total reaction probability of totalflux
@@ -49,12 +54,48 @@ def run_gate(case, iterations, cases_dir=None, waves=None):
     return out, e, a, b
 
 
+def run_sweep_gate(case, js, iterations, cases_dir=None):
+    from . import Propagator
+    from .host import generator, setup
+
+    base = cases_dir or os.path.join(tempfile.gettempdir(), "mw3_gate_cases")
+    d = os.path.join(base, case)
+    if not os.path.exists(os.path.join(d, "pot", "cont.pot")):
+        generator.write_case(d, **generator.CASES[case])
+    runs = setup.load_sweep(os.path.join(d, "input.dat"), js, generator.jsweep_inputs)
+    out = {"case": case, "J": list(js), "iterations": iterations,
+           "blocks": [int(r.ncan) for r in runs], "stored_points": int(sum(r.ntot for r in runs))}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        p = Propagator(runs, prec)
+        p.start()
+        p.sync()
+        t = time.time()
+        p.run(iterations - 1)
+        p.sync()
+        out["seconds_" + prec] = time.time() - t
+        res[prec] = [p.totalflux(w)[0] for w in range(len(runs))]
+        p.close()
+    per = []
+    for w, J in enumerate(js):
+        a, b = res["fp64"][w], res["mixed"][w]
+        per.append({"J": J, "max_abs_dP": float(np.abs(a - b).max()), "max_P": float(np.abs(a).max())})
+    out["per_J"] = per
+    out["max_abs_dP"] = max(x["max_abs_dP"] for x in per)
+    out["pass_1e-4"] = bool(out["max_abs_dP"] <= 1e-4)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="j0_256x128x60")
     ap.add_argument("--iterations", type=int, default=2000)
     ap.add_argument("--out", default=None, help="also write E, P_fp64, P_mixed as text")
+    ap.add_argument("--sweep", default=None, help="comma-separated J of a batched partial-wave gate")
     args = ap.parse_args()
+    if args.sweep:
+        print(json.dumps(run_sweep_gate(args.case, [int(x) for x in args.sweep.split(",")], args.iterations)))
+        return
     out, e, a, b = run_gate(args.case, args.iterations)
     if args.out:
         np.savetxt(args.out, np.stack([e, a, b], 1), header="E(eV) P_fp64 P_mixed")
