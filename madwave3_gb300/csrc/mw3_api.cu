@@ -326,6 +326,20 @@ int build_device(Ctx &c)
     c.tmp_cap = NT;
     TRY(dalloc(c, &c.d_tc_err, 1));
     c.nchunk = (c.npt + 1023) / 1024;
+    if (c.nchunk > 256) {
+        c.err = "more than 256 x 1024 stored points in one angle";
+        return MW3_ERR_UNSUPPORTED;
+    }
+    {
+        std::vector<int> ch;
+        for (int seg = 0; seg < c.nseg; seg++) {
+            int a = seg % na;
+            for (int k = 0; k * 1024 < c.npunreal[a]; k++) ch.push_back(seg * 256 + k);
+        }
+        if (ch.empty()) ch.push_back(0);
+        c.n_upd_chunks = (int)ch.size();
+        TRY(dupload(c, &c.d_upd_chunks, ch));
+    }
     TRY(dalloc(c, &c.d_normpart, (size_t)c.nseg * c.nchunk));
     // ---- accumulators: context-wide arrays, each wave a slice ----
     {

@@ -164,6 +164,8 @@ struct Ctx {
     int64_t tmp_cap = 0;
     int nseg = 0;                    // G*na segments, block-major
     int nchunk = 1;                  // point chunks per segment (kPointChunk points each)
+    int *d_upd_chunks = nullptr;     // non-empty (segment, chunk) pairs, seg * 256 + chunk
+    int n_upd_chunks = 0;
     // context-wide accumulators (all waves share netot, the energy grid, j/v ranges)
     int NF = 0, netot = 0, nj = 0, nv = 0;
     int64_t *d_fl_idx = nullptr, *d_fl_didx = nullptr;

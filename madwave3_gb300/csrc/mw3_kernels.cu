@@ -411,6 +411,8 @@ struct UpdArgs {
     double emindlt, delta2;
     double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
     const double *vr;              // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
+    const int *chunks;             // non-empty (segment, chunk) pairs as seg * 256 + chunk
+    int nchunk;                    // chunks per segment (norm-partial stride)
     int first;
     double *normpart;              // [G*na]
     int nofe;                      // max over waves; 0 = funE off
@@ -419,14 +421,17 @@ struct UpdArgs {
     const int64_t *wflat0;         // [W+1]
 };
 
+// one CTA per non-empty (segment, chunk) pair of the list (angles hold different
+// numbers of stored points, so a full segment x chunk grid is a third empty)
 template <typename T, typename HT>
 __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
 {
-    const int seg = blockIdx.x;
+    const int ent = u.chunks[blockIdx.x];
+    const int seg = ent >> 8, chunk = ent & 255;
     const int g = seg / d.na, a = seg % d.na;
     const int w = d.blk_wave[g];
     const int64_t off = d.foff[seg];
-    const int n = min(d.npunreal[a], (int)(blockIdx.y + 1) * kPointChunk);
+    const int n = min(d.npunreal[a], (chunk + 1) * kPointChunk);
     const int n1 = d.n1, n2 = d.n2, ne = d.ne;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // same-Omega sources of V psi for this segment: potential row and psi_k row
@@ -462,7 +467,7 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
     double *zf = (u.nofe > 0 && !u.first) ? u.zfe[w] : nullptr;
     int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
     constexpr int U = kPointChunk / 256;        // points per thread, loads issued together
-    const int ir0 = blockIdx.y * kPointChunk + threadIdx.x;
+    const int ir0 = chunk * kPointChunk + threadIdx.x;
     int r1[U], r2[U];
     double hv[U], pk[U], p1[U];
 #pragma unroll
@@ -550,7 +555,7 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += s_wsum[i];
-        u.normpart[(size_t)seg * gridDim.y + blockIdx.y] = t;
+        u.normpart[(size_t)seg * u.nchunk + chunk] = t;
     }
 }
 
@@ -1084,6 +1089,8 @@ void launch_update(Ctx &c, int first)
     u.rdelta = 1.0 / c.grid.delta2;
     u.r2delta = 2.0 / c.grid.delta2;
     u.vr = c.d_vr;
+    u.chunks = c.d_upd_chunks;
+    u.nchunk = c.nchunk;
     u.first = first;
     u.normpart = c.d_normpart;
     u.nofe = c.nofemax;
@@ -1093,9 +1100,9 @@ void launch_update(Ctx &c, int first)
     stage_mark(c, 5);
     if (c.h32) {
         u.H = c.d_h32;
-        k_update<T, float><<<dim3(c.nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+        k_update<T, float><<<c.n_upd_chunks, 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
     } else {
-        k_update<T, double><<<dim3(c.nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+        k_update<T, double><<<c.n_upd_chunks, 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
     }
     LAUNCH_CHECK(c);
 }

@@ -35,6 +35,11 @@ constexpr uint32_t AG_APLANE = 128 * AG_K * 4;    // 32 KB: 128 x 64 fp32
 constexpr uint32_t AG_DPLANE = 64 * AG_K * 4;     // 16 KB: 64 x 64 fp32
 constexpr uint32_t AG_SBO = (AG_K / 4) * 128;     // 2 KB between 8-row groups
 constexpr uint32_t AG_BYTES = 2 * AG_APLANE + 2 * AG_DPLANE;   // 96 KB
+// the tile's rectangle -> stored-point map (the same for every block) as 16-bit
+// indices, [angle][tile row], 0xFFFF = not stored; and the block's flat starts
+constexpr uint32_t AG_MAP = AG_K * 128 * 2;       // 16 KB
+constexpr uint32_t AG_FO = AG_K * 8;              // 512 B
+constexpr uint32_t AG_SMEM = AG_BYTES + AG_MAP + AG_FO + 64;
 constexpr uint32_t AG_COLS = 256;                 // three ring slots + the output tile
 constexpr uint32_t AG_OUT = 192;                  // column of the output tile
 
@@ -105,11 +110,15 @@ __device__ __forceinline__ void ang_issue(uint32_t dcol, const unsigned char *a,
 template <typename HT>
 __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
 {
-    extern __shared__ __align__(1024) unsigned char smraw[];
-    unsigned char *sm = smraw + ((1024 - (smem_u32(smraw) & 1023)) & 1023);
+    // the no-swizzle operand layout needs 16-byte alignment only; keeping the
+    // footprint at 113 KB lets two CTAs share an SM
+    extern __shared__ __align__(128) unsigned char smraw[];
+    unsigned char *sm = smraw;
     unsigned char *AS = sm;                            // A operand: X tile, then Hb
     unsigned char *DS = sm + 2 * AG_APLANE;            // B operand: D_fw, then D_bk
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + AG_BYTES);   // [0] bulk copy, [1] MMA
+    uint16_t *s_map = reinterpret_cast<uint16_t *>(sm + AG_BYTES);
+    int64_t *s_fo = reinterpret_cast<int64_t *>(sm + AG_BYTES + AG_MAP);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + AG_BYTES + AG_MAP + AG_FO);   // [0] bulk copy, [1] MMA
     uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) tmem_alloc(slot, AG_COLS);
@@ -127,6 +136,13 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
     const int r1_0 = tile >> 16, r2_0 = tile & 0xFFFF;
     const int ch = p.chain0 + blockIdx.y;
     const int cb = p.chain_ptr[ch], L = p.chain_ptr[ch + 1] - cb;
+    // the tile's map, once for the whole chain (a quarter warp reads 8 consecutive R)
+    for (int e = threadIdx.x; e < AG_K * 128; e += blockDim.x) {
+        int a = e >> 7, mm = e & 127;
+        int gr1 = r1_0 + (mm >> 3), gr2 = r2_0 + (mm & 7);
+        int v = (a < na && gr1 < n1 && gr2 < n2) ? __ldg(p.map + ((size_t)a * n1 + gr1) * n2 + gr2) : -1;
+        s_map[e] = v < 0 ? (uint16_t)0xFFFF : (uint16_t)v;
+    }
     // this thread's tile row (tensor-memory lane) and column half
     const int q4 = warp & 3, half = warp >> 2;
     const int m = q4 * 32 + lane;
@@ -169,6 +185,9 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
         const int om = p.blk_om[g];
         const bool hp = pos > 0 && p.blk_om[p.chain[cb + pos - 1]] == om - 1;
         const bool hn = pos + 1 < L && p.blk_om[p.chain[cb + pos + 1]] == om + 1;
+        // the block's flat starts for the epilogue (every thread is past the previous
+        // epilogue here; the barrier after Hb publishes them)
+        if (threadIdx.x < na) s_fo[threadIdx.x] = __ldg(p.foff + (size_t)g * na + threadIdx.x);
         if (threadIdx.x == 0) {              // D_b^T for the way back, while Hb is formed
             mbar_expect_tx(&bars[0], 2 * AG_DPLANE);
             bulk_g2s(DS, p.dbk + (size_t)g * 2 * 64 * AG_K, 2 * AG_DPLANE, &bars[0]);
@@ -230,7 +249,6 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
         if (__syncthreads_or(bad)) break;
         // ---- H += result at the stored points of this block ----
         {
-            const int64_t *fo = p.foff + (size_t)g * na;
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
                 const int a0 = half * 32 + cc * 16;
@@ -238,18 +256,19 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
                 tmem_ld16(lrow + AG_OUT + a0, v);
 #pragma unroll
                 for (int h8 = 0; h8 < 16; h8 += 8) {
-                    int idx[8];
+                    int64_t at[8];
 #pragma unroll
                     for (int i = 0; i < 8; i++) {
                         int a = a0 + h8 + i;
-                        idx[i] = (inrow && a < na) ? __ldg(p.map + ((size_t)a * n1 + ir1) * n2 + ir2) : -1;
+                        unsigned idx = s_map[a * 128 + m];
+                        at[i] = (a < na && idx != 0xFFFFu) ? s_fo[a] + (int64_t)idx : -1;
                     }
                     HT hv[8];
 #pragma unroll
-                    for (int i = 0; i < 8; i++) hv[i] = idx[i] >= 0 ? p.H[fo[a0 + h8 + i] + idx[i]] : (HT)0;
+                    for (int i = 0; i < 8; i++) hv[i] = at[i] >= 0 ? p.H[at[i]] : (HT)0;
 #pragma unroll
                     for (int i = 0; i < 8; i++)
-                        if (idx[i] >= 0) p.H[fo[a0 + h8 + i] + idx[i]] = hv[i] + (HT)v[h8 + i];
+                        if (at[i] >= 0) p.H[at[i]] = hv[i] + (HT)v[h8 + i];
                 }
             }
         }
@@ -316,6 +335,7 @@ int build_tc_ang(Ctx &c)
     using tc::AG_K;
     c.use_tc_ang = false;
     if (c.fp64 || !c.use_tc || c.na < 2 || c.na > AG_K) return MW3_OK;
+    if (c.npt >= 0xFFFF) return MW3_OK;                // the tile map holds 16-bit point indices
     const int na = c.na, n1 = c.n1, n2 = c.n2, G = c.G;
     std::vector<float> dfw((size_t)G * 2 * 64 * AG_K, 0.f), dbk((size_t)G * 2 * 64 * AG_K, 0.f);
     std::vector<float> yj((size_t)G * n1 * AG_K, 0.f), l2((size_t)G * 3 * n2 * AG_K, 0.f);
@@ -419,7 +439,7 @@ static void tc_ang_launch(Ctx &c, const float *X, HT *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    const size_t smem = AG_BYTES + 64 + 1024;
+    const size_t smem = AG_SMEM;
     if (!attr) {
         cudaFuncSetAttribute(k_tc_ang<HT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
