@@ -77,11 +77,12 @@ __device__ __forceinline__ void d2_split4(unsigned char *hi, uint32_t lo_off, ui
     *reinterpret_cast<float4 *>(hi + lo_off + off) = l;
 }
 
-// X rows r < nn, columns 2j + parity for j in [16 jc, 16 jc + 16): each thread
-// takes two (row, 4 j) groups, reading the 8 consecutive columns that hold them;
-// a quarter warp covers 8 rows of one 16-byte column group (one core matrix)
+// X rows r < nn, columns 2j + parity for j in [16 jc, 16 jc + 16): each of the
+// 512 fill threads takes one (row, 4 j) group, reading the 8 consecutive columns
+// that hold it; a quarter warp covers 8 rows of one 16-byte column group (one
+// core matrix)
 struct XStage {
-    float4 v[2][2];
+    float4 v[2];
     __device__ __forceinline__ static void idx(int e, int &r, int &kg)
     {
         int rest = e >> 3;
@@ -90,41 +91,35 @@ struct XStage {
     }
     __device__ __forceinline__ void load(const float *Xs, int n2, int nn, int jc)
     {
+        int r, kg;
+        idx(threadIdx.x, r, kg);
+        int k = 2 * (jc * D2_KC + kg * 4);              // first of the 8 columns
+        float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0;
+        if (r < nn) {
+            const float *q = Xs + (size_t)r * n2 + k;
+            if (k + 7 < n2 && (n2 & 3) == 0) {
+                x0 = __ldg(reinterpret_cast<const float4 *>(q));
+                x1 = __ldg(reinterpret_cast<const float4 *>(q + 4));
+            } else {
+                float t[8];
 #pragma unroll
-        for (int i = 0; i < 2; i++) {
-            int r, kg;
-            idx(threadIdx.x + 256 * i, r, kg);
-            int k = 2 * (jc * D2_KC + kg * 4);          // first of the 8 columns
-            float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0;
-            if (r < nn) {
-                const float *q = Xs + (size_t)r * n2 + k;
-                if (k + 7 < n2 && (n2 & 3) == 0) {
-                    x0 = __ldg(reinterpret_cast<const float4 *>(q));
-                    x1 = __ldg(reinterpret_cast<const float4 *>(q + 4));
-                } else {
-                    float t[8];
-#pragma unroll
-                    for (int u = 0; u < 8; u++) t[u] = (k + u < n2) ? __ldg(q + u) : 0.f;
-                    x0 = make_float4(t[0], t[1], t[2], t[3]);
-                    x1 = make_float4(t[4], t[5], t[6], t[7]);
-                }
+                for (int u = 0; u < 8; u++) t[u] = (k + u < n2) ? __ldg(q + u) : 0.f;
+                x0 = make_float4(t[0], t[1], t[2], t[3]);
+                x1 = make_float4(t[4], t[5], t[6], t[7]);
             }
-            v[i][0] = x0;
-            v[i][1] = x1;
         }
+        v[0] = x0;
+        v[1] = x1;
     }
     __device__ __forceinline__ void store(unsigned char *dst, int parity) const
     {
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            int r, kg;
-            idx(threadIdx.x + 256 * i, r, kg);
-            const float4 &a = v[i][0], &b = v[i][1];
-            if (parity == 0)
-                d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.x, a.z, b.x, b.z);
-            else
-                d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.y, a.w, b.y, b.w);
-        }
+        int r, kg;
+        idx(threadIdx.x, r, kg);
+        const float4 &a = v[0], &b = v[1];
+        if (parity == 0)
+            d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.x, a.z, b.x, b.z);
+        else
+            d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.y, a.w, b.y, b.w);
     }
 };
 
@@ -134,18 +129,21 @@ struct XStage {
 //   D3 = S1 (D2 o F^T)^T at [0, 256)                     (lane r1, column R)
 //   D4 = D3 S2 folded:   E at [256,384), O at [384,512)  (lane r1, column i < h)
 //
-// Warp roles (320 threads): warps 0-7 build the register-side operand of each
-// chunk (two warps per 32-lane quarter of tensor memory) and write H; warp 8
-// issues the MMAs; warp 9 issues the bulk copies of the DST-matrix operands.
-// They meet only at per-stage mbarriers: copy_full (bytes landed), fill_full
-// (8 fill-warp arrivals) and empty (the MMAs that read the stage completed).
+// Warp roles (576 threads): warps 0-15 build the register-side operand of each
+// chunk (four warps per 32-lane quarter of tensor memory, each a quarter of
+// the chunk) and write H; warp 16 issues the MMAs; warp 17 issues the bulk
+// copies of the DST-matrix operands.  They meet only at per-stage mbarriers:
+// copy_full (bytes landed), fill_full (16 fill-warp arrivals) and empty (the
+// MMAs that read the stage completed).
 // Chunk t uses stage t % NS for the (t / NS)-th time, so every wait names the
 // phase parity (t / NS) & 1; no role can run a full phase ahead of a waiter.
 // The three roles walk the same chunk sequence as nested loops (product, then
 // parity and K chunk), with no integer division per chunk.  After any wait
 // runs out of time the CTA's shared failure flag makes every later wait return
 // at once, so a fault ends the kernel instead of hanging it.
-constexpr int D2_WARPS = 10;
+constexpr int D2_FILL = 16;                        // fill warps
+constexpr int D2_WARPS = D2_FILL + 2;
+constexpr int D2_MMA_WARP = D2_FILL, D2_COPY_WARP = D2_FILL + 1;
 
 __device__ __forceinline__ void mbar_arrive1(uint64_t *mbar)
 {
@@ -188,7 +186,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     if (threadIdx.x == 0) {
         for (int i = 0; i < D2_NS; i++) {
             mbar_init(&copy_full[i], 1);
-            mbar_init(&fill_full[i], 8);
+            mbar_init(&fill_full[i], D2_FILL);
             mbar_init(&empty[i], 1);
         }
         *fail = 0;
@@ -211,9 +209,9 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     const int nkr = (nn + D2_KC - 1) / D2_KC;           // K chunks of the products along r1
     const int total = 4 * nkh + 2 * nkr;
     const float *S1p = p.s1planes + p.s1off[w * na + a];
-    int copies = 0;                                     // copies issued (warp 9, lane 0)
+    int copies = 0;                                     // copies issued (copy warp, lane 0)
 
-    if (warp == 9) {
+    if (warp == D2_COPY_WARP) {
         // ---- bulk copies of the DST-matrix operands ----
         if (lane == 0)
             d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
@@ -228,7 +226,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                 bulk_g2s(alongR ? big : small, src, D2_SMALL, &copy_full[s]);
                 copies = t + 1;
             });
-    } else if (warp == 8) {
+    } else if (warp == D2_MMA_WARP) {
         // ---- MMA issue: descriptors built once, advanced by 16-byte units ----
         if (lane == 0) {
             const uint64_t k16 = 256 >> 4;                  // one K step of 8 (two core matrices)
@@ -280,20 +278,24 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             });
         }
     } else {
-        // ---- operand fills (warps 0-7) and the H epilogue ----
+        // ---- operand fills (warps 0-15) and the H epilogue ----
+        // warp = 4 sub + q4: q4 the 32-lane quarter of tensor memory it reads, sub
+        // the quarter of each chunk it builds
         const float *Xs = p.X + (size_t)seg * n1 * n2;
-        const int q4 = warp & 3, half = warp >> 2;
+        const int q4 = warp & 3, sub = warp >> 2;
         const int m = q4 * 32 + lane;                   // the tensor-memory lane this thread reads
         const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
         const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
         const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
-        const int rR = 128 * half + m;                  // the R row this thread fills in the third product
-        const float e2 = (half < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
+        // second and third products: sub & 1 picks the row set, sub >> 1 the 8-column half
+        const int rset = sub & 1, colh = sub >> 1;
+        const int rR = 128 * rset + m;                  // the R row this thread fills in the third product
+        const float e2 = (rset < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
         const float radcut = p.radcut;
-        // G2 rows: half 0 the sum rows R = i, half 1 the difference rows R = n2-1-i
-        const bool on2 = half == 0 ? (m < h) : (m < n2 - h);
-        const int R2 = half == 0 ? m : n2 - 1 - m;
-        const float sg2 = half == 0 ? 1.f : -1.f;
+        // second product rows: rset 0 the sum rows R = i, rset 1 the difference rows R = n2-1-i
+        const bool on2 = rset == 0 ? (m < h) : (m < n2 - h);
+        const int R2 = rset == 0 ? m : n2 - 1 - m;
+        const float sg2 = rset == 0 ? 1.f : -1.f;
         XStage xs;
         xs.load(Xs, n2, nn, 0);
         d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
@@ -312,66 +314,64 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                 const int nj = jc + 1 < nkh ? jc + 1 : 0;
                 if (par == 0 || jc + 1 < nkh) xs.load(Xs, n2, nn, nj);
             } else if (gi == 1) {
-                // A = D1 rows R into the big slot from the E and O columns of lane i
+                // A = D1 rows R into the big slot from 8 of the E and O columns of lane i
                 // (all lanes load; lanes without a row store nothing)
-                float e[16], o[16];
-                tmem_ld16(lrow + (uint32_t)k0, e);
-                tmem_ld16(lrow + 128u + (uint32_t)k0, o);
+                const int kc = k0 + 8 * colh;
+                float e[8], o[8];
+                tmem_ld8(lrow + (uint32_t)kc, e);
+                tmem_ld8(lrow + 128u + (uint32_t)kc, o);
                 if (on2) {
-                    const bool full = k0 + D2_KC <= nn;
+                    const bool full = kc + 8 <= nn;
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
+                    for (int j = 0; j < 2; j++) {
                         float tv[4];
 #pragma unroll
                         for (int uu = 0; uu < 4; uu++) {
                             float x = e[4 * j + uu] + sg2 * o[4 * j + uu];
-                            tv[uu] = (full || k0 + 4 * j + uu < nn) ? x : 0.f;
+                            tv[uu] = (full || kc + 4 * j + uu < nn) ? x : 0.f;
                         }
-                        d2_split4(big, big_lo, kmaj_off(R2, 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
+                        d2_split4(big, big_lo, kmaj_off(R2, 8 * colh + 4 * j, D2_KC), tv[0], tv[1], tv[2], tv[3]);
                     }
                 }
             } else if (gi == 2) {
-                // B = (D2 o F^T) rows R into the big slot; warp half = R tile (warp-uniform)
-                if (half < NT) {
-                    float v[16];
-                    tmem_ld16(lrow + 256u + 128u * half + (uint32_t)k0, v);
-                    float pv[16];
+                // B = (D2 o F^T) rows R into the big slot: R tile rset, 8 columns (warp-uniform test)
+                if (rset < NT) {
+                    const int kc = k0 + 8 * colh;
+                    float v[8];
+                    tmem_ld8(lrow + 256u + 128u * rset + (uint32_t)kc, v);
+                    float pv[8];
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        float4 q = __ldg(reinterpret_cast<const float4 *>(p1f + k0) + j);
+                    for (int j = 0; j < 2; j++) {
+                        float4 q = __ldg(reinterpret_cast<const float4 *>(p1f + kc) + j);
                         pv[4 * j] = q.x; pv[4 * j + 1] = q.y; pv[4 * j + 2] = q.z; pv[4 * j + 3] = q.w;
                     }
-                    const bool full = k0 + D2_KC <= nn && rR < n2;
+                    const bool full = kc + 8 <= nn && rR < n2;
 #pragma unroll
-                    for (int i = 0; i < 16; i++) {
+                    for (int i = 0; i < 8; i++) {
                         float ek = fminf(pv[i] + e2, radcut);
                         float x = v[i] * ek * divi;
-                        v[i] = (full || (k0 + i < nn && rR < n2)) ? x : 0.f;
+                        v[i] = (full || (kc + i < nn && rR < n2)) ? x : 0.f;
                     }
 #pragma unroll
-                    for (int j = 0; j < 4; j++)
-                        d2_split4(big, big_lo, kmaj_off(rR, 4 * j, D2_KC), v[4 * j], v[4 * j + 1], v[4 * j + 2],
-                                  v[4 * j + 3]);
+                    for (int j = 0; j < 2; j++)
+                        d2_split4(big, big_lo, kmaj_off(rR, 8 * colh + 4 * j, D2_KC), v[4 * j], v[4 * j + 1],
+                                  v[4 * j + 2], v[4 * j + 3]);
                 }
             } else {
-                // A = D3 columns 2j + parity (rows r1) into the small slot; each warp half
-                // reads 16 consecutive columns and keeps the 8 of this parity
-                float v[16];
-                const int col0 = 2 * k0 + 16 * half;
-                tmem_ld16(lrow + (uint32_t)col0, v);
-                const bool full = col0 + 16 <= n2;
+                // A = D3 columns 2j + parity (rows r1) into the small slot; warp sub reads the
+                // 8 consecutive columns of j in [k0 + 4 sub, k0 + 4 sub + 4) and keeps 4
+                float v[8];
+                const int col0 = 2 * k0 + 8 * sub;
+                tmem_ld8(lrow + (uint32_t)col0, v);
+                const bool full = col0 + 8 <= n2;
+                float tv[4];
 #pragma unroll
-                for (int j = 0; j < 2; j++) {
-                    float tv[4];
-#pragma unroll
-                    for (int uu = 0; uu < 4; uu++) {
-                        int cc = 2 * (4 * j + uu);             // register index fixed at compile time
-                        float x = par == 0 ? v[cc] : v[cc + 1];
-                        tv[uu] = (full || col0 + cc + par < n2) ? x : 0.f;
-                    }
-                    d2_split4(small, D2_SMALL_LO, kmaj_off(m, 8 * half + 4 * j, D2_KC), tv[0], tv[1], tv[2],
-                              tv[3]);
+                for (int uu = 0; uu < 4; uu++) {
+                    const int cc = 2 * uu;                     // register index fixed at compile time
+                    float x = par == 0 ? v[cc] : v[cc + 1];
+                    tv[uu] = (full || col0 + cc + par < n2) ? x : 0.f;
                 }
+                d2_split4(small, D2_SMALL_LO, kmaj_off(m, 4 * sub, D2_KC), tv[0], tv[1], tv[2], tv[3]);
             }
             // make the generic shared-memory writes visible to the tensor cores, order the
             // tensor-memory loads before the arrival, then one arrival per warp
@@ -387,8 +387,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             const int *mT = p.mapT + (size_t)a * n2 * n1;
             const int64_t fo = p.foff[seg];
 #pragma unroll
-            for (int cc = 0; cc < 4; cc++) {
-                const int i0 = 64 * half + 16 * cc;
+            for (int cc = 0; cc < 2; cc++) {
+                const int i0 = 32 * sub + 16 * cc;
                 float e[16], o[16];
                 tmem_ld16(lrow + 256u + (uint32_t)i0, e);
                 tmem_ld16(lrow + 384u + (uint32_t)i0, o);
@@ -411,9 +411,9 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     // must be done: the copy warp waits for its last copy, the MMA warp for its
     // last commit (which tracks all its MMAs); both phases were issued, so these
     // bounded waits end at once in a normal run and soon after a failure
-    if (lane == 0 && warp == 9 && copies > 0)
+    if (lane == 0 && warp == D2_COPY_WARP && copies > 0)
         mbar_wait(&copy_full[(copies - 1) & (D2_NS - 1)], ((copies - 1) >> 2) & 1);
-    if (lane == 0 && warp == 8) mbar_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1);
+    if (lane == 0 && warp == D2_MMA_WARP) mbar_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1);
     fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && *fail) atomicExch(p.err, 1);
