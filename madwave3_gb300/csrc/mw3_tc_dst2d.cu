@@ -79,8 +79,9 @@ __device__ __forceinline__ void d2_split4(unsigned char *hi, uint32_t lo_off, ui
 
 // X rows r < nn, columns 2j + parity for j in [16 jc, 16 jc + 16): each of the
 // 512 fill threads takes one (row, 4 j) group, reading the 8 consecutive columns
-// that hold it; a quarter warp covers 8 rows of one 16-byte column group (one
-// core matrix)
+// that hold it (both parities); a quarter warp covers 8 rows of one 16-byte
+// column group (one core matrix).  Loads need only the rectangle's bounds, so
+// they can be issued before the row count is known; rows r >= nn store zeros.
 struct XStage {
     float4 v[2];
     __device__ __forceinline__ static void idx(int e, int &r, int &kg)
@@ -89,13 +90,13 @@ struct XStage {
         kg = rest & 3;
         r = (rest >> 2) * 8 + (e & 7);
     }
-    __device__ __forceinline__ void load(const float *Xs, int n2, int nn, int jc)
+    __device__ __forceinline__ void load(const float *Xs, int n2, int nrow, int jc)
     {
         int r, kg;
         idx(threadIdx.x, r, kg);
         int k = 2 * (jc * D2_KC + kg * 4);              // first of the 8 columns
         float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0;
-        if (r < nn) {
+        if (r < nrow) {
             const float *q = Xs + (size_t)r * n2 + k;
             if (k + 7 < n2 && (n2 & 3) == 0) {
                 x0 = __ldg(reinterpret_cast<const float4 *>(q));
@@ -111,11 +112,12 @@ struct XStage {
         v[0] = x0;
         v[1] = x1;
     }
-    __device__ __forceinline__ void store(unsigned char *dst, int parity) const
+    __device__ __forceinline__ void store(unsigned char *dst, int parity, int nn) const
     {
         int r, kg;
         idx(threadIdx.x, r, kg);
-        const float4 &a = v[0], &b = v[1];
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 &a = r < nn ? v[0] : z, &b = r < nn ? v[1] : z;
         if (parity == 0)
             d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.x, a.z, b.x, b.z);
         else
@@ -159,13 +161,15 @@ __device__ __forceinline__ bool d2_wait(uint64_t *mbar, uint32_t parity, volatil
 }
 
 // the chunk sequence of one slab: product gi in 0..3, parity half par (products
-// along R) and K chunk jc; f(t, gi, par, jc) is called for t = 0, 1, ...
+// along R) and K chunk jc; f(t, gi, par, jc) is called for t = 0, 1, ...  The
+// first product alternates the parities per K chunk, so both of its chunks use
+// one load of X; E and O are separate accumulators, so the order is free.
 template <typename F>
 __device__ __forceinline__ void d2_for_chunks(int nkh, int nkr, F &&f)
 {
     int t = 0;
-    for (int par = 0; par < 2; par++)
-        for (int jc = 0; jc < nkh; jc++) f(t++, 0, par, jc);
+    for (int jc = 0; jc < nkh; jc++)
+        for (int par = 0; par < 2; par++) f(t++, 0, par, jc);
     for (int jc = 0; jc < nkr; jc++) f(t++, 1, 0, jc);
     for (int jc = 0; jc < nkr; jc++) f(t++, 2, 0, jc);
     for (int par = 0; par < 2; par++)
@@ -182,6 +186,18 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     uint32_t *slot = reinterpret_cast<uint32_t *>(empty + D2_NS);
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int na = p.na, n1 = p.n1, n2 = p.n2;
+    const int h = (n2 + 1) >> 1;                        // rows i < h: E + O; row n2-1-i: E - O
+    const int nkh = (h + D2_KC - 1) / D2_KC;            // K chunks of one parity half
+    const int seg = p.seg0 + blockIdx.x;
+    // the fill warps start the first two K chunks of X before anything else: each
+    // X chunk is loaded two chunks of X ahead of its use (four operand fills)
+    const float *Xs = p.X + (size_t)seg * n1 * n2;
+    XStage xa, xb;                                      // X chunks of even and odd jc
+    if (warp < D2_FILL) {
+        xa.load(Xs, n2, n1, 0);
+        if (nkh > 1) xb.load(Xs, n2, n1, 1);
+    }
     if (warp == 0) tmem_alloc(slot, 512);
     if (threadIdx.x == 0) {
         for (int i = 0; i < D2_NS; i++) {
@@ -196,13 +212,9 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     __syncthreads();
     fence_after_sync();
     const uint32_t tb = *slot;
-    const int na = p.na, n1 = p.n1, n2 = p.n2;
-    const int h = (n2 + 1) >> 1;                        // rows i < h: E + O; row n2-1-i: E - O
-    const int nkh = (h + D2_KC - 1) / D2_KC;            // K chunks of one parity half
     const int NT = (n2 + 127) / 128;                    // R tiles of D2 and of the D3 columns
     const int RB = 128 * NT;
     const uint32_t big_lo = (uint32_t)RB * D2_KC * 4;   // lo plane of an RB-row operand
-    const int seg = p.seg0 + blockIdx.x;
     const int g = seg / na, a = seg % na, w = p.blk_wave[g];
     const int nn = p.nopr1[w * na + a];
     const int nnp = (nn + 15) & ~15;                    // N of the products along r1
@@ -281,7 +293,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
         // ---- operand fills (warps 0-15) and the H epilogue ----
         // warp = 4 sub + q4: q4 the 32-lane quarter of tensor memory it reads, sub
         // the quarter of each chunk it builds
-        const float *Xs = p.X + (size_t)seg * n1 * n2;
         const int q4 = warp & 3, sub = warp >> 2;
         const int m = q4 * 32 + lane;                   // the tensor-memory lane this thread reads
         const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
@@ -296,8 +307,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
         const bool on2 = rset == 0 ? (m < h) : (m < n2 - h);
         const int R2 = rset == 0 ? m : n2 - 1 - m;
         const float sg2 = rset == 0 ? 1.f : -1.f;
-        XStage xs;
-        xs.load(Xs, n2, nn, 0);
         d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
             const int s = t & (D2_NS - 1), u = t >> 2;
             unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
@@ -309,10 +318,16 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             if (t >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
             const int k0 = jc * D2_KC;
             if (gi == 0) {
-                // B = Xs columns of this parity (rows r1) into the small slot
-                xs.store(small, par);
-                const int nj = jc + 1 < nkh ? jc + 1 : 0;
-                if (par == 0 || jc + 1 < nkh) xs.load(Xs, n2, nn, nj);
+                // B = Xs columns of this parity (rows r1) into the small slot; after the
+                // second parity the buffer takes chunk jc + 2 (warp-uniform branches keep
+                // the register buffers static)
+                if (jc & 1) {
+                    xb.store(small, par, nn);
+                    if (par == 1 && jc + 2 < nkh) xb.load(Xs, n2, n1, jc + 2);
+                } else {
+                    xa.store(small, par, nn);
+                    if (par == 1 && jc + 2 < nkh) xa.load(Xs, n2, n1, jc + 2);
+                }
             } else if (gi == 1) {
                 // A = D1 rows R into the big slot from 8 of the E and O columns of lane i
                 // (all lanes load; lanes without a row store nothing)
@@ -381,10 +396,19 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             if (lane == 0) mbar_arrive1(&fill_full[s]);
         });
         // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
+        const int *mT = p.mapT + (size_t)a * n2 * n1;
+        if (m < nn) {
+            // the map entries this thread reads, into L1 while the last MMAs run
+#pragma unroll 4
+            for (int uu = 0; uu < 32; uu++) {
+                int i = 32 * sub + uu;
+                if (i < h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)i * n1 + m));
+                if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
+            }
+        }
         d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
         if (!*fail) {
-            const int *mT = p.mapT + (size_t)a * n2 * n1;
             const int64_t fo = p.foff[seg];
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
