@@ -248,6 +248,8 @@ __device__ __forceinline__ double f32_to_f64_int(float f)
     return __longlong_as_double((long long)(sign | (ex << 52) | ((unsigned long long)mt << 29)));
 }
 
+__device__ __forceinline__ double h_val(double h) { return h; }
+__device__ __forceinline__ double h_val(float h) { return f32_to_f64_int(h); }
 __device__ __forceinline__ double h_load(const double *H, int64_t i) { return H[i]; }
 __device__ __forceinline__ double h_load(const float *H, int64_t i) { return f32_to_f64_int(H[i]); }
 __device__ __forceinline__ void h_store(double *H, int64_t i, double v) { H[i] = v; }
@@ -421,10 +423,22 @@ struct UpdArgs {
     const int64_t *wflat0;         // [W+1]
 };
 
+// funE: zfe[e][i] += zcke[w][e] psi_k+1(i) for the selected energies
+__device__ __forceinline__ void upd_fe(const UpdArgs &u, double *zf, int w, int64_t wst, int64_t wlen, int64_t i,
+                                       double nv)
+{
+    for (int e = 0; e < u.nofe; e++) {
+        const double *ck = u.zcke + ((size_t)w * u.nofe + e) * 2;
+        double *zz = zf + ((size_t)e * wlen + (i - wst)) * 2;
+        zz[0] += ck[0] * nv;
+        zz[1] += ck[1] * nv;
+    }
+}
+
 // one CTA per non-empty (segment, chunk) pair of the list (angles hold different
 // numbers of stored points, so a full segment x chunk grid is a third empty)
 template <typename T, typename HT>
-__global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
+__global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
 {
     const int ent = u.chunks[blockIdx.x];
     const int seg = ent >> 8, chunk = ent & 255;
@@ -468,19 +482,20 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
     int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
     constexpr int U = kPointChunk / 256;        // points per thread, loads issued together
     const int ir0 = chunk * kPointChunk + threadIdx.x;
-    int r1[U], r2[U];
-    double hv[U], pk[U], p1[U];
+    float nrmf = 0.f;
+    if constexpr (sizeof(T) == 8) {
+        int r1[U], r2[U];
+        double hv[U], pk[U], p1[U];
 #pragma unroll
-    for (int k = 0; k < U; k++) {
-        int ir = ir0 + k * 256;
-        bool on = ir < n;
-        r1[k] = on ? i1p[ir] - 1 : 0;
-        r2[k] = on ? i2p[ir] - 1 : 0;
-        hv[k] = on ? h_load(Hp, ir) : 0.0;
-        pk[k] = on ? pkp[ir] : 0.0;
-        p1[k] = on && !u.first ? pm1[ir] : 0.0;
-    }
-    if (sizeof(T) == 8) {
+        for (int k = 0; k < U; k++) {
+            int ir = ir0 + k * 256;
+            bool on = ir < n;
+            r1[k] = on ? i1p[ir] - 1 : 0;
+            r2[k] = on ? i2p[ir] - 1 : 0;
+            hv[k] = on ? h_load(Hp, ir) : 0.0;
+            pk[k] = on ? pkp[ir] : 0.0;
+            p1[k] = on && !u.first ? pm1[ir] : 0.0;
+        }
         for (int q = 0; q < nsrc; q++) {
             const double *vr = s_vrow[q], *pr = s_prow[q];
 #pragma unroll
@@ -489,15 +504,12 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
                 if (ir < n) hv[k] += pr[ir] * vr[ir];
             }
         }
-    }
-    float nrmf = 0.f;
 #pragma unroll
-    for (int k = 0; k < U; k++) {
-        int ir = ir0 + k * 256;
-        if (ir >= n) continue;
-        double nv;
-        if (sizeof(T) == 8) {
+        for (int k = 0; k < U; k++) {
+            int ir = ir0 + k * 256;
+            if (ir >= n) continue;
             // FP64 path: the reference's operations in its order
+            double nv;
             if (u.first) {
                 nv = (hv[k] - emin * pk[k]) / u.delta2;
             } else {
@@ -507,20 +519,48 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             }
             rect[(size_t)r1[k] * n2 + r2[k]] = (T)nv;
             nrm += nv * nv;
-        } else {
-            // mixed path, few FP64 instructions (GB300 runs FP64 at 1/64 of FP32):
-            //   t = H 2/delta2 + sum_s vr_s psi_s = 2 (H psi - emindlt psi) / delta2
-            // with the potential pre-scaled, damping only inside the absorbers,
-            // the FP32 copy rounded with integer operations, the norm partial in FP32
-            const bool damp = !u.first && !(__double_as_longlong(ab1[r1[k]]) == 0x3FF0000000000000LL &&
-                                            __double_as_longlong(ab2[r2[k]]) == 0x3FF0000000000000LL);
+            outp[ir] = nv;
+            if (zf) upd_fe(u, zf, w, wst, wlen, off + ir, nv);
+        }
+    } else {
+        // mixed path, few FP64 instructions (GB300 runs FP64 at 1/64 of FP32):
+        //   t = H 2/delta2 + sum_s vr_s psi_s = 2 (H psi - emindlt psi) / delta2
+        // with the potential pre-scaled, damping only inside the absorbers,
+        // the FP32 copy rounded with integer operations, the norm partial in FP32.
+        // The first source's potential is loaded in one batch with the point's own
+        // data; its psi is psi_k itself when the segment has one electronic state.
+        const double *vr0 = nsrc > 0 ? s_vrow[0] : nullptr, *pr0 = nsrc > 0 ? s_prow[0] : nullptr;
+        const bool self0 = pr0 == pkp;
+        int r1[U], r2[U];
+        HT hr[U];
+        double pk[U], p1[U], v0[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            int ir = ir0 + k * 256;
+            bool on = ir < n;
+            r1[k] = on ? i1p[ir] - 1 : 0;
+            r2[k] = on ? i2p[ir] - 1 : 0;
+            hr[k] = on ? Hp[ir] : (HT)0;
+            pk[k] = on ? pkp[ir] : 0.0;
+            p1[k] = on && !u.first ? pm1[ir] : 0.0;
+            v0[k] = on && vr0 ? vr0[ir] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            int ir = ir0 + k * 256;
+            if (ir >= n) continue;
+            const double a1 = u.first ? 1.0 : ab1[r1[k]], a2 = u.first ? 1.0 : ab2[r2[k]];
+            const bool damp = !u.first && !(__double_as_longlong(a1) == 0x3FF0000000000000LL &&
+                                            __double_as_longlong(a2) == 0x3FF0000000000000LL);
             double acc = (u.first || damp) ? 0.0 : -p1[k];
-            for (int q = 0; q < nsrc; q++) acc = fma(s_vrow[q][ir], s_prow[q][ir], acc);
-            double t = fma(hv[k], u.r2delta, acc);
+            if (vr0) acc = fma(v0[k], self0 ? pk[k] : pr0[ir], acc);
+            for (int q = 1; q < nsrc; q++) acc = fma(s_vrow[q][ir], s_prow[q][ir], acc);
+            double t = fma(h_val(hr[k]), u.r2delta, acc);
+            double nv;
             if (u.first) {
                 nv = 0.5 * t;
             } else if (damp) {
-                double fab = ab1[r1[k]] * ab2[r2[k]];
+                double fab = a1 * a2;
                 nv = fma(-fab, p1[k], t) * fab;
             } else {
                 nv = t;
@@ -528,16 +568,8 @@ __global__ void __launch_bounds__(256) k_update(DevGrid d, UpdArgs u, T *__restr
             float nf = f64_to_f32_int(nv);
             rect[(size_t)r1[k] * n2 + r2[k]] = (T)nf;
             nrmf = fmaf(nf, nf, nrmf);
-        }
-        outp[ir] = nv;
-        if (zf) {
-            int64_t i = off + ir;
-            for (int e = 0; e < u.nofe; e++) {
-                const double *ck = u.zcke + ((size_t)w * u.nofe + e) * 2;
-                double *zz = zf + ((size_t)e * wlen + (i - wst)) * 2;
-                zz[0] += ck[0] * nv;
-                zz[1] += ck[1] * nv;
-            }
+            outp[ir] = nv;
+            if (zf) upd_fe(u, zf, w, wst, wlen, off + ir, nv);
         }
     }
     // norm partial: fixed shuffle tree per warp, then the warps in order (deterministic);
