@@ -331,14 +331,26 @@ int build_device(Ctx &c)
         return MW3_ERR_UNSUPPORTED;
     }
     {
-        std::vector<int> ch;
+        std::vector<mw3::UpdChunk> ch;
         for (int seg = 0; seg < c.nseg; seg++) {
-            int a = seg % na;
-            for (int k = 0; k * 1024 < c.npunreal[a]; k++) ch.push_back(seg * 256 + k);
+            int g = seg / na, a = seg % na, ns = 0;
+            long long voff = -1, poff = -1;
+            for (int q = 0; q < ne; q++) {
+                int sb = vsrc[(size_t)g * ne + q];
+                if (sb < 0) continue;
+                if (ns == 0) {
+                    voff = ((((long long)(be[g] - 1) * ne + (be[sb] - 1)) * na) + a) * c.npt;
+                    poff = foff[(size_t)sb * na + a];
+                }
+                ns++;
+            }
+            for (int k = 0; k * 1024 < c.npunreal[a]; k++)
+                ch.push_back(mw3::UpdChunk{foff[seg], voff, poff, seg, k | (ns << 8),
+                                      std::min(c.npunreal[a], (k + 1) * 1024), (bw[g] << 8) | a});
         }
-        if (ch.empty()) ch.push_back(0);
+        if (ch.empty()) ch.push_back(mw3::UpdChunk{0, -1, -1, 0, 0, 0, 0});
         c.n_upd_chunks = (int)ch.size();
-        TRY(dupload(c, &c.d_upd_chunks, ch));
+        TRY(dupload(c, &c.d_upd_desc, ch));
     }
     TRY(dalloc(c, &c.d_normpart, (size_t)c.nseg * c.nchunk));
     // ---- accumulators: context-wide arrays, each wave a slice ----

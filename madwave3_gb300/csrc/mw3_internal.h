@@ -86,6 +86,19 @@ struct WaveDev {
     double *efe = nullptr, *zfe = nullptr;       // PsiE
 };
 
+// one CTA of the update kernel: a non-empty (segment, point chunk) pair with
+// the table entries its prologue needs already resolved, so no CTA starts with
+// a chain of dependent loads (48 bytes, three 16-byte loads)
+struct alignas(16) UpdChunk {
+    long long off;                   // flat offset of the segment
+    long long voff;                  // first same-Omega source: its row in the potential tables
+    long long poff;                  // first source: flat offset of its psi row (off for the segment itself)
+    int seg;
+    int chunk_ns;                    // point chunk | number of sources << 8
+    int n;                           // stored points of the segment up to the chunk's end
+    int wa;                          // wave << 8 | angle
+};
+
 struct Ctx {
     mw3_grid grid;
     int n1, n2, na, ne, npt;
@@ -164,7 +177,7 @@ struct Ctx {
     int64_t tmp_cap = 0;
     int nseg = 0;                    // G*na segments, block-major
     int nchunk = 1;                  // point chunks per segment (kPointChunk points each)
-    int *d_upd_chunks = nullptr;     // non-empty (segment, chunk) pairs, seg * 256 + chunk
+    UpdChunk *d_upd_desc = nullptr;  // non-empty (segment, chunk) pairs with their tables resolved
     int n_upd_chunks = 0;
     // context-wide accumulators (all waves share netot, the energy grid, j/v ranges)
     int NF = 0, netot = 0, nj = 0, nv = 0;

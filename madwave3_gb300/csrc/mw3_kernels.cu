@@ -413,7 +413,7 @@ struct UpdArgs {
     double emindlt, delta2;
     double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
     const double *vr;              // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
-    const int *chunks;             // non-empty (segment, chunk) pairs as seg * 256 + chunk
+    const UpdChunk *desc;          // non-empty (segment, chunk) pairs, tables resolved
     int nchunk;                    // chunks per segment (norm-partial stride)
     int first;
     double *normpart;              // [G*na]
@@ -436,37 +436,42 @@ __device__ __forceinline__ void upd_fe(const UpdArgs &u, double *zf, int w, int6
 }
 
 // one CTA per non-empty (segment, chunk) pair of the list (angles hold different
-// numbers of stored points, so a full segment x chunk grid is a third empty)
+// numbers of stored points, so a full segment x chunk grid is a third empty); the
+// pair's descriptor carries the table entries, so every thread starts its point
+// loads after one independent 48-byte load
 template <typename T, typename HT>
 __global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
 {
-    const int ent = u.chunks[blockIdx.x];
-    const int seg = ent >> 8, chunk = ent & 255;
-    const int g = seg / d.na, a = seg % d.na;
-    const int w = d.blk_wave[g];
-    const int64_t off = d.foff[seg];
-    const int n = min(d.npunreal[a], (chunk + 1) * kPointChunk);
+    const UpdChunk cd = u.desc[blockIdx.x];
+    const int seg = cd.seg, chunk = cd.chunk_ns & 255, nsrc = cd.chunk_ns >> 8;
+    const int a = cd.wa & 255, w = cd.wa >> 8;
+    const int64_t off = cd.off;
+    const int n = cd.n;
     const int n1 = d.n1, n2 = d.n2, ne = d.ne;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // same-Omega sources of V psi for this segment: potential row and psi_k row
+    // same-Omega sources of V psi for this segment: potential row and psi_k row; the
+    // first from the descriptor, a second or later one (several electronic states)
+    // from the tables
+    const double *vbase = sizeof(T) == 4 ? u.vr : d.vvv;
+    const double *vr0 = nsrc > 0 ? vbase + cd.voff : nullptr, *pr0 = nsrc > 0 ? u.pk + cd.poff : nullptr;
     __shared__ const double *s_vrow[8];
     __shared__ const double *s_prow[8];
-    __shared__ int s_nsrc;
     __shared__ double s_wsum[8];
-    if (threadIdx.x == 0) {
-        int et = d.blk_elec[g], ns = 0;
-        for (int q = 0; q < ne; q++) {
-            int sb = u.vsrc[g * ne + q];
-            if (sb < 0) continue;
-            int es = d.blk_elec[sb];
-            s_vrow[ns] = (sizeof(T) == 4 ? u.vr : d.vvv) + ((((size_t)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
-            s_prow[ns] = u.pk + d.foff[(size_t)sb * d.na + a];
-            ns++;
+    if (nsrc > 1) {
+        if (threadIdx.x == 0) {
+            const int g = seg / d.na, et = d.blk_elec[g];
+            int ns = 0;
+            for (int q = 0; q < ne; q++) {
+                int sb = u.vsrc[g * ne + q];
+                if (sb < 0) continue;
+                int es = d.blk_elec[sb];
+                s_vrow[ns] = vbase + ((((size_t)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
+                s_prow[ns] = u.pk + d.foff[(size_t)sb * d.na + a];
+                ns++;
+            }
         }
-        s_nsrc = ns;
+        __syncthreads();
     }
-    __syncthreads();
-    const int nsrc = s_nsrc;
     const HT *__restrict__ Hp = reinterpret_cast<const HT *>(u.H) + off;
     const double *__restrict__ pkp = u.pk + off;
     const double *__restrict__ pm1 = u.pkm1 + off;
@@ -497,7 +502,7 @@ __global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__re
             p1[k] = on && !u.first ? pm1[ir] : 0.0;
         }
         for (int q = 0; q < nsrc; q++) {
-            const double *vr = s_vrow[q], *pr = s_prow[q];
+            const double *vr = q == 0 ? vr0 : s_vrow[q], *pr = q == 0 ? pr0 : s_prow[q];
 #pragma unroll
             for (int k = 0; k < U; k++) {
                 int ir = ir0 + k * 256;
@@ -529,7 +534,6 @@ __global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__re
         // the FP32 copy rounded with integer operations, the norm partial in FP32.
         // The first source's potential is loaded in one batch with the point's own
         // data; its psi is psi_k itself when the segment has one electronic state.
-        const double *vr0 = nsrc > 0 ? s_vrow[0] : nullptr, *pr0 = nsrc > 0 ? s_prow[0] : nullptr;
         const bool self0 = pr0 == pkp;
         int r1[U], r2[U];
         HT hr[U];
@@ -1121,7 +1125,7 @@ void launch_update(Ctx &c, int first)
     u.rdelta = 1.0 / c.grid.delta2;
     u.r2delta = 2.0 / c.grid.delta2;
     u.vr = c.d_vr;
-    u.chunks = c.d_upd_chunks;
+    u.desc = c.d_upd_desc;
     u.nchunk = c.nchunk;
     u.first = first;
     u.normpart = c.d_normpart;
