@@ -14,9 +14,8 @@
 //   D3[r1][R] = S1 (D2 o F^T)^T    A = S1 (bulk copy)      B = D2 o F^T (tensor memory)
 //   D4[r1][R] = D3 S2              A = D3 (tensor memory)  B = S2 (bulk copy)        [R folded]
 // so H[r1][R] = D4, written with lanes along r1 (stored points are r1-major runs).
-// K streams in chunks of 16 through two shared-memory rings (the copied DST-matrix
-// operand, the operand built from tensor memory or X); the DST matrices are
-// split on the host into TF32 hi/lo planes in the canonical K-major chunk
+// K streams in chunks of 16 through four shared-memory stages; the DST matrices
+// are split on the host into TF32 hi/lo planes in the canonical K-major chunk
 // layout and arrive by one bulk (TMA) copy per chunk.  3xTF32 products with
 // FP32 accumulation as the other tensor-core kernels of the mixed path.
 #include "mw3_internal.h"
@@ -38,23 +37,17 @@ namespace tc {
 // 256 x 256 one.  The products along r1 take N = nopr1 rounded up to 16.
 //
 // Pipeline: the four products form one sequence of K chunks of 16 per slab,
-// streamed through two shared-memory rings by three warp roles (below).
+// streamed through four shared-memory stages by three warp roles (below).
 // Every tcgen05.ld is executed by whole warps (its conditions depend on the
 // warp only); lane-dependent choices are made on the loaded values.
 constexpr int D2_KC = 16;
+constexpr int D2_NS = 4;                                // stages
 constexpr uint32_t D2_SBO = (D2_KC / 4) * 128;          // 512 B between 8-row groups
 constexpr uint32_t D2_SMALL = 2 * 128 * D2_KC * 4;      // 16 KB: hi + lo, 128 rows x 16 k
 constexpr uint32_t D2_SMALL_LO = D2_SMALL / 2;          // lo plane of a 128-row operand
 constexpr uint32_t D2_BIGMAX = 2 * 256 * D2_KC * 4;     // 32 KB: hi + lo, 256 rows x 16 k
-// A bulk copy of one 16 KB chunk takes about 4000 cycles to land (measured with
-// clock stamps per chunk), several times the MMAs of a chunk, so the copies get
-// a deeper ring of their own: seven 16 KB slots, and three 32 KB slots for the
-// built operands (a 256-row operand of the products along r1 takes 32 KB).
-constexpr int D2_NC = 7;                                // copy slots
-constexpr int D2_NF = 3;                                // fill slots
-constexpr uint32_t D2_CSLOT = D2_SMALL;
-constexpr uint32_t D2_FSLOT = D2_BIGMAX;
-constexpr uint32_t D2_BYTES = D2_NF * D2_FSLOT + D2_NC * D2_CSLOT;   // 208 KB
+constexpr uint32_t D2_STAGE = D2_BIGMAX + D2_SMALL;     // 48 KB
+constexpr uint32_t D2_BYTES = D2_NS * D2_STAGE;         // 192 KB
 constexpr int D2_NKH = 128 / D2_KC;                     // K chunks of a 128-wide operand
 constexpr size_t D2_CHUNK = D2_SMALL / 4;               // floats of one 128-row chunk (hi + lo)
 
@@ -141,14 +134,17 @@ struct XStage {
 // Warp roles (576 threads): warps 0-15 build the register-side operand of each
 // chunk (four warps per 32-lane quarter of tensor memory, each a quarter of
 // the chunk) and write H; warp 16 issues the MMAs; warp 17 issues the bulk
-// copies of the DST-matrix operands.  They meet only at per-slot mbarriers:
-// copy_full (bytes landed), copy_empty (the MMAs that read the copy slot
-// completed), fill_full (16 fill-warp arrivals) and fill_empty (the same for
-// the fill slot).  Chunk t uses copy slot t % NC for the (t / NC)-th time and
-// fill slot t % NF for the (t / NF)-th time, so every wait names the parity of
-// that use; no role can run a full phase ahead of a waiter.  The three roles
-// walk the same chunk sequence as nested loops (product, then parity and K
-// chunk) and keep their ring positions incrementally.  After any wait
+// copies of the DST-matrix operands.  They meet only at two mbarriers per
+// stage: full (the 16 fill-warp arrivals, the copy warp's arrival and the
+// copied bytes) and empty (the MMAs that read the stage completed).  The MMA
+// warp thus makes one shared-memory wait per chunk: while the tensor cores
+// read their operands, every other shared-memory access of that warp takes a
+// few hundred cycles (measured with clock stamps per chunk), and those waits,
+// not the copies or the fills, set the chunk rate.
+// Chunk t uses stage t % NS for the (t / NS)-th time, so every wait names the
+// phase parity (t / NS) & 1; no role can run a full phase ahead of a waiter.
+// The three roles walk the same chunk sequence as nested loops (product, then
+// parity and K chunk), with no integer division per chunk.  After any wait
 // runs out of time the CTA's shared failure flag makes every later wait return
 // at once, so a fault ends the kernel instead of hanging it.
 constexpr int D2_FILL = 16;                        // fill warps
@@ -160,24 +156,37 @@ __device__ __forceinline__ void mbar_arrive1(uint64_t *mbar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" : : "r"(smem_u32(mbar)) : "memory");
 }
 
-// position of chunk t in a ring of n slots: slot t % n, use t / n
-struct D2Ring {
-    int slot = 0, use = 0;
-    __device__ __forceinline__ void next(int n)
-    {
-        if (++slot == n) {
-            slot = 0;
-            use++;
-        }
-    }
-};
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return done != 0;
+}
 
+// wait for a phase: the first test is the only shared-memory access on the fast
+// path; the failure flag and the clock are read on the slow path only (every
+// 32nd test), so a failure elsewhere in the CTA still ends this wait quickly
 __device__ __forceinline__ bool d2_wait(uint64_t *mbar, uint32_t parity, volatile int *fail)
 {
-    if (*fail) return false;
-    if (mbar_wait(mbar, parity)) return true;
-    *fail = 1;
-    return false;
+    const uint32_t a = smem_u32(mbar);
+    if (mbar_try(a, parity)) return true;
+    const long long t0 = clock64();
+    for (int it = 1;; it++) {
+        if (mbar_try(a, parity)) return true;
+        if ((it & 31) == 0) {
+            if (*fail) return false;
+            if (clock64() - t0 > kWaitCycles) {
+                *fail = 1;
+                return false;
+            }
+        }
+    }
 }
 
 // the chunk sequence of one slab: product gi in 0..3, parity half par (products
@@ -198,14 +207,11 @@ __device__ __forceinline__ void d2_for_chunks(int nkh, int nkr, F &&f)
 
 __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
 {
-    extern __shared__ __align__(128) unsigned char smraw[];
-    unsigned char *sm = smraw + ((128 - (smem_u32(smraw) & 127)) & 127);
-    unsigned char *fring = sm, *cring = sm + D2_NF * D2_FSLOT;
-    uint64_t *copy_full = reinterpret_cast<uint64_t *>(sm + D2_BYTES);
-    uint64_t *copy_empty = copy_full + D2_NC;
-    uint64_t *fill_full = copy_empty + D2_NC;
-    uint64_t *fill_empty = fill_full + D2_NF;
-    uint32_t *slot = reinterpret_cast<uint32_t *>(fill_empty + D2_NF);
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char *sm = smraw + ((1024 - (smem_u32(smraw) & 1023)) & 1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + D2_BYTES);
+    uint64_t *empty = full + D2_NS;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(empty + D2_NS);
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int na = p.na, n1 = p.n1, n2 = p.n2;
@@ -222,13 +228,9 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     }
     if (warp == 0) tmem_alloc(slot, 512);
     if (threadIdx.x == 0) {
-        for (int i = 0; i < D2_NC; i++) {
-            mbar_init(&copy_full[i], 1);
-            mbar_init(&copy_empty[i], 1);
-        }
-        for (int i = 0; i < D2_NF; i++) {
-            mbar_init(&fill_full[i], D2_FILL);
-            mbar_init(&fill_empty[i], 1);
+        for (int i = 0; i < D2_NS; i++) {
+            mbar_init(&full[i], D2_FILL + 1);
+            mbar_init(&empty[i], 1);
         }
         *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -250,76 +252,67 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
 
     if (warp == D2_COPY_WARP) {
         // ---- bulk copies of the DST-matrix operands ----
-        if (lane == 0) {
-            D2Ring cr;
+        if (lane == 0)
             d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
-                const int cs = cr.slot, cu = cr.use;
-                cr.next(D2_NC);
                 if (*fail) return;
-                if (cu > 0 && !d2_wait(&copy_empty[cs], (cu - 1) & 1, fail)) return;
+                const int s = t & (D2_NS - 1), u = t >> 2;
+                if (t >= D2_NS && !d2_wait(&empty[s], (u - 1) & 1, fail)) return;
+                unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
                 const bool alongR = (gi == 0 || gi == 3);
                 const float *src = alongR ? p.s2fold + (size_t)(par * D2_NKH + jc) * D2_CHUNK
                                           : S1p + (size_t)jc * D2_CHUNK;
-                mbar_expect_tx(&copy_full[cs], D2_SMALL);
-                bulk_g2s(cring + cs * D2_CSLOT, src, D2_SMALL, &copy_full[cs]);
+                mbar_expect_tx(&full[s], D2_SMALL);
+                bulk_g2s(alongR ? big : small, src, D2_SMALL, &full[s]);
                 copies = t + 1;
             });
-        }
     } else if (warp == D2_MMA_WARP) {
         // ---- MMA issue: descriptors built once, advanced by 16-byte units ----
         if (lane == 0) {
             const uint64_t k16 = 256 >> 4;                  // one K step of 8 (two core matrices)
-            const uint64_t c0 = sdesc(smem_u32(cring), 128, D2_SBO), f0 = sdesc(smem_u32(fring), 128, D2_SBO);
-            const uint64_t cslot16 = D2_CSLOT >> 4, fslot16 = D2_FSLOT >> 4;
+            const uint64_t d0 = sdesc(smem_u32(sm), 128, D2_SBO);
+            const uint64_t stage16 = D2_STAGE >> 4, small16 = D2_BIGMAX >> 4;
             const uint64_t lo128 = D2_SMALL_LO >> 4, loRB = big_lo >> 4, tile16 = (16 * D2_SBO) >> 4;
             const uint32_t id_nn = idesc_tf32(128, nnp), id_rb = idesc_tf32(128, RB), id_128 = idesc_tf32(128, 128);
-            D2Ring cr, fr;
             d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
-                const int cs = cr.slot, cu = cr.use, fs = fr.slot, fu = fr.use;
-                cr.next(D2_NC);
-                fr.next(D2_NF);
-                d2_wait(&copy_full[cs], cu & 1, fail);
-                d2_wait(&fill_full[fs], fu & 1, fail);
+                const int s = t & (D2_NS - 1), u = t >> 2;
+                const bool ok = d2_wait(&full[s], u & 1, fail);
                 fence_after_sync();
-                if (!*fail) {
-                    // cd: the copied DST-matrix chunk, fd: the built operand
-                    const uint64_t cd = c0 + (uint64_t)cs * cslot16, fd = f0 + (uint64_t)fs * fslot16;
+                if (ok) {
+                    const uint64_t bg = d0 + (uint64_t)s * stage16, sl = bg + small16;
 #pragma unroll
                     for (int ks = 0; ks < D2_KC / 8; ks++) {
                         const uint64_t o = ks * k16;
                         const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
                         if (gi == 0) {
-                            // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (copy), B = Xs (fill)
+                            // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
                             const uint32_t d = tb + 128u * par;
-                            mma_tf32(d, cd + o, fd + o, id_nn, acc0);
-                            mma_tf32(d, cd + o, fd + lo128 + o, id_nn, 1);
-                            mma_tf32(d, cd + lo128 + o, fd + o, id_nn, 1);
+                            mma_tf32(d, bg + o, sl + o, id_nn, acc0);
+                            mma_tf32(d, bg + o, sl + lo128 + o, id_nn, 1);
+                            mma_tf32(d, bg + lo128 + o, sl + o, id_nn, 1);
                         } else if (gi == 1) {
-                            // per R tile: M = 128, N = nnp: A = D1 rows (fill), B = S1 (copy)
+                            // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
                             for (int tt = 0; tt < NT; tt++) {
-                                const uint64_t at = fd + tt * tile16;
+                                const uint64_t at = bg + tt * tile16;
                                 const uint32_t d = tb + 256u + 128u * tt;
-                                mma_tf32(d, at + o, cd + o, id_nn, acc0);
-                                mma_tf32(d, at + o, cd + lo128 + o, id_nn, 1);
-                                mma_tf32(d, at + loRB + o, cd + o, id_nn, 1);
+                                mma_tf32(d, at + o, sl + o, id_nn, acc0);
+                                mma_tf32(d, at + o, sl + lo128 + o, id_nn, 1);
+                                mma_tf32(d, at + loRB + o, sl + o, id_nn, 1);
                             }
                         } else if (gi == 2) {
-                            // M = 128 (r1), N = RB (R): A = S1 (copy), B = scaled D2 rows (fill)
-                            mma_tf32(tb, cd + o, fd + o, id_rb, acc0);
-                            mma_tf32(tb, cd + o, fd + loRB + o, id_rb, 1);
-                            mma_tf32(tb, cd + lo128 + o, fd + o, id_rb, 1);
+                            // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
+                            mma_tf32(tb, sl + o, bg + o, id_rb, acc0);
+                            mma_tf32(tb, sl + o, bg + loRB + o, id_rb, 1);
+                            mma_tf32(tb, sl + lo128 + o, bg + o, id_rb, 1);
                         } else {
-                            // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (fill), B = folded S2 (copy)
+                            // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
                             const uint32_t d = tb + 256u + 128u * par;
-                            mma_tf32(d, fd + o, cd + o, id_128, acc0);
-                            mma_tf32(d, fd + o, cd + lo128 + o, id_128, 1);
-                            mma_tf32(d, fd + lo128 + o, cd + o, id_128, 1);
+                            mma_tf32(d, sl + o, bg + o, id_128, acc0);
+                            mma_tf32(d, sl + o, bg + lo128 + o, id_128, 1);
+                            mma_tf32(d, sl + lo128 + o, bg + o, id_128, 1);
                         }
                     }
                 }
-                // also after a failure, so no waiter is left behind
-                mma_commit(&fill_empty[fs]);
-                mma_commit(&copy_empty[cs]);
+                mma_commit(&empty[s]);        // also after a failure, so no waiter is left behind
             });
         }
     } else {
@@ -340,18 +333,15 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
         const bool on2 = rset == 0 ? (m < h) : (m < n2 - h);
         const int R2 = rset == 0 ? m : n2 - 1 - m;
         const float sg2 = rset == 0 ? 1.f : -1.f;
-        D2Ring fr;
         d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
-            const int fs = fr.slot, fu = fr.use;
-            fr.next(D2_NF);
+            const int s = t & (D2_NS - 1), u = t >> 2;
+            unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
             if (jc == 0 && par == 0 && gi > 0) {
                 // this product reads the previous one from tensor memory: its last chunk done
-                const int ps = fs == 0 ? D2_NF - 1 : fs - 1, pu = fs == 0 ? fu - 1 : fu;
-                d2_wait(&fill_empty[ps], pu & 1, fail);
+                d2_wait(&empty[(t - 1) & (D2_NS - 1)], ((t - 1) >> 2) & 1, fail);
                 fence_after_sync();
             }
-            if (fu > 0) d2_wait(&fill_empty[fs], (fu - 1) & 1, fail);   // the MMAs of chunk t - NF read this slot
-            unsigned char *big = fring + fs * D2_FSLOT, *small = big;
+            if (t >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
             const int k0 = jc * D2_KC;
             if (gi == 0) {
                 // B = Xs columns of this parity (rows r1) into the small slot; after the
@@ -429,7 +419,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             fence_async_smem();
             fence_before_sync();
             __syncwarp();
-            if (lane == 0) mbar_arrive1(&fill_full[fs]);
+            if (lane == 0) mbar_arrive1(&full[s]);
         });
         // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
         const int *mT = p.mapT + (size_t)a * n2 * n1;
@@ -442,7 +432,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                 if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
             }
         }
-        d2_wait(&fill_empty[(total - 1) % D2_NF], ((total - 1) / D2_NF) & 1, fail);
+        d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
         if (!*fail) {
             const int64_t fo = p.foff[seg];
@@ -472,11 +462,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
     // last commit (which tracks all its MMAs); both phases were issued, so these
     // bounded waits end at once in a normal run and soon after a failure
     if (lane == 0 && warp == D2_COPY_WARP && copies > 0)
-        mbar_wait(&copy_full[(copies - 1) % D2_NC], ((copies - 1) / D2_NC) & 1);
-    if (lane == 0 && warp == D2_MMA_WARP) {
-        mbar_wait(&fill_empty[(total - 1) % D2_NF], ((total - 1) / D2_NF) & 1);
-        mbar_wait(&copy_empty[(total - 1) % D2_NC], ((total - 1) / D2_NC) & 1);
-    }
+        mbar_wait(&full[(copies - 1) & (D2_NS - 1)], ((copies - 1) >> 2) & 1);
+    if (lane == 0 && warp == D2_MMA_WARP) mbar_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1);
     fence_before_sync();
     __syncthreads();
     if (threadIdx.x == 0 && *fail) atomicExch(p.err, 1);
@@ -602,7 +589,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    const size_t smem = D2_BYTES + 256 + 128;          // rings, barriers, alignment slack
+    const size_t smem = D2_BYTES + 128 + 1024;
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
