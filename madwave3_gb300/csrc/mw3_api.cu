@@ -483,6 +483,7 @@ int build_device(Ctx &c)
     }
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;
+    if (c.use_tc_dst2d) TRY(mw3::encode_tc_dst2d_xmap(c));
     cudaError_t e = cudaStreamSynchronize(c.stream);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {

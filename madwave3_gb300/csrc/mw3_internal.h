@@ -216,6 +216,7 @@ struct Ctx {
     float *d_dst_s2fold = nullptr;   // S2 split by column parity (DST-I symmetry), hi/lo chunk planes
     int64_t *d_dst_s1off = nullptr;  // [W][na] float offset of the slab's S1
     float *d_p2r1f = nullptr, *d_p2r2f = nullptr;      // FP32 copies of the momenta tables
+    alignas(64) unsigned char dst_xmap[128] = {};       // TMA map of the rectangles (CUtensorMap)
     // mixed path with the fused DSTs: H psi (without V) kept in FP32, and the
     // potential pre-scaled for the update: vr = V 2/delta2 - [same state] emindlt 2/delta2
     bool h32 = false;
@@ -259,6 +260,8 @@ void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end);
 void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end);
 // fused tensor-core radial DSTs of the mixed path (mw3_tc_dst2d.cu); sets c.use_tc_dst2d
 int build_tc_dst2d(Ctx &c);
+// the TMA tensor map of the rectangles (after they are allocated)
+int encode_tc_dst2d_xmap(Ctx &c);
 void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end);
 std::vector<double> dst_matrix(int n);
 

@@ -9,7 +9,7 @@
 // Four 128 x 128 tensor-core GEMMs, oriented so that each result can be read
 // out of tensor memory row by row (a thread owns one lane) and written back as
 // the next GEMM's K-major operand without a transpose:
-//   D1[R][r1] = S2 Xs^T            A = S2 (bulk copy)      B = Xs rows (global)      [R folded]
+//   D1[R][r1] = S2 Xs^T            A = S2 (bulk copy)      B = Xs rows (tensor copy) [R folded]
 //   D2[R][r1] = D1 S1^T            A = D1 (tensor memory)  B = S1 (bulk copy)
 //   D3[r1][R] = S1 (D2 o F^T)^T    A = S1 (bulk copy)      B = D2 o F^T (tensor memory)
 //   D4[r1][R] = D3 S2              A = D3 (tensor memory)  B = S2 (bulk copy)        [R folded]
@@ -20,6 +20,9 @@
 // FP32 accumulation as the other tensor-core kernels of the mixed path.
 #include "mw3_internal.h"
 #include "mw3_tc.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -77,53 +80,35 @@ __device__ __forceinline__ void d2_split4(unsigned char *hi, uint32_t lo_off, ui
     *reinterpret_cast<float4 *>(hi + lo_off + off) = l;
 }
 
-// X rows r < nn, columns 2j + parity for j in [16 jc, 16 jc + 16): each of the
-// 512 fill threads takes one (row, 4 j) group, reading the 8 consecutive columns
-// that hold it (both parities); a quarter warp covers 8 rows of one 16-byte
-// column group (one core matrix).  Loads need only the rectangle's bounds, so
-// they can be issued before the row count is known; rows r >= nn store zeros.
-struct XStage {
-    float4 v[2];
-    __device__ __forceinline__ static void idx(int e, int &r, int &kg)
-    {
-        int rest = e >> 3;
-        kg = rest & 3;
-        r = (rest >> 2) * 8 + (e & 7);
-    }
-    __device__ __forceinline__ void load(const float *Xs, int n2, int nrow, int jc)
-    {
-        int r, kg;
-        idx(threadIdx.x, r, kg);
-        int k = 2 * (jc * D2_KC + kg * 4);              // first of the 8 columns
-        float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0;
-        if (r < nrow) {
-            const float *q = Xs + (size_t)r * n2 + k;
-            if (k + 7 < n2 && (n2 & 3) == 0) {
-                x0 = __ldg(reinterpret_cast<const float4 *>(q));
-                x1 = __ldg(reinterpret_cast<const float4 *>(q + 4));
-            } else {
-                float t[8];
-#pragma unroll
-                for (int u = 0; u < 8; u++) t[u] = (k + u < n2) ? __ldg(q + u) : 0.f;
-                x0 = make_float4(t[0], t[1], t[2], t[3]);
-                x1 = make_float4(t[4], t[5], t[6], t[7]);
-            }
-        }
-        v[0] = x0;
-        v[1] = x1;
-    }
-    __device__ __forceinline__ void store(unsigned char *dst, int parity, int nn) const
-    {
-        int r, kg;
-        idx(threadIdx.x, r, kg);
-        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 &a = r < nn ? v[0] : z, &b = r < nn ? v[1] : z;
-        if (parity == 0)
-            d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.x, a.z, b.x, b.z);
-        else
-            d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.y, a.w, b.y, b.w);
-    }
-};
+// X rows r < nn, columns 2j + parity for j in [16 jc, 16 jc + 16), from the
+// chunk's X tile (128 rows x 32 columns, one 128-byte row each, placed by the
+// tensor copy with the 128-byte swizzle: 16-byte piece q of row r sits at piece
+// q ^ (r & 7)).  Each of the 512 fill threads takes one (row, 4 j) group: the
+// pieces 2 kg and 2 kg + 1 of its row hold both parities.  A quarter warp reads
+// 8 consecutive rows, whose pieces the swizzle spreads over all banks, and
+// writes one core matrix of the K-major operand.
+__device__ __forceinline__ void d2_x_fill(const unsigned char *xt, unsigned char *dst, int parity, int nn)
+{
+    const int e = threadIdx.x, rest = e >> 3, kg = rest & 3, r = (rest >> 2) * 8 + (e & 7);
+    const unsigned char *row = xt + r * 128;
+    float4 a = *reinterpret_cast<const float4 *>(row + (((2 * kg) ^ (r & 7)) << 4));
+    float4 b = *reinterpret_cast<const float4 *>(row + (((2 * kg + 1) ^ (r & 7)) << 4));
+    if (r >= nn) a = b = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (parity == 0)
+        d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.x, a.z, b.x, b.z);
+    else
+        d2_split4(dst, D2_SMALL_LO, kmaj_off(r, kg * 4, D2_KC), a.y, a.w, b.y, b.w);
+}
+
+// 2-D tensor copy of a box at (x, y) of the map into shared memory
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        :
+        : "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+}
 
 // Tensor memory (512 columns):
 //   D1 = S2 Xs^T folded: E at [0,128), O at [128,256)   (lane i < h, column r1)
@@ -205,32 +190,29 @@ __device__ __forceinline__ void d2_for_chunks(int nkh, int nkr, F &&f)
         for (int jc = 0; jc < nkh; jc++) f(t++, 3, par, jc);
 }
 
-__global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
+__global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const __grid_constant__ CUtensorMap xmap)
 {
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char *sm = smraw + ((1024 - (smem_u32(smraw) & 1023)) & 1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(sm + D2_BYTES);
     uint64_t *empty = full + D2_NS;
-    uint32_t *slot = reinterpret_cast<uint32_t *>(empty + D2_NS);
+    uint64_t *xfull = empty + D2_NS;                    // the X tile of a first-product chunk landed
+    uint32_t *slot = reinterpret_cast<uint32_t *>(xfull + D2_NS);
+    float *s_p1f = reinterpret_cast<float *>(sm + D2_BYTES + 128);   // the slab's r1 momenta
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int na = p.na, n1 = p.n1, n2 = p.n2;
     const int h = (n2 + 1) >> 1;                        // rows i < h: E + O; row n2-1-i: E - O
     const int nkh = (h + D2_KC - 1) / D2_KC;            // K chunks of one parity half
     const int seg = p.seg0 + blockIdx.x;
-    // the fill warps start the first two K chunks of X before anything else: each
-    // X chunk is loaded two chunks of X ahead of its use (four operand fills)
-    const float *Xs = p.X + (size_t)seg * n1 * n2;
-    XStage xa, xb;                                      // X chunks of even and odd jc
-    if (warp < D2_FILL) {
-        xa.load(Xs, n2, n1, 0);
-        if (nkh > 1) xb.load(Xs, n2, n1, 1);
-    }
+    if (warp == D2_COPY_WARP && lane == 0)
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&xmap)) : "memory");
     if (warp == 0) tmem_alloc(slot, 512);
     if (threadIdx.x == 0) {
         for (int i = 0; i < D2_NS; i++) {
             mbar_init(&full[i], D2_FILL + 1);
             mbar_init(&empty[i], 1);
+            mbar_init(&xfull[i], 1);
         }
         *fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -261,6 +243,11 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                 const bool alongR = (gi == 0 || gi == 3);
                 const float *src = alongR ? p.s2fold + (size_t)(par * D2_NKH + jc) * D2_CHUNK
                                           : S1p + (size_t)jc * D2_CHUNK;
+                if (gi == 0) {
+                    // the X tile of this chunk (rows of the slab, 32 columns) behind the S2 chunk
+                    mbar_expect_tx(&xfull[s], D2_SMALL);
+                    tma_load_2d(big + D2_SMALL, &xmap, 32 * jc, seg * n1, &xfull[s]);
+                }
                 mbar_expect_tx(&full[s], D2_SMALL);
                 bulk_g2s(alongR ? big : small, src, D2_SMALL, &full[s]);
                 copies = t + 1;
@@ -323,7 +310,12 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
         const int m = q4 * 32 + lane;                   // the tensor-memory lane this thread reads
         const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
         const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
-        const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
+        {
+            // the r1 momenta of the slab into shared memory (read 8 at a time by the third product)
+            const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
+            if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
+            asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
+        }
         // second and third products: sub & 1 picks the row set, sub >> 1 the 8-column half
         const int rset = sub & 1, colh = sub >> 1;
         const int rR = 128 * rset + m;                  // the R row this thread fills in the third product
@@ -344,16 +336,11 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
             if (t >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
             const int k0 = jc * D2_KC;
             if (gi == 0) {
-                // B = Xs columns of this parity (rows r1) into the small slot; after the
-                // second parity the buffer takes chunk jc + 2 (warp-uniform branches keep
-                // the register buffers static)
-                if (jc & 1) {
-                    xb.store(small, par, nn);
-                    if (par == 1 && jc + 2 < nkh) xb.load(Xs, n2, n1, jc + 2);
-                } else {
-                    xa.store(small, par, nn);
-                    if (par == 1 && jc + 2 < nkh) xa.load(Xs, n2, n1, jc + 2);
-                }
+                // B = Xs columns of this parity (rows r1) into the small slot, from the X
+                // tile the copy warp placed behind the S2 chunk (the first product takes the
+                // first uses of every stage, so u counts this barrier's phases too)
+                d2_wait(&xfull[s], u & 1, fail);
+                d2_x_fill(big + D2_SMALL, small, par, nn);
             } else if (gi == 1) {
                 // A = D1 rows R into the big slot from 8 of the E and O columns of lane i
                 // (all lanes load; lanes without a row store nothing)
@@ -383,7 +370,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p)
                     float pv[8];
 #pragma unroll
                     for (int j = 0; j < 2; j++) {
-                        float4 q = __ldg(reinterpret_cast<const float4 *>(p1f + kc) + j);
+                        float4 q = *reinterpret_cast<const float4 *>(s_p1f + kc + 4 * j);
                         pv[4 * j] = q.x; pv[4 * j + 1] = q.y; pv[4 * j + 2] = q.z; pv[4 * j + 3] = q.w;
                     }
                     const bool full = kc + 8 <= nn && rR < n2;
@@ -549,7 +536,8 @@ int build_tc_dst2d(Ctx &c)
 {
     c.use_tc_dst2d = false;
     // n1 a multiple of 4: the kernel reads the r1 momenta as float4
-    if (c.fp64 || !c.use_tc || c.n2 > 256 || (c.n1 & 3) != 0) return MW3_OK;
+    // n2 a multiple of 4: the rectangles' rows are a 16-byte multiple for the tensor copies
+    if (c.fp64 || !c.use_tc || c.n2 > 256 || (c.n1 & 3) != 0 || (c.n2 & 3) != 0) return MW3_OK;
     const int na = c.na, W = (int)c.waves.size();
     for (auto &t : c.waves)
         for (int a = 0; a < na; a++)
@@ -585,11 +573,37 @@ int build_tc_dst2d(Ctx &c)
     return MW3_OK;
 }
 
+int encode_tc_dst2d_xmap(Ctx &c)
+{
+    static_assert(sizeof(CUtensorMap) == sizeof(c.dst_xmap), "tensor map size");
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        c.err = "cuTensorMapEncodeTiled is not available";
+        return MW3_ERR_CUDA;
+    }
+    // rows: every r1 line of every slab, [G * na * n1]; columns: R, [n2]; box 32 x 128
+    const cuuint64_t dims[2] = {(cuuint64_t)c.n2, (cuuint64_t)c.G * c.na * c.n1};
+    const cuuint64_t strides[1] = {(cuuint64_t)c.n2 * sizeof(float)};
+    const cuuint32_t box[2] = {32, 128}, es[2] = {1, 1};
+    CUtensorMap m;
+    CUresult r = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn)(
+        &m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, c.d_X, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        c.err = "cuTensorMapEncodeTiled failed for the rectangles";
+        return MW3_ERR_CUDA;
+    }
+    std::memcpy(c.dst_xmap, &m, sizeof(m));
+    return MW3_OK;
+}
+
 void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    const size_t smem = D2_BYTES + 128 + 1024;
+    const size_t smem = D2_BYTES + 1024 + 1024;         // stages, barriers and momenta, alignment slack
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
@@ -603,7 +617,9 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
     p.err = c.d_tc_err;
-    k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p);
+    CUtensorMap xmap;
+    std::memcpy(&xmap, c.dst_xmap, sizeof(xmap));
+    k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p, xmap);
     c.launches++;
 }
 
