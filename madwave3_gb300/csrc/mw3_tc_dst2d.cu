@@ -66,7 +66,6 @@ struct Dst2Args {
     const int *mapT;              // [na][n2][n1]
     const int64_t *foff;
     const int *blk_wave;
-    const int *npunreal;          // stored points per angle
     int na, n1, n2, seg0;
     int *err;
 };
@@ -410,10 +409,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
             if (lane == 0) mbar_arrive1(&full[s]);
         });
         // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
-        // Once the last MMAs are done the stages are free: every value goes to its
-        // stored-point position in shared memory, then the slab's points leave in one
-        // coalesced pass.  Points with r1 >= nopr1 carry no value here; the kernel that
-        // runs next sets them (they keep psi), so the pass may write anything there.
         const int *mT = p.mapT + (size_t)a * n2 * n1;
         if (m < nn) {
             // the map entries this thread reads, into L1 while the last MMAs run
@@ -424,33 +419,29 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
                 if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
             }
         }
-        const int npts = p.npunreal[a];
         d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
-        float *hs = reinterpret_cast<float *>(sm);
-#pragma unroll
-        for (int cc = 0; cc < 2; cc++) {
-            const int i0 = 32 * sub + 16 * cc;
-            float e[16], o[16];
-            tmem_ld16(lrow + 256u + (uint32_t)i0, e);
-            tmem_ld16(lrow + 384u + (uint32_t)i0, o);
-            int is[16], id[16];
-#pragma unroll
-            for (int uu = 0; uu < 16; uu++) {
-                int i = i0 + uu;
-                is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
-                id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
-            }
-#pragma unroll
-            for (int uu = 0; uu < 16; uu++) {
-                if (is[uu] >= 0) hs[is[uu]] = e[uu] + o[uu];
-                if (id[uu] >= 0) hs[id[uu]] = e[uu] - o[uu];
-            }
-        }
-        asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
         if (!*fail) {
-            float *Hs = p.H + p.foff[seg];
-            for (int q = threadIdx.x; q < npts; q += D2_FILL * 32) Hs[q] = hs[q];
+            const int64_t fo = p.foff[seg];
+#pragma unroll
+            for (int cc = 0; cc < 2; cc++) {
+                const int i0 = 32 * sub + 16 * cc;
+                float e[16], o[16];
+                tmem_ld16(lrow + 256u + (uint32_t)i0, e);
+                tmem_ld16(lrow + 384u + (uint32_t)i0, o);
+                int is[16], id[16];
+#pragma unroll
+                for (int uu = 0; uu < 16; uu++) {
+                    int i = i0 + uu;
+                    is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
+                    id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
+                }
+#pragma unroll
+                for (int uu = 0; uu < 16; uu++) {
+                    if (is[uu] >= 0) p.H[fo + is[uu]] = e[uu] + o[uu];
+                    if (id[uu] >= 0) p.H[fo + id[uu]] = e[uu] - o[uu];
+                }
+            }
         }
     }
     // before shared and tensor memory are released, the async work this CTA issued
@@ -546,9 +537,7 @@ int build_tc_dst2d(Ctx &c)
     c.use_tc_dst2d = false;
     // n1 a multiple of 4: the kernel reads the r1 momenta as float4
     // n2 a multiple of 4: the rectangles' rows are a 16-byte multiple for the tensor copies
-    // the H values of a slab are staged in the stages' shared memory before they leave
     if (c.fp64 || !c.use_tc || c.n2 > 256 || (c.n1 & 3) != 0 || (c.n2 & 3) != 0) return MW3_OK;
-    if ((size_t)c.npt * sizeof(float) > tc::D2_BYTES) return MW3_OK;
     const int na = c.na, W = (int)c.waves.size();
     for (auto &t : c.waves)
         for (int a = 0; a < na; a++)
@@ -625,7 +614,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.X = X; p.H = H;
     p.s2fold = c.d_dst_s2fold; p.s1planes = c.d_dst_planes; p.s1off = c.d_dst_s1off; p.nopr1 = c.d_nopr1;
     p.p2r1f = c.d_p2r1f; p.p2r2f = c.d_p2r2f; p.radcut = (float)c.grid.radcutmax;
-    p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave; p.npunreal = c.d_npunreal;
+    p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
     p.err = c.d_tc_err;
     CUtensorMap xmap;
