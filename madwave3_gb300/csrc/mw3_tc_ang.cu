@@ -147,13 +147,33 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
     const int q4 = warp & 3, half = warp >> 2;
     const int m = q4 * 32 + lane;
     const int ir1 = r1_0 + (m >> 3), ir2 = r2_0 + (m & 7);
-    const bool inrow = ir1 < n1 && ir2 < n2;
     const int cr1 = min(ir1, n1 - 1), cr2 = min(ir2, n2 - 1);
     const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
     uint32_t ph0 = 0, ph1 = 0;
     bool bad = false, copy_out = false;
 
     for (int pos = -1; pos < L; pos++) {
+        // the X tile of the block after next into L2 (one 32-byte run per angle and r1
+        // row), and this block's j-basis rows into L1 for the scaling below
+        if (pos + 2 < L) {
+            const float *Xn = p.X + (size_t)p.chain[cb + pos + 2] * na * n1 * n2;
+            for (int e = threadIdx.x; e < na * AG_R1; e += blockDim.x) {
+                int a = e >> 4, gr1 = r1_0 + (e & 15);
+                if (gr1 < n1) asm volatile("prefetch.global.L2 [%0];" ::"l"(Xn + ((size_t)a * n1 + gr1) * n2 + r2_0));
+            }
+        }
+        if (pos >= 0) {
+            const int g = p.chain[cb + pos];
+            const float *yrow = p.yj + ((size_t)g * n1 + cr1) * AG_K;
+            const float *lr = p.l2 + ((size_t)g * 3 * n2 + cr2) * AG_K;
+            const size_t lslot = (size_t)n2 * AG_K;
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(yrow + 32 * hh));
+#pragma unroll
+                for (int q = 0; q < 3; q++) asm volatile("prefetch.global.L1 [%0];" ::"l"(lr + q * lslot + 32 * hh));
+            }
+        }
         // ---- grid -> j basis for the next block of the chain, into ring slot (pos+1)%3 ----
         if (pos + 1 < L) {
             int gn = p.chain[cb + pos + 1];
@@ -263,12 +283,11 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
                         unsigned idx = s_map[a * 128 + m];
                         at[i] = (a < na && idx != 0xFFFFu) ? s_fo[a] + (int64_t)idx : -1;
                     }
-                    HT hv[8];
-#pragma unroll
-                    for (int i = 0; i < 8; i++) hv[i] = at[i] >= 0 ? p.H[at[i]] : (HT)0;
+                    // one writer per point in this launch: a fire-and-forget add at L2
+                    // instead of a load and a store (no load latency in the epilogue)
 #pragma unroll
                     for (int i = 0; i < 8; i++)
-                        if (at[i] >= 0) p.H[at[i]] = hv[i] + (HT)v[h8 + i];
+                        if (at[i] >= 0) atomicAdd(p.H + at[i], (HT)v[h8 + i]);
                 }
             }
         }
