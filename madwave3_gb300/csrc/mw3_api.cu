@@ -466,20 +466,23 @@ int build_device(Ctx &c)
     TRY(mw3::build_tc_dst2d(c));
     c.h32 = c.use_tc_dst2d && c.use_tc_ang;
     c.d_h32 = nullptr;
-    c.d_vr = nullptr;
+    c.d_vr32 = nullptr;
+    c.d_pk32 = c.d_pkm1_32 = nullptr;
     if (c.use_tc_dst2d) TRY(dalloc(c, &c.d_h32, (size_t)c.NT));
     if (!c.fp64) {
         // potential pre-scaled for the mixed update: V 2/delta2, minus emindlt 2/delta2 on the diagonal
         const double r2d = 2.0 / c.grid.delta2;
-        std::vector<double> vr(c.vvv.size());
+        std::vector<float> vr(c.vvv.size());
         const size_t per = (size_t)c.na * c.npt;
         for (int et = 0; et < c.ne; et++)
             for (int es = 0; es < c.ne; es++) {
                 size_t b = ((size_t)et * c.ne + es) * per;
                 for (size_t i = 0; i < per; i++)
-                    vr[b + i] = c.vvv[b + i] * r2d - (et == es ? c.grid.emindlt * r2d : 0.0);
+                    vr[b + i] = (float)(c.vvv[b + i] * r2d - (et == es ? c.grid.emindlt * r2d : 0.0));
             }
-        TRY(dupload(c, &c.d_vr, vr));
+        TRY(dupload(c, &c.d_vr32, vr));
+        TRY(dalloc(c, &c.d_pk32, c.NT));
+        TRY(dalloc(c, &c.d_pkm1_32, c.NT));
     }
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;
@@ -535,7 +538,8 @@ void hphi_typed(Ctx &c, const double *psi, int g0, int g1)
 template <typename T>
 void scatter_typed(Ctx &c, const double *psi, int g0, int g1)
 {
-    mw3::launch_scatter<T>(c, psi, g0, g1);
+    // the propagation state also refreshes its FP32 copy (the mixed update reads it)
+    mw3::launch_scatter<T>(c, psi, psi == c.d_pk ? c.d_pk32 : nullptr, g0, g1);
 }
 
 void scatter(Ctx &c, const double *psi, int g0, int g1)
@@ -737,6 +741,7 @@ int mw3_start(mw3_ctx *h, const double *const *psi0s)
     hphi_all(c, c.d_pk, 0, c.G);
     update(c, 1);
     std::swap(c.d_pk, c.d_pkm1);
+    std::swap(c.d_pk32, c.d_pkm1_32);
     mw3::launch_norms(c, 0);
     c.it = 1;
     c.norm_slot = 1;
@@ -796,6 +801,7 @@ int mw3_run(mw3_ctx *h, int64_t n)
         hphi_all(c, c.d_pk, 0, c.G);
         update(c, 0);
         std::swap(c.d_pk, c.d_pkm1);
+        std::swap(c.d_pk32, c.d_pkm1_32);
         mw3::launch_accumulators(c, it);
         mw3::launch_norms(c, c.norm_slot);
         if (c.prof && c.prof_n < c.prof_cap) {

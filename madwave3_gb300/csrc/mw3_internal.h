@@ -221,7 +221,8 @@ struct Ctx {
     // potential pre-scaled for the update: vr = V 2/delta2 - [same state] emindlt 2/delta2
     bool h32 = false;
     float *d_h32 = nullptr;          // [NT]
-    double *d_vr = nullptr;          // like vvv
+    float *d_vr32 = nullptr;         // like vvv, FP32 (mixed update)
+    float *d_pk32 = nullptr, *d_pkm1_32 = nullptr;   // FP32 copies of psi_k and of the next psi (mixed update)
     int *d_tc_err = nullptr;         // set by a tensor-core kernel whose mbarrier wait ran out
     // optional per-stage event timing (mw3_profile)
     bool prof = false;
@@ -276,7 +277,7 @@ void riccati_fg(int l, double x, double *f, double *g);
 // kernels (mw3_kernels.cu)
 // ---------------------------------------------------------------------------
 template <typename T>
-void launch_scatter(Ctx &c, const double *psi, int g_begin, int g_end);
+void launch_scatter(Ctx &c, const double *psi, float *psi32, int g_begin, int g_end);
 template <typename T>
 void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end);
 // records the boundary event of a stage when per-stage timing is on

@@ -27,8 +27,11 @@ namespace mw3 {
 // ---------------------------------------------------------------------------
 constexpr int kPointChunk = 1024;   // stored points per CTA in the point kernels
 
+// psi32 (optional): the FP32 copy of psi at the stored points, which the mixed
+// update reads for the potential term
 template <typename T>
-__global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict__ psi, int seg0)
+__global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict__ psi, float *__restrict__ psi32,
+                          int seg0)
 {
     int seg = seg0 + blockIdx.x;
     int a = seg % d.na;
@@ -39,7 +42,9 @@ __global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict
     for (int ir = i0 + threadIdx.x; ir < i1; ir += blockDim.x) {
         int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
         int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
-        base[(size_t)ir1 * d.n2 + ir2] = (T)psi[off + ir];
+        const double v = psi[off + ir];
+        base[(size_t)ir1 * d.n2 + ir2] = (T)v;
+        if (psi32) psi32[off + ir] = (float)v;
     }
 }
 
@@ -250,6 +255,8 @@ __device__ __forceinline__ double f32_to_f64_int(float f)
 
 __device__ __forceinline__ double h_val(double h) { return h; }
 __device__ __forceinline__ double h_val(float h) { return f32_to_f64_int(h); }
+__device__ __forceinline__ float h_f32(float h) { return h; }
+__device__ __forceinline__ float h_f32(double h) { return f64_to_f32_int(h); }
 __device__ __forceinline__ double h_load(const double *H, int64_t i) { return H[i]; }
 __device__ __forceinline__ double h_load(const float *H, int64_t i) { return f32_to_f64_int(H[i]); }
 __device__ __forceinline__ void h_store(double *H, int64_t i, double v) { H[i] = v; }
@@ -412,7 +419,10 @@ struct UpdArgs {
     const double *absfr1, *absfr2; // [W][n1], [W][n2]
     double emindlt, delta2;
     double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
-    const double *vr;              // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
+    const float *vr32;             // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
+    const float *pk32;             // mixed path: FP32 copy of psi_k
+    float *out32;                  // mixed path: FP32 copy of psi_k+1
+    float r2df;                    // 2/delta2 in FP32
     const UpdChunk *desc;          // non-empty (segment, chunk) pairs, tables resolved
     int nchunk;                    // chunks per segment (norm-partial stride)
     int first;
@@ -440,7 +450,7 @@ __device__ __forceinline__ void upd_fe(const UpdArgs &u, double *zf, int w, int6
 // pair's descriptor carries the table entries, so every thread starts its point
 // loads after one independent 48-byte load
 template <typename T, typename HT>
-__global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
 {
     const UpdChunk cd = u.desc[blockIdx.x];
     const int seg = cd.seg, chunk = cd.chunk_ns & 255, nsrc = cd.chunk_ns >> 8;
@@ -449,13 +459,10 @@ __global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__re
     const int n = cd.n;
     const int n1 = d.n1, n2 = d.n2, ne = d.ne;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // same-Omega sources of V psi for this segment: potential row and psi_k row; the
-    // first from the descriptor, a second or later one (several electronic states)
-    // from the tables
-    const double *vbase = sizeof(T) == 4 ? u.vr : d.vvv;
-    const double *vr0 = nsrc > 0 ? vbase + cd.voff : nullptr, *pr0 = nsrc > 0 ? u.pk + cd.poff : nullptr;
-    __shared__ const double *s_vrow[8];
-    __shared__ const double *s_prow[8];
+    // same-Omega sources of V psi for this segment: offsets of the potential row and
+    // of the psi_k row; the first from the descriptor, a second or later one (several
+    // electronic states) from the tables
+    __shared__ long long s_voff[8], s_poff[8];
     __shared__ double s_wsum[8];
     if (nsrc > 1) {
         if (threadIdx.x == 0) {
@@ -465,8 +472,8 @@ __global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__re
                 int sb = u.vsrc[g * ne + q];
                 if (sb < 0) continue;
                 int es = d.blk_elec[sb];
-                s_vrow[ns] = vbase + ((((size_t)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
-                s_prow[ns] = u.pk + d.foff[(size_t)sb * d.na + a];
+                s_voff[ns] = ((((long long)(et - 1) * ne + (es - 1)) * d.na) + a) * d.npt;
+                s_poff[ns] = d.foff[(size_t)sb * d.na + a];
                 ns++;
             }
         }
@@ -502,7 +509,7 @@ __global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__re
             p1[k] = on && !u.first ? pm1[ir] : 0.0;
         }
         for (int q = 0; q < nsrc; q++) {
-            const double *vr = q == 0 ? vr0 : s_vrow[q], *pr = q == 0 ? pr0 : s_prow[q];
+            const double *vr = d.vvv + (q == 0 ? cd.voff : s_voff[q]), *pr = u.pk + (q == 0 ? cd.poff : s_poff[q]);
 #pragma unroll
             for (int k = 0; k < U; k++) {
                 int ir = ir0 + k * 256;
@@ -528,49 +535,52 @@ __global__ void __launch_bounds__(256, 3) k_update(DevGrid d, UpdArgs u, T *__re
             if (zf) upd_fe(u, zf, w, wst, wlen, off + ir, nv);
         }
     } else {
-        // mixed path, few FP64 instructions (GB300 runs FP64 at 1/64 of FP32):
-        //   t = H 2/delta2 + sum_s vr_s psi_s = 2 (H psi - emindlt psi) / delta2
-        // with the potential pre-scaled, damping only inside the absorbers,
-        // the FP32 copy rounded with integer operations, the norm partial in FP32.
-        // The first source's potential is loaded in one batch with the point's own
-        // data; its psi is psi_k itself when the segment has one electronic state.
-        const bool self0 = pr0 == pkp;
+        // mixed path: the FP64 pipe of GB300 is narrow (the FP64 recursion kept it two
+        // thirds busy), so everything that is H psi stays in FP32 and only the
+        // recursion itself is FP64:
+        //   t = H 2/delta2 + sum_s vr_s psi32_s          (FP32: H psi and V psi)
+        //   psi_k+1 = t - psi_k-1, or (t - f psi_k-1) f   (FP64; f the absorption inside the absorbers)
+        // with the FP32 copies of psi_k read and psi_k+1 written beside the FP64
+        // vectors, the conversions done with integer instructions, the norm in FP32
+        const float *vr0 = nsrc > 0 ? u.vr32 + cd.voff : nullptr, *pr0 = nsrc > 0 ? u.pk32 + cd.poff : nullptr;
+        float *__restrict__ o32 = u.out32 + off;
         int r1[U], r2[U];
-        HT hr[U];
-        double pk[U], p1[U], v0[U];
+        float hr[U], v0[U], q0[U];
+        double p1[U];
 #pragma unroll
         for (int k = 0; k < U; k++) {
             int ir = ir0 + k * 256;
             bool on = ir < n;
             r1[k] = on ? i1p[ir] - 1 : 0;
             r2[k] = on ? i2p[ir] - 1 : 0;
-            hr[k] = on ? Hp[ir] : (HT)0;
-            pk[k] = on ? pkp[ir] : 0.0;
+            hr[k] = on ? h_f32(Hp[ir]) : 0.f;
+            v0[k] = on && vr0 ? vr0[ir] : 0.f;
+            q0[k] = on && pr0 ? pr0[ir] : 0.f;
             p1[k] = on && !u.first ? pm1[ir] : 0.0;
-            v0[k] = on && vr0 ? vr0[ir] : 0.0;
         }
 #pragma unroll
         for (int k = 0; k < U; k++) {
             int ir = ir0 + k * 256;
             if (ir >= n) continue;
-            const double a1 = u.first ? 1.0 : ab1[r1[k]], a2 = u.first ? 1.0 : ab2[r2[k]];
-            const bool damp = !u.first && !(__double_as_longlong(a1) == 0x3FF0000000000000LL &&
-                                            __double_as_longlong(a2) == 0x3FF0000000000000LL);
-            double acc = (u.first || damp) ? 0.0 : -p1[k];
-            if (vr0) acc = fma(v0[k], self0 ? pk[k] : pr0[ir], acc);
-            for (int q = 1; q < nsrc; q++) acc = fma(s_vrow[q][ir], s_prow[q][ir], acc);
-            double t = fma(h_val(hr[k]), u.r2delta, acc);
+            float acc = v0[k] * q0[k];
+            for (int q = 1; q < nsrc; q++) acc = fmaf(u.vr32[s_voff[q] + ir], u.pk32[s_poff[q] + ir], acc);
+            const float t32 = fmaf(hr[k], u.r2df, acc);
             double nv;
             if (u.first) {
-                nv = 0.5 * t;
-            } else if (damp) {
-                double fab = a1 * a2;
-                nv = fma(-fab, p1[k], t) * fab;
+                nv = f32_to_f64_int(0.5f * t32);
             } else {
-                nv = t;
+                const double t = f32_to_f64_int(t32);
+                const double a1 = ab1[r1[k]], a2 = ab2[r2[k]];
+                if (__double_as_longlong(a1) == 0x3FF0000000000000LL && __double_as_longlong(a2) == 0x3FF0000000000000LL) {
+                    nv = t - p1[k];
+                } else {
+                    const double fab = a1 * a2;
+                    nv = fma(-fab, p1[k], t) * fab;
+                }
             }
             float nf = f64_to_f32_int(nv);
             rect[(size_t)r1[k] * n2 + r2[k]] = (T)nf;
+            o32[ir] = nf;
             nrmf = fmaf(nf, nf, nrmf);
             outp[ir] = nv;
             if (zf) upd_fe(u, zf, w, wst, wlen, off + ir, nv);
@@ -1017,11 +1027,11 @@ __global__ void k_build_xl2p(KinBuildArgs k, T *__restrict__ xl2p, int s, int sl
 // launchers
 // ---------------------------------------------------------------------------
 template <typename T>
-void launch_scatter(Ctx &c, const double *psi, int g_begin, int g_end)
+void launch_scatter(Ctx &c, const double *psi, float *psi32, int g_begin, int g_end)
 {
     int nseg = (g_end - g_begin) * c.na;
     if (nseg <= 0) return;
-    k_scatter<T><<<dim3(nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, g_begin * c.na);
+    k_scatter<T><<<dim3(nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, psi32, g_begin * c.na);
     LAUNCH_CHECK(c);
 }
 
@@ -1124,7 +1134,10 @@ void launch_update(Ctx &c, int first)
     u.delta2 = c.grid.delta2;
     u.rdelta = 1.0 / c.grid.delta2;
     u.r2delta = 2.0 / c.grid.delta2;
-    u.vr = c.d_vr;
+    u.vr32 = c.d_vr32;
+    u.pk32 = c.d_pk32;
+    u.out32 = c.d_pkm1_32;
+    u.r2df = (float)(2.0 / c.grid.delta2);
     u.desc = c.d_upd_desc;
     u.nchunk = c.nchunk;
     u.first = first;
@@ -1310,7 +1323,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     const double *P = psi - t.flat0;
     double *H = hpsi - t.flat0;
     DevGrid d = devgrid(c);
-    k_scatter<T><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, X, P, g0 * na);
+    k_scatter<T><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, X, P, nullptr, g0 * na);
     LAUNCH_CHECK(c);
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g0 * na * n1, nrows = (int64_t)ng * na * n1;
@@ -1392,8 +1405,8 @@ extern "C" int mw3_hphi_noalloc(mw3_ctx *h, int32_t wave_id, const double *psi, 
 
 namespace mw3 {
 
-template void launch_scatter<double>(Ctx &, const double *, int, int);
-template void launch_scatter<float>(Ctx &, const double *, int, int);
+template void launch_scatter<double>(Ctx &, const double *, float *, int, int);
+template void launch_scatter<float>(Ctx &, const double *, float *, int, int);
 template void launch_hphi<double>(Ctx &, const double *, int, int);
 template void launch_hphi<float>(Ctx &, const double *, int, int);
 template void launch_update<double>(Ctx &, int);
