@@ -424,6 +424,16 @@ int build_device(Ctx &c)
         TRY(dupload(c, &c.d_blk_isref, bref));
         TRY(dupload(c, &c.d_r2abs, r2abs));
         TRY(dupload(c, &c.d_fd, t0.fd));
+        c.d_cvring = c.d_cvcring = c.d_dj32 = c.d_fd32 = c.d_xj32 = nullptr;
+        c.cvring_n = 0;
+        if (!c.fp64) {
+            std::vector<float> fd32(t0.fd.begin(), t0.fd.end());
+            TRY(dupload(c, &c.d_fd32, fd32));
+            TRY(dalloc(c, &c.d_cvring, (size_t)mw3::kFluxRing * G * c.nj * c.nv, false));
+            TRY(dalloc(c, &c.d_cvcring, (size_t)mw3::kFluxRing * c.netot * 2, false));
+            TRY(dalloc(c, &c.d_dj32, (size_t)G * c.nj * na));
+            TRY(dalloc(c, &c.d_xj32, (size_t)G * n1 * c.nj));
+        }
         TRY(dupload(c, &c.d_nobc, t0.nobc));
     }
     c.wdev.assign(W, WaveDev());
@@ -487,6 +497,7 @@ int build_device(Ctx &c)
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;
     if (c.use_tc_dst2d) TRY(mw3::encode_tc_dst2d_xmap(c));
+    if (c.d_dj32) mw3::build_cvj32(c);
     cudaError_t e = cudaStreamSynchronize(c.stream);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -587,6 +598,7 @@ int reset_accumulators(Ctx &c)
 {
     size_t nf = (size_t)std::max(c.NF, 1) * c.netot * 2;
     c.fring_n = 0;
+    c.cvring_n = 0;
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcr, 0, sizeof(double) * nf, c.stream));
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcdr, 0, sizeof(double) * nf, c.stream));
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zs2, 0, sizeof(double) * 2 * (size_t)c.G * c.nj * c.nv * c.netot, c.stream));
@@ -862,6 +874,7 @@ int mw3_totalflux(mw3_ctx *h, int32_t w, double *tot, double *elec)
     WaveTables &t = c.waves[w];
     double *d = nullptr;
     mw3::flush_flux(c);
+    mw3::flush_cvj(c);
     MW3_CUDA_TRY(cudaMallocAsync(&d, sizeof(double) * (size_t)t.netot * (1 + c.ne), c.stream));
     mw3::launch_totalflux(c, w, d, d + t.netot);
     MW3_CUDA_TRY(cudaMemcpyAsync(tot, d, sizeof(double) * t.netot, cudaMemcpyDeviceToHost, c.stream));
@@ -891,6 +904,7 @@ int mw3_download_accumulators(mw3_ctx *h, int32_t w, double *zcr, double *zcdr, 
     size_t nf = (size_t)t.nflux * t.netot * 2;
     size_t ns = (size_t)t.ncan * t.nj * t.nv;
     mw3::flush_flux(c);
+    mw3::flush_cvj(c);
     if (zcr && nf) MW3_CUDA_TRY(cudaMemcpyAsync(zcr, d.zcr, sizeof(double) * nf, cudaMemcpyDeviceToHost, c.stream));
     if (zcdr && nf)
         MW3_CUDA_TRY(cudaMemcpyAsync(zcdr, d.zcdr, sizeof(double) * nf, cudaMemcpyDeviceToHost, c.stream));

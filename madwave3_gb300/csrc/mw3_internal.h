@@ -190,6 +190,15 @@ struct Ctx {
     float *d_fring = nullptr;        // [kFluxRing][NF][3]
     float *d_cring = nullptr;        // [kFluxRing][netot][2]
     int fring_n = 0;                 // slots filled since the last flush
+    // mixed path: the Cvj projection in FP32 (from the FP32 copy of psi) and Cvj of up
+    // to kFluxRing iterations with their C_k(E), added into zS2 every kFluxRing
+    // iterations and before every read
+    float *d_cvring = nullptr;       // [kFluxRing][G nj nv]
+    float *d_cvcring = nullptr;      // [kFluxRing][netot][2]
+    float *d_dj32 = nullptr;         // [G][nj][na]: Djmmp columns of the projection, 0 where Cvj is off
+    float *d_fd32 = nullptr;         // fd in FP32
+    float *d_xj32 = nullptr;         // [G][n1][nj]
+    int cvring_n = 0;
     double *d_zcr = nullptr, *d_zcdr = nullptr;          // [NF][netot][2]
     double *d_xj = nullptr;          // [G][n1][nj] angular projection at ir2abs
     double *d_cvj = nullptr;         // [G][nj][nv]
@@ -289,6 +298,9 @@ void launch_build_kinetic(Ctx &c);
 void launch_accumulators(Ctx &c, int64_t it);
 // mixed path: add the pending ring slots to the FP64 flux accumulators
 void flush_flux(Ctx &c);
+void flush_cvj(Ctx &c);
+// the FP32 Djmmp columns of the Cvj projection (mixed path), once the tables are on the device
+void build_cvj32(Ctx &c);
 constexpr int kFluxRing = 32;
 void launch_norms(Ctx &c, int64_t slot);
 void launch_addv(Ctx &c, const double *psi, int g0, int g1);

@@ -652,7 +652,8 @@ __global__ void k_norms(const double *__restrict__ part, const int *__restrict__
 // ---------------------------------------------------------------------------
 // CoefEcheby (main_madwave3.f:462-490): C_k(E) = d hbar/Delta e^{-ik acos Es}/sqrt(1-Es^2)
 __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double emindlt, double delta2,
-                             double hbr, int64_t k, double *__restrict__ zck, float *__restrict__ cring)
+                             double hbr, int64_t k, double *__restrict__ zck, float *__restrict__ cring,
+                             float *__restrict__ cvring)
 {
     int ie = blockIdx.x * blockDim.x + threadIdx.x;
     if (ie >= netot) return;
@@ -668,6 +669,10 @@ __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double 
     if (cring) {                    // mixed path: this iteration's slot of the flux ring
         cring[2 * ie] = (float)(zf * c / deno);
         cring[2 * ie + 1] = (float)(zf * s / deno);
+    }
+    if (cvring) {                   // mixed path: this iteration's slot of the Cvj ring
+        cvring[2 * ie] = (float)(zf * c / deno);
+        cvring[2 * ie + 1] = (float)(zf * s / deno);
     }
 }
 
@@ -841,6 +846,10 @@ struct CvjArgs {
     const int *nobc;              // [nelec][nj]
     double *xj, *cvj, *zs2;
     const double *zck;
+    // mixed path
+    const float *pk32, *dj32, *fd32;
+    float *xj32, *ring;           // ring: this iteration's slot [G nj nv]
+    float rsah2f;
     int jini, jmax, nvini, nvmax, nj, nv, netot, jref, nvref, gate;
     double sah2;
 };
@@ -906,6 +915,137 @@ __global__ void __launch_bounds__(256) k_cvj_fd(DevGrid d, CvjArgs c)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
     if (lane == 0) c.cvj[((size_t)g * nj + jj) * nv + iv] = on ? r : 0.0;
+}
+
+// Mixed path, 1 and 2 in FP32: the projection reads the FP32 copy of psi and the
+// FP32 Djmmp columns (0 where Cvj is off), Cvj goes to this iteration's ring slot
+// (0 for the gated elastic channel) and, as FP64, to cvj
+__global__ void __launch_bounds__(256) k_cvj_proj32(DevGrid d, CvjArgs c)
+{
+    extern __shared__ float cvs[];
+    const int g = blockIdx.x, n1 = d.n1, na = d.na, nj = c.nj;
+    const int r1a = blockIdx.y * kCvjR1, r1b = min(n1, r1a + kCvjR1), cw = r1b - r1a;
+    const int w = d.blk_wave[g];
+    float *fr = cvs;                          // [na][kCvjR1]
+    float *dj = cvs + (size_t)na * kCvjR1;    // [nj][na]
+    const int *m = c.r2abs + (size_t)w * na * n1;
+    for (int e = threadIdx.x; e < na * cw; e += blockDim.x) {
+        int a = e / cw, i = e % cw;
+        int ir = m[(size_t)a * n1 + r1a + i];
+        fr[a * kCvjR1 + i] = (ir >= 0) ? c.pk32[d.foff[(size_t)g * na + a] + ir] * c.rsah2f : 0.f;
+    }
+    for (int e = threadIdx.x; e < nj * na; e += blockDim.x) dj[e] = c.dj32[(size_t)g * nj * na + e];
+    __syncthreads();
+    for (int e = threadIdx.x; e < cw * nj; e += blockDim.x) {
+        int i = e / nj, jj = e % nj;
+        float xj = 0.f;
+        for (int ia = 0; ia < na; ia++) {
+            int a = na - 1 - ia;                  // angle order of the flat vector
+            xj = fmaf(fr[a * kCvjR1 + i], dj[jj * na + a], xj);
+        }
+        c.xj32[((size_t)g * n1 + r1a + i) * nj + jj] = xj;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cvj_fd32(DevGrid d, CvjArgs c)
+{
+    int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    int nj = c.nj, nv = c.nv, n1 = d.n1;
+    if (wid >= d.G * nj * nv) return;
+    int g = wid / (nj * nv), jv = wid % (nj * nv), jj = jv / nv, iv = jv % nv;
+    int j = c.jini + jj, el = d.blk_elec[g];
+    int nob = c.nobc[(size_t)(el - 1) * nj + jj];
+    int maxnv = c.nvmax < nob ? c.nvmax : nob;
+    bool on = cvj_on(c, g, j) && c.nvini + iv <= maxnv;
+    float r = 0.f;
+    if (on) {
+        const float *f = c.fd32 + (((size_t)(el - 1) * nj + jj) * nv + iv) * n1;
+        const float *x = c.xj32 + (size_t)g * n1 * nj + jj;
+        for (int ir1 = lane; ir1 < n1; ir1 += 32) r = fmaf(x[(size_t)ir1 * nj], f[ir1], r);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane == 0) {
+        const bool gated = c.gate && c.blk_isref[g] && j == c.jref && c.nvini + iv == c.nvref;
+        c.cvj[wid] = on ? (double)r : 0.0;
+        c.ring[wid] = (on && !gated) ? r : 0.f;
+    }
+}
+
+// the FP32 Djmmp columns of the projection: dj32[g][jj][a], 0 where Cvj is off
+__global__ void k_cvj_dj32(DevGrid d, CvjArgs c, float *__restrict__ dj32)
+{
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int na = d.na, nj = c.nj;
+    if (e >= (int64_t)d.G * nj * na) return;
+    int a = (int)(e % na), jj = (int)((e / na) % nj), g = (int)(e / ((int64_t)na * nj));
+    int w = d.blk_wave[g], el = d.blk_elec[g], om = d.blk_om[g], j = c.jini + jj;
+    dj32[e] =
+        cvj_on(c, g, j)
+            ? (float)c.djall[c.djoff[w] + (((size_t)om * d.ne + (el - 1)) * (c.wnangu2[w] + 1) + j) * na + a]
+            : 0.f;
+}
+
+// zS2(E, row) += sum_s Cvj_s(row) C_s(E) over the ring slots: FP32 products and
+// sums (a 64 x 64 (E, row) tile per CTA, 4 x 4 per thread), added once to the
+// FP64 accumulators, so zS2 is read and written once per flush instead of once
+// per iteration
+constexpr int kCvFlushR = 64, kCvFlushE = 64;
+__global__ void __launch_bounds__(256) k_cvj_flush(const float *__restrict__ ring, const float *__restrict__ cring,
+                                                   int nslots, int R, int netot, double *__restrict__ zs2)
+{
+    __shared__ float sc[kFluxRing][kCvFlushE][2];
+    __shared__ float sr[kFluxRing][kCvFlushR];
+    const int r0 = blockIdx.x * kCvFlushR, e0 = blockIdx.y * kCvFlushE;
+    for (int i = threadIdx.x; i < nslots * kCvFlushE * 2; i += blockDim.x) {
+        int s = i / (kCvFlushE * 2), q = i % (kCvFlushE * 2);
+        int e = e0 + q / 2;
+        sc[s][q / 2][q & 1] = e < netot ? cring[((size_t)s * netot + e) * 2 + (q & 1)] : 0.f;
+    }
+    for (int i = threadIdx.x; i < nslots * kCvFlushR; i += blockDim.x) {
+        int s = i / kCvFlushR, q = i % kCvFlushR;
+        int row = r0 + q;
+        sr[s][q] = row < R ? ring[(size_t)s * R + row] : 0.f;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // E = e0 + tx + 16 i, row = r0 + ty + 16 j
+    float ar[4][4], ai[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) ar[i][j] = ai[i][j] = 0.f;
+    for (int s = 0; s < nslots; s++) {
+        float cr[4], ci[4], v[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            cr[i] = sc[s][tx + 16 * i][0];
+            ci[i] = sc[s][tx + 16 * i][1];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = sr[s][ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                ar[i][j] = fmaf(v[j], cr[i], ar[i][j]);
+                ai[i][j] = fmaf(v[j], ci[i], ai[i][j]);
+            }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int row = r0 + ty + 16 * j;
+        if (row >= R) continue;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int e = e0 + tx + 16 * i;
+            if (e >= netot) continue;
+            double2 *z = reinterpret_cast<double2 *>(zs2 + ((size_t)row * netot + e) * 2);
+            double2 a = *z;
+            a.x += (double)ar[i][j];
+            a.y += (double)ai[i][j];
+            *z = a;
+        }
+    }
 }
 
 // 3. zS2(E, v, j, g) += Cvj C_k(E), the elastic reference channel gated below kminelastic
@@ -1198,6 +1338,36 @@ size_t max_smem_needed(Ctx &c)
 }
 
 // accumulators of iteration it for every wave (CoefEcheby, totalflux_k, Cvjflux_k, funE coefficients)
+static CvjArgs cvj_args(Ctx &c, bool gate)
+{
+    CvjArgs a;
+    a.psi = c.d_pk;
+    a.r2abs = c.d_r2abs;
+    a.djall = c.d_djall;
+    a.djoff = c.d_djoff;
+    a.wnangu2 = c.d_wnangu2;
+    a.blk_j00 = c.d_blk_j00;
+    a.blk_inc = c.d_blk_inc;
+    a.blk_isref = c.d_blk_isref;
+    a.fd = c.d_fd;
+    a.nobc = c.d_nobc;
+    a.xj = c.d_xj;
+    a.cvj = c.d_cvj;
+    a.zs2 = c.d_zs2;
+    a.zck = c.d_zck;
+    a.jini = c.jini; a.jmax = c.jmax; a.nvini = c.nvini; a.nvmax = c.nvmax;
+    a.nj = c.nj; a.nv = c.nv; a.netot = c.netot; a.jref = c.jref; a.nvref = c.nvref;
+    a.gate = gate ? 1 : 0;
+    a.sah2 = c.sah2;
+    a.pk32 = c.d_pk32;
+    a.dj32 = c.d_dj32;
+    a.fd32 = c.d_fd32;
+    a.xj32 = c.d_xj32;
+    a.ring = nullptr;
+    a.rsah2f = (float)(1.0 / c.sah2);
+    return a;
+}
+
 void launch_accumulators(Ctx &c, int64_t it)
 {
     stage_mark(c, 6);
@@ -1205,14 +1375,16 @@ void launch_accumulators(Ctx &c, int64_t it)
     const bool ring = c.d_fring != nullptr;
     k_coefecheby<<<(c.netot + 127) / 128, 128, 0, c.stream>>>(
         c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2, c.grid.hbr, it, c.d_zck,
-        ring ? c.d_cring + (size_t)c.fring_n * c.netot * 2 : nullptr);
+        ring ? c.d_cring + (size_t)c.fring_n * c.netot * 2 : nullptr,
+        c.d_cvcring ? c.d_cvcring + (size_t)c.cvring_n * c.netot * 2 : nullptr);
     LAUNCH_CHECK(c);
     for (size_t w = 0; w < c.waves.size(); w++) {
         WaveTables &t = c.waves[w];
         if (t.nofe > 0) {
             k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(c.wdev[w].efe, t.nofe, c.grid.emindlt,
                                                                      c.grid.delta2, c.grid.hbr, it,
-                                                                     c.d_zcke + (size_t)w * c.nofemax * 2, nullptr);
+                                                                     c.d_zcke + (size_t)w * c.nofemax * 2, nullptr,
+                                                                     nullptr);
             LAUNCH_CHECK(c);
         }
     }
@@ -1231,26 +1403,18 @@ void launch_accumulators(Ctx &c, int64_t it)
             LAUNCH_CHECK(c);
         }
     }
-    if (c.n2 > 1) {
-        CvjArgs a;
-        a.psi = c.d_pk;
-        a.r2abs = c.d_r2abs;
-        a.djall = c.d_djall;
-        a.djoff = c.d_djoff;
-        a.wnangu2 = c.d_wnangu2;
-        a.blk_j00 = c.d_blk_j00;
-        a.blk_inc = c.d_blk_inc;
-        a.blk_isref = c.d_blk_isref;
-        a.fd = c.d_fd;
-        a.nobc = c.d_nobc;
-        a.xj = c.d_xj;
-        a.cvj = c.d_cvj;
-        a.zs2 = c.d_zs2;
-        a.zck = c.d_zck;
-        a.jini = c.jini; a.jmax = c.jmax; a.nvini = c.nvini; a.nvmax = c.nvmax;
-        a.nj = c.nj; a.nv = c.nv; a.netot = c.netot; a.jref = c.jref; a.nvref = c.nvref;
-        a.gate = gate ? 1 : 0;
-        a.sah2 = c.sah2;
+    if (c.n2 > 1 && c.d_cvring) {
+        // mixed path: FP32 projection, Cvj into the ring, zS2 at the flush
+        CvjArgs a = cvj_args(c, gate);
+        a.ring = c.d_cvring + (size_t)c.cvring_n * c.G * c.nj * c.nv;
+        size_t sm32 = sizeof(float) * ((size_t)c.na * kCvjR1 + (size_t)c.nj * c.na);
+        k_cvj_proj32<<<dim3(c.G, (c.n1 + kCvjR1 - 1) / kCvjR1), 256, sm32, c.stream>>>(d, a);
+        LAUNCH_CHECK(c);
+        k_cvj_fd32<<<(c.G * c.nj * c.nv * 32 + 255) / 256, 256, 0, c.stream>>>(d, a);
+        LAUNCH_CHECK(c);
+        if (++c.cvring_n == kFluxRing) flush_cvj(c);
+    } else if (c.n2 > 1) {
+        CvjArgs a = cvj_args(c, gate);
         size_t smp = sizeof(double) * ((size_t)c.na * c.n1 + (size_t)c.nj * c.na);
         k_cvj_proj<<<dim3(c.G, (c.n1 + kCvjR1 - 1) / kCvjR1), 256, smp, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
@@ -1260,6 +1424,25 @@ void launch_accumulators(Ctx &c, int64_t it)
         k_cvj_acc<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
     }
+}
+
+void flush_cvj(Ctx &c)
+{
+    if (!c.d_cvring || c.cvring_n == 0) return;
+    const int R = c.G * c.nj * c.nv;
+    dim3 g((R + kCvFlushR - 1) / kCvFlushR, (c.netot + kCvFlushE - 1) / kCvFlushE);
+    k_cvj_flush<<<g, 256, 0, c.stream>>>(c.d_cvring, c.d_cvcring, c.cvring_n, R, c.netot, c.d_zs2);
+    LAUNCH_CHECK(c);
+    c.cvring_n = 0;
+}
+
+void build_cvj32(Ctx &c)
+{
+    if (!c.d_dj32 || c.n2 <= 1) return;
+    CvjArgs a = cvj_args(c, false);
+    int64_t tot = (int64_t)c.G * c.nj * c.na;
+    k_cvj_dj32<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(devgrid(c), a, c.d_dj32);
+    LAUNCH_CHECK(c);
 }
 
 void flush_flux(Ctx &c)

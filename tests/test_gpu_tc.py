@@ -69,3 +69,28 @@ def test_batched_waves_mixed(runs):
         assert np.abs(x - y).max() / np.abs(y).max() < 1e-12
         one.close()
     both.close()
+
+
+@pytest.mark.parametrize("case", ["tiny_j0", "tiny_j3", "tiny_e2"])
+def test_mixed_accumulators_track_fp64(runs, case):
+    """After 150 iterations (four flushes of the FP32 rings and a partial one) the
+    mixed path's norms, P(E), flux accumulators and state-resolved zS2 / Cvj stay
+    within 1e-4 of the FP64 path, relative to each quantity's largest magnitude;
+    the case with two electronic states takes the update's several-source branch."""
+    from madwave3_gb300 import Propagator
+
+    run = runs[case]
+    pmx = Propagator(run, "mixed")
+    p64 = Propagator(run, "fp64")
+    for p in (pmx, p64):
+        p.start()
+        p.run(150)
+    rel = lambda a, b: np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+    assert rel(pmx.norms(), p64.norms()) < 1e-4
+    assert rel(pmx.totalflux()[0], p64.totalflux()[0]) < 1e-4
+    am, a64 = pmx.accumulators(), p64.accumulators()
+    for key in ("zcr", "zcdr", "zs2", "cvj"):
+        if np.abs(a64[key]).max() > 0:
+            assert rel(am[key], a64[key]) < 1e-4, key
+    pmx.close()
+    p64.close()
