@@ -398,6 +398,15 @@ int build_device(Ctx &c)
         }
         fdptr.push_back((int)fdidx.size());
         c.NF = (int)nf;
+        // the stored points run along r1 for each R (ir2 outer, ir1 inner), so a flux
+        // line's derivative terms are normally one run of consecutive points and r1
+        c.fl_regular = true;
+        for (int64_t f = 0; f < nf && c.fl_regular; f++)
+            for (int q = fdptr[f]; q < fdptr[f + 1]; q++)
+                if (fdidx[q] != fdidx[fdptr[f]] + (q - fdptr[f]) || fdir1[q] != fdir1[fdptr[f]] + (q - fdptr[f])) {
+                    c.fl_regular = false;
+                    break;
+                }
         TRY(dupload(c, &c.d_fl_idx, fidx));
         TRY(dupload(c, &c.d_fl_poti, fpoti));
         TRY(dupload(c, &c.d_fl_dptr, fdptr));
@@ -412,9 +421,12 @@ int build_device(Ctx &c)
         c.d_fring = nullptr;
         c.d_cring = nullptr;
         c.fring_n = 0;
+        c.d_zar32 = nullptr;
         if (!c.fp64 && nf > 0) {
             TRY(dalloc(c, &c.d_fring, (size_t)mw3::kFluxRing * nf * 3, false));
             TRY(dalloc(c, &c.d_cring, (size_t)mw3::kFluxRing * c.netot * 2, false));
+            std::vector<float> zar32(t0.zar1flux.begin(), t0.zar1flux.end());
+            TRY(dupload(c, &c.d_zar32, zar32));
         }
         TRY(dalloc(c, &c.d_xj, (size_t)G * n1 * c.nj));
         TRY(dalloc(c, &c.d_cvj, (size_t)G * c.nj * c.nv));

@@ -188,6 +188,8 @@ struct Ctx {
     // mixed path: the last iterations' flux samples and C_k(E), FP32, flushed
     // into zCR/zCdR every kFluxRing iterations and before every read
     float *d_fring = nullptr;        // [kFluxRing][NF][3]
+    float *d_zar32 = nullptr;        // the r1 derivative row at the flux line, FP32 (mixed path)
+    bool fl_regular = false;         // every flux line's terms are consecutive points with consecutive r1
     float *d_cring = nullptr;        // [kFluxRing][netot][2]
     int fring_n = 0;                 // slots filled since the last flush
     // mixed path: the Cvj projection in FP32 (from the FP32 copy of psi) and Cvj of up

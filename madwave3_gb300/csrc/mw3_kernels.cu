@@ -682,20 +682,35 @@ __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double 
 __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ psi, const int64_t *__restrict__ fidx,
                                                     const int *__restrict__ dptr, const int64_t *__restrict__ didx,
                                                     const int *__restrict__ dir1, const double *__restrict__ zar,
-                                                    int NF, double *__restrict__ fpsi, float *__restrict__ fring)
+                                                    int NF, double *__restrict__ fpsi, float *__restrict__ fring,
+                                                    const float *__restrict__ psi32, const float *__restrict__ zar32,
+                                                    int regular)
 {
     int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (f >= NF) return;
     if (fring) {
-        // mixed path: FP32 products and sums (the ring holds FP32 anyway), so
-        // no FP64 instruction per term; zar rows read as FP32 from the FP64 table
+        // mixed path: FP32 products and sums (the ring holds FP32 anyway) from the FP32
+        // copy of psi; a regular line (one run of points and of r1) needs no per-term index
         float sr = 0.f, si = 0.f;
-        for (int q = dptr[f] + lane; q < dptr[f + 1]; q += 32) {
-            float p = f64_to_f32_int(psi[didx[q]]);
-            int ir1 = dir1[q];
-            sr = fmaf(f64_to_f32_int(zar[2 * ir1]), p, sr);
-            si = fmaf(f64_to_f32_int(zar[2 * ir1 + 1]), p, si);
+        const int q0 = dptr[f], q1 = dptr[f + 1];
+        if (regular) {
+            if (q1 > q0) {
+                const float *p = psi32 + didx[q0];
+                const int r0 = dir1[q0];
+                for (int q = lane; q < q1 - q0; q += 32) {
+                    const float v = p[q];
+                    sr = fmaf(zar32[2 * (r0 + q)], v, sr);
+                    si = fmaf(zar32[2 * (r0 + q) + 1], v, si);
+                }
+            }
+        } else {
+            for (int q = q0 + lane; q < q1; q += 32) {
+                const float v = psi32[didx[q]];
+                const int ir1 = dir1[q];
+                sr = fmaf(zar32[2 * ir1], v, sr);
+                si = fmaf(zar32[2 * ir1 + 1], v, si);
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -703,7 +718,7 @@ __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ p
             si += __shfl_xor_sync(0xffffffffu, si, o);
         }
         if (lane == 0) {
-            fring[3 * (size_t)f] = f64_to_f32_int(psi[fidx[f]]);
+            fring[3 * (size_t)f] = psi32[fidx[f]];
             fring[3 * (size_t)f + 1] = sr;
             fring[3 * (size_t)f + 2] = si;
         }
@@ -1392,7 +1407,7 @@ void launch_accumulators(Ctx &c, int64_t it)
     if (c.NF > 0 && !(gate && c.waves[0].iprod == 1)) {
         k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(
             c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx, c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi,
-            ring ? c.d_fring + (size_t)c.fring_n * c.NF * 3 : nullptr);
+            ring ? c.d_fring + (size_t)c.fring_n * c.NF * 3 : nullptr, c.d_pk32, c.d_zar32, c.fl_regular ? 1 : 0);
         LAUNCH_CHECK(c);
         if (ring) {
             if (++c.fring_n == kFluxRing) flush_flux(c);
