@@ -260,66 +260,46 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
             const uint64_t stage16 = D2_STAGE >> 4, small16 = D2_BIGMAX >> 4;
             const uint64_t lo128 = D2_SMALL_LO >> 4, loRB = big_lo >> 4, tile16 = (16 * D2_SBO) >> 4;
             const uint32_t id_nn = idesc_tf32(128, nnp), id_rb = idesc_tf32(128, RB), id_128 = idesc_tf32(128, 128);
-            // The wait for chunk t + 1 is made before the last MMA of chunk t is issued, while
-            // the tensor pipe still holds queued MMAs of chunk t, so its shared-memory latency
-            // does not leave the pipe idle.  Not across a product boundary: the first chunk of
-            // a product is filled from the previous product, whose last commit it waits for.
-            const int b1 = 2 * nkh, b2 = b1 + nkr, b3 = b2 + nkr;   // first chunks of products 1, 2, 3
-            bool ready = false, ok = false;                         // chunk t's wait made, and its result
             d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
                 const int s = t & (D2_NS - 1), u = t >> 2;
-                if (!ready) {
-                    ok = d2_wait(&full[s], u & 1, fail);
-                    fence_after_sync();
-                }
-                const bool look = t + 1 < total && t + 1 != b1 && t + 1 != b2 && t + 1 != b3;
-                bool ok_next = false;
-                auto ahead = [&]() {
-                    if (look) {
-                        ok_next = d2_wait(&full[(t + 1) & (D2_NS - 1)], ((t + 1) >> 2) & 1, fail);
-                        fence_after_sync();
-                    }
-                };
+                const bool ok = d2_wait(&full[s], u & 1, fail);
+                fence_after_sync();
                 if (ok) {
                     const uint64_t bg = d0 + (uint64_t)s * stage16, sl = bg + small16;
-                    // the MMAs of one K step; i in [i0, i1) of its n products
-                    auto step = [&](int ks, int i0, int i1) {
+#pragma unroll
+                    for (int ks = 0; ks < D2_KC / 8; ks++) {
                         const uint64_t o = ks * k16;
                         const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
-                        for (int i = i0; i < i1; i++) {
-                            const int term = i % 3;
-                            const int ah = term == 2, bh = term == 1;   // lo plane of A / of B
-                            if (gi == 0) {
-                                // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
-                                mma_tf32(tb + 128u * par, bg + (ah ? lo128 : 0) + o, sl + (bh ? lo128 : 0) + o, id_nn,
-                                         term == 0 ? acc0 : 1);
-                            } else if (gi == 1) {
-                                // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
-                                const int tt = i / 3;
-                                mma_tf32(tb + 256u + 128u * tt, bg + tt * tile16 + (ah ? loRB : 0) + o,
-                                         sl + (bh ? lo128 : 0) + o, id_nn, term == 0 ? acc0 : 1);
-                            } else if (gi == 2) {
-                                // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
-                                mma_tf32(tb, sl + (ah ? lo128 : 0) + o, bg + (bh ? loRB : 0) + o, id_rb,
-                                         term == 0 ? acc0 : 1);
-                            } else {
-                                // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
-                                mma_tf32(tb + 256u + 128u * par, sl + (ah ? lo128 : 0) + o, bg + (bh ? lo128 : 0) + o,
-                                         id_128, term == 0 ? acc0 : 1);
+                        if (gi == 0) {
+                            // E or O: M = 128 (i), N = nnp (r1): A = folded S2 (big), B = Xs (small)
+                            const uint32_t d = tb + 128u * par;
+                            mma_tf32(d, bg + o, sl + o, id_nn, acc0);
+                            mma_tf32(d, bg + o, sl + lo128 + o, id_nn, 1);
+                            mma_tf32(d, bg + lo128 + o, sl + o, id_nn, 1);
+                        } else if (gi == 1) {
+                            // per R tile: M = 128, N = nnp: A = D1 rows (big), B = S1 (small)
+                            for (int tt = 0; tt < NT; tt++) {
+                                const uint64_t at = bg + tt * tile16;
+                                const uint32_t d = tb + 256u + 128u * tt;
+                                mma_tf32(d, at + o, sl + o, id_nn, acc0);
+                                mma_tf32(d, at + o, sl + lo128 + o, id_nn, 1);
+                                mma_tf32(d, at + loRB + o, sl + o, id_nn, 1);
                             }
+                        } else if (gi == 2) {
+                            // M = 128 (r1), N = RB (R): A = S1 (small), B = scaled D2 rows (big)
+                            mma_tf32(tb, sl + o, bg + o, id_rb, acc0);
+                            mma_tf32(tb, sl + o, bg + loRB + o, id_rb, 1);
+                            mma_tf32(tb, sl + lo128 + o, bg + o, id_rb, 1);
+                        } else {
+                            // E or O: M = 128 (r1), N = 128 (i): A = D3 columns (small), B = folded S2 (big)
+                            const uint32_t d = tb + 256u + 128u * par;
+                            mma_tf32(d, sl + o, bg + o, id_128, acc0);
+                            mma_tf32(d, sl + o, bg + lo128 + o, id_128, 1);
+                            mma_tf32(d, sl + lo128 + o, bg + o, id_128, 1);
                         }
-                    };
-                    const int n = gi == 1 ? 3 * NT : 3;
-                    for (int ks = 0; ks + 1 < D2_KC / 8; ks++) step(ks, 0, n);
-                    step(D2_KC / 8 - 1, 0, n - 1);
-                    ahead();
-                    step(D2_KC / 8 - 1, n - 1, n);
-                } else {
-                    ahead();
+                    }
                 }
                 mma_commit(&empty[s]);        // also after a failure, so no waiter is left behind
-                ready = look;
-                ok = ok_next;
             });
         }
     } else {
