@@ -58,23 +58,6 @@ struct AngArgs {
     int *err;
 };
 
-// Streamed data (the X tile, the map) is read without allocating in L1: with two
-// CTAs per SM the shared memory leaves about 28 KB of L1, which the j-basis
-// scale rows (yyy and xl2mat, 10 KB per tile and block, read by every thread of
-// the tile) should keep.
-__device__ __forceinline__ float ldg_stream(const float *p)
-{
-    float v;
-    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ int ldg_stream(const int *p)
-{
-    int v;
-    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
-    return v;
-}
-
 // X tile of block g: A operand rows m = (r1 offset)*8 + (R offset), K = angle.
 // A quarter warp takes 8 consecutive R of one r1 row: its global loads are one
 // 32-byte sector per angle and its shared stores one 128-byte core-matrix block.
@@ -93,7 +76,7 @@ __device__ __forceinline__ void ang_stage_x(const AngArgs<HT> &p, int g, int r1_
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             int a = kg * 4 + c;
-            v[it][c] = (in && a < p.na) ? ldg_stream(Xg + ((size_t)a * p.n1 + gr1) * p.n2 + gr2) : 0.f;
+            v[it][c] = (in && a < p.na) ? __ldg(Xg + ((size_t)a * p.n1 + gr1) * p.n2 + gr2) : 0.f;
         }
     }
 #pragma unroll
@@ -157,7 +140,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
     for (int e = threadIdx.x; e < AG_K * 128; e += blockDim.x) {
         int a = e >> 7, mm = e & 127;
         int gr1 = r1_0 + (mm >> 3), gr2 = r2_0 + (mm & 7);
-        int v = (a < na && gr1 < n1 && gr2 < n2) ? ldg_stream(p.map + ((size_t)a * n1 + gr1) * n2 + gr2) : -1;
+        int v = (a < na && gr1 < n1 && gr2 < n2) ? __ldg(p.map + ((size_t)a * n1 + gr1) * n2 + gr2) : -1;
         s_map[e] = v < 0 ? (uint16_t)0xFFFF : (uint16_t)v;
     }
     // this thread's tile row (tensor-memory lane) and column half
