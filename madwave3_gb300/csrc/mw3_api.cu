@@ -274,6 +274,11 @@ int build_device(Ctx &c)
     TRY(dupload(c, &c.d_p2r2, p2r2));
     TRY(dupload(c, &c.d_absfr1, a1));
     TRY(dupload(c, &c.d_absfr2, a2));
+    {
+        std::vector<float> f1(a1.begin(), a1.end()), f2(a2.begin(), a2.end());
+        TRY(dupload(c, &c.d_absfr1f, f1));
+        TRY(dupload(c, &c.d_absfr2f, f2));
+    }
     TRY(dupload(c, &c.d_djall, djall));
     TRY(dupload(c, &c.d_djoff, djoff));
     TRY(dupload(c, &c.d_l2all, l2all));

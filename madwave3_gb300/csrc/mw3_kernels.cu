@@ -417,6 +417,7 @@ struct UpdArgs {
     double *out;
     const int *vsrc;               // [G][ne]
     const double *absfr1, *absfr2; // [W][n1], [W][n2]
+    const float *absfr1f, *absfr2f; // FP32 copies (mixed path)
     double emindlt, delta2;
     double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
     const float *vr32;             // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
@@ -539,9 +540,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
         // thirds busy), so everything that is H psi stays in FP32 and only the
         // recursion itself is FP64:
         //   t = H 2/delta2 + sum_s vr_s psi32_s          (FP32: H psi and V psi)
-        //   psi_k+1 = t - psi_k-1, or (t - f psi_k-1) f   (FP64; f the absorption inside the absorbers)
-        // with the FP32 copies of psi_k read and psi_k+1 written beside the FP64
-        // vectors, the conversions done with integer instructions, the norm in FP32
+        //   psi_k+1 = (t - psi_k-1) + d                  (one FP64 add, and a second inside the absorbers)
+        //   d = (f - 1) t + (1 - f^2) psi_k-1             (FP32; f the absorption, 0 outside the absorbers)
+        // so that psi_k+1 = f t - f^2 psi_k-1 = (t - f psi_k-1) f to FP32 accuracy in d;
+        // a warp then runs one FP64 add, or two, instead of both branches of a
+        // damped/undamped split.  The FP32 copies of psi_k are read and of psi_k+1
+        // written beside the FP64 vectors, the conversions done with integer
+        // instructions, the norm in FP32
         const float *vr0 = nsrc > 0 ? u.vr32 + cd.voff : nullptr, *pr0 = nsrc > 0 ? u.pk32 + cd.poff : nullptr;
         float *__restrict__ o32 = u.out32 + off;
         int r1[U], r2[U];
@@ -569,13 +574,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
             if (u.first) {
                 nv = f32_to_f64_int(0.5f * t32);
             } else {
-                const double t = f32_to_f64_int(t32);
-                const double a1 = ab1[r1[k]], a2 = ab2[r2[k]];
-                if (__double_as_longlong(a1) == 0x3FF0000000000000LL && __double_as_longlong(a2) == 0x3FF0000000000000LL) {
-                    nv = t - p1[k];
-                } else {
-                    const double fab = a1 * a2;
-                    nv = fma(-fab, p1[k], t) * fab;
+                nv = f32_to_f64_int(t32) - p1[k];
+                const float a1 = u.absfr1f[(size_t)w * n1 + r1[k]], a2 = u.absfr2f[(size_t)w * n2 + r2[k]];
+                if (!(__float_as_uint(a1) == 0x3F800000u && __float_as_uint(a2) == 0x3F800000u)) {
+                    const float f = a1 * a2, p1f = f64_to_f32_int(p1[k]);
+                    nv += f32_to_f64_int(fmaf(f - 1.f, t32, (1.f - f * f) * p1f));
                 }
             }
             float nf = f64_to_f32_int(nv);
@@ -1285,6 +1288,8 @@ void launch_update(Ctx &c, int first)
     u.vsrc = c.d_vsrc;
     u.absfr1 = c.d_absfr1;
     u.absfr2 = c.d_absfr2;
+    u.absfr1f = c.d_absfr1f;
+    u.absfr2f = c.d_absfr2f;
     u.emindlt = c.grid.emindlt;
     u.delta2 = c.grid.delta2;
     u.rdelta = 1.0 / c.grid.delta2;
