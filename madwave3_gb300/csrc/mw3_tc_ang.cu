@@ -219,29 +219,43 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
             const float *yrow = p.yj + ((size_t)g * n1 + cr1) * AG_K;
             const float *lrow0 = p.l2 + ((size_t)g * 3 * n2 + cr2) * AG_K;
             const size_t lslot = (size_t)n2 * AG_K;
+            // The scale rows are shared: the 32 lanes of a warp cover 4 r1 rows (lane >> 3)
+            // and 8 R rows (lane & 7).  Each lane loads a slice of its rows (two yyy
+            // values, four of each xl2mat slot) and the values are passed between lanes,
+            // instead of every lane loading all of its own rows.
+            const int gq = lane >> 3, rq = lane & 7;
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
                 const int j0 = half * 32 + cc * 16;
+                const float2 ys = *reinterpret_cast<const float2 *>(yrow + j0 + 2 * rq);
+                const float4 l0s = *reinterpret_cast<const float4 *>(lrow0 + lslot + j0 + 4 * gq);
+                const float4 lms = hp ? *reinterpret_cast<const float4 *>(lrow0 + j0 + 4 * gq)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 lqs = hn ? *reinterpret_cast<const float4 *>(lrow0 + 2 * lslot + j0 + 4 * gq)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
                 float b0[16], bp[16], bn[16];
                 tmem_ld16(s0 + j0, b0);
                 if (hp) tmem_ld16(sp + j0, bp);
                 if (hn) tmem_ld16(sn + j0, bn);
 #pragma unroll
                 for (int i4 = 0; i4 < 4; i4++) {
-                    int j = j0 + 4 * i4;
-                    float4 y = __ldg(reinterpret_cast<const float4 *>(yrow + j));
-                    float4 l0 = __ldg(reinterpret_cast<const float4 *>(lrow0 + lslot + j));
-                    float hb[4] = {(y.x + l0.x) * b0[4 * i4], (y.y + l0.y) * b0[4 * i4 + 1],
-                                   (y.z + l0.z) * b0[4 * i4 + 2], (y.w + l0.w) * b0[4 * i4 + 3]};
-                    if (hp) {
-                        float4 lm = __ldg(reinterpret_cast<const float4 *>(lrow0 + j));
-                        hb[0] += lm.x * bp[4 * i4]; hb[1] += lm.y * bp[4 * i4 + 1];
-                        hb[2] += lm.z * bp[4 * i4 + 2]; hb[3] += lm.w * bp[4 * i4 + 3];
-                    }
-                    if (hn) {
-                        float4 lq = __ldg(reinterpret_cast<const float4 *>(lrow0 + 2 * lslot + j));
-                        hb[0] += lq.x * bn[4 * i4]; hb[1] += lq.y * bn[4 * i4 + 1];
-                        hb[2] += lq.z * bn[4 * i4 + 2]; hb[3] += lq.w * bn[4 * i4 + 3];
+                    const int j = j0 + 4 * i4;
+                    float hb[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        // yyy(j0 + 4 i4 + e) of this lane's r1 row, xl2mat of its R row
+                        const float y = __shfl_sync(0xffffffffu, (e & 1) ? ys.y : ys.x, (lane & 24) + 2 * i4 + (e >> 1));
+                        const int src = 8 * i4 + rq;
+                        const float l0 = __shfl_sync(0xffffffffu, e == 0 ? l0s.x : e == 1 ? l0s.y : e == 2 ? l0s.z : l0s.w, src);
+                        hb[e] = (y + l0) * b0[4 * i4 + e];
+                        if (hp) {
+                            const float lm = __shfl_sync(0xffffffffu, e == 0 ? lms.x : e == 1 ? lms.y : e == 2 ? lms.z : lms.w, src);
+                            hb[e] += lm * bp[4 * i4 + e];
+                        }
+                        if (hn) {
+                            const float lq = __shfl_sync(0xffffffffu, e == 0 ? lqs.x : e == 1 ? lqs.y : e == 2 ? lqs.z : lqs.w, src);
+                            hb[e] += lq * bn[4 * i4 + e];
+                        }
                     }
                     float4 h = make_float4(tf32_hi(hb[0]), tf32_hi(hb[1]), tf32_hi(hb[2]), tf32_hi(hb[3]));
                     float4 l = make_float4(hb[0] - h.x, hb[1] - h.y, hb[2] - h.z, hb[3] - h.w);
