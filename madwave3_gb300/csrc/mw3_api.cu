@@ -405,7 +405,8 @@ int build_device(Ctx &c)
         c.NF = (int)nf;
         // the stored points run along r1 for each R (ir2 outer, ir1 inner), so a flux
         // line's derivative terms are normally one run of consecutive points and r1
-        c.fl_regular = true;
+        // MW3_GENERAL_TABLES=1 keeps the general (indexed) form, so tests can compare both
+        c.fl_regular = !mw3::general_tables();
         for (int64_t f = 0; f < nf && c.fl_regular; f++)
             for (int q = fdptr[f]; q < fdptr[f + 1]; q++)
                 if (fdidx[q] != fdidx[fdptr[f]] + (q - fdptr[f]) || fdir1[q] != fdir1[fdptr[f]] + (q - fdptr[f])) {

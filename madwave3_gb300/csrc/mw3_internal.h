@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <cstdlib>
 
 #include <string>
 #include <vector>
@@ -275,6 +276,13 @@ void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end);
 void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end);
 // fused tensor-core radial DSTs of the mixed path (mw3_tc_dst2d.cu); sets c.use_tc_dst2d
 int build_tc_dst2d(Ctx &c);
+// true when the environment asks for the general (indexed) tables even where the
+// stored points form regular lines (MW3_GENERAL_TABLES=1; for tests)
+inline bool general_tables()
+{
+    const char *v = std::getenv("MW3_GENERAL_TABLES");
+    return v && v[0] == '1';
+}
 // the TMA tensor map of the rectangles (after they are allocated)
 int encode_tc_dst2d_xmap(Ctx &c);
 void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end);

@@ -601,7 +601,7 @@ int build_tc_dst2d(Ctx &c)
     // a point's index as base + r1 instead of reading the map
     {
         std::vector<int2> rl((size_t)na * c.n2);
-        bool regular = c.n1 < 32768;
+        bool regular = c.n1 < 32768 && !general_tables();
         for (int a = 0; a < na && regular; a++) {
             std::vector<int> first(c.n2, -1), lo(c.n2, 0), hi(c.n2, -1);
             for (int ir = 0; ir < c.npunreal[a] && regular; ir++) {

@@ -97,3 +97,24 @@ def test_mixed_accumulators_track_fp64(runs, case):
         assert rel(am[key], a64[key]) < 5e-4, key
     pmx.close()
     p64.close()
+
+
+@pytest.mark.parametrize("case", ["tiny_j0", "tiny_e2"])
+def test_regular_lines_match_general_tables(runs, case, monkeypatch):
+    """When every (angle, R) line of stored points is one run with consecutive r1,
+    the fused DST writes H through line bases and the flux derivative reads its
+    runs without indices; MW3_GENERAL_TABLES=1 keeps the indexed form.  Both give
+    the same bits."""
+    from madwave3_gb300 import Propagator
+
+    run = runs[case]
+    out = []
+    for general in ("0", "1"):
+        monkeypatch.setenv("MW3_GENERAL_TABLES", general)
+        p = Propagator(run, "mixed")
+        p.start()
+        p.run(40)
+        out.append((p.state()[1], p.totalflux()[0], p.accumulators()["zcdr"]))
+        p.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
