@@ -166,8 +166,11 @@ def stage_model(runs, prop, stages=None):
         "dst_R_gather": ("flop", 2.0 * rows * n2 * n2),
         "angular": (("byte", 20.0 * nsto) if fused else ("flop", 2.0 * na * nsto)),
         "angular_l2": ("flop", 2.0 * na * nsto * 3),
-        # psi_k, psi_k-1, H read, psi_k+1 written, V row, rectangle store, two grid indices
-        "update": ("byte", nsto * (8 * 4 + 8 * ne + tsz + 8)),
+        # FP64 path: psi_k, psi_k-1, H read, psi_k+1 written, V row, rectangle store, two
+        # grid indices.  Mixed path: two grid indices, H (FP32), per source the FP32
+        # potential and FP32 psi_k, psi_k-1 (FP64), psi_k+1 (FP64 and FP32), rectangle (FP32)
+        "update": ("byte", nsto * (8 * 4 + 8 * ne + tsz + 8)) if prop.precision == "fp64"
+        else ("byte", nsto * (8 + 4 + 8 * ne + 8 + 8 + 4 + 4)),
         "accumulators": ("byte", sum(prop.nflux(w) * r.inp.netot * 2 * 2 * 16 for w, r in enumerate(runs))),
     }
 
@@ -220,25 +223,20 @@ def run_gpu(args, rank, world, local):
     ms_step = ms_max / args.steps
     value = world * nsto * args.steps / (ms_max * 1e-3)
 
-    # end to end through the C-ABI: host state in pinned memory, uploaded every
-    # step, one iteration, psi_k read back
+    # end to end through the C-ABI: the host keeps the whole state (all waves back to
+    # back, pinned); every step uploads it, runs one iteration and reads it back
     e2e_steps = max(1, min(args.steps, 10))
-    pins = []
-    for w, r in enumerate(runs):
-        km1, k, it = prop.state(w)
-        a = torch.from_numpy(km1).pin_memory()
-        b = torch.from_numpy(k).pin_memory()
-        pins.append((a, b, it))
+    km1, k, it = prop.state_all()
+    a = torch.from_numpy(km1).pin_memory()
+    b = torch.from_numpy(k).pin_memory()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for s in range(e2e_steps):
-        for w, (a, b, it) in enumerate(pins):
-            prop.upload_state(w, a.numpy(), b.numpy(), it + s)
+        prop.upload_state_all(a.numpy(), b.numpy(), it + s)
         prop.run(1)
-        for w, (a, b, it) in enumerate(pins):
-            prop.state(w, out_km1=a.numpy(), out_k=b.numpy())   # the host keeps the state
+        prop.state_all(out_km1=a.numpy(), out_k=b.numpy())
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps

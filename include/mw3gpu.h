@@ -128,6 +128,13 @@ int mw3_sync(mw3_ctx *ctx);
 int mw3_download_state(mw3_ctx *ctx, int32_t wave_id, double *psi_km1, double *psi_k,
                        int64_t *it);
 
+/* mw3_upload_state / mw3_download_state for every wave at once: the host arrays
+ * hold the waves' vectors back to back in wave order (wave w starts after the
+ * ntot of waves 0..w-1), moved with one copy each way for the whole context and
+ * one synchronisation per call. */
+int mw3_upload_state_all(mw3_ctx *ctx, const double *psi_km1, const double *psi_k, int64_t it);
+int mw3_download_state_all(mw3_ctx *ctx, double *psi_km1, double *psi_k, int64_t *it);
+
 /* ||psi_k||^2 after each iteration since the last mw3_start/upload
  * (check, SRC/main_madwave3.f:431-442): norms[0..*n-1]; *n in: capacity,
  * out: number written. */

@@ -871,6 +871,40 @@ int mw3_download_state(mw3_ctx *h, int32_t w, double *km1, double *k, int64_t *i
     return check_device_flags(c, "mw3_download_state");
 }
 
+int mw3_upload_state_all(mw3_ctx *h, const double *psi_km1, const double *psi_k, int64_t it)
+{
+    if (!h || !psi_km1 || !psi_k || it < 1) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    int rc = build_device(c);
+    if (rc) return rc;
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, psi_km1, sizeof(double) * c.NT, cudaMemcpyHostToDevice, c.stream));
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pk, psi_k, sizeof(double) * c.NT, cudaMemcpyHostToDevice, c.stream));
+    scatter(c, c.d_pk, 0, c.G);
+    if (!c.started) {
+        rc = reset_accumulators(c);
+        if (rc) return rc;
+    }
+    c.it = it;
+    c.norm_slot = 0;
+    c.started = true;
+    rc = check_launch(c, "mw3_upload_state_all");
+    if (rc) return rc;
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return MW3_OK;
+}
+
+int mw3_download_state_all(mw3_ctx *h, double *km1, double *k, int64_t *it)
+{
+    if (!h) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (!c.started) return MW3_ERR_STATE;
+    if (km1) MW3_CUDA_TRY(cudaMemcpyAsync(km1, c.d_pkm1, sizeof(double) * c.NT, cudaMemcpyDeviceToHost, c.stream));
+    if (k) MW3_CUDA_TRY(cudaMemcpyAsync(k, c.d_pk, sizeof(double) * c.NT, cudaMemcpyDeviceToHost, c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    if (it) *it = c.it;
+    return check_device_flags(c, "mw3_download_state_all");
+}
+
 int mw3_norms(mw3_ctx *h, int32_t w, double *norms, int64_t *n)
 {
     if (!h || !n) return MW3_ERR_ARG;

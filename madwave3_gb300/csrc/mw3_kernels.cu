@@ -27,6 +27,11 @@ namespace mw3 {
 // ---------------------------------------------------------------------------
 constexpr int kPointChunk = 1024;   // stored points per CTA in the point kernels
 
+__device__ __forceinline__ float f64_to_f32_int(double x);
+template <typename T> __device__ __forceinline__ T rect_value(double v) { return (T)v; }
+// FP32 rectangles take the update kernel's rounding, so a restart reproduces a run
+template <> __device__ __forceinline__ float rect_value<float>(double v) { return f64_to_f32_int(v); }
+
 // psi32 (optional): the FP32 copy of psi at the stored points, which the mixed
 // update reads for the potential term
 template <typename T>
@@ -43,8 +48,8 @@ __global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict
         int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
         int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
         const double v = psi[off + ir];
-        base[(size_t)ir1 * d.n2 + ir2] = (T)v;
-        if (psi32) psi32[off + ir] = (float)v;
+        base[(size_t)ir1 * d.n2 + ir2] = rect_value<T>(v);
+        if (psi32) psi32[off + ir] = rect_value<float>(v);
     }
 }
 

@@ -64,7 +64,8 @@ class Wave(ct.Structure):
 
 HEADER_FUNCS = [
     "mw3_create", "mw3_add_wave", "mw3_wave_size", "mw3_hphi", "mw3_start", "mw3_upload_state",
-    "mw3_run", "mw3_sync", "mw3_download_state", "mw3_norms", "mw3_totalflux", "mw3_flux_count",
+    "mw3_run", "mw3_sync", "mw3_download_state", "mw3_upload_state_all", "mw3_download_state_all",
+    "mw3_norms", "mw3_totalflux", "mw3_flux_count",
     "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_path_flags", "mw3_get_stream",
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_last_error", "mw3_destroy",
@@ -104,6 +105,8 @@ def load_library(build_if_missing=True):
     L.mw3_run.argtypes = [vp, ct.c_int64]
     L.mw3_sync.argtypes = [vp]
     L.mw3_download_state.argtypes = [vp, ct.c_int32, F64P, F64P, ct.POINTER(ct.c_int64)]
+    L.mw3_upload_state_all.argtypes = [vp, F64P, F64P, ct.c_int64]
+    L.mw3_download_state_all.argtypes = [vp, F64P, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_norms.argtypes = [vp, ct.c_int32, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_totalflux.argtypes = [vp, ct.c_int32, F64P, F64P]
     L.mw3_flux_count.argtypes = [vp, ct.c_int32, I32P]
@@ -240,6 +243,23 @@ class Propagator:
         a = np.ascontiguousarray(psi_km1, np.float64)
         b = np.ascontiguousarray(psi_k, np.float64)
         self._check(self.L.mw3_upload_state(self.h, wave, _p(a), _p(b), it), "mw3_upload_state")
+
+    def upload_state_all(self, psi_km1, psi_k, it):
+        """Every wave's state at once: the vectors back to back in wave order."""
+        a = np.ascontiguousarray(psi_km1, np.float64)
+        b = np.ascontiguousarray(psi_k, np.float64)
+        assert a.size == b.size == sum(self.ntot)
+        self._check(self.L.mw3_upload_state_all(self.h, _p(a), _p(b), it), "mw3_upload_state_all")
+
+    def state_all(self, out_km1=None, out_k=None):
+        """Every wave's state at once, back to back in wave order."""
+        n = sum(self.ntot)
+        a = np.empty(n) if out_km1 is None else out_km1
+        b = np.empty(n) if out_k is None else out_k
+        assert a.size == b.size == n and a.dtype == b.dtype == np.float64
+        it = ct.c_int64()
+        self._check(self.L.mw3_download_state_all(self.h, _p(a), _p(b), ct.byref(it)), "mw3_download_state_all")
+        return a, b, it.value
 
     def run(self, n):
         self._check(self.L.mw3_run(self.h, n), "mw3_run")

@@ -118,3 +118,24 @@ def test_regular_lines_match_general_tables(runs, case, monkeypatch):
         p.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+def test_state_all_round_trip(runs):
+    """mw3_upload_state_all / mw3_download_state_all move every wave's state at
+    once and agree with the per-wave calls."""
+    from madwave3_gb300 import Propagator
+
+    r0, r3 = runs["tiny_j0"], runs["tiny_j3"]
+    p = Propagator([r0, r3], "mixed")
+    p.start()
+    p.run(5)
+    km1, k, it = p.state_all()
+    per = [p.state(w) for w in range(2)]
+    assert np.array_equal(km1, np.concatenate([x[0] for x in per]))
+    assert np.array_equal(k, np.concatenate([x[1] for x in per]))
+    p.run(7)
+    ref = p.state_all()[1]
+    p.upload_state_all(km1, k, it)
+    p.run(7)
+    assert np.array_equal(p.state_all()[1], ref)
+    p.close()
