@@ -59,35 +59,48 @@ struct AngArgs {
 };
 
 // X tile of block g: A operand rows m = (r1 offset)*8 + (R offset), K = angle.
-// A quarter warp takes 8 consecutive R of one r1 row: its global loads are one
-// 32-byte sector per angle and its shared stores one 128-byte core-matrix block.
+// The tile arrives by asynchronous 4-byte copies straight into the lo plane at
+// each element's operand position (zero outside the grid and beyond the angles),
+// issued as soon as the operand space is free; later each thread splits its own
+// elements into the hi and lo planes in place.  A quarter warp takes 8
+// consecutive R of one r1 row: one 32-byte sector per angle in global memory.
 template <typename HT>
-__device__ __forceinline__ void ang_stage_x(const AngArgs<HT> &p, int g, int r1_0, int r2_0, unsigned char *hi,
-                                            unsigned char *lo)
+__device__ __forceinline__ void ang_copy_x(const AngArgs<HT> &p, int g, int r1_0, int r2_0, unsigned char *lo)
 {
     const float *Xg = p.X + (size_t)g * p.na * p.n1 * p.n2;
-    float v[8][4];
+    const uint32_t lo_s = smem_u32(lo);
 #pragma unroll
     for (int it = 0; it < 8; it++) {
-        int e = threadIdx.x + 256 * it;
-        int r2o = e & 7, r1o = (e >> 3) & 15, kg = e >> 7;
-        int gr1 = r1_0 + r1o, gr2 = r2_0 + r2o;
-        bool in = gr1 < p.n1 && gr2 < p.n2;
+        const int e = threadIdx.x + 256 * it;
+        const int r2o = e & 7, r1o = (e >> 3) & 15, kg = e >> 7;
+        const int gr1 = r1_0 + r1o, gr2 = r2_0 + r2o;
+        const bool in = gr1 < p.n1 && gr2 < p.n2;
+        const uint32_t dst = lo_s + kmaj_off(r1o * 8 + r2o, kg * 4, AG_K);
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            int a = kg * 4 + c;
-            v[it][c] = (in && a < p.na) ? __ldg(Xg + ((size_t)a * p.n1 + gr1) * p.n2 + gr2) : 0.f;
+            const int a = kg * 4 + c;
+            const bool ok = in && a < p.na;
+            const float *src = ok ? Xg + ((size_t)a * p.n1 + gr1) * p.n2 + gr2 : Xg;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst + 4 * c), "l"(src), "r"(ok ? 4 : 0)
+                         : "memory");
         }
     }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// this thread's elements of the copied tile: wait for its copies, split in place
+__device__ __forceinline__ void ang_split_x(unsigned char *hi, unsigned char *lo)
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
 #pragma unroll
     for (int it = 0; it < 8; it++) {
-        int e = threadIdx.x + 256 * it;
-        int m = ((e >> 3) & 15) * 8 + (e & 7), kg = e >> 7;
-        float4 h = make_float4(tf32_hi(v[it][0]), tf32_hi(v[it][1]), tf32_hi(v[it][2]), tf32_hi(v[it][3]));
-        float4 l = make_float4(v[it][0] - h.x, v[it][1] - h.y, v[it][2] - h.z, v[it][3] - h.w);
-        uint32_t off = kmaj_off(m, kg * 4, AG_K);
+        const int e = threadIdx.x + 256 * it;
+        const int m = ((e >> 3) & 15) * 8 + (e & 7), kg = e >> 7;
+        const uint32_t off = kmaj_off(m, kg * 4, AG_K);
+        const float4 x = *reinterpret_cast<const float4 *>(lo + off);
+        const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
         *reinterpret_cast<float4 *>(hi + off) = h;
-        *reinterpret_cast<float4 *>(lo + off) = l;
+        *reinterpret_cast<float4 *>(lo + off) = make_float4(x.x - h.x, x.y - h.y, x.z - h.z, x.w - h.w);
     }
 }
 
@@ -151,6 +164,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
     const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
     uint32_t ph0 = 0, ph1 = 0;
     bool bad = false, copy_out = false;
+    if (L > 0) ang_copy_x(p, p.chain[cb], r1_0, r2_0, AS + AG_APLANE);
 
     for (int pos = -1; pos < L; pos++) {
         // the X tile of the block after next into L2 (one 32-byte run per angle and r1
@@ -182,7 +196,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
                 bulk_g2s(DS, p.dfw + (size_t)gn * 2 * 64 * AG_K, 2 * AG_DPLANE, &bars[0]);
                 copy_out = true;
             }
-            ang_stage_x(p, gn, r1_0, r2_0, AS, AS + AG_APLANE);
+            ang_split_x(AS, AS + AG_APLANE);
             fence_async_smem();
             fence_before_sync();
             if (__syncthreads_or(bad)) break;
@@ -198,7 +212,11 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
             ph1 ^= 1u;
             fence_after_sync();
         }
-        if (pos < 0) continue;
+        if (pos < 0) {
+            // the first block's tile has been read: the second block's tile can come in
+            if (!__syncthreads_or(bad) && L > 1) ang_copy_x(p, p.chain[cb + 1], r1_0, r2_0, AS + AG_APLANE);
+            continue;
+        }
         if (__syncthreads_or(bad)) break;
         // ---- scaling and coupling in the j basis ----
         const int g = p.chain[cb + pos];
@@ -281,6 +299,9 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
         ph1 ^= 1u;
         fence_after_sync();
         if (__syncthreads_or(bad)) break;
+        // the operand space is free again: the X tile of the block after next starts
+        // arriving while this block's H is written
+        if (pos + 2 < L) ang_copy_x(p, p.chain[cb + pos + 2], r1_0, r2_0, AS + AG_APLANE);
         // ---- H += result at the stored points of this block ----
         {
 #pragma unroll
@@ -308,6 +329,8 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
         fence_before_sync();
     }
     if (bad && threadIdx.x == 0) atomicExch(p.err, 1);
+    // copies of an X tile still in flight (after a failure) land before the CTA exits
+    asm volatile("cp.async.wait_all;" ::: "memory");
     // a bulk copy left in flight by a failed wait must land before the CTA exits
     if (copy_out) mbar_wait(&bars[0], ph0);
     fence_before_sync();

@@ -261,6 +261,13 @@ class Propagator:
         self._check(self.L.mw3_download_state_all(self.h, _p(a), _p(b), ct.byref(it)), "mw3_download_state_all")
         return a, b, it.value
 
+    def state_k_all(self, out_k):
+        """psi_k of every wave (back to back in wave order) into out_k."""
+        assert out_k.size == sum(self.ntot) and out_k.dtype == np.float64
+        it = ct.c_int64()
+        self._check(self.L.mw3_download_state_all(self.h, None, _p(out_k), ct.byref(it)), "mw3_download_state_all")
+        return it.value
+
     def run(self, n):
         self._check(self.L.mw3_run(self.h, n), "mw3_run")
 
