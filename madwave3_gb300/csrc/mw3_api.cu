@@ -877,18 +877,8 @@ int mw3_upload_state_all(mw3_ctx *h, const double *psi_km1, const double *psi_k,
     Ctx &c = h->c;
     int rc = build_device(c);
     if (rc) return rc;
-    // the two vectors on two streams, so two copy engines share the host link
-    if (!c.copy_stream) {
-        MW3_CUDA_TRY(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
-        MW3_CUDA_TRY(cudaEventCreateWithFlags(&c.copy_event, cudaEventDisableTiming));
-    }
-    MW3_CUDA_TRY(cudaEventRecord(c.copy_event, c.stream));               // after the queued work
-    MW3_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.copy_event, 0));
-    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, psi_km1, sizeof(double) * c.NT, cudaMemcpyHostToDevice,
-                                 c.copy_stream));
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, psi_km1, sizeof(double) * c.NT, cudaMemcpyHostToDevice, c.stream));
     MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pk, psi_k, sizeof(double) * c.NT, cudaMemcpyHostToDevice, c.stream));
-    MW3_CUDA_TRY(cudaEventRecord(c.copy_event, c.copy_stream));
-    MW3_CUDA_TRY(cudaStreamWaitEvent(c.stream, c.copy_event, 0));
     scatter(c, c.d_pk, 0, c.G);
     if (!c.started) {
         rc = reset_accumulators(c);
@@ -908,25 +898,8 @@ int mw3_download_state_all(mw3_ctx *h, double *km1, double *k, int64_t *it)
     if (!h) return MW3_ERR_ARG;
     Ctx &c = h->c;
     if (!c.started) return MW3_ERR_STATE;
-    // each vector in two halves on two streams, so two copy engines share the host link
-    if (!c.copy_stream) {
-        MW3_CUDA_TRY(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
-        MW3_CUDA_TRY(cudaEventCreateWithFlags(&c.copy_event, cudaEventDisableTiming));
-    }
-    MW3_CUDA_TRY(cudaEventRecord(c.copy_event, c.stream));
-    MW3_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.copy_event, 0));
-    const size_t h1 = (size_t)c.NT / 2, h2 = (size_t)c.NT - h1;
-    if (km1) {
-        MW3_CUDA_TRY(cudaMemcpyAsync(km1, c.d_pkm1, sizeof(double) * h1, cudaMemcpyDeviceToHost, c.stream));
-        MW3_CUDA_TRY(cudaMemcpyAsync(km1 + h1, c.d_pkm1 + h1, sizeof(double) * h2, cudaMemcpyDeviceToHost,
-                                     c.copy_stream));
-    }
-    if (k) {
-        MW3_CUDA_TRY(cudaMemcpyAsync(k, c.d_pk, sizeof(double) * h1, cudaMemcpyDeviceToHost, c.stream));
-        MW3_CUDA_TRY(cudaMemcpyAsync(k + h1, c.d_pk + h1, sizeof(double) * h2, cudaMemcpyDeviceToHost,
-                                     c.copy_stream));
-    }
-    MW3_CUDA_TRY(cudaStreamSynchronize(c.copy_stream));
+    if (km1) MW3_CUDA_TRY(cudaMemcpyAsync(km1, c.d_pkm1, sizeof(double) * c.NT, cudaMemcpyDeviceToHost, c.stream));
+    if (k) MW3_CUDA_TRY(cudaMemcpyAsync(k, c.d_pk, sizeof(double) * c.NT, cudaMemcpyDeviceToHost, c.stream));
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
     if (it) *it = c.it;
     return check_device_flags(c, "mw3_download_state_all");
@@ -1078,10 +1051,7 @@ int mw3_destroy(mw3_ctx *h)
     Ctx &c = h->c;
     if (c.stream) cudaStreamSynchronize(c.stream);
     for (cudaEvent_t e : c.prof_ev) cudaEventDestroy(e);
-    if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
     free_device(c);
-    if (c.copy_event) cudaEventDestroy(c.copy_event);
-    if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete h;
     return MW3_OK;

@@ -106,8 +106,6 @@ struct Ctx {
     bool fp64;
     std::string err;
     cudaStream_t stream = nullptr;
-    cudaStream_t copy_stream = nullptr;  // second stream for whole-state copies (created on first use)
-    cudaEvent_t copy_event = nullptr;
     int64_t launches = 0;
     bool started = false;
     int64_t it = 0;                  // Chebyshev index of psi_k (all waves advance together)
