@@ -175,19 +175,6 @@ __device__ __forceinline__ bool d2_wait(uint64_t *mbar, uint32_t parity, volatil
     }
 }
 
-// a whole warp waits: lane 0 polls the barrier, the others learn the outcome at
-// the warp barrier (which also orders their later accesses after lane 0's
-// observation of the phase), so a waiting warp costs one shared-memory poll per
-// test instead of 32
-__device__ __forceinline__ bool d2_wait_warp(uint64_t *mbar, uint32_t parity, volatile int *fail)
-{
-    const int lane = threadIdx.x & 31;
-    int ok = 1;
-    if (lane == 0) ok = d2_wait(mbar, parity, fail) ? 1 : 0;
-    __syncwarp();
-    return __shfl_sync(0xffffffffu, ok, 0) != 0;
-}
-
 // the chunk sequence of one slab: product gi in 0..3, parity half par (products
 // along R) and K chunk jc; f(t, gi, par, jc) is called for t = 0, 1, ...  The
 // first product alternates the parities per K chunk, so both of its chunks use
@@ -347,16 +334,16 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
             unsigned char *big = sm + s * D2_STAGE, *small = big + D2_BIGMAX;
             if (jc == 0 && par == 0 && gi > 0) {
                 // this product reads the previous one from tensor memory: its last chunk done
-                d2_wait_warp(&empty[(t - 1) & (D2_NS - 1)], ((t - 1) >> 2) & 1, fail);
+                d2_wait(&empty[(t - 1) & (D2_NS - 1)], ((t - 1) >> 2) & 1, fail);
                 fence_after_sync();
             }
-            if (t >= D2_NS) d2_wait_warp(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
+            if (t >= D2_NS) d2_wait(&empty[s], (u - 1) & 1, fail);   // the MMAs of chunk t - NS read this stage
             const int k0 = jc * D2_KC;
             if (gi == 0) {
                 // B = Xs columns of this parity (rows r1) into the small slot, from the X
                 // tile the copy warp placed behind the S2 chunk (the first product takes the
                 // first uses of every stage, so u counts this barrier's phases too)
-                d2_wait_warp(&xfull[s], u & 1, fail);
+                d2_wait(&xfull[s], u & 1, fail);
                 d2_x_fill(big + D2_SMALL, small, par, nn);
             } else if (gi == 1) {
                 // A = D1 rows R into the big slot from 8 of the E and O columns of lane i
@@ -436,7 +423,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
                 if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
             }
         }
-        d2_wait_warp(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
+        d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
         if (!*fail && p.rline) {
             // every R line is one run of points with consecutive r1: the index is the
