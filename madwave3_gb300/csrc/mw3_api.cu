@@ -404,15 +404,30 @@ int build_device(Ctx &c)
         fdptr.push_back((int)fdidx.size());
         c.NF = (int)nf;
         // the stored points run along r1 for each R (ir2 outer, ir1 inner), so a flux
-        // line's derivative terms are normally one run of consecutive points and r1
-        // MW3_GENERAL_TABLES=1 keeps the general (indexed) form, so tests can compare both
-        c.fl_regular = !mw3::general_tables();
-        for (int64_t f = 0; f < nf && c.fl_regular; f++)
-            for (int q = fdptr[f]; q < fdptr[f + 1]; q++)
-                if (fdidx[q] != fdidx[fdptr[f]] + (q - fdptr[f]) || fdir1[q] != fdir1[fdptr[f]] + (q - fdptr[f])) {
-                    c.fl_regular = false;
-                    break;
+        // line's derivative terms are a few runs of consecutive points and r1 (one per
+        // valley the potential cut leaves); the mixed path reads runs when they are long
+        // enough.  MW3_GENERAL_TABLES=1 keeps the indexed form, so tests can compare both.
+        std::vector<int> frptr;
+        std::vector<int4> fruns;
+        for (int64_t f = 0; f < nf; f++) {
+            frptr.push_back((int)fruns.size());
+            for (int q = fdptr[f]; q < fdptr[f + 1]; q++) {
+                if (q > fdptr[f] && fdidx[q] == fdidx[q - 1] + 1 && fdir1[q] == fdir1[q - 1] + 1) {
+                    fruns.back().w++;
+                } else {
+                    const unsigned long long i = (unsigned long long)fdidx[q];
+                    fruns.push_back(make_int4((int)(unsigned)(i & 0xFFFFFFFFull), (int)(unsigned)(i >> 32), fdir1[q], 1));
                 }
+            }
+        }
+        frptr.push_back((int)fruns.size());
+        c.fl_runs = !c.fp64 && !mw3::general_tables() && !fruns.empty() && fdidx.size() >= 8 * fruns.size();
+        c.d_fl_rptr = nullptr;
+        c.d_fl_runs = nullptr;
+        if (c.fl_runs) {
+            TRY(dupload(c, &c.d_fl_rptr, frptr));
+            TRY(dupload(c, &c.d_fl_runs, fruns));
+        }
         TRY(dupload(c, &c.d_fl_idx, fidx));
         TRY(dupload(c, &c.d_fl_poti, fpoti));
         TRY(dupload(c, &c.d_fl_dptr, fdptr));

@@ -128,8 +128,8 @@ struct Ctx {
     double *d_vvv = nullptr;
     int *d_map = nullptr;            // [na][n1][n2] local point index, -1 = not stored
     int *d_mapT = nullptr;           // [na][n2][n1] the same, r1 fastest (stored points are r1-major runs)
-    int2 *d_rline = nullptr;         // [na][n2]: (first index - first r1, first r1 | last r1 << 16) of each R line
-    bool rline_regular = false;      // every (angle, R) line is one run of points with consecutive r1
+    int2 *d_rline = nullptr;         // [na][n2][4] runs of each R line: (first index - first r1, first r1 | last r1 << 16)
+    bool rline_regular = false;      // every (angle, R) line is at most 4 runs of points with consecutive r1
     // block tables
     int *d_blk_wave = nullptr, *d_blk_elec = nullptr, *d_blk_om = nullptr;
     int64_t *d_foff = nullptr;       // [G][na] context-wide flat start of (block, angle)
@@ -193,7 +193,11 @@ struct Ctx {
     // into zCR/zCdR every kFluxRing iterations and before every read
     float *d_fring = nullptr;        // [kFluxRing][NF][3]
     float *d_zar32 = nullptr;        // the r1 derivative row at the flux line, FP32 (mixed path)
-    bool fl_regular = false;         // every flux line's terms are consecutive points with consecutive r1
+    // mixed path: each flux line's derivative terms as runs of consecutive points with
+    // consecutive r1 (CSR: fl_rptr[f]..fl_rptr[f+1]), when the runs are long enough
+    int *d_fl_rptr = nullptr;
+    int4 *d_fl_runs = nullptr;       // (flat index lo, flat index hi, first r1, length)
+    bool fl_runs = false;
     float *d_cring = nullptr;        // [kFluxRing][netot][2]
     int fring_n = 0;                 // slots filled since the last flush
     // mixed path: the Cvj projection in FP32 (from the FP32 copy of psi) and Cvj of up

@@ -692,25 +692,29 @@ __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ p
                                                     const int *__restrict__ dir1, const double *__restrict__ zar,
                                                     int NF, double *__restrict__ fpsi, float *__restrict__ fring,
                                                     const float *__restrict__ psi32, const float *__restrict__ zar32,
-                                                    int regular)
+                                                    const int *__restrict__ rptr, const int4 *__restrict__ runs)
 {
     int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (f >= NF) return;
     if (fring) {
         // mixed path: FP32 products and sums (the ring holds FP32 anyway) from the FP32
-        // copy of psi; a regular line (one run of points and of r1) needs no per-term index
+        // copy of psi; with runs (consecutive points and r1) no per-term index is read.
+        // Either way lane l takes the line's terms l, l + 32, ... in order.
         float sr = 0.f, si = 0.f;
         const int q0 = dptr[f], q1 = dptr[f + 1];
-        if (regular) {
-            if (q1 > q0) {
-                const float *p = psi32 + didx[q0];
-                const int r0 = dir1[q0];
-                for (int q = lane; q < q1 - q0; q += 32) {
-                    const float v = p[q];
-                    sr = fmaf(zar32[2 * (r0 + q)], v, sr);
-                    si = fmaf(zar32[2 * (r0 + q) + 1], v, si);
+        if (runs) {
+            int qs = 0;                                     // the run's first term within the line
+            for (int r = rptr[f]; r < rptr[f + 1]; r++) {
+                const int4 rn = runs[r];
+                const int64_t st = (int64_t)(((unsigned long long)(unsigned)rn.y << 32) | (unsigned)rn.x);
+                for (int q = qs + ((lane - qs) & 31); q < qs + rn.w; q += 32) {
+                    const float v = psi32[st + (q - qs)];
+                    const int ir1 = rn.z + (q - qs);
+                    sr = fmaf(zar32[2 * ir1], v, sr);
+                    si = fmaf(zar32[2 * ir1 + 1], v, si);
                 }
+                qs += rn.w;
             }
         } else {
             for (int q = q0 + lane; q < q1; q += 32) {
@@ -1417,7 +1421,8 @@ void launch_accumulators(Ctx &c, int64_t it)
     if (c.NF > 0 && !(gate && c.waves[0].iprod == 1)) {
         k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(
             c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx, c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi,
-            ring ? c.d_fring + (size_t)c.fring_n * c.NF * 3 : nullptr, c.d_pk32, c.d_zar32, c.fl_regular ? 1 : 0);
+            ring ? c.d_fring + (size_t)c.fring_n * c.NF * 3 : nullptr, c.d_pk32, c.d_zar32,
+            c.fl_runs ? c.d_fl_rptr : nullptr, c.fl_runs ? c.d_fl_runs : nullptr);
         LAUNCH_CHECK(c);
         if (ring) {
             if (++c.fring_n == kFluxRing) flush_flux(c);

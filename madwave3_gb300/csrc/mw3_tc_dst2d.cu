@@ -53,6 +53,9 @@ constexpr uint32_t D2_STAGE = D2_BIGMAX + D2_SMALL;     // 48 KB
 constexpr uint32_t D2_BYTES = D2_NS * D2_STAGE;         // 192 KB
 constexpr int D2_NKH = 128 / D2_KC;                     // K chunks of a 128-wide operand
 constexpr size_t D2_CHUNK = D2_SMALL / 4;               // floats of one 128-row chunk (hi + lo)
+// stored points of one (angle, R) line: up to D2_RUNS runs of consecutive points
+// with consecutive r1 (the potential cut leaves a reactant and a product valley)
+constexpr int D2_RUNS = 4;
 
 struct Dst2Args {
     const float *X;               // rectangle [G][na][n1][n2]
@@ -66,7 +69,7 @@ struct Dst2Args {
     const int *mapT;              // [na][n2][n1]
     const int64_t *foff;
     const int *blk_wave;
-    const int2 *rline;            // [na][n2] regular R lines, or null (then mapT)
+    const int2 *rline;            // [na][n2][D2_RUNS] runs of the R lines, or null (then mapT)
     int na, n1, n2, seg0;
     int *err;
 };
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
     uint64_t *xfull = empty + D2_NS;                    // the X tile of a first-product chunk landed
     uint32_t *slot = reinterpret_cast<uint32_t *>(xfull + D2_NS);
     float *s_p1f = reinterpret_cast<float *>(sm + D2_BYTES + 128);   // the slab's r1 momenta
-    int2 *s_rl = reinterpret_cast<int2 *>(sm + D2_BYTES + 1024);      // the angle's R lines (regular case)
+    int2 *s_rl = reinterpret_cast<int2 *>(sm + D2_BYTES + 1024);      // the angle's R-line runs
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int na = p.na, n1 = p.n1, n2 = p.n2;
@@ -317,7 +320,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
             const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
             if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
             if (p.rline)
-                for (int i = threadIdx.x; i < n2; i += D2_FILL * 32) s_rl[i] = p.rline[(size_t)a * n2 + i];
+                for (int i = threadIdx.x; i < n2 * D2_RUNS; i += D2_FILL * 32)
+                    s_rl[i] = p.rline[(size_t)a * n2 * D2_RUNS + i];
             asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
         }
         // second and third products: sub & 1 picks the row set, sub >> 1 the 8-column half
@@ -426,8 +430,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
         d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
         if (!*fail && p.rline) {
-            // every R line is one run of points with consecutive r1: the index is the
-            // line's base + r1, and a warp (consecutive r1) writes consecutive points
+            // every R line is a few runs of points with consecutive r1: the index is the
+            // run's base + r1, and a warp (consecutive r1) writes consecutive points
             float *Hs = p.H + p.foff[seg];
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
@@ -439,12 +443,22 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
                 for (int uu = 0; uu < 16; uu++) {
                     const int i = i0 + uu;
                     if (i < h) {
-                        const int2 l = s_rl[i];
-                        if (m < nn && m >= (l.y & 0xFFFF) && m <= (l.y >> 16)) Hs[l.x + m] = e[uu] + o[uu];
+                        int at = -1;
+#pragma unroll
+                        for (int q = 0; q < D2_RUNS; q++) {
+                            const int2 l = s_rl[i * D2_RUNS + q];
+                            if (m >= (l.y & 0xFFFF) && m <= (l.y >> 16)) at = l.x + m;
+                        }
+                        if (m < nn && at >= 0) Hs[at] = e[uu] + o[uu];
                     }
                     if (i < n2 - h) {
-                        const int2 l = s_rl[n2 - 1 - i];
-                        if (m < nn && m >= (l.y & 0xFFFF) && m <= (l.y >> 16)) Hs[l.x + m] = e[uu] - o[uu];
+                        int at = -1;
+#pragma unroll
+                        for (int q = 0; q < D2_RUNS; q++) {
+                            const int2 l = s_rl[(n2 - 1 - i) * D2_RUNS + q];
+                            if (m >= (l.y & 0xFFFF) && m <= (l.y >> 16)) at = l.x + m;
+                        }
+                        if (m < nn && at >= 0) Hs[at] = e[uu] - o[uu];
                     }
                 }
             }
@@ -596,28 +610,29 @@ int build_tc_dst2d(Ctx &c)
     if ((rc = upload_vec(c, &c.d_dst_s1off, s1off))) return rc;
     if ((rc = upload_vec(c, &c.d_p2r1f, p1f))) return rc;
     if ((rc = upload_vec(c, &c.d_p2r2f, p2f))) return rc;
-    // R lines: the stored points are written ir2 outer, ir1 inner, so normally each
-    // (angle, R) line is one run of points with consecutive r1; then the kernel finds
-    // a point's index as base + r1 instead of reading the map
+    // R lines: the stored points are written ir2 outer, ir1 inner, so each (angle, R)
+    // line is a few runs of consecutive points with consecutive r1 (one per valley
+    // the potential cut leaves); with at most D2_RUNS runs per line the kernel finds a
+    // point's index as run base + r1 instead of reading the map
     {
-        std::vector<int2> rl((size_t)na * c.n2);
+        std::vector<int2> rl((size_t)na * c.n2 * tc::D2_RUNS, make_int2(0, 1));   // empty run: lo 1 > hi 0
         bool regular = c.n1 < 32768 && !general_tables();
         for (int a = 0; a < na && regular; a++) {
-            std::vector<int> first(c.n2, -1), lo(c.n2, 0), hi(c.n2, -1);
+            std::vector<int> nrun(c.n2, 0), last_ir(c.n2, -2), last_r1(c.n2, -2);
             for (int ir = 0; ir < c.npunreal[a] && regular; ir++) {
                 int r1 = c.indr1[(size_t)a * c.npt + ir] - 1, r2 = c.indr2[(size_t)a * c.npt + ir] - 1;
-                if (first[r2] < 0) {
-                    first[r2] = ir;
-                    lo[r2] = hi[r2] = r1;
-                } else if (r1 == hi[r2] + 1 && ir == first[r2] + (r1 - lo[r2])) {
-                    hi[r2] = r1;
+                int2 *run = &rl[((size_t)a * c.n2 + r2) * tc::D2_RUNS];
+                if (nrun[r2] > 0 && ir == last_ir[r2] + 1 && r1 == last_r1[r2] + 1) {
+                    int2 &q = run[nrun[r2] - 1];
+                    q.y = (q.y & 0xFFFF) | (r1 << 16);                    // extend the run
+                } else if (nrun[r2] < tc::D2_RUNS && r1 > last_r1[r2]) {
+                    run[nrun[r2]++] = make_int2(ir - r1, r1 | (r1 << 16));   // a new run
                 } else {
                     regular = false;
                 }
+                last_ir[r2] = ir;
+                last_r1[r2] = r1;
             }
-            for (int r2 = 0; r2 < c.n2; r2++)
-                rl[(size_t)a * c.n2 + r2] = first[r2] < 0 ? make_int2(0, 1)      // empty: lo 1 > hi 0
-                                                          : make_int2(first[r2] - lo[r2], lo[r2] | (hi[r2] << 16));
         }
         c.rline_regular = regular;
         if (regular && (rc = upload_vec(c, &c.d_rline, rl))) return rc;
@@ -656,7 +671,8 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    const size_t smem = D2_BYTES + 1024 + 1024 + 2048;  // stages, barriers and momenta, R lines, alignment slack
+    // stages, barriers and momenta, R-line runs, alignment slack
+    const size_t smem = D2_BYTES + 1024 + 1024 + (size_t)256 * D2_RUNS * sizeof(int2);
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;

@@ -101,10 +101,10 @@ def test_mixed_accumulators_track_fp64(runs, case):
 
 @pytest.mark.parametrize("case", ["tiny_j0", "tiny_e2"])
 def test_regular_lines_match_general_tables(runs, case, monkeypatch):
-    """When every (angle, R) line of stored points is one run with consecutive r1,
-    the fused DST writes H through line bases and the flux derivative reads its
-    runs without indices; MW3_GENERAL_TABLES=1 keeps the indexed form.  Both give
-    the same bits."""
+    """When the (angle, R) lines of stored points are a few runs with consecutive
+    r1, the fused DST writes H through run bases and the flux derivative reads the
+    runs without per-term indices; MW3_GENERAL_TABLES=1 keeps the indexed forms.
+    Both give the same bits."""
     from madwave3_gb300 import Propagator
 
     run = runs[case]
