@@ -128,8 +128,6 @@ struct Ctx {
     double *d_vvv = nullptr;
     int *d_map = nullptr;            // [na][n1][n2] local point index, -1 = not stored
     int *d_mapT = nullptr;           // [na][n2][n1] the same, r1 fastest (stored points are r1-major runs)
-    int2 *d_rline = nullptr;         // [na][n2][4] runs of each R line: (first index - first r1, first r1 | last r1 << 16)
-    bool rline_regular = false;      // every (angle, R) line is at most 4 runs of points with consecutive r1
     // block tables
     int *d_blk_wave = nullptr, *d_blk_elec = nullptr, *d_blk_om = nullptr;
     int64_t *d_foff = nullptr;       // [G][na] context-wide flat start of (block, angle)

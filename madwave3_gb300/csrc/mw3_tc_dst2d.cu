@@ -53,9 +53,6 @@ constexpr uint32_t D2_STAGE = D2_BIGMAX + D2_SMALL;     // 48 KB
 constexpr uint32_t D2_BYTES = D2_NS * D2_STAGE;         // 192 KB
 constexpr int D2_NKH = 128 / D2_KC;                     // K chunks of a 128-wide operand
 constexpr size_t D2_CHUNK = D2_SMALL / 4;               // floats of one 128-row chunk (hi + lo)
-// stored points of one (angle, R) line: up to D2_RUNS runs of consecutive points
-// with consecutive r1 (the potential cut leaves a reactant and a product valley)
-constexpr int D2_RUNS = 4;
 
 struct Dst2Args {
     const float *X;               // rectangle [G][na][n1][n2]
@@ -69,7 +66,6 @@ struct Dst2Args {
     const int *mapT;              // [na][n2][n1]
     const int64_t *foff;
     const int *blk_wave;
-    const int2 *rline;            // [na][n2][D2_RUNS] runs of the R lines, or null (then mapT)
     int na, n1, n2, seg0;
     int *err;
 };
@@ -203,7 +199,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
     uint64_t *xfull = empty + D2_NS;                    // the X tile of a first-product chunk landed
     uint32_t *slot = reinterpret_cast<uint32_t *>(xfull + D2_NS);
     float *s_p1f = reinterpret_cast<float *>(sm + D2_BYTES + 128);   // the slab's r1 momenta
-    int2 *s_rl = reinterpret_cast<int2 *>(sm + D2_BYTES + 1024);      // the angle's R-line runs
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int na = p.na, n1 = p.n1, n2 = p.n2;
@@ -319,9 +314,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
             // the r1 momenta of the slab into shared memory (read 8 at a time by the third product)
             const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
             if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
-            if (p.rline)
-                for (int i = threadIdx.x; i < n2 * D2_RUNS; i += D2_FILL * 32)
-                    s_rl[i] = p.rline[(size_t)a * n2 * D2_RUNS + i];
             asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
         }
         // second and third products: sub & 1 picks the row set, sub >> 1 the 8-column half
@@ -418,7 +410,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
         });
         // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
         const int *mT = p.mapT + (size_t)a * n2 * n1;
-        if (m < nn && !p.rline) {
+        if (m < nn) {
             // the map entries this thread reads, into L1 while the last MMAs run
 #pragma unroll 4
             for (int uu = 0; uu < 32; uu++) {
@@ -429,40 +421,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
         }
         d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
-        if (!*fail && p.rline) {
-            // every R line is a few runs of points with consecutive r1: the index is the
-            // run's base + r1, and a warp (consecutive r1) writes consecutive points
-            float *Hs = p.H + p.foff[seg];
-#pragma unroll
-            for (int cc = 0; cc < 2; cc++) {
-                const int i0 = 32 * sub + 16 * cc;
-                float e[16], o[16];
-                tmem_ld16(lrow + 256u + (uint32_t)i0, e);
-                tmem_ld16(lrow + 384u + (uint32_t)i0, o);
-#pragma unroll
-                for (int uu = 0; uu < 16; uu++) {
-                    const int i = i0 + uu;
-                    if (i < h) {
-                        int at = -1;
-#pragma unroll
-                        for (int q = 0; q < D2_RUNS; q++) {
-                            const int2 l = s_rl[i * D2_RUNS + q];
-                            if (m >= (l.y & 0xFFFF) && m <= (l.y >> 16)) at = l.x + m;
-                        }
-                        if (m < nn && at >= 0) Hs[at] = e[uu] + o[uu];
-                    }
-                    if (i < n2 - h) {
-                        int at = -1;
-#pragma unroll
-                        for (int q = 0; q < D2_RUNS; q++) {
-                            const int2 l = s_rl[(n2 - 1 - i) * D2_RUNS + q];
-                            if (m >= (l.y & 0xFFFF) && m <= (l.y >> 16)) at = l.x + m;
-                        }
-                        if (m < nn && at >= 0) Hs[at] = e[uu] - o[uu];
-                    }
-                }
-            }
-        } else if (!*fail) {
+        if (!*fail) {
             const int64_t fo = p.foff[seg];
 #pragma unroll
             for (int cc = 0; cc < 2; cc++) {
@@ -610,33 +569,6 @@ int build_tc_dst2d(Ctx &c)
     if ((rc = upload_vec(c, &c.d_dst_s1off, s1off))) return rc;
     if ((rc = upload_vec(c, &c.d_p2r1f, p1f))) return rc;
     if ((rc = upload_vec(c, &c.d_p2r2f, p2f))) return rc;
-    // R lines: the stored points are written ir2 outer, ir1 inner, so each (angle, R)
-    // line is a few runs of consecutive points with consecutive r1 (one per valley
-    // the potential cut leaves); with at most D2_RUNS runs per line the kernel finds a
-    // point's index as run base + r1 instead of reading the map
-    {
-        std::vector<int2> rl((size_t)na * c.n2 * tc::D2_RUNS, make_int2(0, 1));   // empty run: lo 1 > hi 0
-        bool regular = c.n1 < 32768 && !general_tables();
-        for (int a = 0; a < na && regular; a++) {
-            std::vector<int> nrun(c.n2, 0), last_ir(c.n2, -2), last_r1(c.n2, -2);
-            for (int ir = 0; ir < c.npunreal[a] && regular; ir++) {
-                int r1 = c.indr1[(size_t)a * c.npt + ir] - 1, r2 = c.indr2[(size_t)a * c.npt + ir] - 1;
-                int2 *run = &rl[((size_t)a * c.n2 + r2) * tc::D2_RUNS];
-                if (nrun[r2] > 0 && ir == last_ir[r2] + 1 && r1 == last_r1[r2] + 1) {
-                    int2 &q = run[nrun[r2] - 1];
-                    q.y = (q.y & 0xFFFF) | (r1 << 16);                    // extend the run
-                } else if (nrun[r2] < tc::D2_RUNS && r1 > last_r1[r2]) {
-                    run[nrun[r2]++] = make_int2(ir - r1, r1 | (r1 << 16));   // a new run
-                } else {
-                    regular = false;
-                }
-                last_ir[r2] = ir;
-                last_r1[r2] = r1;
-            }
-        }
-        c.rline_regular = regular;
-        if (regular && (rc = upload_vec(c, &c.d_rline, rl))) return rc;
-    }
     c.use_tc_dst2d = true;
     return MW3_OK;
 }
@@ -671,8 +603,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    // stages, barriers and momenta, R-line runs, alignment slack
-    const size_t smem = D2_BYTES + 1024 + 1024 + (size_t)256 * D2_RUNS * sizeof(int2);
+    const size_t smem = D2_BYTES + 1024 + 1024;         // stages, barriers and momenta, alignment slack
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
@@ -684,7 +615,6 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.s2fold = c.d_dst_s2fold; p.s1planes = c.d_dst_planes; p.s1off = c.d_dst_s1off; p.nopr1 = c.d_nopr1;
     p.p2r1f = c.d_p2r1f; p.p2r2f = c.d_p2r2f; p.radcut = (float)c.grid.radcutmax;
     p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
-    p.rline = c.rline_regular ? c.d_rline : nullptr;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
     p.err = c.d_tc_err;
     CUtensorMap xmap;

@@ -101,10 +101,9 @@ def test_mixed_accumulators_track_fp64(runs, case):
 
 @pytest.mark.parametrize("case", ["tiny_j0", "tiny_e2"])
 def test_regular_lines_match_general_tables(runs, case, monkeypatch):
-    """When the (angle, R) lines of stored points are a few runs with consecutive
-    r1, the fused DST writes H through run bases and the flux derivative reads the
-    runs without per-term indices; MW3_GENERAL_TABLES=1 keeps the indexed forms.
-    Both give the same bits."""
+    """When the flux lines' derivative terms are runs of consecutive points with
+    consecutive r1, the mixed flux derivative reads the runs without per-term
+    indices; MW3_GENERAL_TABLES=1 keeps the indexed form.  Both give the same bits."""
     from madwave3_gb300 import Propagator
 
     run = runs[case]
