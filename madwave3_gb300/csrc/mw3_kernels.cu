@@ -455,13 +455,8 @@ __device__ __forceinline__ void upd_fe(const UpdArgs &u, double *zf, int w, int6
 // numbers of stored points, so a full segment x chunk grid is a third empty); the
 // pair's descriptor carries the table entries, so every thread starts its point
 // loads after one independent 48-byte load
-// threads per CTA: the mixed path takes eight points per thread (more loads in flight
-// per thread for the same registers per point), the FP64 path four
-template <typename T> __host__ __device__ constexpr int upd_threads() { return sizeof(T) == 4 ? 128 : 256; }
-
 template <typename T, typename HT>
-__global__ void __launch_bounds__(sizeof(T) == 4 ? 128 : 256, sizeof(T) == 4 ? 5 : 3)
-    k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid d, UpdArgs u, T *__restrict__ X)
 {
     const UpdChunk cd = u.desc[blockIdx.x];
     const int seg = cd.seg, chunk = cd.chunk_ns & 255, nsrc = cd.chunk_ns >> 8;
@@ -503,8 +498,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 128 : 256, sizeof(T) == 4 ? 5
     double nrm = 0.0;
     double *zf = (u.nofe > 0 && !u.first) ? u.zfe[w] : nullptr;
     int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
-    constexpr int NTH = upd_threads<T>();
-    constexpr int U = kPointChunk / NTH;        // points per thread, loads issued together
+    constexpr int U = kPointChunk / 256;        // points per thread, loads issued together
     const int ir0 = chunk * kPointChunk + threadIdx.x;
     float nrmf = 0.f;
     if constexpr (sizeof(T) == 8) {
@@ -512,7 +506,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 128 : 256, sizeof(T) == 4 ? 5
         double hv[U], pk[U], p1[U];
 #pragma unroll
         for (int k = 0; k < U; k++) {
-            int ir = ir0 + k * NTH;
+            int ir = ir0 + k * 256;
             bool on = ir < n;
             r1[k] = on ? i1p[ir] - 1 : 0;
             r2[k] = on ? i2p[ir] - 1 : 0;
@@ -524,13 +518,13 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 128 : 256, sizeof(T) == 4 ? 5
             const double *vr = d.vvv + (q == 0 ? cd.voff : s_voff[q]), *pr = u.pk + (q == 0 ? cd.poff : s_poff[q]);
 #pragma unroll
             for (int k = 0; k < U; k++) {
-                int ir = ir0 + k * NTH;
+                int ir = ir0 + k * 256;
                 if (ir < n) hv[k] += pr[ir] * vr[ir];
             }
         }
 #pragma unroll
         for (int k = 0; k < U; k++) {
-            int ir = ir0 + k * NTH;
+            int ir = ir0 + k * 256;
             if (ir >= n) continue;
             // FP64 path: the reference's operations in its order
             double nv;
@@ -565,7 +559,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 128 : 256, sizeof(T) == 4 ? 5
         double p1[U];
 #pragma unroll
         for (int k = 0; k < U; k++) {
-            int ir = ir0 + k * NTH;
+            int ir = ir0 + k * 256;
             bool on = ir < n;
             r1[k] = on ? i1p[ir] - 1 : 0;
             r2[k] = on ? i2p[ir] - 1 : 0;
@@ -576,7 +570,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 128 : 256, sizeof(T) == 4 ? 5
         }
 #pragma unroll
         for (int k = 0; k < U; k++) {
-            int ir = ir0 + k * NTH;
+            int ir = ir0 + k * 256;
             if (ir >= n) continue;
             float acc = v0[k] * q0[k];
             for (int q = 1; q < nsrc; q++) acc = fmaf(u.vr32[s_voff[q] + ir], u.pk32[s_poff[q] + ir], acc);
@@ -1324,9 +1318,9 @@ void launch_update(Ctx &c, int first)
     stage_mark(c, 5);
     if (c.h32) {
         u.H = c.d_h32;
-        k_update<T, float><<<c.n_upd_chunks, upd_threads<T>(), 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+        k_update<T, float><<<c.n_upd_chunks, 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
     } else {
-        k_update<T, double><<<c.n_upd_chunks, upd_threads<T>(), 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
+        k_update<T, double><<<c.n_upd_chunks, 256, 0, c.stream>>>(devgrid(c), u, (T *)c.d_X);
     }
     LAUNCH_CHECK(c);
 }
