@@ -67,7 +67,6 @@ struct Dst2Args {
     const int64_t *foff;
     const int *blk_wave;
     int na, n1, n2, seg0;
-    int seg_end;                  // one past the last segment of this launch
     int *err;
 };
 
@@ -234,20 +233,6 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
     int copies = 0;                                     // copies issued (copy warp, lane 0)
 
     if (warp == D2_COPY_WARP) {
-        // the slab that starts on an SM after this one is, in launch order, about one
-        // SM count further on: lanes 1-31 bring its X rows (128 rows of 128-byte
-        // pieces) into L2, so its first tensor copies do not wait on DRAM
-        if (lane > 0) {
-            int nsm;
-            asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
-            const int nxt = seg + nsm;
-            if (nxt < p.seg_end) {
-                const char *xr = reinterpret_cast<const char *>(p.X + (size_t)nxt * n1 * n2);
-                const int pieces = (n2 * 4 + 127) / 128, rows = n1 < 128 ? n1 : 128;
-                for (int e = lane - 1; e < rows * pieces; e += 31)
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(xr + (size_t)(e / pieces) * n2 * 4 + (e % pieces) * 128));
-            }
-        }
         // ---- bulk copies of the DST-matrix operands ----
         if (lane == 0)
             d2_for_chunks(nkh, nkr, [&](int t, int gi, int par, int jc) {
@@ -630,7 +615,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.s2fold = c.d_dst_s2fold; p.s1planes = c.d_dst_planes; p.s1off = c.d_dst_s1off; p.nopr1 = c.d_nopr1;
     p.p2r1f = c.d_p2r1f; p.p2r2f = c.d_p2r2f; p.radcut = (float)c.grid.radcutmax;
     p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
-    p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na; p.seg_end = g_end * c.na;
+    p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
     p.err = c.d_tc_err;
     CUtensorMap xmap;
     std::memcpy(&xmap, c.dst_xmap, sizeof(xmap));
