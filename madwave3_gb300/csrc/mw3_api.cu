@@ -17,7 +17,6 @@ using mw3::WaveTables;
 
 namespace {
 
-constexpr int kAngCW = 64;   // column chunk of the angular kernels (must match mw3_kernels.cu)
 
 template <typename V>
 int dupload(Ctx &c, V **dst, const V *src, size_t n)
@@ -296,6 +295,7 @@ int build_device(Ctx &c)
     TRY(dupload(c, &c.d_quirk, qlist));
     // ---- target lists of the angular kernels ----
     {
+        const int kAngCW = c.ang_cw;
         c.ncj = (n2 + kAngCW - 1) / kAngCW;
         c.ncl = (n1 + kAngCW - 1) / kAngCW;
         std::vector<std::vector<int>> bj((size_t)n1 * c.ncj), bl((size_t)n2 * c.ncl);
@@ -704,9 +704,9 @@ int mw3_create(mw3_ctx **out, const mw3_grid *g, const int32_t *npunreal, const 
     int dev = 0;
     cudaDeviceProp prop;
     if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) {
-        // the dynamic shared memory the kernels need must fit the device
-        size_t need = mw3::max_smem_needed(c);
-        if (need > prop.sharedMemPerBlockOptin) {
+        // the dynamic shared memory the kernels need must fit the device (the
+        // explicit angular kernels narrow their column chunk for large angle counts)
+        if (!mw3::fit_smem(c, prop.sharedMemPerBlockOptin)) {
             cudaStreamDestroy(c.stream);
             delete h;
             return MW3_ERR_UNSUPPORTED;

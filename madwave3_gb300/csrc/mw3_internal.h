@@ -174,6 +174,7 @@ struct Ctx {
     int *d_tl_ptr = nullptr, *d_tl = nullptr;   // per (ir2, chunk of ir1)
     int *d_quirk_ptr = nullptr, *d_quirk = nullptr;  // per (wave, angle): local points with ir1 > nopr1
     int ncj = 0, ncl = 0;
+    int ang_cw = 64;                 // column chunk of the explicit angular kernels (fit_smem)
     // scratch for mw3_hphi
     double *d_tmp = nullptr;
     int64_t tmp_cap = 0;
@@ -321,7 +322,8 @@ void launch_norms(Ctx &c, int64_t slot);
 void launch_addv(Ctx &c, const double *psi, int g0, int g1);
 void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec);
 void set_kernel_attributes(Ctx &c);
-size_t max_smem_needed(Ctx &c);
+// picks c.ang_cw so that every kernel's dynamic shared memory fits optin bytes
+bool fit_smem(Ctx &c, size_t optin);
 
 }  // namespace mw3
 

@@ -297,7 +297,8 @@ __global__ void k_quirk(DevGrid d, const double *__restrict__ psi, HT *__restric
 // ---------------------------------------------------------------------------
 // angular kinetic terms in the grid representation
 // ---------------------------------------------------------------------------
-constexpr int ANG_CW = 64;
+// the column chunk of the explicit angular kernels is c.ang_cw (64, or narrower
+// when the angle count makes the staged matrices too large for shared memory)
 
 // Target descriptors of one angular CTA: angle, column inside the chunk and
 // output index, with eight independent loads in flight per thread.
@@ -336,7 +337,7 @@ __device__ __forceinline__ void stage_targets(const DevGrid &d, const int *__res
 template <typename T>
 __global__ void __launch_bounds__(256) k_ang_j(DevGrid d, const T *__restrict__ X, const T *__restrict__ xj2,
                                                double *__restrict__ H, const int *__restrict__ tptr,
-                                               const int *__restrict__ tlist, int ncj, int g0)
+                                               const int *__restrict__ tlist, int ncj, int g0, int ANG_CW)
 {
     extern __shared__ unsigned char smraw[];
     int chunk = blockIdx.x, ir1 = blockIdx.y, g = g0 + blockIdx.z;
@@ -372,7 +373,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_ang_l(DevGrid d, const T *__restrict__ X, const T *__restrict__ xl2p,
                                                double *__restrict__ H, const int *__restrict__ tptr,
                                                const int *__restrict__ tlist, const int *__restrict__ cpl, int ncl,
-                                               int g0)
+                                               int g0, int ANG_CW)
 {
     extern __shared__ unsigned char smraw[];
     int chunk = blockIdx.x, ir2 = blockIdx.y, t = g0 + blockIdx.z;
@@ -894,14 +895,14 @@ __global__ void __launch_bounds__(256) k_cvj_proj(DevGrid d, CvjArgs c)
     int n1 = d.n1, na = d.na, nj = c.nj;
     int r1a = blockIdx.y * kCvjR1, r1b = min(n1, r1a + kCvjR1);     // this CTA's r1 chunk
     int w = d.blk_wave[g], el = d.blk_elec[g], om = d.blk_om[g];
-    double *fr = cvsm;                       // [na][n1] psi / sqrt(ah2) (chunk columns used)
-    double *dj = cvsm + (size_t)na * n1;     // [nj][na]
+    double *fr = cvsm;                       // [na][kCvjR1] psi / sqrt(ah2) of this CTA's r1 chunk
+    double *dj = cvsm + (size_t)na * kCvjR1; // [nj][na]
     const int *m = c.r2abs + (size_t)w * na * n1;
     int cw = r1b - r1a;
     for (int e = threadIdx.x; e < na * cw; e += blockDim.x) {
         int a = e / cw, ir1 = r1a + e % cw;
         int ir = m[(size_t)a * n1 + ir1];
-        fr[(size_t)a * n1 + ir1] = (ir >= 0) ? c.psi[d.foff[(size_t)g * na + a] + ir] / c.sah2 : 0.0;
+        fr[(size_t)a * kCvjR1 + (ir1 - r1a)] = (ir >= 0) ? c.psi[d.foff[(size_t)g * na + a] + ir] / c.sah2 : 0.0;
     }
     for (int e = threadIdx.x; e < nj * na; e += blockDim.x) {
         int jj = e / na, a = e % na;
@@ -916,7 +917,7 @@ __global__ void __launch_bounds__(256) k_cvj_proj(DevGrid d, CvjArgs c)
         double xj = 0.0;
         for (int ia = 0; ia < na; ia++) {
             int a = na - 1 - ia;                  // angle order of the flat vector
-            xj = xj + fr[(size_t)a * n1 + ir1] * dj[(size_t)jj * na + a];
+            xj = xj + fr[(size_t)a * kCvjR1 + (ir1 - r1a)] * dj[(size_t)jj * na + a];
         }
         c.xj[((size_t)g * n1 + ir1) * nj + jj] = xj;
     }
@@ -1203,14 +1204,14 @@ void launch_scatter(Ctx &c, const double *psi, float *psi32, int g_begin, int g_
 }
 
 static size_t col_smem(Ctx &c, size_t tsz) { return tsz * (size_t)c.n1 * (COL_W + COL_KC); }
-static size_t ang_desc(Ctx &c) { return (size_t)c.na * ANG_CW * 16 + 16; }
+static size_t ang_desc(Ctx &c) { return (size_t)c.na * c.ang_cw * 16 + 16; }
 static size_t angj_smem(Ctx &c, size_t tsz)
 {
-    return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1)) + ang_desc(c);
+    return tsz * ((size_t)c.na * c.ang_cw + (size_t)c.na * (c.na + 1)) + ang_desc(c);
 }
 static size_t angl_smem(Ctx &c, size_t tsz)
 {
-    return tsz * ((size_t)c.na * ANG_CW + (size_t)c.na * ANG_CW + (size_t)c.na * (c.na + 1)) + ang_desc(c);
+    return tsz * ((size_t)c.na * c.ang_cw + (size_t)c.na * c.ang_cw + (size_t)c.na * (c.na + 1)) + ang_desc(c);
 }
 
 template <typename T>
@@ -1276,12 +1277,12 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     } else if (c.na > 1) {
         dim3 gj(c.ncj, c.n1, ng);
         k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_xj2, c.d_h,
-                                                                    c.d_tj_ptr, c.d_tj, c.ncj, g_begin);
+                                                                    c.d_tj_ptr, c.d_tj, c.ncj, g_begin, c.ang_cw);
         LAUNCH_CHECK(c);
         stage_mark(c, 4);
         dim3 gl(c.ncl, c.n2, ng);
         k_ang_l<T><<<gl, 256, angl_smem(c, sizeof(T)), c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_xl2p, c.d_h,
-                                                                    c.d_tl_ptr, c.d_tl, c.d_cpl, c.ncl, g_begin);
+                                                                    c.d_tl_ptr, c.d_tl, c.d_cpl, c.ncl, g_begin, c.ang_cw);
         LAUNCH_CHECK(c);
     }
 }
@@ -1358,12 +1359,17 @@ void set_kernel_attributes(Ctx &c)
     cudaFuncSetAttribute(k_ang_l<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 4));
 }
 
-size_t max_smem_needed(Ctx &c)
+bool fit_smem(Ctx &c, size_t optin)
 {
-    size_t m = col_smem(c, 8);
-    if (angj_smem(c, 8) > m) m = angj_smem(c, 8);
-    if (angl_smem(c, 8) > m) m = angl_smem(c, 8);
-    return m;
+    // the widest angular column chunk whose staged matrices fit (FP64 sizes)
+    for (int cw = 64; cw >= 8; cw /= 2) {
+        c.ang_cw = cw;
+        size_t m = col_smem(c, 8);
+        if (angj_smem(c, 8) > m) m = angj_smem(c, 8);
+        if (angl_smem(c, 8) > m) m = angl_smem(c, 8);
+        if (m <= optin) return true;
+    }
+    return false;
 }
 
 // accumulators of iteration it for every wave (CoefEcheby, totalflux_k, Cvjflux_k, funE coefficients)
@@ -1445,7 +1451,7 @@ void launch_accumulators(Ctx &c, int64_t it)
         if (++c.cvring_n == kFluxRing) flush_cvj(c);
     } else if (c.n2 > 1) {
         CvjArgs a = cvj_args(c, gate);
-        size_t smp = sizeof(double) * ((size_t)c.na * c.n1 + (size_t)c.nj * c.na);
+        size_t smp = sizeof(double) * ((size_t)c.na * kCvjR1 + (size_t)c.nj * c.na);
         k_cvj_proj<<<dim3(c.G, (c.n1 + kCvjR1 - 1) / kCvjR1), 256, smp, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
         k_cvj_fd<<<(c.G * c.nj * c.nv * 32 + 255) / 256, 256, 0, c.stream>>>(d, a);
@@ -1556,11 +1562,11 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     } else if (na > 1) {
         dim3 gj(c.ncj, n1, ng);
         k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, X, (const T *)c.d_xj2, H, c.d_tj_ptr, c.d_tj,
-                                                                    c.ncj, g0);
+                                                                    c.ncj, g0, c.ang_cw);
         LAUNCH_CHECK(c);
         dim3 gl(c.ncl, n2, ng);
         k_ang_l<T><<<gl, 256, angl_smem(c, sizeof(T)), c.stream>>>(d, X, (const T *)c.d_xl2p, H, c.d_tl_ptr, c.d_tl,
-                                                                    c.d_cpl, c.ncl, g0);
+                                                                    c.d_cpl, c.ncl, g0, c.ang_cw);
         LAUNCH_CHECK(c);
     }
     k_addv<double><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, P, H, H, c.d_vsrc, g0 * na);

@@ -110,3 +110,36 @@ def test_batched_waves(runs):
         assert rel(both.totalflux(w)[0], one.totalflux()[0]) < 1e-13
         one.close()
     both.close()
+
+
+def test_wide_angle_grid_fp64_and_mixed(tmp_path):
+    """120 angles (the larger workload's angle count): the explicit angular
+    kernels narrow their column chunk to fit shared memory and the Cvj
+    projection stages one r1 chunk; FP64 H psi and the accumulators after 20
+    iterations match the oracle, and the mixed path (explicit FP32 angular
+    kernels: the tensor-core form takes at most 64 angles) tracks FP64."""
+    import os
+    from madwave3_gb300.host import generator, setup
+
+    d = str(tmp_path / "wide")
+    generator.write_case(d, npun2=24, npun1=16, nangu=120, jmax=39, nvmax=2, netot=32, npun1min=8,
+                         alpha0_bohr=1.2)
+    run = setup.load(os.path.join(d, "input.dat"))
+    prop = Propagator(run, "fp64")
+    ref = Oracle(run)
+    rng = np.random.default_rng(20261203)
+    psi = rng.uniform(-1, 1, run.ntot)
+    h64 = prop.hphi(psi)
+    assert rel(h64, ref.hphi(psi)) < 1e-12
+    prop.start()
+    ref.start(run.psi0)
+    prop.run(20)
+    ref.run_iters(20)
+    acc = prop.accumulators()
+    zs2, cvj = ref.s2()
+    assert rel(acc["cvj"], cvj) < 1e-10
+    assert rel(acc["zs2"], zs2) < 1e-10
+    prop.close()
+    pmx = Propagator(run, "mixed")
+    assert rel(pmx.hphi(psi), h64) < 1e-6
+    pmx.close()
