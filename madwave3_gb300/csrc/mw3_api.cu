@@ -62,6 +62,12 @@ int dalloc(Ctx &c, V **dst, size_t n, bool zero = true)
 
 void free_device(Ctx &c)
 {
+    for (int p = 0; p < 2; p++) {
+        if (c.graph_exec[p]) cudaGraphExecDestroy(c.graph_exec[p]);
+        c.graph_exec[p] = nullptr;
+        c.graph_launches[p] = 0;
+    }
+    c.d_itbase = nullptr;
     for (void *p : c.allocs) cudaFree(p);
     c.allocs.clear();
     c.built = false;
@@ -679,6 +685,8 @@ int mw3_create(mw3_ctx **out, const mw3_grid *g, const int32_t *npunreal, const 
     c.ne = g->nelec;
     c.npt = g->npuntot;
     c.fp64 = (g->precision == MW3_PREC_FP64);
+    const char *ng = std::getenv("MW3_NO_GRAPHS");
+    c.graphs_off = ng && ng[0] == '1';
     c.npunreal.assign(npunreal, npunreal + c.na);
     c.indr1.assign(indr1, indr1 + (size_t)c.na * c.npt);
     c.indr2.assign(indr2, indr2 + (size_t)c.na * c.npt);
@@ -824,6 +832,87 @@ int mw3_upload_state(mw3_ctx *h, int32_t w, const double *psi_km1, const double 
     return MW3_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// one Chebyshev iteration of every wave, launched on the context's stream
+void run_iteration(Ctx &c)
+{
+    int64_t it = c.it + 1;
+    hphi_all(c, c.d_pk, 0, c.G);
+    update(c, 0);
+    std::swap(c.d_pk, c.d_pkm1);
+    std::swap(c.d_pk32, c.d_pkm1_32);
+    mw3::launch_accumulators(c, it);
+    mw3::launch_norms(c, c.norm_slot);
+    if (c.prof && c.prof_n < c.prof_cap) {
+        mw3::stage_mark(c, MW3_NSTAGES);
+        c.prof_n++;
+    }
+    c.it = it;
+    c.norm_slot++;
+}
+
+// a block of kGraphIters iterations repeats exactly when the rings start empty (they
+// cycle with that period), no iteration of the block is gated (the elastic channel
+// below kminelastic changes the launches) and no stage timing is recorded
+bool graph_ready(Ctx &c, int64_t left)
+{
+    if (c.graphs_off || c.prof || left < mw3::kGraphIters) return false;
+    if (c.fring_n != 0 || c.cvring_n != 0) return false;
+    if (c.gate_elastic && c.it + 1 < c.kminelastic) return false;
+    return true;
+}
+
+// capture kGraphIters iterations starting from the current psi buffer parity; the
+// host-side state the eager launches advance is put back afterwards
+void capture_graph(Ctx &c, int par)
+{
+    if (!c.d_itbase) {
+        if (cudaMalloc((void **)&c.d_itbase, 2 * sizeof(int64_t)) != cudaSuccess) {
+            c.graphs_off = true;
+            return;
+        }
+        c.allocs.push_back(c.d_itbase);
+    }
+    const int64_t it0 = c.it, slot0 = c.norm_slot, l0 = c.launches;
+    double *pk = c.d_pk, *pkm1 = c.d_pkm1;
+    float *pk32 = c.d_pk32, *pkm1_32 = c.d_pkm1_32;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        c.graphs_off = true;
+        return;
+    }
+    c.capturing = true;
+    c.cap_it0 = it0;
+    c.cap_slot0 = slot0;
+    for (int i = 0; i < mw3::kGraphIters; i++) run_iteration(c);
+    c.capturing = false;
+    cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+    const int64_t launches = c.launches - l0;
+    c.it = it0;
+    c.norm_slot = slot0;
+    c.d_pk = pk;
+    c.d_pkm1 = pkm1;
+    c.d_pk32 = pk32;
+    c.d_pkm1_32 = pkm1_32;
+    c.launches = l0;
+    c.fring_n = c.cvring_n = 0;
+    if (e == cudaSuccess && g && cudaGraphInstantiate(&c.graph_exec[par], g, 0) == cudaSuccess) {
+        c.graph_launches[par] = launches;
+    } else {
+        c.graph_exec[par] = nullptr;
+        c.graphs_off = true;
+        cudaGetLastError();
+    }
+    if (g) cudaGraphDestroy(g);
+}
+
+}  // namespace
+
+extern "C" {
+
 int mw3_run(mw3_ctx *h, int64_t n)
 {
     if (!h || n < 0) return MW3_ERR_ARG;
@@ -841,20 +930,23 @@ int mw3_run(mw3_ctx *h, int64_t n)
         for (size_t i = old; i < c.prof_ev.size(); i++) MW3_CUDA_TRY(cudaEventCreate(&c.prof_ev[i]));
         c.prof_cap = need;
     }
-    for (int64_t s = 0; s < n; s++) {
-        int64_t it = c.it + 1;
-        hphi_all(c, c.d_pk, 0, c.G);
-        update(c, 0);
-        std::swap(c.d_pk, c.d_pkm1);
-        std::swap(c.d_pk32, c.d_pkm1_32);
-        mw3::launch_accumulators(c, it);
-        mw3::launch_norms(c, c.norm_slot);
-        if (c.prof && c.prof_n < c.prof_cap) {
-            mw3::stage_mark(c, MW3_NSTAGES);
-            c.prof_n++;
+    for (int64_t s = 0; s < n;) {
+        if (graph_ready(c, n - s)) {
+            // kGraphIters iterations as one graph replay
+            const int par = c.d_pk == c.d_psiA ? 0 : 1;
+            if (!c.graph_exec[par]) capture_graph(c, par);
+            if (c.graph_exec[par]) {
+                mw3::launch_set_itbase(c);
+                MW3_CUDA_TRY(cudaGraphLaunch(c.graph_exec[par], c.stream));
+                c.launches += c.graph_launches[par];
+                c.it += mw3::kGraphIters;
+                c.norm_slot += mw3::kGraphIters;
+                s += mw3::kGraphIters;
+                continue;
+            }
         }
-        c.it = it;
-        c.norm_slot++;
+        run_iteration(c);
+        s++;
     }
     return check_launch(c, "mw3_run");
 }

@@ -208,6 +208,15 @@ struct Ctx {
     float *d_fd32 = nullptr;         // fd in FP32
     float *d_xj32 = nullptr;         // [G][n1][nj]
     int cvring_n = 0;
+    // CUDA graphs of kGraphIters iterations, one per parity of the psi buffers: the
+    // kernels read the iteration and the norm slot as d_itbase[0/1] plus the offset
+    // captured, so one graph serves every block of iterations
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    int64_t graph_launches[2] = {0, 0};  // kernel launches one replay stands for
+    int64_t *d_itbase = nullptr;
+    bool capturing = false;
+    int64_t cap_it0 = 0, cap_slot0 = 0;
+    bool graphs_off = false;         // MW3_NO_GRAPHS=1, or a capture that failed
     double *d_zcr = nullptr, *d_zcdr = nullptr;          // [NF][netot][2]
     double *d_xj = nullptr;          // [G][n1][nj] angular projection at ir2abs
     double *d_cvj = nullptr;         // [G][nj][nv]
@@ -319,6 +328,10 @@ void flush_cvj(Ctx &c);
 void build_cvj32(Ctx &c);
 constexpr int kFluxRing = 32;
 void launch_norms(Ctx &c, int64_t slot);
+// writes the context's iteration and norm slot where a graph replay reads them
+void launch_set_itbase(Ctx &c);
+constexpr int kGraphIters = 32;      // iterations per captured graph (one ring cycle)
+static_assert(kFluxRing == kGraphIters, "a captured block must cycle the FP32 rings exactly once");
 void launch_addv(Ctx &c, const double *psi, int g0, int g1);
 void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec);
 void set_kernel_attributes(Ctx &c);

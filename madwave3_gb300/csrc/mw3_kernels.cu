@@ -639,9 +639,12 @@ __global__ void k_addv(DevGrid d, const double *__restrict__ psi, const HT *__re
 }
 
 // check (main_madwave3.f:431-442): sum the norm partials of each wave
+// base (optional): graph replays read the slot as base[1] + slot
 __global__ void k_norms(const double *__restrict__ part, const int *__restrict__ wseg0, const int *__restrict__ wseg1,
-                        int nchunk, double *const *norms_out, const int64_t *__restrict__ cap, int64_t slot)
+                        int nchunk, double *const *norms_out, const int64_t *__restrict__ cap, int64_t slot,
+                        const int64_t *__restrict__ base)
 {
+    if (base) slot += base[1];
     int w = blockIdx.x;
     __shared__ double red[256];
     double s = 0.0;
@@ -660,10 +663,12 @@ __global__ void k_norms(const double *__restrict__ part, const int *__restrict__
 // accumulators
 // ---------------------------------------------------------------------------
 // CoefEcheby (main_madwave3.f:462-490): C_k(E) = d hbar/Delta e^{-ik acos Es}/sqrt(1-Es^2)
+// base (optional): graph replays read the iteration as base[0] + k
 __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double emindlt, double delta2,
                              double hbr, int64_t k, double *__restrict__ zck, float *__restrict__ cring,
-                             float *__restrict__ cvring)
+                             float *__restrict__ cvring, const int64_t *__restrict__ base)
 {
+    if (base) k += base[0];
     int ie = blockIdx.x * blockDim.x + threadIdx.x;
     if (ie >= netot) return;
     double dd = (k == 0) ? 1.0 : 2.0;
@@ -1409,17 +1414,18 @@ void launch_accumulators(Ctx &c, int64_t it)
     DevGrid d = devgrid(c);
     const bool ring = c.d_fring != nullptr;
     k_coefecheby<<<(c.netot + 127) / 128, 128, 0, c.stream>>>(
-        c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2, c.grid.hbr, it, c.d_zck,
+        c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2, c.grid.hbr, c.capturing ? it - c.cap_it0 : it, c.d_zck,
         ring ? c.d_cring + (size_t)c.fring_n * c.netot * 2 : nullptr,
-        c.d_cvcring ? c.d_cvcring + (size_t)c.cvring_n * c.netot * 2 : nullptr);
+        c.d_cvcring ? c.d_cvcring + (size_t)c.cvring_n * c.netot * 2 : nullptr, c.capturing ? c.d_itbase : nullptr);
     LAUNCH_CHECK(c);
     for (size_t w = 0; w < c.waves.size(); w++) {
         WaveTables &t = c.waves[w];
         if (t.nofe > 0) {
             k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(c.wdev[w].efe, t.nofe, c.grid.emindlt,
-                                                                     c.grid.delta2, c.grid.hbr, it,
+                                                                     c.grid.delta2, c.grid.hbr,
+                                                                     c.capturing ? it - c.cap_it0 : it,
                                                                      c.d_zcke + (size_t)w * c.nofemax * 2, nullptr,
-                                                                     nullptr);
+                                                                     nullptr, c.capturing ? c.d_itbase : nullptr);
             LAUNCH_CHECK(c);
         }
     }
@@ -1503,10 +1509,25 @@ void launch_addv(Ctx &c, const double *psi, int g0, int g1)
     LAUNCH_CHECK(c);
 }
 
+// the iteration and norm-slot base of a graph replay
+__global__ void k_set_itbase(int64_t *base, int64_t it, int64_t slot)
+{
+    base[0] = it;
+    base[1] = slot;
+}
+
+void launch_set_itbase(Ctx &c)
+{
+    k_set_itbase<<<1, 1, 0, c.stream>>>(c.d_itbase, c.it, c.norm_slot);
+    LAUNCH_CHECK(c);
+}
+
 void launch_norms(Ctx &c, int64_t slot)
 {
     k_norms<<<(int)c.waves.size(), 256, 0, c.stream>>>(c.d_normpart, c.d_wseg0, c.d_wseg1, c.nchunk,
-                                                       c.d_norm_ptrs, c.d_norm_cap, slot);
+                                                       c.d_norm_ptrs, c.d_norm_cap,
+                                                       c.capturing ? slot - c.cap_slot0 : slot,
+                                                       c.capturing ? c.d_itbase : nullptr);
     LAUNCH_CHECK(c);
 }
 
