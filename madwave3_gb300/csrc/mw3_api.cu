@@ -447,11 +447,18 @@ int build_device(Ctx &c)
         TRY(dalloc(c, &c.d_zcdr, (size_t)std::max<int64_t>(nf, 1) * c.netot * 2));
         c.d_fring = nullptr;
         c.d_cring = nullptr;
-        c.fring_n = 0;
         c.d_zar32 = nullptr;
         if (!c.fp64 && nf > 0) {
-            TRY(dalloc(c, &c.d_fring, (size_t)mw3::kFluxRing * nf * 3, false));
-            TRY(dalloc(c, &c.d_cring, (size_t)mw3::kFluxRing * c.netot * 2, false));
+            // zeroed: a slot no iteration has written yet adds 0 x 0
+            TRY(dalloc(c, &c.d_fring, (size_t)mw3::kFluxSlots * nf * 3));
+            TRY(dalloc(c, &c.d_cring, (size_t)mw3::kFluxSlots * c.netot * 2));
+            // slices: as many as keep a slice flush at one wave of CTAs or more
+            // (2 resident per SM, 64 x 64 tiles), between 4 (a quarter every 32
+            // iterations) and kFluxSlots (one slice every iteration)
+            const int64_t etiles = (c.netot + 63) / 64;
+            int P = 4;
+            while (P < mw3::kFluxSlots && ((int64_t)nf / (64 * 2 * P)) * etiles >= 2 * 152) P *= 2;
+            c.fl_q = mw3::kFluxSlots / P;
             std::vector<float> zar32(t0.zar1flux.begin(), t0.zar1flux.end());
             TRY(dupload(c, &c.d_zar32, zar32));
         }
@@ -464,12 +471,12 @@ int build_device(Ctx &c)
         TRY(dupload(c, &c.d_r2abs, r2abs));
         TRY(dupload(c, &c.d_fd, t0.fd));
         c.d_cvring = c.d_cvcring = c.d_dj32 = c.d_fd32 = c.d_xj32 = nullptr;
-        c.cvring_n = 0;
         if (!c.fp64) {
             std::vector<float> fd32(t0.fd.begin(), t0.fd.end());
             TRY(dupload(c, &c.d_fd32, fd32));
-            TRY(dalloc(c, &c.d_cvring, (size_t)mw3::kFluxRing * G * c.nj * c.nv, false));
-            TRY(dalloc(c, &c.d_cvcring, (size_t)mw3::kFluxRing * c.netot * 2, false));
+            // zeroed: a slot no iteration has written yet adds 0 x 0
+            TRY(dalloc(c, &c.d_cvring, (size_t)mw3::kFluxRing * G * c.nj * c.nv));
+            TRY(dalloc(c, &c.d_cvcring, (size_t)mw3::kFluxRing * c.netot * 2));
             TRY(dalloc(c, &c.d_dj32, (size_t)G * c.nj * na));
             TRY(dalloc(c, &c.d_xj32, (size_t)G * n1 * c.nj));
         }
@@ -636,8 +643,10 @@ int check_device_flags(Ctx &c, const char *where)
 int reset_accumulators(Ctx &c)
 {
     size_t nf = (size_t)std::max(c.NF, 1) * c.netot * 2;
-    c.fring_n = 0;
-    c.cvring_n = 0;
+    if (c.d_cvcring)
+        MW3_CUDA_TRY(cudaMemsetAsync(c.d_cvcring, 0, sizeof(float) * mw3::kFluxRing * c.netot * 2, c.stream));
+    if (c.d_cring)
+        MW3_CUDA_TRY(cudaMemsetAsync(c.d_cring, 0, sizeof(float) * mw3::kFluxSlots * c.netot * 2, c.stream));
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcr, 0, sizeof(double) * nf, c.stream));
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zcdr, 0, sizeof(double) * nf, c.stream));
     MW3_CUDA_TRY(cudaMemsetAsync(c.d_zs2, 0, sizeof(double) * 2 * (size_t)c.G * c.nj * c.nv * c.netot, c.stream));
@@ -823,6 +832,10 @@ int mw3_upload_state(mw3_ctx *h, int32_t w, const double *psi_km1, const double 
         rc = reset_accumulators(c);
         if (rc) return rc;
     }
+    if (c.started && it != c.it) {   // the rings' slots follow the iteration
+        mw3::flush_flux(c);
+        mw3::flush_cvj(c);
+    }
     c.it = it;
     c.norm_slot = 0;
     c.started = true;
@@ -854,13 +867,15 @@ void run_iteration(Ctx &c)
     c.norm_slot++;
 }
 
-// a block of kGraphIters iterations repeats exactly when the rings start empty (they
-// cycle with that period), no iteration of the block is gated (the elastic channel
-// below kminelastic changes the launches) and no stage timing is recorded
+// a block of kGraphIters iterations repeats exactly when it starts at an iteration
+// that is a multiple of kGraphIters (the rings' slots and flushes follow the
+// iteration number modulo 32, or, for the flux ring's slots, a replay reads it on
+// the device), no iteration of the block is gated (the elastic channel below
+// kminelastic changes the launches) and no stage timing is recorded
 bool graph_ready(Ctx &c, int64_t left)
 {
     if (c.graphs_off || c.prof || left < mw3::kGraphIters) return false;
-    if (c.fring_n != 0 || c.cvring_n != 0) return false;
+    if (c.it % mw3::kGraphIters != 0) return false;
     if (c.gate_elastic && c.it + 1 < c.kminelastic) return false;
     return true;
 }
@@ -898,7 +913,6 @@ void capture_graph(Ctx &c, int par)
     c.d_pk32 = pk32;
     c.d_pkm1_32 = pkm1_32;
     c.launches = l0;
-    c.fring_n = c.cvring_n = 0;
     if (e == cudaSuccess && g && cudaGraphInstantiate(&c.graph_exec[par], g, 0) == cudaSuccess) {
         c.graph_launches[par] = launches;
     } else {
@@ -990,6 +1004,10 @@ int mw3_upload_state_all(mw3_ctx *h, const double *psi_km1, const double *psi_k,
     if (!c.started) {
         rc = reset_accumulators(c);
         if (rc) return rc;
+    }
+    if (c.started && it != c.it) {   // the rings' slots follow the iteration
+        mw3::flush_flux(c);
+        mw3::flush_cvj(c);
     }
     c.it = it;
     c.norm_slot = 0;

@@ -188,26 +188,27 @@ struct Ctx {
     int *d_fl_dptr = nullptr, *d_fl_dir1 = nullptr;
     double *d_fl_poti = nullptr, *d_zar = nullptr, *d_etot = nullptr, *d_zck = nullptr;
     double *d_fpsi = nullptr;        // [NF][4]: psi, dpsi (re, im)
-    // mixed path: the last iterations' flux samples and C_k(E), FP32, flushed
-    // into zCR/zCdR every kFluxRing iterations and before every read
-    float *d_fring = nullptr;        // [kFluxRing][NF][3]
+    // mixed path: the flux samples and C_k(E) of the last kFluxSlots iterations,
+    // FP32, slot = iteration mod kFluxSlots; every iteration adds one slice of the
+    // flux points over all slots into zCR/zCdR, and everything pending is added
+    // before the accumulators are read
+    float *d_fring = nullptr;        // [kFluxSlots][NF][3]
     float *d_zar32 = nullptr;        // the r1 derivative row at the flux line, FP32 (mixed path)
     // mixed path: each flux line's derivative terms as runs of consecutive points with
     // consecutive r1 (CSR: fl_rptr[f]..fl_rptr[f+1]), when the runs are long enough
     int *d_fl_rptr = nullptr;
     int4 *d_fl_runs = nullptr;       // (flat index lo, flat index hi, first r1, length)
     bool fl_runs = false;
-    float *d_cring = nullptr;        // [kFluxRing][netot][2]
-    int fring_n = 0;                 // slots filled since the last flush
-    // mixed path: the Cvj projection in FP32 (from the FP32 copy of psi) and Cvj of up
-    // to kFluxRing iterations with their C_k(E), added into zS2 every kFluxRing
-    // iterations and before every read
+    float *d_cring = nullptr;        // [kFluxSlots][netot][2]
+    int fl_q = 32;                   // a slice of the flux points is flushed every fl_q iterations
+    // mixed path: the Cvj projection in FP32 (from the FP32 copy of psi) and Cvj of the
+    // last kFluxRing iterations with their C_k(E) (slot = iteration mod kFluxRing),
+    // added into zS2 at the iterations = kFluxRing - 1 mod kFluxRing and before every read
     float *d_cvring = nullptr;       // [kFluxRing][G nj nv]
     float *d_cvcring = nullptr;      // [kFluxRing][netot][2]
     float *d_dj32 = nullptr;         // [G][nj][na]: Djmmp columns of the projection, 0 where Cvj is off
     float *d_fd32 = nullptr;         // fd in FP32
     float *d_xj32 = nullptr;         // [G][n1][nj]
-    int cvring_n = 0;
     // CUDA graphs of kGraphIters iterations, one per parity of the psi buffers: the
     // kernels read the iteration and the norm slot as d_itbase[0/1] plus the offset
     // captured, so one graph serves every block of iterations
@@ -326,12 +327,14 @@ void flush_flux(Ctx &c);
 void flush_cvj(Ctx &c);
 // the FP32 Djmmp columns of the Cvj projection (mixed path), once the tables are on the device
 void build_cvj32(Ctx &c);
-constexpr int kFluxRing = 32;
+constexpr int kFluxRing = 32;       // Cvj ring: iterations between its flushes
+constexpr int kFluxSlots = 128;     // flux ring: iterations in each accumulated sum
 void launch_norms(Ctx &c, int64_t slot);
 // writes the context's iteration and norm slot where a graph replay reads them
 void launch_set_itbase(Ctx &c);
 constexpr int kGraphIters = 32;      // iterations per captured graph (one ring cycle)
-static_assert(kFluxRing == kGraphIters, "a captured block must cycle the FP32 rings exactly once");
+static_assert(kFluxRing == kGraphIters, "a captured block must cycle the Cvj ring exactly once");
+static_assert(kGraphIters % (kFluxSlots / 4) == 0, "flux slice flushes must repeat with the captured block");
 void launch_addv(Ctx &c, const double *psi, int g0, int g1);
 void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec);
 void set_kernel_attributes(Ctx &c);

@@ -666,7 +666,7 @@ __global__ void k_norms(const double *__restrict__ part, const int *__restrict__
 // base (optional): graph replays read the iteration as base[0] + k
 __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double emindlt, double delta2,
                              double hbr, int64_t k, double *__restrict__ zck, float *__restrict__ cring,
-                             float *__restrict__ cvring, const int64_t *__restrict__ base)
+                             int cring_zero, float *__restrict__ cvring, const int64_t *__restrict__ base)
 {
     if (base) k += base[0];
     int ie = blockIdx.x * blockDim.x + threadIdx.x;
@@ -680,9 +680,10 @@ __global__ void k_coefecheby(const double *__restrict__ etot, int netot, double 
     sincos(expo, &s, &c);
     zck[2 * ie] = zf * c / deno;
     zck[2 * ie + 1] = zf * s / deno;
-    if (cring) {                    // mixed path: this iteration's slot of the flux ring
-        cring[2 * ie] = (float)(zf * c / deno);
-        cring[2 * ie + 1] = (float)(zf * s / deno);
+    if (cring) {                    // mixed path: this iteration's slot of the flux ring (0: no flux sample)
+        float *q = cring + (size_t)(k % kFluxSlots) * netot * 2;
+        q[2 * ie] = cring_zero ? 0.f : (float)(zf * c / deno);
+        q[2 * ie + 1] = cring_zero ? 0.f : (float)(zf * s / deno);
     }
     if (cvring) {                   // mixed path: this iteration's slot of the Cvj ring
         cvring[2 * ie] = (float)(zf * c / deno);
@@ -698,12 +699,15 @@ __global__ void __launch_bounds__(256) k_flux_deriv(const double *__restrict__ p
                                                     const int *__restrict__ dir1, const double *__restrict__ zar,
                                                     int NF, double *__restrict__ fpsi, float *__restrict__ fring,
                                                     const float *__restrict__ psi32, const float *__restrict__ zar32,
-                                                    const int *__restrict__ rptr, const int4 *__restrict__ runs)
+                                                    const int *__restrict__ rptr, const int4 *__restrict__ runs,
+                                                    int64_t it, const int64_t *__restrict__ base)
 {
     int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (f >= NF) return;
     if (fring) {
+        if (base) it += base[0];
+        fring += (size_t)(it % kFluxSlots) * NF * 3;   // this iteration's slot
         // mixed path: FP32 products and sums (the ring holds FP32 anyway) from the FP32
         // copy of psi; with runs (consecutive points and r1) no per-term index is read.
         // Either way lane l takes the line's terms l, l + 32, ... in order.
@@ -789,65 +793,92 @@ __global__ void __launch_bounds__(128) k_flux_acc(const double *__restrict__ fps
     }
 }
 
-// Mixed path: the flux accumulation of up to kFluxRing iterations at once.
-// zCR(E,f) += sum_s C_s(E) psi_s(f) and zCdR(E,f) += sum_s C_s(E) dpsi_s(f) for
-// E > V(f): the products and the sum over the ring slots in FP32 (a 64 x 64
-// (E, f) tile per CTA, 4 x 4 per thread), added once to the FP64 accumulators,
-// so each accumulator is read and written once per flush instead of once per
-// iteration.
-constexpr int kFlushE = 64, kFlushF = 64;
+// Mixed path: the flux accumulation zCR(E,f) += sum_k C_k(E) psi_k(f) and
+// zCdR(E,f) += sum_k C_k(E) dpsi_k(f) for E > V(f), through a ring of the last
+// S = kFluxSlots iterations (slot = iteration mod S).  The flux points are cut into
+// P = S / q slices of `chunk` points; slice p is flushed over all slots (its last S
+// iterations) at the iterations k with k mod S = p q + q - 1, so every (point,
+// iteration) is added exactly once and the cost is spread evenly (one slice every
+// q iterations).  Products and the sum over the slots in FP32 (a 64 x 64 (E, f)
+// tile per CTA, 4 x 4 per thread), added once to the FP64 accumulators.
+// final != 0: every slice's iterations since its last flush (slice p: the slots
+// with (now - s) mod S < (now - p q - q + 1) mod S), before the accumulators are
+// read; the host then clears the C ring, so no iteration is added twice.
+constexpr int kFlushE = 64, kFlushF = 64, kFlushS = 32;
 __global__ void __launch_bounds__(256) k_flux_flush(const float *__restrict__ fring, const float *__restrict__ cring,
-                                                    int nslots, const double *__restrict__ poti,
-                                                    const double *__restrict__ etot, int netot, int NF,
+                                                    const double *__restrict__ poti,
+                                                    const double *__restrict__ etot, int netot, int NF, int chunk,
+                                                    int q, int64_t now, const int64_t *__restrict__ base, int final_,
                                                     double *__restrict__ zcr, double *__restrict__ zcdr)
 {
-    __shared__ float sc[kFluxRing][kFlushE][2];
-    __shared__ float sp[kFluxRing][kFlushF][3];
-    const int f0 = blockIdx.x * kFlushF, e0 = blockIdx.y * kFlushE;
-    for (int i = threadIdx.x; i < nslots * kFlushE * 2; i += blockDim.x) {
-        int s = i / (kFlushE * 2), r = i % (kFlushE * 2);
-        int e = e0 + r / 2;
-        sc[s][r / 2][r & 1] = e < netot ? cring[((size_t)s * netot + e) * 2 + (r & 1)] : 0.f;
+    __shared__ float sc[kFlushS][kFlushE][2];
+    __shared__ float sp[kFlushS][kFlushF][3];
+    if (base) now += base[0];
+    const int nowm = (int)(now % kFluxSlots);
+    int f0, f1;
+    if (final_) {
+        f0 = blockIdx.x * kFlushF;
+        f1 = min(NF, f0 + kFlushF);
+    } else {
+        const int p = nowm / q;
+        f0 = p * chunk + blockIdx.x * kFlushF;
+        f1 = min(min(NF, (p + 1) * chunk), f0 + kFlushF);
     }
-    for (int i = threadIdx.x; i < nslots * kFlushF * 3; i += blockDim.x) {
-        int s = i / (kFlushF * 3), r = i % (kFlushF * 3);
-        int f = f0 + r / 3;
-        sp[s][r / 3][r % 3] = f < NF ? fring[((size_t)s * NF + f) * 3 + r % 3] : 0.f;
-    }
-    __syncthreads();
+    if (f0 >= f1) return;
+    const int e0 = blockIdx.y * kFlushE;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // E = e0 + tx + 16 i, f = f0 + ty + 16 j
     float ar[4][4], ai[4][4], br[4][4], bi[4][4];
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) ar[i][j] = ai[i][j] = br[i][j] = bi[i][j] = 0.f;
-    for (int s = 0; s < nslots; s++) {
-        float cr[4], ci[4], p[4], dr[4], di[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            cr[i] = sc[s][tx + 16 * i][0];
-            ci[i] = sc[s][tx + 16 * i][1];
+    for (int s0 = 0; s0 < kFluxSlots; s0 += kFlushS) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < kFlushS * kFlushE * 2; i += blockDim.x) {
+            int s = i / (kFlushE * 2), r = i % (kFlushE * 2);
+            int e = e0 + r / 2;
+            sc[s][r / 2][r & 1] = e < netot ? cring[((size_t)(s0 + s) * netot + e) * 2 + (r & 1)] : 0.f;
         }
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            p[j] = sp[s][ty + 16 * j][0];
-            dr[j] = sp[s][ty + 16 * j][1];
-            di[j] = sp[s][ty + 16 * j][2];
+        for (int i = threadIdx.x; i < kFlushS * kFlushF * 3; i += blockDim.x) {
+            int s = i / (kFlushF * 3), r = i % (kFlushF * 3);
+            int f = f0 + r / 3;
+            float v = f < f1 ? fring[((size_t)(s0 + s) * NF + f) * 3 + r % 3] : 0.f;
+            if (final_ && f < f1) {
+                const int p = f / chunk;
+                const int np = ((nowm - p * q - q + 1) % kFluxSlots + kFluxSlots) % kFluxSlots;
+                if ((nowm - (s0 + s) + kFluxSlots) % kFluxSlots >= np) v = 0.f;
+            }
+            sp[s][r / 3][r % 3] = v;
         }
+        __syncthreads();
+        for (int s = 0; s < kFlushS; s++) {
+            float cr[4], ci[4], p[4], dr[4], di[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+            for (int i = 0; i < 4; i++) {
+                cr[i] = sc[s][tx + 16 * i][0];
+                ci[i] = sc[s][tx + 16 * i][1];
+            }
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                ar[i][j] = fmaf(cr[i], p[j], ar[i][j]);
-                ai[i][j] = fmaf(ci[i], p[j], ai[i][j]);
-                br[i][j] = fmaf(cr[i], dr[j], fmaf(-ci[i], di[j], br[i][j]));
-                bi[i][j] = fmaf(cr[i], di[j], fmaf(ci[i], dr[j], bi[i][j]));
+                p[j] = sp[s][ty + 16 * j][0];
+                dr[j] = sp[s][ty + 16 * j][1];
+                di[j] = sp[s][ty + 16 * j][2];
             }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    ar[i][j] = fmaf(cr[i], p[j], ar[i][j]);
+                    ai[i][j] = fmaf(ci[i], p[j], ai[i][j]);
+                    br[i][j] = fmaf(cr[i], dr[j], fmaf(-ci[i], di[j], br[i][j]));
+                    bi[i][j] = fmaf(cr[i], di[j], fmaf(ci[i], dr[j], bi[i][j]));
+                }
+        }
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         int f = f0 + ty + 16 * j;
-        if (f >= NF) continue;
+        if (f >= f1) continue;
         double v = poti[f];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -1025,17 +1056,18 @@ __global__ void k_cvj_dj32(DevGrid d, CvjArgs c, float *__restrict__ dj32)
 // per iteration
 constexpr int kCvFlushR = 64, kCvFlushE = 64;
 __global__ void __launch_bounds__(256) k_cvj_flush(const float *__restrict__ ring, const float *__restrict__ cring,
-                                                   int nslots, int R, int netot, double *__restrict__ zs2)
+                                                   unsigned slot_mask, int R, int netot, double *__restrict__ zs2)
 {
     __shared__ float sc[kFluxRing][kCvFlushE][2];
     __shared__ float sr[kFluxRing][kCvFlushR];
     const int r0 = blockIdx.x * kCvFlushR, e0 = blockIdx.y * kCvFlushE;
-    for (int i = threadIdx.x; i < nslots * kCvFlushE * 2; i += blockDim.x) {
+    for (int i = threadIdx.x; i < kFluxRing * kCvFlushE * 2; i += blockDim.x) {
         int s = i / (kCvFlushE * 2), q = i % (kCvFlushE * 2);
         int e = e0 + q / 2;
-        sc[s][q / 2][q & 1] = e < netot ? cring[((size_t)s * netot + e) * 2 + (q & 1)] : 0.f;
+        sc[s][q / 2][q & 1] =
+            (e < netot && ((slot_mask >> s) & 1u)) ? cring[((size_t)s * netot + e) * 2 + (q & 1)] : 0.f;
     }
-    for (int i = threadIdx.x; i < nslots * kCvFlushR; i += blockDim.x) {
+    for (int i = threadIdx.x; i < kFluxRing * kCvFlushR; i += blockDim.x) {
         int s = i / kCvFlushR, q = i % kCvFlushR;
         int row = r0 + q;
         sr[s][q] = row < R ? ring[(size_t)s * R + row] : 0.f;
@@ -1047,7 +1079,7 @@ __global__ void __launch_bounds__(256) k_cvj_flush(const float *__restrict__ rin
     for (int i = 0; i < 4; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) ar[i][j] = ai[i][j] = 0.f;
-    for (int s = 0; s < nslots; s++) {
+    for (int s = 0; s < kFluxRing; s++) {
         float cr[4], ci[4], v[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -1413,32 +1445,45 @@ void launch_accumulators(Ctx &c, int64_t it)
     stage_mark(c, 6);
     DevGrid d = devgrid(c);
     const bool ring = c.d_fring != nullptr;
+    const int64_t itarg = c.capturing ? it - c.cap_it0 : it;
+    const int64_t *bp = c.capturing ? c.d_itbase : nullptr;
+    bool gate = c.gate_elastic && it < c.kminelastic;
+    const bool flux_on = c.NF > 0 && !(gate && c.waves[0].iprod == 1);
     k_coefecheby<<<(c.netot + 127) / 128, 128, 0, c.stream>>>(
-        c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2, c.grid.hbr, c.capturing ? it - c.cap_it0 : it, c.d_zck,
-        ring ? c.d_cring + (size_t)c.fring_n * c.netot * 2 : nullptr,
-        c.d_cvcring ? c.d_cvcring + (size_t)c.cvring_n * c.netot * 2 : nullptr, c.capturing ? c.d_itbase : nullptr);
+        c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2, c.grid.hbr, itarg, c.d_zck, ring ? c.d_cring : nullptr,
+        flux_on ? 0 : 1, c.d_cvcring ? c.d_cvcring + (size_t)(it % kFluxRing) * c.netot * 2 : nullptr, bp);
     LAUNCH_CHECK(c);
     for (size_t w = 0; w < c.waves.size(); w++) {
         WaveTables &t = c.waves[w];
         if (t.nofe > 0) {
             k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(c.wdev[w].efe, t.nofe, c.grid.emindlt,
                                                                      c.grid.delta2, c.grid.hbr,
-                                                                     c.capturing ? it - c.cap_it0 : it,
-                                                                     c.d_zcke + (size_t)w * c.nofemax * 2, nullptr,
-                                                                     nullptr, c.capturing ? c.d_itbase : nullptr);
+                                                                     itarg, c.d_zcke + (size_t)w * c.nofemax * 2,
+                                                                     nullptr, 0, nullptr, bp);
             LAUNCH_CHECK(c);
         }
     }
-    bool gate = c.gate_elastic && it < c.kminelastic;
-    if (c.NF > 0 && !(gate && c.waves[0].iprod == 1)) {
+    if (ring) {
+        if (flux_on) {
+            k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(
+                c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx, c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi, c.d_fring,
+                c.d_pk32, c.d_zar32, c.fl_runs ? c.d_fl_rptr : nullptr, c.fl_runs ? c.d_fl_runs : nullptr, itarg, bp);
+            LAUNCH_CHECK(c);
+        }
+        // a slice every fl_q iterations, also while the flux is gated (its C slot is 0 then)
+        if (it % c.fl_q == c.fl_q - 1) {
+            const int P = kFluxSlots / c.fl_q, chunk = (c.NF + P - 1) / P;
+            dim3 g((chunk + kFlushF - 1) / kFlushF, (c.netot + kFlushE - 1) / kFlushE);
+            k_flux_flush<<<g, 256, 0, c.stream>>>(c.d_fring, c.d_cring, c.d_fl_poti, c.d_etot, c.netot, c.NF, chunk,
+                                                  c.fl_q, itarg, bp, 0, c.d_zcr, c.d_zcdr);
+            LAUNCH_CHECK(c);
+        }
+    } else if (flux_on) {
         k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(
-            c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx, c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi,
-            ring ? c.d_fring + (size_t)c.fring_n * c.NF * 3 : nullptr, c.d_pk32, c.d_zar32,
-            c.fl_runs ? c.d_fl_rptr : nullptr, c.fl_runs ? c.d_fl_runs : nullptr);
+            c.d_pk, c.d_fl_idx, c.d_fl_dptr, c.d_fl_didx, c.d_fl_dir1, c.d_zar, c.NF, c.d_fpsi, nullptr, c.d_pk32,
+            c.d_zar32, nullptr, nullptr, itarg, bp);
         LAUNCH_CHECK(c);
-        if (ring) {
-            if (++c.fring_n == kFluxRing) flush_flux(c);
-        } else {
+        {
             dim3 g((c.NF + kFluxPerBlock - 1) / kFluxPerBlock, (c.netot + 127) / 128);
             k_flux_acc<<<g, 128, 0, c.stream>>>(c.d_fpsi, c.d_fl_poti, c.d_etot, c.d_zck, c.netot, c.NF, c.d_zcr,
                                                 c.d_zcdr);
@@ -1448,13 +1493,18 @@ void launch_accumulators(Ctx &c, int64_t it)
     if (c.n2 > 1 && c.d_cvring) {
         // mixed path: FP32 projection, Cvj into the ring, zS2 at the flush
         CvjArgs a = cvj_args(c, gate);
-        a.ring = c.d_cvring + (size_t)c.cvring_n * c.G * c.nj * c.nv;
+        a.ring = c.d_cvring + (size_t)(it % kFluxRing) * c.G * c.nj * c.nv;
         size_t sm32 = sizeof(float) * ((size_t)c.na * kCvjR1 + (size_t)c.nj * c.na);
         k_cvj_proj32<<<dim3(c.G, (c.n1 + kCvjR1 - 1) / kCvjR1), 256, sm32, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
         k_cvj_fd32<<<(c.G * c.nj * c.nv * 32 + 255) / 256, 256, 0, c.stream>>>(d, a);
         LAUNCH_CHECK(c);
-        if (++c.cvring_n == kFluxRing) flush_cvj(c);
+        if (it % kFluxRing == kFluxRing - 1) {   // the ring's 32 iterations into zS2
+            const int R = c.G * c.nj * c.nv;
+            dim3 g((R + kCvFlushR - 1) / kCvFlushR, (c.netot + kCvFlushE - 1) / kCvFlushE);
+            k_cvj_flush<<<g, 256, 0, c.stream>>>(c.d_cvring, c.d_cvcring, 0xffffffffu, R, c.netot, c.d_zs2);
+            LAUNCH_CHECK(c);
+        }
     } else if (c.n2 > 1) {
         CvjArgs a = cvj_args(c, gate);
         size_t smp = sizeof(double) * ((size_t)c.na * kCvjR1 + (size_t)c.nj * c.na);
@@ -1470,12 +1520,21 @@ void launch_accumulators(Ctx &c, int64_t it)
 
 void flush_cvj(Ctx &c)
 {
-    if (!c.d_cvring || c.cvring_n == 0) return;
-    const int R = c.G * c.nj * c.nv;
-    dim3 g((R + kCvFlushR - 1) / kCvFlushR, (c.netot + kCvFlushE - 1) / kCvFlushE);
-    k_cvj_flush<<<g, 256, 0, c.stream>>>(c.d_cvring, c.d_cvcring, c.cvring_n, R, c.netot, c.d_zs2);
-    LAUNCH_CHECK(c);
-    c.cvring_n = 0;
+    if (!c.d_cvring) return;
+    // slot = iteration mod 32, flushed whole at the iterations = 31 mod 32: pending
+    // are the (now + 1) mod 32 iterations since, the slots (now - s) mod 32 < n
+    const int n = (int)((c.it + 1) % kFluxRing);
+    unsigned mask = 0;
+    for (int s = 0; s < kFluxRing; s++)
+        if ((int)(((c.it - s) % kFluxRing + kFluxRing) % kFluxRing) < n) mask |= 1u << s;
+    if (mask) {
+        const int R = c.G * c.nj * c.nv;
+        dim3 g((R + kCvFlushR - 1) / kCvFlushR, (c.netot + kCvFlushE - 1) / kCvFlushE);
+        k_cvj_flush<<<g, 256, 0, c.stream>>>(c.d_cvring, c.d_cvcring, mask, R, c.netot, c.d_zs2);
+        LAUNCH_CHECK(c);
+    }
+    // every pending iteration is in zS2 now: clear the C slots so no later flush adds them again
+    cudaMemsetAsync(c.d_cvcring, 0, sizeof(float) * kFluxRing * c.netot * 2, c.stream);
 }
 
 void build_cvj32(Ctx &c)
@@ -1489,12 +1548,15 @@ void build_cvj32(Ctx &c)
 
 void flush_flux(Ctx &c)
 {
-    if (!c.d_fring || c.fring_n == 0) return;
+    if (!c.d_fring || c.NF == 0) return;
+    const int P = kFluxSlots / c.fl_q, chunk = (c.NF + P - 1) / P;
     dim3 g((c.NF + kFlushF - 1) / kFlushF, (c.netot + kFlushE - 1) / kFlushE);
-    k_flux_flush<<<g, 256, 0, c.stream>>>(c.d_fring, c.d_cring, c.fring_n, c.d_fl_poti, c.d_etot, c.netot, c.NF,
-                                          c.d_zcr, c.d_zcdr);
+    k_flux_flush<<<g, 256, 0, c.stream>>>(c.d_fring, c.d_cring, c.d_fl_poti, c.d_etot, c.netot, c.NF, chunk,
+                                          c.fl_q, c.it, nullptr, 1, c.d_zcr, c.d_zcdr);
     LAUNCH_CHECK(c);
-    c.fring_n = 0;
+    // every pending iteration is in the accumulators now: clear the C slots so no
+    // later slice flush adds them again
+    cudaMemsetAsync(c.d_cring, 0, sizeof(float) * kFluxSlots * c.netot * 2, c.stream);
 }
 
 void launch_addv(Ctx &c, const double *psi, int g0, int g1)
