@@ -1,0 +1,235 @@
+"""Bound states on the propagation grid by Lanczos: the host side of the
+reference's bndgrid.out (SRC/bound-lanz/main_boundlanz.f), the second caller
+of the H psi boundary besides the Chebyshev loop.
+
+The reference evaluates H phi through Hmatrix (main_boundlanz.f:332-357),
+which copies phi into the propagation vector, calls difs and copies H phi
+back; here the operator is any callable psi -> H psi on the wave's state
+vector layout, normally ``Propagator(run, "fp64").hphi`` (mw3_hphi, host
+arrays in and out, like Hmatrix).  The algorithms follow
+SRC/bound-lanz/liboctdynlanz.f:
+
+* ``lanczos_eigenvalues``: lanzvalpariter (:3-278), the non-orthogonal Lanczos
+  recursion of Cullum and Willoughby, with the converged eigenvalues taken
+  every ``ntimes`` steps by ``converged_eigenvalues`` (valnkry, :472-575):
+  eigenvalues of the tridiagonal T and of T with its first row and column
+  removed; multiple copies are true, simple ones are true unless T-hat has
+  them too (spurious), both to 1e-8 zot.
+* ``cg_eigenvector``: cgradvecpar (:280-470), the eigenvector of a converged
+  eigenvalue by conjugate gradients on H - E from the initial guess.
+* ``initial_vector``: initia_lanzvec (main_boundlanz.f:270-330), a flat vector
+  on the stored points whose diagonal potential lies below Emax_lanzini.
+
+The tridiagonal eigenvalues come from LAPACK (scipy's eigh_tridiagonal)
+instead of the reference's QL routine (TQLI, SRC/liboctdyn.f:233-289); both are
+backward stable, so the eigenvalues agree to rounding, far inside the 1e-8
+zot that separates true from spurious copies.  State assignment (bndassign)
+and the plotting of the states need the product-channel functions and are
+not part of this module.
+"""
+import numpy as np
+
+from .host.constants import conve1, eV2cm, ev_to_zot
+
+GHOST_TOL = 1.0e-8          # zot; valnkry's critener
+
+
+def initial_vector(run, emax_zot):
+    """initia_lanzvec (main_boundlanz.f:270-330): 1 on every stored point whose
+    diagonal potential V(ir, iang, e, e) of its block's electronic state is
+    below emax_zot, 0 elsewhere, normalised.  Raises if no point qualifies (the
+    reference stops with 'Norm too low')."""
+    blk, ang, _, _ = run.point_table()
+    ir = np.empty(run.ntot, np.int64)
+    for iang in run.angle_order():
+        n = run.npunreal[iang - 1]
+        for b in range(run.ncan):
+            o = run.offs[iang - 1, b]
+            ir[o:o + n] = np.arange(n)
+    ele = np.asarray(run.nelebas)[blk] - 1
+    v = run.vvv[ele, ele, ang - 1, ir]
+    x = np.where(v < emax_zot, 1.0, 0.0)
+    nrm = float(np.dot(x, x))
+    if abs(nrm) < 1e-10:
+        raise ValueError("initial Lanczos vector has no point below Emax_lanzini (norm too low)")
+    return x / np.sqrt(nrm)
+
+
+def converged_eigenvalues(alpha, beta, tol=GHOST_TOL):
+    """valnkry (liboctdynlanz.f:472-575).  alpha[0..n-1] is the diagonal of the
+    Lanczos matrix T, beta[i] couples i and i+1 (beta[n-1], if given, is not
+    used).  Returns the sorted eigenvalues judged true."""
+    from scipy.linalg import eigh_tridiagonal
+
+    a = np.asarray(alpha, np.float64)
+    n = a.size
+    if n == 0:
+        return np.zeros(0)
+    b = np.asarray(beta, np.float64)[:n - 1]
+    ev = np.sort(eigh_tridiagonal(a, b, eigvals_only=True)) if n > 1 else a.copy()
+    # T-hat: first row and column decoupled (betar(1) = 0)
+    if n > 2:
+        evr = np.sort(np.concatenate([[a[0]], eigh_tridiagonal(a[1:], b[1:], eigvals_only=True)]))
+    else:
+        evr = np.sort(a.copy())
+    # group the sorted eigenvalues: a value within tol of its group's first joins it
+    groups = []                 # [first value, copies]
+    for e in ev:
+        if groups and abs(groups[-1][0] - e) < tol:
+            groups[-1][1] += 1
+        else:
+            groups.append([e, 1])
+    out = []
+    for e, deg in groups:
+        if deg > 1:
+            out.append(e)
+        elif not np.any(np.abs(evr - e) < tol):
+            out.append(e)
+    return np.asarray(out)
+
+
+def lanczos_eigenvalues(hphi, v1, nkrymax=10000, ntimes=1000, on_block=None):
+    """lanzvalpariter (liboctdynlanz.f:3-278) from the normalised start vector v1.
+
+    The recursion runs in blocks of ``ntimes`` steps; after each block the
+    converged eigenvalues of the Krylov matrix so far are computed (and passed
+    to ``on_block(nkry, etrue)`` if given).  As in the reference the loop ends
+    once the Krylov dimension reaches nkrymax - 1 or more, so the last block
+    can take it to nkrymax + 1.  Returns (etrue, alpha, beta)."""
+    if ntimes < 2:
+        raise ValueError("ntimes must be at least 2")
+    v1 = np.ascontiguousarray(v1, np.float64)
+    alpha, beta = [], []
+    f2 = v1                                   # flanz(:,2)
+    hu = hphi(f2)
+    alpha.append(float(np.dot(hu, f2)))
+    f1 = hu - alpha[0] * f2
+    beta.append(float(np.sqrt(np.dot(f1, f1))))
+    f1 = f1 / beta[0]
+    hu = hphi(f1)
+    alpha.append(float(np.dot(hu, f1) - beta[0] * np.dot(f2, f1)))
+    nkry = 2                                  # alpha(1), alpha(2) known
+    etrue = np.zeros(0)
+    first = True
+    while True:
+        target = (1 + ntimes) if first else nkry + ntimes
+        first = False
+        while nkry < target:
+            f0 = hu - alpha[nkry - 1] * f1 - beta[nkry - 2] * f2
+            b = float(np.sqrt(np.dot(f0, f0)))
+            if len(beta) < nkry:
+                beta.append(b)
+            else:
+                beta[nkry - 1] = b
+            f0 = f0 / b
+            hu = hphi(f0)
+            alpha.append(float(np.dot(hu, f0) - b * np.dot(f1, f0)))
+            f2, f1 = f1, f0
+            nkry += 1
+        # beta(nkry): the norm of the next residual
+        x = hu - alpha[nkry - 1] * f1 - beta[nkry - 2] * f2
+        b = float(np.sqrt(np.dot(x, x)))
+        if len(beta) < nkry:
+            beta.append(b)
+        else:
+            beta[nkry - 1] = b
+        etrue = converged_eigenvalues(alpha[:nkry], beta[:nkry])
+        if on_block is not None:
+            on_block(nkry, etrue)
+        if nkry + 1 >= nkrymax:
+            break
+    return etrue, np.asarray(alpha), np.asarray(beta)
+
+
+def cg_eigenvector(hphi, v0, ediag, nomxiter, criter):
+    """cgradvecpar (liboctdynlanz.f:280-470): conjugate gradients on A = H - ediag
+    from v0, renormalising v every step, until the mean energy <v|H|v> is
+    within criter of ediag or nomxiter steps are done.  Returns
+    (v, emean, iterations, converged)."""
+    v = np.array(v0, np.float64)
+
+    def a_op(x):
+        return hphi(x) - ediag * x
+
+    r = a_op(v)
+    p = -r
+    ap = a_op(p)
+    lam = -float(np.dot(r, p)) / float(np.dot(p, ap))
+    it = 0
+    emean = ediag
+    while True:
+        it += 1
+        v = v + lam * p
+        v = v / np.sqrt(float(np.dot(v, v)))
+        hv = hphi(v)
+        emean = float(np.dot(hv, v))
+        r = hv - ediag * v
+        ap = a_op(p)
+        eps = float(np.dot(r, ap)) / float(np.dot(p, ap))
+        p = eps * p - r
+        ap = a_op(p)
+        lam = -float(np.dot(r, p)) / float(np.dot(p, ap))
+        if it > nomxiter:
+            return v, emean, it, False
+        if abs(emean - ediag) <= criter:
+            return v, emean, it, True
+
+
+def write_levels(path, etrue, vcutmax):
+    """niveles.dat (main_boundlanz.f:186-200): index, zot, cm^-1 and eV of
+    every converged eigenvalue below vcutmax, format (1x,i5,3(2x,e15.7))."""
+    with open(path, "w") as f:
+        for i, e in enumerate(etrue, 1):
+            if e < vcutmax:
+                f.write(" %5d  %s  %s  %s\n" % (i, _e15(e), _e15(e / conve1), _e15(e / conve1 / eV2cm)))
+
+
+def _e15(x):
+    """Fortran e15.7: 0.ddddddd E+xx mantissa form, right-aligned in 15."""
+    if x == 0.0:
+        return "%15s" % "0.0000000E+00"
+    m, ex = "%.6E" % abs(x), 0
+    # the reference's form has a leading "0." and the exponent one larger
+    mant = float(m.split("E")[0]) / 10.0
+    ex = int(m.split("E")[1]) + 1
+    s = "%.7fE%+03d" % (mant, ex)
+    if mant >= 1.0:                     # rounding carried: 0.99999995 -> 1.0000000
+        s = "%.7fE%+03d" % (mant / 10.0, ex + 1)
+    return "%15s" % (("-" if x < 0 else "") + s)
+
+
+class BoundStates:
+    """bndgrid.out's Lanczos part for one wave: eigenvalues, then eigenvectors of
+    the lowest ones.  Parameters are the reference's &lanczos_parameters
+    (mod_lanczos_01y2.f:31-55, defaults as there), energies in eV."""
+
+    def __init__(self, run, hphi, emax_lanzini_ev, ntimes=1000, nkrymax=10000, criter_ev=1e-4,
+                 nomxiter=None, nvecmin=1, nvecmax=10):
+        self.run = run
+        self.hphi = hphi
+        self.emax = ev_to_zot(emax_lanzini_ev)
+        self.ntimes = ntimes
+        self.nkrymax = nkrymax
+        self.criter = ev_to_zot(criter_ev)
+        self.nomxiter = nkrymax if nomxiter is None else nomxiter
+        self.nvecmin, self.nvecmax = nvecmin, nvecmax
+        self.etrue = None
+
+    def eigenvalues(self, on_block=None):
+        v1 = initial_vector(self.run, self.emax)
+        self.etrue, self.alpha, self.beta = lanczos_eigenvalues(self.hphi, v1, self.nkrymax, self.ntimes,
+                                                                on_block)
+        return self.etrue
+
+    def eigenvectors(self):
+        """cgradvecpar for the states nvecmin..min(nvecmax, ntrue), each from the
+        initial guess (main_boundlanz.f:213-236).  Returns [(E, v, emean, its, ok)]."""
+        if self.etrue is None:
+            self.eigenvalues()
+        v0 = initial_vector(self.run, self.emax)
+        out = []
+        for iv in range(self.nvecmin, min(self.nvecmax, len(self.etrue)) + 1):
+            e = float(self.etrue[iv - 1])
+            v, em, its, ok = cg_eigenvector(self.hphi, v0, e, self.nomxiter, self.criter)
+            out.append((e, v, em, its, ok))
+        return out

@@ -1,0 +1,88 @@
+"""Lanczos bound states (SRC/bound-lanz): the recursion, the Cullum-Willoughby
+selection of true eigenvalues, the conjugate-gradient eigenvectors and the
+initial guess, on CPU with the oracle's H psi as the operator (the GPU's
+H psi against it is in test_gpu_bndlanz.py)."""
+import numpy as np
+import pytest
+
+from madwave3_gb300 import bndlanz
+from madwave3_gb300.host.constants import ev_to_zot, zot_to_ev
+
+
+def test_true_eigenvalues_of_a_known_spectrum():
+    """300 Lanczos steps on a 30-dimensional operator: T has 301 Ritz values
+    (many ghost copies); valnkry's selection keeps each of the 30 once."""
+    rng = np.random.default_rng(20261203)
+    d = np.sort(rng.uniform(-1, 1, 30))
+    v1 = rng.uniform(-1, 1, 30)
+    v1 /= np.linalg.norm(v1)
+    et, a, b = bndlanz.lanczos_eigenvalues(lambda x: d * x, v1, nkrymax=300, ntimes=100)
+    assert a.size == 301                       # the last block overshoots nkrymax as the reference does
+    assert et.size == 30
+    assert np.max(np.abs(et - d)) < 1e-8
+
+
+def test_selection_rules():
+    """Multiple copies are true even when T-hat (T without its first row and
+    column) has them; a simple value that T-hat also has is spurious."""
+    # T = [[5, .3, 0], [.3, 1, 0], [0, 0, 2]]: 2 is simple and in T-hat -> spurious;
+    # the two eigenvalues of the coupled 2 x 2 block are not in T-hat -> true
+    et = bndlanz.converged_eigenvalues([5.0, 1.0, 2.0], [0.3, 0.0])
+    assert np.allclose(et, np.linalg.eigvalsh([[5.0, 0.3], [0.3, 1.0]]), atol=1e-14)
+    # T = diag(5, 2, 2): 2 twice -> true once; 5 simple and in T-hat -> spurious
+    et = bndlanz.converged_eigenvalues([5.0, 2.0, 2.0], [0.0, 0.0])
+    assert np.allclose(et, [2.0])
+
+
+@pytest.fixture(scope="module")
+def tiny(runs):
+    from oracle.mw3ref import Oracle
+    run = runs["tiny_j0"]
+    return run, Oracle(run)
+
+
+def test_initial_vector(tiny):
+    run, _ = tiny
+    emax = run.vmintot + ev_to_zot(1.0)
+    v = bndlanz.initial_vector(run, emax)
+    assert abs(np.dot(v, v) - 1.0) < 1e-14
+    nz = v > 0
+    assert 0 < nz.sum() < run.ntot
+    assert np.allclose(v[nz], v[nz][0])
+    with pytest.raises(ValueError):
+        bndlanz.initial_vector(run, run.vmintot - 1.0)
+
+
+def test_lanczos_matches_a_direct_eigensolver(tiny):
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    run, o = tiny
+    v1 = bndlanz.initial_vector(run, run.vmintot + ev_to_zot(1.0))
+    et, a, b = bndlanz.lanczos_eigenvalues(o.hphi, v1, nkrymax=400, ntimes=200)
+    A = LinearOperator((run.ntot, run.ntot), matvec=o.hphi, dtype=np.float64)
+    w = np.sort(eigsh(A, k=4, which="SA", tol=1e-12)[0])
+    assert np.max(np.abs(et[:4] - w)) < 1e-10
+
+
+def test_cg_eigenvectors(tiny):
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    run, o = tiny
+    bs = bndlanz.BoundStates(run, o.hphi, zot_to_ev(run.vmintot) + 1.0, ntimes=200, nkrymax=400,
+                             criter_ev=1e-6, nomxiter=3000, nvecmax=2)
+    bs.eigenvalues()
+    A = LinearOperator((run.ntot, run.ntot), matvec=o.hphi, dtype=np.float64)
+    w, V = eigsh(A, k=2, which="SA", tol=1e-12)
+    for k, (e, v, em, its, ok) in enumerate(bs.eigenvectors()):
+        assert ok
+        assert abs(em - e) <= bs.criter
+        assert abs(np.dot(v, V[:, k])) > 0.9999
+
+
+def test_levels_file(tmp_path):
+    p = tmp_path / "niveles.dat"
+    bndlanz.write_levels(str(p), [-0.0123456789, 0.5, 3.0], vcutmax=2.0)
+    lines = p.read_text().splitlines()
+    assert len(lines) == 2
+    assert lines[0] == "     1   -0.1234568E-01   -0.1031385E+03   -0.1278761E-01"
+    assert bndlanz._e15(0.5) == "  0.5000000E+00"
+    assert bndlanz._e15(123.45678) == "  0.1234568E+03"
+    assert bndlanz._e15(0.99999999) == "  0.1000000E+01"
