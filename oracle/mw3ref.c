@@ -359,7 +359,20 @@ struct mw3ref {
     double *cvj;              /* [ncan][nj][nv] */
     cplx *zfe;                /* [nofe][ntot] */
     dstcache *caches;         /* one per thread */
+    struct prodproj *prod;    /* product-state projection (iprod = 2), or NULL */
 };
+
+/* the tables of the product-state projection (mod_coortrans01_02.f:21-22, 90-97,
+   255-260), 0-based copies; ranges inclusive as in the reference */
+typedef struct prodproj {
+    int n2p0, n2p1, a0, a1, om0, om1, jp0, jp1, vp0, vp1;
+    int32_t *nobcprod;        /* [njp] */
+    double *transrgjac;       /* [ntot] */
+    double *dtrans;           /* [ncan][nom][nang][n2p] */
+    double *prodwf;           /* [nom][njp][nvp][nelec][nang][n2p] */
+    double *cvjprod;          /* [nom][njp][nvp] */
+    cplx *zs2prod;            /* [nom][njp][nvp][netot] */
+} prodproj;
 
 static inline const double *DJ(const mw3ref *r, int iom, int ielec, int j, int iang)
 {
@@ -766,6 +779,10 @@ void mw3ref_destroy(mw3ref *r)
     free(r->zar1flux); free(r->ir1flux); free(r->fl_ang); free(r->fl_can); free(r->fl_r2); free(r->fl_idx); free(r->potiflux);
     free(r->zcr); free(r->zcdr); free(r->etot); free(r->reacfct); free(r->apaqini); free(r->s2factor);
     free(r->zck); free(r->zs2); free(r->cvj); free(r->zfe);
+    if (r->prod) {
+        free(r->prod->nobcprod); free(r->prod->transrgjac); free(r->prod->dtrans); free(r->prod->prodwf);
+        free(r->prod->cvjprod); free(r->prod->zs2prod); free(r->prod);
+    }
     free(r);
 }
 
@@ -1113,6 +1130,120 @@ static void fune(mw3ref *r, int64_t k)
     }
 }
 
+/* prodpaq (mod_coortrans01_02.f:694-788): psi_k binned on (block, angle, R)
+   with the weights transRgjac over the projection's R and angle ranges, then
+   Cvjprod(v,j,Omega) = sum over blocks and (angle, R) of
+   prodwf(R,angle,e,v,j,Omega) funprod(R,angle,block) dtrans(R,angle,Omega,block) */
+static void prodpaq(mw3ref *r)
+{
+    const mw3ref_in *in = &r->in;
+    prodproj *p = r->prod;
+    const int nc = r->nc, n2p = p->n2p1 - p->n2p0 + 1, nang = p->a1 - p->a0 + 1;
+    const int njp = p->jp1 - p->jp0 + 1, nvp = p->vp1 - p->vp0 + 1;
+    double *fun = (double *)calloc((size_t)nc * nang * n2p, sizeof(double));
+    double *aux = (double *)malloc(sizeof(double) * r->n2);
+    double *aux2 = (double *)malloc(sizeof(double) * (size_t)nang * n2p);
+    for (int b = 0; b < nc; b++)
+        for (int iang = p->a0; iang <= p->a1; iang++) {
+            for (int k = 0; k < r->n2; k++) aux[k] = 0.0;
+            int np = in->npunreal[iang - 1];
+            int64_t i0 = r->offs[(size_t)(iang - 1) * nc + b];
+            for (int ir = 0; ir < np; ir++) {
+                int ir2 = in->indr2[(size_t)(iang - 1) * in->npuntot + ir];
+                aux[ir2 - 1] = aux[ir2 - 1] + p->transrgjac[i0 + ir] * r->psi_k[i0 + ir];
+            }
+            for (int ir2 = p->n2p0; ir2 <= p->n2p1; ir2++)
+                fun[((size_t)b * nang + (iang - p->a0)) * n2p + (ir2 - p->n2p0)] = aux[ir2 - 1];
+        }
+    memset(p->cvjprod, 0, sizeof(double) * (size_t)(p->om1 - p->om0 + 1) * njp * nvp);
+    for (int b = 0; b < nc; b++) {
+        int ielec = in->nelebas[b];
+        for (int iom = p->om0; iom <= p->om1; iom++) {
+            const int o = iom - p->om0;
+            int jinip = p->jp0 > iom ? p->jp0 : iom;
+            const double *dt = p->dtrans + (((size_t)b * (p->om1 - p->om0 + 1) + o) * nang) * n2p;
+            const double *fb = fun + (size_t)b * nang * n2p;
+            for (size_t k = 0; k < (size_t)nang * n2p; k++) aux2[k] = fb[k] * dt[k];
+            for (int j = jinip; j <= p->jp1; j++)
+                for (int iv = p->vp0; iv <= p->nobcprod[j - p->jp0]; iv++) {
+                    const double *wf =
+                        p->prodwf + ((((size_t)o * njp + (j - p->jp0)) * nvp + (iv - p->vp0)) * in->nelec + (ielec - 1)) *
+                                        nang * n2p;
+                    double x = 0.0;
+                    for (size_t k = 0; k < (size_t)nang * n2p; k++) x = x + wf[k] * aux2[k];
+                    double *c = &p->cvjprod[((size_t)o * njp + (j - p->jp0)) * nvp + (iv - p->vp0)];
+                    *c = *c + x;
+                }
+        }
+    }
+    free(fun); free(aux); free(aux2);
+}
+
+/* prodcvj (mod_coortrans01_02.f:791-825): zS2prod(E,v,j,Omega) += Cvjprod C_k(E) */
+static void prodcvj(mw3ref *r)
+{
+    prodproj *p = r->prod;
+    const int netot = r->in.netot, njp = p->jp1 - p->jp0 + 1, nvp = p->vp1 - p->vp0 + 1;
+    for (int iom = p->om0; iom <= p->om1; iom++) {
+        int jinip = p->jp0 > iom ? p->jp0 : iom;
+        for (int j = jinip; j <= p->jp1; j++)
+            for (int iv = p->vp0; iv <= p->nobcprod[j - p->jp0]; iv++) {
+                size_t o = ((size_t)(iom - p->om0) * njp + (j - p->jp0)) * nvp + (iv - p->vp0);
+                double z = p->cvjprod[o];
+                for (int ie = 0; ie < netot; ie++) {
+                    cplx *s = &p->zs2prod[o * netot + ie];
+                    cplx ck = r->zck[ie];
+                    s->re = s->re + (z * ck.re - 0.0 * ck.im);
+                    s->im = s->im + (z * ck.im + 0.0 * ck.re);
+                }
+            }
+    }
+}
+
+int mw3ref_set_product(mw3ref *r, int n2prod0, int n2prod1, int nangproj0, int nangproj1, int iomminprod,
+                       int iommaxprod, int jiniprod, int jmaxprod, int nviniprod, int nvmaxprod,
+                       const int32_t *nobcprod, const double *transrgjac, const double *dtrans, const double *prodwf)
+{
+    if (n2prod0 < 1 || n2prod1 > r->n2 || n2prod1 < n2prod0 || nangproj0 < 1 || nangproj1 > r->na ||
+        nangproj1 < nangproj0 || iommaxprod < iomminprod || jmaxprod < jiniprod || nvmaxprod < nviniprod)
+        return 1;
+    for (int j = jiniprod; j <= jmaxprod; j++)
+        if (nobcprod[j - jiniprod] > nvmaxprod) return 1;
+    prodproj *p = (prodproj *)calloc(1, sizeof(prodproj));
+    p->n2p0 = n2prod0; p->n2p1 = n2prod1; p->a0 = nangproj0; p->a1 = nangproj1;
+    p->om0 = iomminprod; p->om1 = iommaxprod; p->jp0 = jiniprod; p->jp1 = jmaxprod;
+    p->vp0 = nviniprod; p->vp1 = nvmaxprod;
+    size_t n2p = n2prod1 - n2prod0 + 1, nang = nangproj1 - nangproj0 + 1, nom = iommaxprod - iomminprod + 1;
+    size_t njp = jmaxprod - jiniprod + 1, nvp = nvmaxprod - nviniprod + 1;
+    size_t ndt = (size_t)r->nc * nom * nang * n2p, nwf = nom * njp * nvp * r->in.nelec * nang * n2p;
+    p->nobcprod = (int32_t *)malloc(sizeof(int32_t) * njp);
+    memcpy(p->nobcprod, nobcprod, sizeof(int32_t) * njp);
+    p->transrgjac = (double *)malloc(sizeof(double) * r->ntot);
+    memcpy(p->transrgjac, transrgjac, sizeof(double) * r->ntot);
+    p->dtrans = (double *)malloc(sizeof(double) * ndt);
+    memcpy(p->dtrans, dtrans, sizeof(double) * ndt);
+    p->prodwf = (double *)malloc(sizeof(double) * nwf);
+    memcpy(p->prodwf, prodwf, sizeof(double) * nwf);
+    p->cvjprod = (double *)calloc(nom * njp * nvp, sizeof(double));
+    p->zs2prod = (cplx *)calloc(nom * njp * nvp * r->in.netot, sizeof(cplx));
+    if (r->prod) {
+        free(r->prod->nobcprod); free(r->prod->transrgjac); free(r->prod->dtrans); free(r->prod->prodwf);
+        free(r->prod->cvjprod); free(r->prod->zs2prod); free(r->prod);
+    }
+    r->prod = p;
+    return 0;
+}
+
+int mw3ref_get_product(const mw3ref *r, double *zs2prod, double *cvjprod)
+{
+    const prodproj *p = r->prod;
+    if (!p) return 1;
+    size_t n = (size_t)(p->om1 - p->om0 + 1) * (p->jp1 - p->jp0 + 1) * (p->vp1 - p->vp0 + 1);
+    if (zs2prod) memcpy(zs2prod, p->zs2prod, sizeof(cplx) * n * r->in.netot);
+    if (cvjprod) memcpy(cvjprod, p->cvjprod, sizeof(double) * n);
+    return 0;
+}
+
 int mw3ref_start(mw3ref *r, const double *psi0)
 {
     int64_t n = r->ntot;
@@ -1153,6 +1284,10 @@ int mw3ref_run(mw3ref *r, int nit, double *norms)
         mw3ref_coefecheby(r, it, (double *)r->zck);
         if (r->n1 > 1) totalflux_k(r, it);
         if (r->n2 > 1) cvjflux_k(r, it);
+        if (r->prod && r->n1 > 1 && r->n2 > 1) {
+            prodpaq(r);
+            prodcvj(r);
+        }
         if (norms) {
             double x = 0.0;
             for (int64_t i = 0; i < r->ntot; i++) x = x + r->psi_k[i] * r->psi_k[i];
@@ -1250,6 +1385,12 @@ int mw3ref_flux_tables(const mw3ref *r, double *etot, double *reacfct, double *a
     if (apaqini) memcpy(apaqini, r->apaqini, sizeof(double) * netot);
     if (zar1flux) memcpy(zar1flux, r->zar1flux, sizeof(cplx) * r->n1);
     if (ir4flux) *ir4flux = r->ir4flux;
+    return 0;
+}
+
+int mw3ref_s2factor(const mw3ref *r, double *s2factor)
+{
+    memcpy(s2factor, r->s2factor, sizeof(double) * (size_t)r->in.nelec * r->nj * r->nv * r->in.netot);
     return 0;
 }
 

@@ -107,6 +107,16 @@ int mw3ref_tables(const mw3ref *r, int32_t *nopr1, double *p2r1, double *p2r2,
                   double *absfr1, double *absfr2, int32_t *ir1abs_ir2abs);
 int mw3ref_flux_tables(const mw3ref *r, double *etot, double *reacfct, double *apaqini,
                        double *zar1flux, int32_t *ir4flux);
+int mw3ref_s2factor(const mw3ref *r, double *s2factor);  /* [nelec][nj][nv][netot] */
+/* product-state projection (iprod = 2, prodpaq/prodcvj): the tables ini_transcoor
+   builds, in the C order of the Fortran arrays: transrgjac[ntot],
+   dtrans[ncan][nom][nang][n2p], prodwf[nom][njp][nvp][nelec][nang][n2p],
+   nobcprod[njp]; results zs2prod[nom][njp][nvp][netot] complex, cvjprod[nom][njp][nvp] */
+int mw3ref_set_product(mw3ref *r, int n2prod0, int n2prod1, int nangproj0, int nangproj1, int iomminprod,
+                       int iommaxprod, int jiniprod, int jmaxprod, int nviniprod, int nvmaxprod,
+                       const int32_t *nobcprod, const double *transrgjac, const double *dtrans,
+                       const double *prodwf);
+int mw3ref_get_product(const mw3ref *r, double *zs2prod, double *cvjprod);
 int mw3ref_xj2(const mw3ref *r, double *xj2);    /* [ncan][nangu(jang)][nangu(iang)][npun1] */
 int mw3ref_xl2p(const mw3ref *r, double *xl2p);  /* [3][ncan][nangu][nangu][npun2] */
 /* Stand-alone restatements used by the known-answer tests against the

@@ -85,6 +85,9 @@ def lib():
         L.mw3ref_coefecheby.argtypes = [ct.c_void_p, ct.c_int64, F64P]
         L.mw3ref_tables.argtypes = [ct.c_void_p, I32P, F64P, F64P, F64P, F64P, I32P]
         L.mw3ref_flux_tables.argtypes = [ct.c_void_p, F64P, F64P, F64P, F64P, I32P]
+        L.mw3ref_s2factor.argtypes = [ct.c_void_p, F64P]
+        L.mw3ref_set_product.argtypes = [ct.c_void_p] + [ct.c_int] * 10 + [I32P, F64P, F64P, F64P]
+        L.mw3ref_get_product.argtypes = [ct.c_void_p, F64P, F64P]
         L.mw3ref_xj2.argtypes = [ct.c_void_p, F64P]
         L.mw3ref_xl2p.argtypes = [ct.c_void_p, F64P]
         L.mw3ref_dst1.argtypes = [ct.c_int, F64P, F64P, ct.c_int]
@@ -299,6 +302,31 @@ class Oracle:
         lib().mw3ref_flux_tables(self.h, _p(et, ct.c_double), _p(rf, ct.c_double), _p(ap, ct.c_double),
                                  _p(za, ct.c_double), ct.byref(ir4))
         return dict(etot=et, reacfct=rf, apaqini=ap, zar1flux=za[:, 0] + 1j * za[:, 1], ir4flux=ir4.value)
+
+    def set_product(self, pp):
+        """pp: ProductProjection (madwave3_gb300.product) with the tables of
+        ini_transcoor; the run then does prodpaq and prodcvj every iteration."""
+        self._prod = (np.ascontiguousarray(pp.nobcprod, np.int32), np.ascontiguousarray(pp.transrgjac, np.float64),
+                      np.ascontiguousarray(pp.dtrans, np.float64), np.ascontiguousarray(pp.prodwf, np.float64))
+        rc = lib().mw3ref_set_product(self.h, pp.n2prod0, pp.n2prod1, pp.nangproj0, pp.nangproj1, pp.iomminprod,
+                                      pp.iommaxprod, pp.jiniprod, pp.jmaxprod, pp.nviniprod, pp.nvmaxprod,
+                                      _p(self._prod[0], ct.c_int32), _p(self._prod[1], ct.c_double),
+                                      _p(self._prod[2], ct.c_double), _p(self._prod[3], ct.c_double))
+        if rc:
+            raise ValueError("bad product projection ranges")
+        self._prodshape = (pp.iommaxprod - pp.iomminprod + 1, pp.jmaxprod - pp.jiniprod + 1,
+                           pp.nvmaxprod - pp.nviniprod + 1)
+
+    def product(self):
+        z = np.zeros(self._prodshape + (self.netot, 2))
+        c = np.zeros(self._prodshape)
+        lib().mw3ref_get_product(self.h, _p(z, ct.c_double), _p(c, ct.c_double))
+        return z[..., 0] + 1j * z[..., 1], c
+
+    def s2factor(self):
+        out = np.zeros((self.run.nelec, self.nj, self.nv, self.netot))
+        lib().mw3ref_s2factor(self.h, _p(out, ct.c_double))
+        return out
 
     def xj2(self):
         r = self.run

@@ -8,7 +8,8 @@ Run once in a checkout where the reference is available:
 Sources (inside the reference): EXAMPLES/HD+H_collision/J000-check/sal.000
 (the log of the shipped J=0 run: its namelists, Gauss-Legendre angles,
 absorber start, kinetic energy range, collision packet, flux line, energy
-interval and the energy-domain norm of the packet) and
+interval and the energy-domain norm of the packet), the layout and first
+lines of the same run's S2prod.v00.J000.k00008, and
 EXAMPLES/HD+H_collision/README.md (the 60-angle list of its pot.out run).
 Only numbers that do not depend on the example's neural-network PES are kept.
 """
@@ -72,6 +73,11 @@ def main(ref):
         elif a60 and "..." in l:
             break
     out["angles_deg_60_head"] = a60
+    # the shipped run's S2prod file (iprod = 2): its layout and first lines, for
+    # the format of the probability files the post-processing programs read
+    s2p = open(os.path.join(ref, "EXAMPLES/HD+H_collision/J000-check/S2prod.v00.J000.k00008")).read().splitlines()
+    out["s2prod"] = {"file": "EXAMPLES/HD+H_collision/J000-check/S2prod.v00.J000.k00008",
+                     "lines": len(s2p), "columns": len(s2p[0].split()), "head": s2p[:3], "tail": s2p[-1:]}
     with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_pins.json"), "w") as f:
         json.dump(out, f, indent=1)
 
