@@ -203,6 +203,32 @@ int mw3_stage_times(mw3_ctx *ctx, double *ms, int64_t *iterations);
 #define MW3_NOALLOC_SCRATCH_BYTES (64u << 20)
 int mw3_hphi_noalloc(mw3_ctx *ctx, int32_t wave_id, const double *psi, double *hpsi);
 
+/* Product-state projection (iprod = 2): prodpaq and prodcvj
+ * (SRC/mod_coortrans01_02.f:694-825) every iteration of mw3_run, after the
+ * Cvj projection.  The tables are the ones ini_transcoor builds
+ * (SRC/mod_coortrans01_02.f:32-207, allocated at :90-97 and :255-260), passed
+ * in Fortran order like every other table; ranges are inclusive, R and angle
+ * indices 1-based.  Set before the context's device tables exist (before the
+ * first mw3_hphi / mw3_start / mw3_upload_state), else MW3_ERR_STATE. */
+typedef struct mw3_prodproj {
+    int32_t n2prod0, n2prod1;             /* R range of the projection */
+    int32_t nangproj0, nangproj1;         /* angle range */
+    int32_t iomminprod, iommaxprod;       /* product Omega range */
+    int32_t jiniprod, jmaxprod;           /* product j range */
+    int32_t nviniprod, nvmaxprod;         /* product v range */
+    const int32_t *nobcprod;              /* noBCprod(jiniprod:jmaxprod), each <= nvmaxprod */
+    const double *transrgjac;             /* transRgjac on the wave's state vector (mw3_wave_size doubles) */
+    const double *dtrans;                 /* dtrans(n2prod0:n2prod1,nangproj0:nangproj1,iomminprod:iommaxprod,ncan) */
+    const double *prodwf;                 /* prodwf(n2prod0:n2prod1,nangproj0:nangproj1,nelec,
+                                             nviniprod:nvmaxprod,jiniprod:jmaxprod,iomminprod:iommaxprod) */
+} mw3_prodproj;
+int mw3_set_product_projection(mw3_ctx *ctx, int32_t wave_id, const mw3_prodproj *proj);
+
+/* zS2prod(netot,nviniprod:nvmaxprod,jiniprod:jmaxprod,iomminprod:iommaxprod)
+ * complex as (re,im) pairs, and the last iteration's Cvjprod(v,j,Omega)
+ * (either may be NULL). */
+int mw3_download_product(mw3_ctx *ctx, int32_t wave_id, double *zs2prod, double *cvjprod);
+
 const char *mw3_last_error(const mw3_ctx *ctx);
 int mw3_destroy(mw3_ctx *ctx);
 

@@ -185,17 +185,9 @@ def write_levels(path, etrue, vcutmax):
 
 
 def _e15(x):
-    """Fortran e15.7: 0.ddddddd E+xx mantissa form, right-aligned in 15."""
-    if x == 0.0:
-        return "%15s" % "0.0000000E+00"
-    m, ex = "%.6E" % abs(x), 0
-    # the reference's form has a leading "0." and the exponent one larger
-    mant = float(m.split("E")[0]) / 10.0
-    ex = int(m.split("E")[1]) + 1
-    s = "%.7fE%+03d" % (mant, ex)
-    if mant >= 1.0:                     # rounding carried: 0.99999995 -> 1.0000000
-        s = "%.7fE%+03d" % (mant / 10.0, ex + 1)
-    return "%15s" % (("-" if x < 0 else "") + s)
+    """Fortran e15.7."""
+    from .printprob import fortran_e
+    return fortran_e(x, 15, 7, 2)
 
 
 class BoundStates:

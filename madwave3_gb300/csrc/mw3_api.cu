@@ -516,6 +516,47 @@ int build_device(Ctx &c)
     TRY(dupload(c, &c.d_zfe_ptrs, zfeptr));
     TRY(dupload(c, &c.d_norm_ptrs, normptr));
     TRY(dupload(c, &c.d_norm_cap, normcap));
+    // ---- product-state projections (prodpaq / prodcvj) ----
+    for (int w = 0; w < W && w < (int)c.prodt.size(); w++) {
+        const mw3::ProdTables &pt = c.prodt[w];
+        if (!pt.on) continue;
+        WaveTables &t = c.waves[w];
+        mw3::ProdDev &d = c.wdev[w].prod;
+        const int nc = t.ncan, nang = pt.a1 - pt.a0 + 1, n2p = pt.n2p1 - pt.n2p0 + 1;
+        std::vector<int> ptr(1, 0);
+        std::vector<int64_t> idx;
+        std::vector<double> wt;
+        std::vector<std::vector<int>> byr2((size_t)n2p);
+        for (int b = 0; b < nc; b++)
+            for (int iang = pt.a0; iang <= pt.a1; iang++) {
+                for (auto &v : byr2) v.clear();
+                const int np = c.npunreal[iang - 1];
+                for (int ir = 0; ir < np; ir++) {
+                    const int ir2 = c.indr2[(size_t)(iang - 1) * c.npt + ir];
+                    if (ir2 >= pt.n2p0 && ir2 <= pt.n2p1) byr2[ir2 - pt.n2p0].push_back(ir);
+                }
+                const int64_t o = t.offs[(size_t)(iang - 1) * nc + b];
+                for (int k = 0; k < n2p; k++) {
+                    for (int ir : byr2[k]) {
+                        idx.push_back(t.flat0 + o + ir);
+                        wt.push_back(pt.transrgjac[o + ir]);
+                    }
+                    ptr.push_back((int)idx.size());
+                }
+            }
+        d.nbins = nc * nang * n2p;
+        d.nrow = (pt.om1 - pt.om0 + 1) * (pt.jp1 - pt.jp0 + 1) * (pt.vp1 - pt.vp0 + 1);
+        TRY(dupload(c, &d.bin_ptr, ptr));
+        TRY(dupload(c, &d.bin_idx, idx));
+        TRY(dupload(c, &d.bin_w, wt));
+        TRY(dalloc(c, &d.fun, (size_t)d.nbins));
+        TRY(dupload(c, &d.dtrans, pt.dtrans));
+        TRY(dupload(c, &d.prodwf, pt.prodwf));
+        TRY(dupload(c, &d.nobcprod, pt.nobcprod));
+        TRY(dupload(c, &d.blk_elec, t.nelebas));
+        TRY(dalloc(c, &d.cvjprod, (size_t)d.nrow));
+        TRY(dalloc(c, &d.zs2prod, (size_t)d.nrow * c.netot * 2));
+    }
     // ---- typed tables ----
     mw3::set_kernel_attributes(c);
     TRY(mw3::build_tc_ang(c));
@@ -655,6 +696,11 @@ int reset_accumulators(Ctx &c)
         WaveTables &t = c.waves[w];
         WaveDev &d = c.wdev[w];
         if (d.zfe) MW3_CUDA_TRY(cudaMemsetAsync(d.zfe, 0, sizeof(double) * 2 * (size_t)t.nofe * t.ntot, c.stream));
+        if (d.prod.zs2prod) {
+            MW3_CUDA_TRY(cudaMemsetAsync(d.prod.zs2prod, 0, sizeof(double) * 2 * (size_t)d.prod.nrow * c.netot,
+                                         c.stream));
+            MW3_CUDA_TRY(cudaMemsetAsync(d.prod.cvjprod, 0, sizeof(double) * (size_t)d.prod.nrow, c.stream));
+        }
     }
     return MW3_OK;
 }
@@ -1162,6 +1208,62 @@ int mw3_stage_times(mw3_ctx *h, double *ms, int64_t *iterations)
     if (iterations) *iterations = c.prof_n;
     c.prof_n = 0;
     return MW3_OK;
+}
+
+int mw3_set_product_projection(mw3_ctx *h, int32_t w, const mw3_prodproj *p)
+{
+    if (!h || !p) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) return MW3_ERR_ARG;
+    if (c.built) {
+        c.err = "mw3_set_product_projection: set it before the device tables are built";
+        return MW3_ERR_STATE;
+    }
+    if (!p->nobcprod || !p->transrgjac || !p->dtrans || !p->prodwf) return MW3_ERR_ARG;
+    if (p->n2prod0 < 1 || p->n2prod1 < p->n2prod0 || p->n2prod1 > c.n2 || p->nangproj0 < 1 ||
+        p->nangproj1 < p->nangproj0 || p->nangproj1 > c.na || p->iommaxprod < p->iomminprod ||
+        p->jmaxprod < p->jiniprod || p->nvmaxprod < p->nviniprod || p->iomminprod < 0)
+        return MW3_ERR_ARG;
+    const WaveTables &t = c.waves[w];
+    const size_t n2p = p->n2prod1 - p->n2prod0 + 1, nang = p->nangproj1 - p->nangproj0 + 1;
+    const size_t nom = p->iommaxprod - p->iomminprod + 1, njp = p->jmaxprod - p->jiniprod + 1;
+    const size_t nvp = p->nvmaxprod - p->nviniprod + 1;
+    if ((double)nom * njp * nvp * c.netot > 2.0e9 || (double)t.ncan * nang * n2p > 2.0e9) return MW3_ERR_ARG;
+    for (size_t j = 0; j < njp; j++)
+        if (p->nobcprod[j] > p->nvmaxprod) return MW3_ERR_ARG;
+    if (c.prodt.size() < c.waves.size()) c.prodt.resize(c.waves.size());
+    mw3::ProdTables &pt = c.prodt[w];
+    pt.on = true;
+    pt.n2p0 = p->n2prod0; pt.n2p1 = p->n2prod1; pt.a0 = p->nangproj0; pt.a1 = p->nangproj1;
+    pt.om0 = p->iomminprod; pt.om1 = p->iommaxprod; pt.jp0 = p->jiniprod; pt.jp1 = p->jmaxprod;
+    pt.vp0 = p->nviniprod; pt.vp1 = p->nvmaxprod;
+    pt.nobcprod.assign(p->nobcprod, p->nobcprod + njp);
+    pt.transrgjac.assign(p->transrgjac, p->transrgjac + t.ntot);
+    pt.dtrans.assign(p->dtrans, p->dtrans + (size_t)t.ncan * nom * nang * n2p);
+    pt.prodwf.assign(p->prodwf, p->prodwf + nom * njp * nvp * (size_t)c.ne * nang * n2p);
+    return MW3_OK;
+}
+
+int mw3_download_product(mw3_ctx *h, int32_t w, double *zs2prod, double *cvjprod)
+{
+    if (!h) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) return MW3_ERR_ARG;
+    if (w >= (int)c.prodt.size() || !c.prodt[w].on) {
+        c.err = "mw3_download_product: the wave has no product projection";
+        return MW3_ERR_STATE;
+    }
+    int rc = build_device(c);
+    if (rc) return rc;
+    const mw3::ProdDev &d = c.wdev[w].prod;
+    if (zs2prod)
+        MW3_CUDA_TRY(cudaMemcpyAsync(zs2prod, d.zs2prod, sizeof(double) * 2 * (size_t)d.nrow * c.netot,
+                                     cudaMemcpyDeviceToHost, c.stream));
+    if (cvjprod)
+        MW3_CUDA_TRY(cudaMemcpyAsync(cvjprod, d.cvjprod, sizeof(double) * (size_t)d.nrow, cudaMemcpyDeviceToHost,
+                                     c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return check_device_flags(c, "mw3_download_product");
 }
 
 const char *mw3_last_error(const mw3_ctx *h)

@@ -72,6 +72,31 @@ struct WaveTables {
 };
 
 // device pointers of one wave
+// product-state projection of one wave (iprod = 2; prodpaq / prodcvj): the host's
+// tables as given to mw3_set_product_projection
+struct ProdTables {
+    bool on = false;
+    int n2p0 = 0, n2p1 = 0, a0 = 0, a1 = 0, om0 = 0, om1 = 0, jp0 = 0, jp1 = 0, vp0 = 0, vp1 = 0;
+    std::vector<int> nobcprod;                   // [njp]
+    std::vector<double> transrgjac;              // [ntot]
+    std::vector<double> dtrans;                  // [ncan][nom][nang][n2p]
+    std::vector<double> prodwf;                  // [nom][njp][nvp][nelec][nang][n2p]
+};
+
+// its device side: the points of every (block, angle, R) bin as a CSR list in
+// the reference's summation order, the tables, and the results
+struct ProdDev {
+    int nbins = 0, nrow = 0;                     // bins = ncan nang n2p; rows = nom njp nvp
+    int *bin_ptr = nullptr;                      // [nbins + 1]
+    int64_t *bin_idx = nullptr;                  // context-wide flat index of each term
+    double *bin_w = nullptr;                     // its transRgjac
+    double *fun = nullptr;                       // funprod [ncan][nang][n2p]
+    double *dtrans = nullptr, *prodwf = nullptr;
+    int *nobcprod = nullptr, *blk_elec = nullptr;
+    double *cvjprod = nullptr;                   // [nrow]
+    double *zs2prod = nullptr;                   // [nrow][netot][2]
+};
+
 struct WaveDev {
     double *norms = nullptr;                     // norm trace
     int64_t norms_cap = 0;
@@ -85,6 +110,7 @@ struct WaveDev {
     int *nobc = nullptr, *r2abs_map = nullptr;
     double *djmmp = nullptr;                     // wave's Djmmp
     double *efe = nullptr, *zfe = nullptr;       // PsiE
+    ProdDev prod;                                // product-state projection, if set
 };
 
 // one CTA of the update kernel: a non-empty (segment, point chunk) pair with
@@ -117,6 +143,7 @@ struct Ctx {
 
     std::vector<WaveTables> waves;
     std::vector<WaveDev> wdev;
+    std::vector<ProdTables> prodt;   // per wave (empty or .on = false: no projection)
 
     // context-wide block list (all waves)
     int G = 0;                       // total blocks
@@ -332,6 +359,8 @@ constexpr int kFluxSlots = 128;     // flux ring: iterations in each accumulated
 void launch_norms(Ctx &c, int64_t slot);
 // writes the context's iteration and norm slot where a graph replay reads them
 void launch_set_itbase(Ctx &c);
+// prodpaq + prodcvj of every wave that has a product projection
+void launch_product(Ctx &c);
 constexpr int kGraphIters = 32;      // iterations per captured graph (one ring cycle)
 static_assert(kFluxRing == kGraphIters, "a captured block must cycle the Cvj ring exactly once");
 static_assert(kGraphIters % (kFluxSlots / 4) == 0, "flux slice flushes must repeat with the captured block");

@@ -833,22 +833,43 @@ __global__ void __launch_bounds__(256) k_flux_flush(const float *__restrict__ fr
 #pragma unroll
         for (int j = 0; j < 4; j++) ar[i][j] = ai[i][j] = br[i][j] = bi[i][j] = 0.f;
     for (int s0 = 0; s0 < kFluxSlots; s0 += kFlushS) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < kFlushS * kFlushE * 2; i += blockDim.x) {
-            int s = i / (kFlushE * 2), r = i % (kFlushE * 2);
-            int e = e0 + r / 2;
-            sc[s][r / 2][r & 1] = e < netot ? cring[((size_t)(s0 + s) * netot + e) * 2 + (r & 1)] : 0.f;
+        // the tile's 4-byte pieces by cp.async (zero-filled outside the slice or the
+        // energies), all in flight at once
+        constexpr int kNC = kFlushS * kFlushE * 2 / 256, kNP = kFlushS * kFlushF * 3 / 256;
+        const uint32_t sc_s = (uint32_t)__cvta_generic_to_shared(&sc[0][0][0]);
+        const uint32_t sp_s = (uint32_t)__cvta_generic_to_shared(&sp[0][0][0]);
+        __syncthreads();            // the previous chunk's reads of sc / sp are done
+#pragma unroll 4
+        for (int k = 0; k < kNC; k++) {
+            const int i = threadIdx.x + 256 * k, s = i / (kFlushE * 2), r = i % (kFlushE * 2);
+            const int e = e0 + r / 2;
+            const bool ok = e < netot;
+            const float *src = ok ? cring + ((size_t)(s0 + s) * netot + e) * 2 + (r & 1) : cring;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(sc_s + 4 * i), "l"(src),
+                         "r"(ok ? 4 : 0)
+                         : "memory");
         }
-        for (int i = threadIdx.x; i < kFlushS * kFlushF * 3; i += blockDim.x) {
-            int s = i / (kFlushF * 3), r = i % (kFlushF * 3);
-            int f = f0 + r / 3;
-            float v = f < f1 ? fring[((size_t)(s0 + s) * NF + f) * 3 + r % 3] : 0.f;
-            if (final_ && f < f1) {
+#pragma unroll 4
+        for (int k = 0; k < kNP; k++) {
+            const int i = threadIdx.x + 256 * k, s = i / (kFlushF * 3), r = i % (kFlushF * 3);
+            const int f = f0 + r / 3;
+            const bool ok = f < f1;
+            const float *src = ok ? fring + ((size_t)(s0 + s) * NF + f) * 3 + r % 3 : fring;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(sp_s + 4 * i), "l"(src),
+                         "r"(ok ? 4 : 0)
+                         : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (final_) {               // this thread's own pieces outside its slice's window
+            for (int k = 0; k < kNP; k++) {
+                const int i = threadIdx.x + 256 * k, s = i / (kFlushF * 3), r = i % (kFlushF * 3);
+                const int f = f0 + r / 3;
+                if (f >= f1) continue;
                 const int p = f / chunk;
                 const int np = ((nowm - p * q - q + 1) % kFluxSlots + kFluxSlots) % kFluxSlots;
-                if ((nowm - (s0 + s) + kFluxSlots) % kFluxSlots >= np) v = 0.f;
+                if ((nowm - (s0 + s) + kFluxSlots) % kFluxSlots >= np) sp[s][r / 3][r % 3] = 0.f;
             }
-            sp[s][r / 3][r % 3] = v;
         }
         __syncthreads();
         for (int s = 0; s < kFlushS; s++) {
@@ -1514,6 +1535,94 @@ void launch_accumulators(Ctx &c, int64_t it)
         LAUNCH_CHECK(c);
         int64_t tot = (int64_t)c.G * c.nj * c.nv * c.netot;
         k_cvj_acc<<<(unsigned)((tot + 255) / 256), 256, 0, c.stream>>>(d, a);
+        LAUNCH_CHECK(c);
+    }
+    // prodpaq + prodcvj (main_madwave3.f:346-349), after Cvjflux_k
+    if (c.n1 > 1 && c.n2 > 1) launch_product(c);
+}
+
+// ---------------------------------------------------------------------------
+// Product-state projection (iprod = 2), mod_coortrans01_02.f:694-825
+// ---------------------------------------------------------------------------
+// prodpaq, step 1: funprod(R, angle, block) = sum of transRgjac psi over the
+// stored points of (block, angle) at R, in the points' order; one thread per bin
+__global__ void __launch_bounds__(256) k_prod_bins(const double *__restrict__ psi, const int *__restrict__ bin_ptr,
+                                                   const int64_t *__restrict__ bin_idx,
+                                                   const double *__restrict__ bin_w, int nbins,
+                                                   double *__restrict__ fun)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbins) return;
+    double s = 0.0;
+    for (int k = bin_ptr[b]; k < bin_ptr[b + 1]; k++) s = s + bin_w[k] * psi[bin_idx[k]];
+    fun[b] = s;
+}
+
+// prodpaq, step 2: Cvjprod(v, j, Omega) = sum over blocks and (angle, R) of
+// prodwf(R, angle, e, v, j, Omega) (funprod dtrans(R, angle, Omega, block)); one
+// warp per (Omega, j, v), 0 outside j >= max(jiniprod, Omega), v <= noBCprod(j)
+__global__ void __launch_bounds__(256) k_prod_proj(const double *__restrict__ fun, const double *__restrict__ dtrans,
+                                                   const double *__restrict__ prodwf,
+                                                   const int *__restrict__ nobcprod,
+                                                   const int *__restrict__ blk_elec, int ncan, int nelec, int K,
+                                                   int om0, int nom, int jp0, int njp, int vp0, int nvp,
+                                                   double *__restrict__ cvjprod)
+{
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (row >= nom * njp * nvp) return;                 // whole warps
+    const int o = row / (njp * nvp), jj = (row / nvp) % njp, vv = row % nvp;
+    const bool on = jp0 + jj >= max(jp0, om0 + o) && vp0 + vv <= nobcprod[jj];
+    double x = 0.0;
+    if (on) {
+        for (int b = 0; b < ncan; b++) {
+            const double *wf = prodwf + ((((size_t)o * njp + jj) * nvp + vv) * nelec + (blk_elec[b] - 1)) * K;
+            const double *dt = dtrans + ((size_t)b * nom + o) * K;
+            const double *fb = fun + (size_t)b * K;
+            for (int k = lane; k < K; k += 32) x += wf[k] * (fb[k] * dt[k]);
+        }
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) x += __shfl_xor_sync(0xffffffffu, x, m);
+    }
+    if (lane == 0) cvjprod[row] = x;
+}
+
+// prodcvj: zS2prod(E, v, j, Omega) += Cvjprod C_k(E); one thread per (row, E)
+__global__ void __launch_bounds__(256) k_prod_acc(const double *__restrict__ cvjprod, const double *__restrict__ zck,
+                                                  const int *__restrict__ nobcprod, int om0, int jp0, int njp,
+                                                  int vp0, int nvp, int nrow, int netot,
+                                                  double *__restrict__ zs2prod)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nrow * netot) return;
+    const int row = (int)(t / netot), ie = (int)(t % netot);
+    const int o = row / (njp * nvp), jj = (row / nvp) % njp, vv = row % nvp;
+    if (jp0 + jj < max(jp0, om0 + o) || vp0 + vv > nobcprod[jj]) return;
+    const double z = cvjprod[row];
+    double2 *s = reinterpret_cast<double2 *>(zs2prod) + t;
+    double2 a = *s;
+    a.x = a.x + (z * zck[2 * ie] - 0.0 * zck[2 * ie + 1]);
+    a.y = a.y + (z * zck[2 * ie + 1] + 0.0 * zck[2 * ie]);
+    *s = a;
+}
+
+void launch_product(Ctx &c)
+{
+    for (size_t w = 0; w < c.wdev.size() && w < c.prodt.size(); w++) {
+        const ProdTables &pt = c.prodt[w];
+        if (!pt.on) continue;
+        const ProdDev &d = c.wdev[w].prod;
+        const int nom = pt.om1 - pt.om0 + 1, njp = pt.jp1 - pt.jp0 + 1, nvp = pt.vp1 - pt.vp0 + 1;
+        const int K = (pt.a1 - pt.a0 + 1) * (pt.n2p1 - pt.n2p0 + 1);
+        k_prod_bins<<<(d.nbins + 255) / 256, 256, 0, c.stream>>>(c.d_pk, d.bin_ptr, d.bin_idx, d.bin_w, d.nbins,
+                                                                d.fun);
+        LAUNCH_CHECK(c);
+        k_prod_proj<<<(d.nrow * 32 + 255) / 256, 256, 0, c.stream>>>(d.fun, d.dtrans, d.prodwf, d.nobcprod,
+                                                                    d.blk_elec, c.waves[w].ncan, c.ne, K, pt.om0,
+                                                                    nom, pt.jp0, njp, pt.vp0, nvp, d.cvjprod);
+        LAUNCH_CHECK(c);
+        const int64_t n = (int64_t)d.nrow * c.netot;
+        k_prod_acc<<<(unsigned)((n + 255) / 256), 256, 0, c.stream>>>(d.cvjprod, c.d_zck, d.nobcprod, pt.om0, pt.jp0,
+                                                                      njp, pt.vp0, nvp, d.nrow, c.netot, d.zs2prod);
         LAUNCH_CHECK(c);
     }
 }

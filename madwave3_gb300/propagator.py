@@ -68,7 +68,8 @@ HEADER_FUNCS = [
     "mw3_norms", "mw3_totalflux", "mw3_flux_count",
     "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_path_flags", "mw3_get_stream",
     "mw3_profile",
-    "mw3_stage_times", "mw3_hphi_noalloc", "mw3_last_error", "mw3_destroy",
+    "mw3_stage_times", "mw3_hphi_noalloc", "mw3_set_product_projection", "mw3_download_product",
+    "mw3_last_error", "mw3_destroy",
 ]
 # stage 0 holds the whole radial DST chain when the mixed path runs it as one
 # fused kernel (stages 1 and 2 are then empty); stage 3 is the whole angular
@@ -117,6 +118,8 @@ def load_library(build_if_missing=True):
     L.mw3_get_stream.argtypes = [vp, ct.POINTER(ct.c_void_p)]
     L.mw3_profile.argtypes = [vp, ct.c_int]
     L.mw3_stage_times.argtypes = [vp, F64P, ct.POINTER(ct.c_int64)]
+    L.mw3_set_product_projection.argtypes = [vp, ct.c_int32, ct.POINTER(ProdProj)]
+    L.mw3_download_product.argtypes = [vp, ct.c_int32, F64P, F64P]
     L.mw3_last_error.argtypes = [vp]
     L.mw3_last_error.restype = ct.c_char_p
     L.mw3_destroy.argtypes = [vp]
@@ -126,6 +129,13 @@ def load_library(build_if_missing=True):
 
 def _p(a, typ=ct.c_double):
     return a.ctypes.data_as(ct.POINTER(typ))
+
+
+class ProdProj(ct.Structure):
+    """mw3_prodproj"""
+    _fields_ = [(n, ct.c_int32) for n in ("n2prod0", "n2prod1", "nangproj0", "nangproj1", "iomminprod",
+                                          "iommaxprod", "jiniprod", "jmaxprod", "nviniprod", "nvmaxprod")] + \
+               [("nobcprod", I32P), ("transrgjac", F64P), ("dtrans", F64P), ("prodwf", F64P)]
 
 
 class Propagator:
@@ -238,6 +248,27 @@ class Propagator:
         arrs = [np.ascontiguousarray(p, np.float64) for p in psi0s]
         ptrs = (F64P * len(arrs))(*[_p(a) for a in arrs])
         self._check(self.L.mw3_start(self.h, ptrs), "mw3_start")
+
+    def set_product_projection(self, pp, wave=0):
+        """prodpaq / prodcvj every iteration for this wave (iprod = 2); pp is a
+        madwave3_gb300.product.ProductProjection.  Before the first hphi/start."""
+        keep = (np.ascontiguousarray(pp.nobcprod, np.int32), np.ascontiguousarray(pp.transrgjac, np.float64),
+                np.ascontiguousarray(pp.dtrans, np.float64), np.ascontiguousarray(pp.prodwf, np.float64))
+        s = ProdProj(pp.n2prod0, pp.n2prod1, pp.nangproj0, pp.nangproj1, pp.iomminprod, pp.iommaxprod,
+                     pp.jiniprod, pp.jmaxprod, pp.nviniprod, pp.nvmaxprod, _p(keep[0], ct.c_int32), _p(keep[1]),
+                     _p(keep[2]), _p(keep[3]))
+        self._check(self.L.mw3_set_product_projection(self.h, wave, ct.byref(s)), "mw3_set_product_projection")
+        if not hasattr(self, "_prodshape"):
+            self._prodshape = {}
+        self._prodshape[wave] = pp.shape
+
+    def product(self, wave=0):
+        """(zS2prod [nom][njp][nvp][netot] complex, last Cvjprod [nom][njp][nvp])."""
+        shp = self._prodshape[wave]
+        z = np.empty(shp + (self.runs[wave].inp.netot, 2))
+        c = np.empty(shp)
+        self._check(self.L.mw3_download_product(self.h, wave, _p(z), _p(c)), "mw3_download_product")
+        return z[..., 0] + 1j * z[..., 1], c
 
     def upload_state(self, wave, psi_km1, psi_k, it):
         a = np.ascontiguousarray(psi_km1, np.float64)

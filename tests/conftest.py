@@ -29,3 +29,26 @@ def case_dirs(tmp_path_factory):
 def runs(case_dirs):
     from madwave3_gb300.host import setup
     return {k: setup.load(os.path.join(d, "input.dat")) for k, d in case_dirs.items()}
+
+
+def synthetic_product_tables(run, seed=20261203):
+    """Seeded product-projection tables for a generated case (the parity of
+    prodpaq / prodcvj is pure arithmetic on whatever ini_transcoor produced)."""
+    import numpy as np
+    from madwave3_gb300.product import ProductProjection
+
+    rng = np.random.default_rng(seed)
+    i = run.inp
+    n2p0, n2p1 = 3, max(3, i.npun2 - 4)
+    a0, a1 = 2, max(2, i.nangu - 1)
+    om0, om1 = 0, min(2, i.Jtot)
+    jp0, jp1 = 0, 5
+    vp0, vp1 = 0, 2
+    nobc = rng.integers(vp0, vp1 + 1, size=jp1 - jp0 + 1).astype(np.int32)
+    nom, njp, nvp = om1 - om0 + 1, jp1 - jp0 + 1, vp1 - vp0 + 1
+    nang, n2p = a1 - a0 + 1, n2p1 - n2p0 + 1
+    return ProductProjection(
+        n2p0, n2p1, a0, a1, om0, om1, jp0, jp1, vp0, vp1, nobc,
+        rng.uniform(0.5, 1.5, run.ntot),
+        rng.uniform(-1.0, 1.0, (run.ncan, nom, nang, n2p)),
+        rng.standard_normal((nom, njp, nvp, run.nelec, nang, n2p)))
