@@ -4,20 +4,24 @@ reference's formats, so the post-processing programs of
 SRC/AUXILIARy-CODES (sigmaFromS2prod, CRP-fast, ...) read them unchanged.
 
 Written for the collision workloads (iphoto = 0, photonorm = 1,
-mod_flux_01y2.f:416) with a diatom (xm2 > 1e-3) and iprod = 0 or 1:
+mod_flux_01y2.f:416) with a diatom (xm2 > 1e-3) and iprod = 0, 1 or 2:
 
 * ``S2prod.vVV.JJJJ.kKKKKK``, one line per energy, format (501(1x,e17.7e3)):
   iprod = 0: E (eV), P(E) (S2prodtot), P(E) + S2reac, reacfct(E)
   (main_madwave3.f:712-716); iprod = 1: E, S2reac, P(E) + S2reac, then the
-  vibrational distribution of every electronic state (:719-725).
+  vibrational distribution of every electronic state (:719-725); iprod = 2
+  (product projection, one product electronic state or diabatic products,
+  :734-741): E, P(E), P(E) + S2reac, S2no, the product v' distribution, from
+  zS2prod with S2pro(v,j,Omega) = |zS2prod|^2 / (4 pi^2) S2prodfac(E,v,j)
+  (:669-684).
 * ``S2prodelec``: E and the per-electronic-state P(E) (:717-718, :726-727).
 
 S2reac(E) is the sum over the reactant-channel elements
 S2(v,j,block) = |zS2(E,v,j,block) / 2 pi|^2 S2factor(E,v,j,e) for j = j00(block)
 ..jmax step inc and v = nvini..noBCstates(j,e) (:640-652).  Values below 1e-90
-are written as 0 (:700-705).  iprod = 2 needs the product projection
-(prodpaq/prodcvj) and the diatom-only case has its own H psi; neither is
-written here.
+are written as 0 (:700-705).  The diatom-only case and the adiabatic
+product assignment of iprod = 2 with several product states (vibelecprod)
+are not written here.
 """
 import os
 
@@ -68,18 +72,41 @@ def s2_elements(run, zs2, s2factor):
     return out
 
 
-def write_s2prod(outdir, run, iloop, s2prodtot, s2prodelec, zs2, etot, reacfct, s2factor, nvmaxprod=None):
+def s2prod_products(zs2prod, s2prodfac, pp):
+    """S2pro summed over Omega and j into (S2no(E), vibprod(v', E)) for iprod = 2
+    (main_madwave3.f:669-684).  zs2prod [nom][njp][nvp][netot] complex (the
+    library's mw3_download_product), s2prodfac [njp][nvp][netot]."""
+    z = np.asarray(zs2prod)
+    a = (z.real * z.real + z.imag * z.imag) * 0.25 / (pi * pi) * np.asarray(s2prodfac)[None]
+    nom, njp, nvp = pp.shape
+    mask = np.zeros((njp, nvp), bool)
+    for jj in range(njp):
+        mask[jj, : int(pp.nobcprod[jj]) - pp.nviniprod + 1] = True
+    a = a * mask[None, :, :, None]
+    return a.sum(axis=(0, 1, 2)), a.sum(axis=(0, 1))
+
+
+def write_s2prod(outdir, run, iloop, s2prodtot, s2prodelec, zs2, etot, reacfct, s2factor, nvmaxprod=None,
+                 iprod=None, product=None):
     """Writes S2prod.vVV.JJJJ.kKKKKK and S2prodelec for one loop; returns the
     S2prod path.  Arguments as the library returns them (``Propagator.totalflux``,
-    ``.accumulators()['zs2']``, ``.tables()``)."""
+    ``.accumulators()['zs2']``, ``.tables()``); iprod defaults to the run's,
+    and iprod = 2 takes product = (zs2prod, s2prodfac, ProductProjection)."""
     i = run.inp
-    if run.inp.iprod not in (0, 1):
-        raise ValueError("printprob is written for iprod = 0 or 1")
+    iprod = run.inp.iprod if iprod is None else iprod
+    if iprod not in (0, 1, 2):
+        raise ValueError("printprob is written for iprod = 0, 1 or 2")
     s2 = s2_elements(run, np.asarray(zs2), np.asarray(s2factor))
     s2reac = s2.sum(axis=(0, 1, 2))
     nelec = run.nelec
     vib = None
-    if run.inp.iprod == 1:
+    if iprod == 2:
+        if product is None:
+            raise ValueError("iprod = 2 needs product = (zs2prod, s2prodfac, projection)")
+        s2no, vib = s2prod_products(*product)
+        s2no = np.where(s2no < 1e-90, 0.0, s2no)
+        vib = np.where(vib < 1e-90, 0.0, vib)
+    if iprod == 1:
         if nvmaxprod is None:
             raise ValueError("iprod = 1 needs nvmaxprod (&inputprod)")
         vtop = min(nvmaxprod, i.nvmax)
@@ -97,8 +124,10 @@ def write_s2prod(outdir, run, iloop, s2prodtot, s2prodelec, zs2, etot, reacfct, 
     e_ev = np.asarray(etot) / conve1 / eV2cm
     with open(name, "w") as f, open(os.path.join(outdir, "S2prodelec"), "w") as fe:
         for ie in range(len(etot)):
-            if run.inp.iprod == 0:
+            if iprod == 0:
                 f.write(_line([e_ev[ie], tot[ie], tot[ie] + s2reac[ie], reacfct[ie]]))
+            elif iprod == 2:
+                f.write(_line([e_ev[ie], tot[ie], tot[ie] + s2reac[ie], s2no[ie]] + list(vib[:, ie])))
             else:
                 f.write(_line([e_ev[ie], s2reac[ie], tot[ie] + s2reac[ie]] + list(vib[:, :, ie].ravel())))
             fe.write(_line([e_ev[ie]] + [s2prodelec[e][ie] for e in range(nelec)]))

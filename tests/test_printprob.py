@@ -72,3 +72,43 @@ def test_s2prod_from_oracle(runs, tmp_path):
     b = printprob.read_s2prod(os.path.join(str(tmp_path), "S2prodelec"))
     assert b.shape == (i.netot, 1 + run.nelec)
     np.testing.assert_allclose(b[:, 1:], el.T, rtol=5.01e-7, atol=1e-300)
+
+
+def test_s2prod_iprod2_layout_matches_the_shipped_file(runs, tmp_path):
+    """iprod = 2 from the oracle's product projection (seeded tables with
+    v' = 0..10, as in the shipped run): 15 columns like the reference's
+    S2prod.v00.J000.k00008; S2no and the v' columns are the S2pro sums."""
+    from dataclasses import replace
+
+    from conftest import synthetic_product_tables
+    from oracle.mw3ref import Oracle
+
+    g = json.load(open(GOLDEN))["s2prod"]
+    run = runs["tiny_j3"]
+    i = run.inp
+    pp = synthetic_product_tables(run)
+    rng = np.random.default_rng(7)
+    njp = pp.jmaxprod - pp.jiniprod + 1
+    pp = replace(pp, nvmaxprod=10, nobcprod=rng.integers(0, 11, njp).astype(np.int32),
+                 prodwf=rng.standard_normal(pp.prodwf.shape[:2] + (11,) + pp.prodwf.shape[3:]))
+    o = Oracle(run)
+    o.set_product(pp)
+    o.start(run.psi0)
+    o.run_iters(20)
+    zp, _ = o.product()
+    fac = rng.uniform(0.5, 2.0, (njp, 11, i.netot))
+    tot, el = o.totalflux()
+    zs2, _ = o.s2()
+    ft = o.flux_tables()
+    path = printprob.write_s2prod(str(tmp_path), run, 3, tot, el, zs2, ft["etot"], ft["reacfct"], o.s2factor(),
+                                  iprod=2, product=(zp, fac, pp))
+    a = printprob.read_s2prod(path)
+    assert a.shape == (i.netot, g["columns"])
+    s2pro = np.abs(zp) ** 2 / (4 * pi * pi) * fac[None]
+    for jj in range(njp):
+        s2pro[:, jj, pp.nobcprod[jj] + 1:] = 0
+    vib = s2pro.sum(axis=(0, 1))
+    vib = np.where(vib < 1e-90, 0, vib)
+    np.testing.assert_allclose(a[:, 4:], vib.T, rtol=5.01e-7, atol=1e-300)
+    np.testing.assert_allclose(a[:, 3], vib.sum(axis=0), rtol=5.01e-7, atol=1e-300)
+    assert np.any(a[:, 3] > 0)
