@@ -206,6 +206,52 @@ def write_func(outdir, p):
     p["_eref"] = eref
 
 
+def product_states(run, n2prod1, jiniprod, jmaxprod, nviniprod, nvmaxprod, **over):
+    """The product diatom's (atoms 0-2, atom 1 far away) states on the R grid,
+    as product_radialf_read builds them for diabatic products
+    (SRC/mod_baseYfunciones_01y2.f:1085-1250): the coupled nelec-state sine DVR
+    of the 02 diatom per j, each state discrete-normalised over the grid and
+    kept on its first n2prod1 points.  ``over`` are the case's generator
+    parameters (for the surface).  Returns (fdprod[njp][nvp][nelec][n2prod1],
+    ediatprod[njp][nvp] in zot, nobcprod[njp] = noBCprod(jiniprod:jmaxprod),
+    nviniprod - 1 where no state is bound)."""
+    _, p = make_inputs(**over)
+    inp = run.inp
+    n = inp.npun2
+    ah = run.ah2
+    r = inp.rmis2 + ah * np.arange(n)
+    far = np.full_like(r, 100.0)
+    ne = run.nelec
+    V = diabatic_matrix(far, r, far, p) * C.eV2cm * C.conve1          # [ne][ne][n], zot
+    mu = run.xm1prod
+    L = (n + 1) * ah
+    kk = np.arange(1, n + 1) * math.pi / L
+    S = math.sqrt(2.0 / (n + 1)) * np.sin(np.outer(np.arange(1, n + 1), np.arange(1, n + 1)) * math.pi / (n + 1))
+    T = (S * (C.hbr ** 2 * kk ** 2 / (2.0 * mu))) @ S
+    asym = min(V[e, e, -1] for e in range(ne))
+    njp, nvp = jmaxprod - jiniprod + 1, nvmaxprod - nviniprod + 1
+    fd = np.zeros((njp, nvp, ne, n2prod1))
+    ed = np.zeros((njp, nvp))
+    nob = np.full(njp, nviniprod - 1, np.int32)
+    for jj, j in enumerate(range(jiniprod, jmaxprod + 1)):
+        cent = j * (j + 1) * C.hbr ** 2 / (2.0 * mu * r * r)
+        H = np.zeros((ne * n, ne * n))
+        for e in range(ne):
+            H[e * n:(e + 1) * n, e * n:(e + 1) * n] = T + np.diag(cent)
+            for f in range(ne):
+                H[e * n:(e + 1) * n, f * n:(f + 1) * n] += np.diag(V[e, f])
+        w, v = np.linalg.eigh(H)
+        nbound = int(np.sum(w < asym))
+        nob[jj] = min(nbound - 1, nvmaxprod) if nbound - 1 >= nviniprod else nviniprod - 1
+        for vv, iv in enumerate(range(nviniprod, nvmaxprod + 1)):
+            c = v[:, iv]
+            if c[np.argmax(np.abs(c))] < 0:
+                c = -c
+            ed[jj, vv] = w[iv]
+            fd[jj, vv] = c.reshape(ne, n)[:, :n2prod1]
+    return fd, ed, nob
+
+
 def write_pot(outdir, p):
     from .wigner import gauleg
     n1, n2, na, ne = p["npun1"], p["npun2"], p["nangu"], p["nelecmax"]

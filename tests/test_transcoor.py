@@ -135,3 +135,34 @@ def test_ini_transcoor_feeds_the_oracle_projection(runs):
                               np.full((4, 2), -0.1), nob, vp0, vp1)
     assert fac.shape == (4, 2, run.inp.netot) and np.all(fac >= 0) and np.any(fac > 0)
     assert np.all(fac[2, 1] == 0)                                                # v > noBCprod(j)
+
+
+def test_product_chain_from_the_generator_to_the_probability_file(runs, tmp_path):
+    """Synthetic product states (the 02 diatom of the LEPS surface) -> the
+    ini_transcoor tables -> the oracle's prodpaq / prodcvj -> printprob's
+    iprod = 2 S2prod with S2prodfac from the states' energies."""
+    from madwave3_gb300 import printprob
+    from madwave3_gb300.host import generator
+    from oracle.mw3ref import Oracle
+
+    run = runs["tiny_j3"]
+    over = generator.CASES["tiny_j3"]
+    fd, ed, nob = generator.product_states(run, 30, 0, 4, 0, 2, **over)
+    assert fd.shape == (5, 3, run.nelec, 30) and np.all(nob >= 0)
+    # lowest state: discrete-normalised over the whole grid, so at most 1 on 30 points
+    assert 0.5 < np.sum(fd[0, 0] ** 2) <= 1.0 + 1e-12
+    assert np.all(np.diff(ed[0]) > 0) and np.all(ed[1:, 0] > ed[:-1, 0])        # v and j ladders
+    pp = transcoor.ini_transcoor(run, 1.8, 3, 30, 1, run.inp.nangu, 0, 2, 0, 4, 0, 2, nob, fd)
+    o = Oracle(run)
+    o.set_product(pp)
+    o.start(run.psi0)
+    o.run_iters(30)
+    z, _ = o.product()
+    ft = o.flux_tables()
+    fac = transcoor.s2prodfac(run, ft["etot"], ft["apaqini"], ed, nob, 0, 2)
+    zs2, _ = o.s2()
+    path = printprob.write_s2prod(str(tmp_path), run, 1, *o.totalflux(), zs2, ft["etot"], ft["reacfct"],
+                                  o.s2factor(), iprod=2, product=(z, fac, pp))
+    a = printprob.read_s2prod(path)
+    assert a.shape == (run.inp.netot, 4 + 3)
+    assert np.all(np.isfinite(a)) and np.all(a[:, 3:] >= 0) and np.any(a[:, 3] > 0)
