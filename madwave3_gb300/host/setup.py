@@ -18,13 +18,13 @@ then Omega/electronic block, then stored point.
 """
 import math
 import os
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
 from . import constants as C
 from . import namelist
-from .wigner import dwigner, dwigner_vec, gauleg
+from .wigner import dwigner_vec, gauleg
 
 
 def _get(d, key, default):

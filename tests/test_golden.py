@@ -9,7 +9,6 @@ import json
 import math
 import os
 
-import numpy as np
 import pytest
 
 from madwave3_gb300.host import constants as C

@@ -5,7 +5,6 @@ import os
 import socket
 
 import numpy as np
-import pytest
 
 from madwave3_gb300 import replicas
 

@@ -4,7 +4,6 @@ tables, and the whole set feeding the oracle's prodpaq / prodcvj."""
 import math
 
 import numpy as np
-import pytest
 
 from madwave3_gb300.host import transcoor
 
