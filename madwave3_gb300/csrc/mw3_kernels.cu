@@ -617,7 +617,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
 // V psi alone, for mw3_hphi: H(t) += sum_s V(e_s, e_t) psi(s) over same-Omega blocks
 // (difs V part, mod_Hphi_01y2.f:838-853)
 template <typename HT>
-__global__ void k_addv(DevGrid d, const double *__restrict__ psi, const HT *__restrict__ Hin, double *__restrict__ H,
+// Hin and H may be the same array (each element is read, then written, by one thread)
+__global__ void k_addv(DevGrid d, const double *__restrict__ psi, const HT *Hin, double *H,
                        const int *__restrict__ vsrc, int seg0)
 {
     int seg = seg0 + blockIdx.x;
