@@ -153,6 +153,14 @@ int mw3_download_accumulators(mw3_ctx *ctx, int32_t wave_id, double *zcr, double
 
 /* Set-up tables for inspection: nopr1[nangu], reacfct[netot], S2factor
  * [nelec][nj][nv][netot], etot[netot], absfr1[npun1], absfr2[npun2]. */
+/* Continuation: the accumulators a restart reads back from cont##.S2
+ * (SRC/mod_flux_01y2.f:296-320; written by wvpcont, SRC/main_madwave3.f:519-525),
+ * same layouts as mw3_download_accumulators (any pointer may be NULL).  Call
+ * after the state (mw3_upload_state / mw3_upload_state_all): every wave's
+ * pending ring samples are added first, then this wave's accumulators are
+ * replaced. */
+int mw3_upload_accumulators(mw3_ctx *ctx, int32_t wave_id, const double *zcr, const double *zcdr,
+                            const double *zs2);
 int mw3_tables(mw3_ctx *ctx, int32_t wave_id, int32_t *nopr1, double *etot, double *reacfct,
                double *s2factor, double *absfr1, double *absfr2);
 
@@ -228,6 +236,8 @@ int mw3_set_product_projection(mw3_ctx *ctx, int32_t wave_id, const mw3_prodproj
  * complex as (re,im) pairs, and the last iteration's Cvjprod(v,j,Omega)
  * (either may be NULL). */
 int mw3_download_product(mw3_ctx *ctx, int32_t wave_id, double *zs2prod, double *cvjprod);
+/* zS2prod of a restart (cont##.S2prod, SRC/mod_coortrans01_02.f:183-197). */
+int mw3_upload_product(mw3_ctx *ctx, int32_t wave_id, const double *zs2prod);
 
 const char *mw3_last_error(const mw3_ctx *ctx);
 int mw3_destroy(mw3_ctx *ctx);

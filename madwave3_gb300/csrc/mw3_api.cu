@@ -1141,6 +1141,30 @@ int mw3_download_accumulators(mw3_ctx *h, int32_t w, double *zcr, double *zcdr, 
     return MW3_OK;
 }
 
+int mw3_upload_accumulators(mw3_ctx *h, int32_t w, const double *zcr, const double *zcdr, const double *zs2)
+{
+    if (!h) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) return MW3_ERR_ARG;
+    if (!c.built || !c.started) {
+        c.err = "mw3_upload_accumulators: upload the state first";
+        return MW3_ERR_STATE;
+    }
+    WaveTables &t = c.waves[w];
+    WaveDev &d = c.wdev[w];
+    size_t nf = (size_t)t.nflux * t.netot * 2;
+    size_t ns = (size_t)t.ncan * t.nj * t.nv;
+    mw3::flush_flux(c);
+    mw3::flush_cvj(c);
+    if (zcr && nf) MW3_CUDA_TRY(cudaMemcpyAsync(d.zcr, zcr, sizeof(double) * nf, cudaMemcpyHostToDevice, c.stream));
+    if (zcdr && nf)
+        MW3_CUDA_TRY(cudaMemcpyAsync(d.zcdr, zcdr, sizeof(double) * nf, cudaMemcpyHostToDevice, c.stream));
+    if (zs2)
+        MW3_CUDA_TRY(cudaMemcpyAsync(d.zs2, zs2, sizeof(double) * ns * t.netot * 2, cudaMemcpyHostToDevice, c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return check_launch(c, "mw3_upload_accumulators");
+}
+
 int mw3_tables(mw3_ctx *h, int32_t w, int32_t *nopr1, double *etot, double *reacfct, double *s2factor,
                double *absfr1, double *absfr2)
 {
@@ -1264,6 +1288,22 @@ int mw3_download_product(mw3_ctx *h, int32_t w, double *zs2prod, double *cvjprod
                                      c.stream));
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return check_device_flags(c, "mw3_download_product");
+}
+
+int mw3_upload_product(mw3_ctx *h, int32_t w, const double *zs2prod)
+{
+    if (!h || !zs2prod) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) return MW3_ERR_ARG;
+    if (w >= (int)c.prodt.size() || !c.prodt[w].on || !c.built || !c.started) {
+        c.err = "mw3_upload_product: the wave has no product projection, or its state is not uploaded";
+        return MW3_ERR_STATE;
+    }
+    const mw3::ProdDev &d = c.wdev[w].prod;
+    MW3_CUDA_TRY(cudaMemcpyAsync(d.zs2prod, zs2prod, sizeof(double) * 2 * (size_t)d.nrow * c.netot,
+                                 cudaMemcpyHostToDevice, c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return MW3_OK;
 }
 
 const char *mw3_last_error(const mw3_ctx *h)

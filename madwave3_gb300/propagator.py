@@ -69,6 +69,7 @@ HEADER_FUNCS = [
     "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_path_flags", "mw3_get_stream",
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_set_product_projection", "mw3_download_product",
+    "mw3_upload_accumulators", "mw3_upload_product",
     "mw3_last_error", "mw3_destroy",
 ]
 # stage 0 holds the whole radial DST chain when the mixed path runs it as one
@@ -120,6 +121,8 @@ def load_library(build_if_missing=True):
     L.mw3_stage_times.argtypes = [vp, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_set_product_projection.argtypes = [vp, ct.c_int32, ct.POINTER(ProdProj)]
     L.mw3_download_product.argtypes = [vp, ct.c_int32, F64P, F64P]
+    L.mw3_upload_accumulators.argtypes = [vp, ct.c_int32, F64P, F64P, F64P]
+    L.mw3_upload_product.argtypes = [vp, ct.c_int32, F64P]
     L.mw3_last_error.argtypes = [vp]
     L.mw3_last_error.restype = ct.c_char_p
     L.mw3_destroy.argtypes = [vp]
@@ -269,6 +272,17 @@ class Propagator:
         c = np.empty(shp)
         self._check(self.L.mw3_download_product(self.h, wave, _p(z), _p(c)), "mw3_download_product")
         return z[..., 0] + 1j * z[..., 1], c
+
+    def upload_accumulators(self, wave, zcr, zcdr, zs2):
+        """A restart's zCR, zCdR, zS2 (complex arrays as .accumulators() returns)."""
+        arr = [None if a is None else np.ascontiguousarray(np.stack([np.real(a), np.imag(a)], -1), np.float64)
+               for a in (zcr, zcdr, zs2)]
+        ptr = [None if a is None else _p(a) for a in arr]
+        self._check(self.L.mw3_upload_accumulators(self.h, wave, *ptr), "mw3_upload_accumulators")
+
+    def upload_product(self, zs2prod, wave=0):
+        a = np.ascontiguousarray(np.stack([np.real(zs2prod), np.imag(zs2prod)], -1), np.float64)
+        self._check(self.L.mw3_upload_product(self.h, wave, _p(a)), "mw3_upload_product")
 
     def upload_state(self, wave, psi_km1, psi_k, it):
         a = np.ascontiguousarray(psi_km1, np.float64)

@@ -1,0 +1,35 @@
+"""Stop and resume through the continuation files: a fresh context that reads
+contNN.paq / contNN.S2 (mw3_upload_state_all, mw3_upload_accumulators) and
+runs on gives the same bits as the run that never stopped."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_continuation_through_cont_files(runs, precision, tmp_path):
+    from madwave3_gb300 import Propagator, contfiles
+
+    run = runs["tiny_j3"]
+    a = Propagator(run, precision)
+    a.start()
+    a.run(50)
+    km1, k, it = a.state_all()
+    acc = a.accumulators()
+    contfiles.write_cont(str(tmp_path), km1, k, acc["zs2"], acc["zcr"], acc["zcdr"], iit0=it, indt=0, iloop=1)
+    a.run(45)
+    ref = (a.state_all()[1], a.totalflux()[0], a.accumulators())
+    a.close()
+
+    r = contfiles.read_cont(str(tmp_path), zs2_shape=acc["zs2"].shape, flux_shape=acc["zcr"].shape)
+    b = Propagator(run, precision)
+    b.upload_state_all(r["psi_km1"], r["psi_k"], r["iit0"])
+    b.upload_accumulators(0, r["zcr"], r["zcdr"], r["zs2"])
+    b.run(45)
+    got = (b.state_all()[1], b.totalflux()[0], b.accumulators())
+    b.close()
+    assert np.array_equal(got[0], ref[0])
+    assert np.array_equal(got[1], ref[1])
+    for key in ("zcr", "zcdr", "zs2", "cvj"):
+        assert np.array_equal(got[2][key], ref[2][key]), key
