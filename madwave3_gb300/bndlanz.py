@@ -58,7 +58,7 @@ def initial_vector(run, emax_zot):
 def converged_eigenvalues(alpha, beta, tol=GHOST_TOL):
     """valnkry (liboctdynlanz.f:472-575).  alpha[0..n-1] is the diagonal of the
     Lanczos matrix T, beta[i] couples i and i+1 (beta[n-1], if given, is not
-    used).  Returns the sorted eigenvalues judged true."""
+    used).  Returns the sorted eigenvalues accepted as true."""
     from scipy.linalg import eigh_tridiagonal
 
     a = np.asarray(alpha, np.float64)
