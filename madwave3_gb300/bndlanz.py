@@ -190,6 +190,83 @@ def _e15(x):
     return fortran_e(x, 15, 7, 2)
 
 
+def _point_labels(run):
+    """Per flat point: (icanp, ielec, iom, iangp, ir, ir1, ir2, iang), 1-based as
+    indiproc gives them for one process (SRC/mod_pot_01y2.f:628-654)."""
+    order = list(run.angle_order())
+    rows = np.zeros((run.ntot, 8), np.int64)
+    for iangp, iang in enumerate(order, 1):
+        n = run.npunreal[iang - 1]
+        for b in range(run.ncan):
+            o = run.offs[iang - 1, b]
+            rows[o:o + n, 0] = b + 1
+            rows[o:o + n, 1] = run.nelebas[b]
+            rows[o:o + n, 2] = run.iombas[b]
+            rows[o:o + n, 3] = iangp
+            rows[o:o + n, 4] = np.arange(1, n + 1)
+            rows[o:o + n, 5] = run.indr1[iang - 1, :n]
+            rows[o:o + n, 6] = run.indr2[iang - 1, :n]
+            rows[o:o + n, 7] = iang
+    return rows
+
+
+def write_bnd(outdir, run, iv, energy_zot, vec, idproc=0):
+    """write_bnd (main_boundlanz.f:360-400): bnd.ivNNN.ipNNN (iv, E in eV, then
+    the vector one value per line) and grid.ipNNN (the grid and every point's
+    indices, (9(1x,i7)))."""
+    import os
+    lab = _point_labels(run)
+    i = run.inp
+    with open(os.path.join(outdir, "bnd.iv%03d.ip%03d" % (iv, idproc)), "w") as f:
+        f.write(" %d %r\n" % (iv, float(energy_zot) / conve1 / eV2cm))
+        f.writelines(" %r\n" % float(x) for x in vec)
+    with open(os.path.join(outdir, "grid.ip%03d" % idproc), "w") as f:
+        f.write(" %d\n" % run.ntot)
+        f.write(" %r %r %d\n" % (float(i.rmis1), float(i.rfin1), i.npun1))
+        f.write(" %r %r %d\n" % (float(i.rmis2), float(i.rfin2), i.npun2))
+        f.write(" %d %d\n" % (i.nangu, i.inc))
+        for k in range(run.ntot):
+            f.write("".join(" %7d" % x for x in (k + 1,) + tuple(lab[k])) + "\n")
+
+
+def initial_from_bound(run, outdir, iv, nelec_bnd=None, idproc=0):
+    """dip_bndgrid for iphoto = 2 (SRC/mod_photoini_01y2.f:509-717): the initial
+    packet from a bound state that write_bnd stored on the same radial and
+    angular grid, point by point through (ir1, ir2, gamma, Omega, electronic
+    state); points of the run outside the stored state's range stay 0.
+    Returns (psi0, energy in eV, norm of the mapped part)."""
+    import os
+    i = run.inp
+    with open(os.path.join(outdir, "grid.ip%03d" % idproc)) as f:
+        n = int(f.readline())
+        r1 = f.readline().split()
+        r2 = f.readline().split()
+        na, inc = (int(x) for x in f.readline().split())
+        ah1b = (float(r1[1]) - float(r1[0])) / (int(r1[2]) - 1)
+        ah2b = (float(r2[1]) - float(r2[0])) / (int(r2[2]) - 1)
+        if abs(i.rmis1 - float(r1[0])) > 1e-4 or abs(run.ah1 - ah1b) > 1e-4 or \
+                abs(i.rmis2 - float(r2[0])) > 1e-4 or abs(run.ah2 - ah2b) > 1e-4 or na != i.nangu or inc != i.inc:
+            raise ValueError("the bound state was computed on another grid")
+        lab = np.array([[int(x) for x in f.readline().split()] for _ in range(n)])
+    with open(os.path.join(outdir, "bnd.iv%03d.ip%03d" % (iv, idproc))) as f:
+        e_ev = float(f.readline().split()[1])
+        val = np.array([float(f.readline()) for _ in range(n)])
+    key = {}
+    # columns: i, icanp, ielec, iom, iangp, ir, ir1, ir2, iang
+    for row, x in zip(lab, val):
+        key[(row[6], row[7], row[8], row[3], row[2])] = x     # ir1, ir2, iang, iom, ielec
+    nr1, nr2, nang = lab[:, 6].max(), lab[:, 7].max(), lab[:, 8].max()
+    omax = lab[:, 3].max()
+    nel = lab[:, 2].max() if nelec_bnd is None else nelec_bnd
+    me = _point_labels(run)
+    psi0 = np.zeros(run.ntot)
+    for k in range(run.ntot):
+        icanp, ielec, iom, iangp, ir, ir1, ir2, iang = me[k]
+        if ir1 <= nr1 and ir2 <= nr2 and iang <= nang and iom <= omax and ielec <= nel:
+            psi0[k] = key.get((ir1, ir2, iang, iom, ielec), 0.0)
+    return psi0, e_ev, float(np.dot(psi0, psi0))
+
+
 class BoundStates:
     """bndgrid.out's Lanczos part for one wave: eigenvalues, then eigenvectors of
     the lowest ones.  Parameters are the reference's &lanczos_parameters

@@ -86,3 +86,24 @@ def test_levels_file(tmp_path):
     assert bndlanz._e15(0.5) == "  0.5000000E+00"
     assert bndlanz._e15(123.45678) == "  0.1234568E+03"
     assert bndlanz._e15(0.99999999) == "  0.1000000E+01"
+
+
+def test_bound_state_files_and_the_photodissociation_start(tiny, tmp_path):
+    """write_bnd's files, read back by dip_bndgrid's mapping (iphoto = 2) on the
+    same grid, give the bound state itself as the initial packet, which then
+    propagates."""
+    run, o = tiny
+    bs = bndlanz.BoundStates(run, o.hphi, zot_to_ev(run.vmintot) + 1.0, ntimes=200, nkrymax=400,
+                             criter_ev=1e-6, nomxiter=3000, nvecmax=1)
+    bs.eigenvalues()
+    e, v, em, its, ok = bs.eigenvectors()[0]
+    bndlanz.write_bnd(str(tmp_path), run, 1, e, v)
+    lines = (tmp_path / "grid.ip000").read_text().splitlines()
+    assert int(lines[0]) == run.ntot and len(lines) == 4 + run.ntot
+    assert len(lines[4]) == 9 * 8
+    psi0, e_ev, nrm = bndlanz.initial_from_bound(run, str(tmp_path), 1)
+    assert np.allclose(psi0, v, rtol=0, atol=1e-15)
+    assert abs(e_ev - zot_to_ev(e)) < 1e-12 and abs(nrm - 1.0) < 1e-12
+    o.start(psi0)
+    o.run_iters(5)
+    assert np.all(np.isfinite(o.state()[1]))
