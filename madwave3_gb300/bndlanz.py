@@ -267,6 +267,42 @@ def initial_from_bound(run, outdir, iv, nelec_bnd=None, idproc=0):
     return psi0, e_ev, float(np.dot(psi0, psi0))
 
 
+def assign(run, vec, fdprod=None, nviniprod=0):
+    """bndassign (main_boundlanz.f:437-617): the distributions that label a
+    bound state.  disv1[v] = sum over blocks and (angle, R) of (sum over r1 of
+    fd(r1, v, j=0, e) psi)^2 with the reactant diatom's functions; disv2[v'] the
+    same over R with the product diatom's (fdprod[nvp][nelec][n2prod1] at
+    j' = 0, from ``generator.product_states`` or the host's own), when given;
+    <cos gamma>; the populations of every Omega and electronic state."""
+    i = run.inp
+    lab = _point_labels(run)
+    blk, ele, iom, ir1, ir2, iang = (lab[:, 0] - 1, lab[:, 1] - 1, lab[:, 2], lab[:, 5] - 1, lab[:, 6] - 1,
+                                     lab[:, 7] - 1)
+    v = np.asarray(vec, np.float64)
+    nv = i.nvmax - i.nvini + 1
+    if i.jini != 0:
+        raise ValueError("bndassign projects on j = 0: needs jini = 0")
+    key = (blk * i.nangu + iang) * i.npun2 + ir2                 # (block, angle, R) line of each point
+    disv1 = np.zeros(nv)
+    for k in range(nv):
+        w = run.fd[ele, 0, k, ir1] * v
+        disv1[k] = np.sum(np.bincount(key, weights=w) ** 2)
+    disv2 = None
+    if fdprod is not None:
+        fdprod = np.asarray(fdprod)
+        n2p = fdprod.shape[-1]
+        key2 = (blk * i.nangu + iang) * i.npun1 + ir1            # (block, angle, r1) line
+        inside = ir2 < n2p
+        disv2 = np.zeros(fdprod.shape[0])
+        for k in range(fdprod.shape[0]):
+            w = np.where(inside, fdprod[k, ele, np.minimum(ir2, n2p - 1)], 0.0) * v
+            disv2[k] = np.sum(np.bincount(key2, weights=w) ** 2)
+    cos_mean = float(np.sum(v * v * run.cgamma[iang]))
+    disomg = {int(o): float(np.sum(v[iom == o] ** 2)) for o in range(i.iommin, i.iommax + 1)}
+    diselec = np.array([np.sum(v[ele == e] ** 2) for e in range(run.nelec)])
+    return dict(disv1=disv1, disv2=disv2, cos_mean=cos_mean, disomg=disomg, diselec=diselec)
+
+
 class BoundStates:
     """bndgrid.out's Lanczos part for one wave: eigenvalues, then eigenvectors of
     the lowest ones.  Parameters are the reference's &lanczos_parameters

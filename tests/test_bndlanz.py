@@ -107,3 +107,28 @@ def test_bound_state_files_and_the_photodissociation_start(tiny, tmp_path):
     o.start(psi0)
     o.run_iters(5)
     assert np.all(np.isfinite(o.state()[1]))
+
+
+def test_assignment_distributions(tiny):
+    """bndassign: for a state on a single (angle, R) line the v distribution is
+    the squared overlap with each diatomic function; populations of Omega and
+    of the electronic states add up to the norm."""
+    from madwave3_gb300.host import generator
+
+    run, _ = tiny
+    blk, ang, r1, r2 = run.point_table()
+    line = (blk == 0) & (ang == ang[0]) & (r2 == r2[0])
+    rng = np.random.default_rng(5)
+    v = np.zeros(run.ntot)
+    v[line] = rng.standard_normal(line.sum())
+    v /= np.linalg.norm(v)
+    fdp, _, _ = generator.product_states(run, 30, 0, 0, 0, 2, **generator.CASES["tiny_j0"])
+    a = bndlanz.assign(run, v, fdprod=fdp[0])
+    e = run.nelebas[0] - 1
+    for k in range(a["disv1"].size):
+        want = np.dot(run.fd[e, 0, k, r1[line] - 1], v[line]) ** 2
+        assert abs(a["disv1"][k] - want) < 1e-14
+    assert a["disv2"].shape == (3,) and np.all(a["disv2"] >= 0)
+    assert abs(sum(a["disomg"].values()) - 1.0) < 1e-12
+    assert abs(a["diselec"].sum() - 1.0) < 1e-12
+    assert abs(a["cos_mean"] - run.cgamma[ang[0] - 1]) < 1e-12
