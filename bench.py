@@ -175,75 +175,126 @@ def stage_model(runs, prop, stages=None):
     }
 
 
+RING = 32   # iterations in one cycle of the Cvj ring and in one captured CUDA-graph block
+
+
+def warmup_count(it_now, warmup, steps):
+    """Untimed iterations before the timed window: at least ``warmup``, then up to
+    the iteration where the window must start.  A window of a multiple of 32
+    steps starts at an iteration that is a multiple of 32 (whole ring cycles,
+    replayed as CUDA graphs; one block is run first so the graph is captured
+    outside the timing); a shorter or ragged window ends on the iteration
+    congruent to 31 mod 32, so the once-per-cycle Cvj flush falls inside it."""
+    target = 0 if steps % RING == 0 else (RING - 1 - steps) % RING
+    w = warmup
+    while (it_now + w) % RING != target:
+        w += 1
+    if steps >= RING and steps % RING == 0:
+        w += RING
+    return w
+
+
 def run_gpu(args, rank, world, local):
     import torch
-    from madwave3_gb300 import Propagator
+    from madwave3_gb300 import Propagator, replicas
 
     torch.cuda.set_device(local)
-    runs = case_runs(args.workload, rank)
+    all_runs = case_runs(args.workload, rank)
+    nsto_job = sum(r.ntot for r in all_runs)
+    if world > 1 and len(all_runs) >= world:
+        # the partial waves are independent: each rank propagates its share of the
+        # sweep (longest-processing-time split by stored points), no exchange
+        part = replicas.partition([float(r.ntot) for r in all_runs], world)
+        runs = [all_runs[i] for i in part[rank]]
+        scaling, parallelism = "strong", "partial waves split over %d GPUs" % world
+    else:
+        runs = all_runs
+        scaling = "weak"
+        parallelism = "replicas" if world > 1 else "single GPU"
+        nsto_job = world * nsto_job
     nsto = sum(r.ntot for r in runs)
     prop = Propagator(runs, args.precision)
     prop.start()
-    for _ in range(args.warmup):
-        prop.run(1)
-    prop.sync()
-    stream = torch.cuda.ExternalStream(prop.stream())
     working_set = nsto * 8 * 4
     flush = working_set < 2 * L2_BYTES
+    nwarm = warmup_count(1, args.warmup, args.steps) if not flush else args.warmup
+    prop.run(nwarm)
+    prop.sync()
+    it0 = 1 + nwarm
+    stream = torch.cuda.ExternalStream(prop.stream())
     fbuf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda") if flush else None
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = prop.kernel_launches()
-    prop.profile(True)
     clocks = ClockSampler(local)
-    evs = []
-    for _ in range(args.steps):
-        if flush:
+    if flush:
+        # a small workload: L2 flushed before every step, each step timed alone
+        evs = []
+        for _ in range(args.steps):
             with torch.cuda.stream(stream):
                 fbuf.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prop.run(1)
+            e1.record(stream)
+            evs.append((e0, e1))
+        prop.sync()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+    else:
+        # inputs larger than L2: the K steps back to back as the production loop
+        # runs them (whole ring cycles replay as CUDA graphs)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        prop.run(1)
+        prop.run(args.steps)
         e1.record(stream)
-        evs.append((e0, e1))
-    prop.sync()
-    torch.cuda.synchronize()
+        prop.sync()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     launches = prop.kernel_launches() - launches0
-    ms = sum(a.elapsed_time(b) for a, b in evs)
-    stages, nrec = prop.stage_times()
-    prop.profile(False)
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.barrier()
     ms_max = float(t.item())
     ms_step = ms_max / args.steps
-    value = world * nsto * args.steps / (ms_max * 1e-3)
+    value = nsto_job * args.steps / (ms_max * 1e-3)
 
-    # end to end through the C-ABI: the host keeps the whole state (all waves back to
-    # back, pinned); every step uploads psi_k-1 and psi_k, runs one iteration and
-    # reads back the new psi_k (the new psi_k-1 is the psi_k the host already holds)
+    # stage breakdown: one more ring cycle with per-stage events (untimed; event
+    # recording switches graph replay off)
+    prop.profile(True)
+    prop.run(RING)
+    stages, nrec = prop.stage_times()
+    prop.profile(False)
+
+    # end to end through the C-ABI with host buffers (all waves back to back,
+    # pinned): every step hands psi_k in from the host, runs one iteration and
+    # reads the new psi_k back; psi_k-1 is the device's own (the psi_k it held)
     e2e_steps = max(1, min(args.steps, 10))
-    km1, k, it = prop.state_all()
-    bufs = [torch.from_numpy(km1).pin_memory(), torch.from_numpy(k).pin_memory(),
-            torch.empty(k.size, dtype=torch.float64).pin_memory()]
+    _, k, it = prop.state_all()
+    bufs = [torch.from_numpy(k).pin_memory(), torch.empty(k.size, dtype=torch.float64).pin_memory()]
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for s in range(e2e_steps):
-        a, b, c = bufs
-        prop.upload_state_all(a.numpy(), b.numpy(), it + s)
+        a, b = bufs
+        prop.upload_state_all(None, a.numpy(), it + s)
         prop.run(1)
-        prop.state_k_all(c.numpy())
-        bufs = [b, c, a]
+        prop.state_k_all(b.numpy())
+        bufs = [b, a]
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    e2e_value = world * nsto / (e2e_ms * 1e-3)
+    if world > 1:
+        te = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(te.item())
+    e2e_value = nsto_job / (e2e_ms * 1e-3) if scaling == "strong" else world * nsto / (e2e_ms * 1e-3)
 
     # roofline of the dominant stage
     hbm, tf, src = load_peaks()
@@ -268,18 +319,20 @@ def run_gpu(args, rank, world, local):
     out = {
         "metric": metric_name(), "value": value, "unit": "grid-pt*iter/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "higher_is_better": True, "scaling": scaling, "vs_baseline": None,
         "dtype": "f64 recursion, f32 transforms" if args.precision == "mixed" else "f64",
         "data": "synthetic LEPS surface, generated on the fly",
         "config": {"workload": args.workload, "precision": args.precision,
-                   "stored_points": nsto, "waves": len(runs), "blocks": sum(r.ncan for r in runs),
+                   "stored_points": nsto_job if scaling == "strong" else nsto,
+                   "waves": len(all_runs), "blocks": sum(r.ncan for r in all_runs),
                    "grid": [runs[0].inp.npun2, runs[0].inp.npun1, runs[0].inp.nangu],
                    "netot": runs[0].inp.netot,
                    "l2": "flushed before every timed step" if flush else "working set larger than L2",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "window": {"iterations": [it0 + 1, it0 + args.steps], "untimed_warmup_iterations": nwarm,
+                              "graph_blocks": (not flush) and args.steps % RING == 0},
+                   "parallelism": parallelism},
         "e2e": {"value": e2e_value, "unit": "grid-pt*iter/s",
-                "h2d_bytes_per_step": int(sum(2 * 8 * r.ntot for r in runs)),
-                "d2h_bytes_per_step": int(sum(8 * r.ntot for r in runs))},
+                "h2d_bytes_per_step": int(8 * nsto), "d2h_bytes_per_step": int(8 * nsto)},
         "gpu_launches": launches,
         "stages_ms_per_step": {k: v / max(nrec, 1) for k, v in stages.items()},
         "roofline": roof,
@@ -289,15 +342,29 @@ def run_gpu(args, rank, world, local):
     prop.close()
     del prop
     if args.precision == "mixed" and args.fp64_steps > 0:
-        out["fp64_plain"] = fp64_plain(runs, args.fp64_steps, stream_world=world)
-        out["fp64_plain"]["speedup_mixed_over_fp64"] = value / out["fp64_plain"]["value"]
+        fp = fp64_plain(runs, args.fp64_steps)
+        fp["speedup_mixed_over_fp64"] = nsto * args.steps / (ms_max * 1e-3) / fp["value"]
+        out["fp64_plain"] = fp
+    if rank == 0 and world == 1 and args.gate_iterations > 0 and args.precision == "mixed":
+        out["gate"] = precision_gate(args.gate_iterations)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(sample_waves(runs), budget_s=args.cpu_seconds)
     return out
 
 
-def fp64_plain(runs, steps, stream_world=1, warmup=3):
-    """The plain FP64 path on the same workload, for the mixed/FP64 ratio."""
+def precision_gate(iterations, case="j0_256x128x60"):
+    """|Delta P(E)| of the mixed path against FP64 after a full propagation of the
+    J=0 wave on the sweep's grid (the metric's gate); both paths on this GPU."""
+    from madwave3_gb300 import gate
+    res = gate.run_gate(case, iterations)[0]
+    keep = ("case", "iterations", "max_abs_dP", "at_energy_ev", "max_P", "pass_1e-4", "seconds_fp64",
+            "seconds_mixed")
+    return {k: res[k] for k in keep}
+
+
+def fp64_plain(runs, steps, warmup=3):
+    """The plain FP64 path on the same waves (this GPU's share), for the
+    mixed/FP64 ratio."""
     import torch
     from madwave3_gb300 import Propagator
     prop = Propagator(runs, "fp64")
@@ -316,7 +383,7 @@ def fp64_plain(runs, steps, stream_world=1, warmup=3):
     ms = e0.elapsed_time(e1)
     prop.close()
     nsto = sum(r.ntot for r in runs)
-    return {"value": stream_world * nsto * steps / (ms * 1e-3), "unit": "grid-pt*iter/s",
+    return {"value": nsto * steps / (ms * 1e-3), "unit": "grid-pt*iter/s",
             "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
 
 
@@ -391,6 +458,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=3,
                     help="timed steps of the plain FP64 path on the same workload (0: skip)")
+    ap.add_argument("--gate-iterations", type=int, default=2000,
+                    help="iterations of the |dP(E)| gate of the mixed path against FP64 on the J=0 wave (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -131,7 +131,9 @@ int mw3_download_state(mw3_ctx *ctx, int32_t wave_id, double *psi_km1, double *p
 /* mw3_upload_state / mw3_download_state for every wave at once: the host arrays
  * hold the waves' vectors back to back in wave order (wave w starts after the
  * ntot of waves 0..w-1), moved with one copy each way for the whole context and
- * one synchronisation per call. */
+ * one synchronisation per call.  Once the context holds a state, psi_km1 may
+ * be NULL: the device keeps its current psi_{k-1} and only psi_k is replaced
+ * (a host loop that reads psi_k back every iteration and hands it in again). */
 int mw3_upload_state_all(mw3_ctx *ctx, const double *psi_km1, const double *psi_k, int64_t it);
 int mw3_download_state_all(mw3_ctx *ctx, double *psi_km1, double *psi_k, int64_t *it);
 
@@ -197,17 +199,23 @@ int mw3_stage_times(mw3_ctx *ctx, double *ms, int64_t *iterations);
  * example a host whose device memory is owned by another allocator that
  * holds the whole GPU, or a loop where the implicit device synchronisation
  * of cudaMalloc/cudaFree would stall every iteration.  psi and hpsi are
- * DEVICE pointers to the wave's state vector layout (mw3_wave_size doubles).
+ * DEVICE pointers to the wave's state vector layout (mw3_wave_size doubles);
+ * they must not overlap (MW3_ERR_ARG otherwise: psi is still read after
+ * hpsi is first written).
  * The transform scratch lives in one file-scope device array of
  * MW3_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
  * exit; waves whose scratch (two rectangles of ncan*nangu*npun1*npun2
  * elements, 8 bytes each in FP64, 4 in mixed) exceeds it are rejected with
  * MW3_ERR_UNSUPPORTED.  The context's device tables must already exist (any
  * earlier mw3_hphi, mw3_start or mw3_upload_state builds them).  The first
- * call on a device looks up the array's device address once; make that
- * first call before any stream capture.  All calls share the array, so calls
- * that overlap on the GPU (other threads or contexts on the same device) race.
- * Returns after the result is in hpsi. */
+ * call on a device looks up the array's device address once (under a lock,
+ * so threads may make it concurrently) and keeps it for the life of the
+ * process, which assumes the device's primary context is not reset
+ * (cudaDeviceReset) while the library is loaded; make that first call before
+ * any stream capture.  All calls share the array, so calls that overlap on
+ * the GPU (other threads or contexts on the same device) race.  Returns after
+ * the result is in hpsi, with MW3_ERR_CUDA if a launch failed or a
+ * tensor-core kernel gave up waiting for its MMAs. */
 #define MW3_NOALLOC_SCRATCH_BYTES (64u << 20)
 int mw3_hphi_noalloc(mw3_ctx *ctx, int32_t wave_id, const double *psi, double *hpsi);
 

@@ -713,6 +713,8 @@ void stage_mark(Ctx &c, int stage)
     if (!c.prof || c.prof_n >= c.prof_cap) return;
     cudaEventRecord(c.prof_ev[(size_t)c.prof_n * (MW3_NSTAGES + 1) + stage], c.stream);
 }
+int api_check_launch(Ctx &c, const char *where) { return check_launch(c, where); }
+int api_check_device_flags(Ctx &c, const char *where) { return check_device_flags(c, where); }
 }  // namespace mw3
 
 // ===========================================================================
@@ -1040,11 +1042,16 @@ int mw3_download_state(mw3_ctx *h, int32_t w, double *km1, double *k, int64_t *i
 
 int mw3_upload_state_all(mw3_ctx *h, const double *psi_km1, const double *psi_k, int64_t it)
 {
-    if (!h || !psi_km1 || !psi_k || it < 1) return MW3_ERR_ARG;
+    if (!h || !psi_k || it < 1) return MW3_ERR_ARG;
     Ctx &c = h->c;
+    if (!psi_km1 && !c.started) {
+        c.err = "mw3_upload_state_all: psi_km1 may be NULL only once the context holds a state";
+        return MW3_ERR_STATE;
+    }
     int rc = build_device(c);
     if (rc) return rc;
-    MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, psi_km1, sizeof(double) * c.NT, cudaMemcpyHostToDevice, c.stream));
+    if (psi_km1)
+        MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, psi_km1, sizeof(double) * c.NT, cudaMemcpyHostToDevice, c.stream));
     MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pk, psi_k, sizeof(double) * c.NT, cudaMemcpyHostToDevice, c.stream));
     scatter(c, c.d_pk, 0, c.G);
     if (!c.started) {

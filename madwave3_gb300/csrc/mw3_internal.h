@@ -369,6 +369,10 @@ void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec);
 void set_kernel_attributes(Ctx &c);
 // picks c.ang_cw so that every kernel's dynamic shared memory fits optin bytes
 bool fit_smem(Ctx &c, size_t optin);
+// the C-ABI's error reporting: a failed launch (cudaGetLastError), and after a
+// synchronisation the tensor-core kernels' wait-timeout flag
+int api_check_launch(Ctx &c, const char *where);
+int api_check_device_flags(Ctx &c, const char *where);
 
 }  // namespace mw3
 

@@ -16,6 +16,8 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <mutex>
+
 #include "mw3_internal.h"
 
 namespace mw3 {
@@ -1720,7 +1722,10 @@ void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec)
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MW3_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
-static void *s_noalloc_ptr[kMaxDevices];   // device address of g_noalloc_scratch, per device
+// device address of g_noalloc_scratch per device ordinal, looked up once with
+// that device current; it stays valid while the device's primary context lives
+static void *s_noalloc_ptr[kMaxDevices];
+static std::mutex s_noalloc_mu;
 
 template <typename T>
 static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, const double *psi, double *hpsi)
@@ -1790,19 +1795,32 @@ extern "C" int mw3_hphi_noalloc(mw3_ctx *h, int32_t wave_id, const double *psi, 
                 " bytes of scratch, more than the static array's " + std::to_string((size_t)MW3_NOALLOC_SCRATCH_BYTES);
         return MW3_ERR_UNSUPPORTED;
     }
+    // psi is read after hpsi is first written (the V psi term of the other
+    // same-Omega blocks, the ir1 > nopr1 points), so the two must not overlap
+    const char *pb = reinterpret_cast<const char *>(psi), *hb = reinterpret_cast<const char *>(hpsi);
+    size_t vbytes = sizeof(double) * (size_t)t.ntot;
+    if (pb < hb + vbytes && hb < pb + vbytes) {
+        c.err = "mw3_hphi_noalloc: psi and hpsi overlap";
+        return MW3_ERR_ARG;
+    }
     int dev = 0;
     MW3_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) {
         c.err = "mw3_hphi_noalloc: device index out of range";
         return MW3_ERR_UNSUPPORTED;
     }
-    if (!s_noalloc_ptr[dev]) {
-        // once per device, with that device current: the device address of the array
-        void *p = nullptr;
-        MW3_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        s_noalloc_ptr[dev] = p;
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(s_noalloc_mu);
+        if (!s_noalloc_ptr[dev]) {
+            // once per device, with that device current: the device address of the array
+            void *p = nullptr;
+            MW3_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            s_noalloc_ptr[dev] = p;
+        }
+        base = s_noalloc_ptr[dev];
     }
-    unsigned char *scratch = static_cast<unsigned char *>(s_noalloc_ptr[dev]);
+    unsigned char *scratch = static_cast<unsigned char *>(base);
     // the array keeps the previous call's contents; the psi rectangle must be
     // zero outside the stored points
     MW3_CUDA_TRY(cudaMemsetAsync(scratch, 0, rect_bytes, c.stream));
@@ -1810,9 +1828,10 @@ extern "C" int mw3_hphi_noalloc(mw3_ctx *h, int32_t wave_id, const double *psi, 
         noalloc_hphi<double>(c, t, scratch, psi, hpsi);
     else
         noalloc_hphi<float>(c, t, scratch, psi, hpsi);
-    MW3_CUDA_TRY(cudaGetLastError());
+    int rc = api_check_launch(c, "mw3_hphi_noalloc");
+    if (rc) return rc;
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    return MW3_OK;
+    return api_check_device_flags(c, "mw3_hphi_noalloc");
 }
 
 namespace mw3 {

@@ -290,11 +290,17 @@ class Propagator:
         self._check(self.L.mw3_upload_state(self.h, wave, _p(a), _p(b), it), "mw3_upload_state")
 
     def upload_state_all(self, psi_km1, psi_k, it):
-        """Every wave's state at once: the vectors back to back in wave order."""
-        a = np.ascontiguousarray(psi_km1, np.float64)
+        """Every wave's state at once: the vectors back to back in wave order.
+        psi_km1 None keeps the device's psi_k-1 (only psi_k is replaced)."""
         b = np.ascontiguousarray(psi_k, np.float64)
-        assert a.size == b.size == sum(self.ntot)
-        self._check(self.L.mw3_upload_state_all(self.h, _p(a), _p(b), it), "mw3_upload_state_all")
+        assert b.size == sum(self.ntot)
+        if psi_km1 is None:
+            pa = None
+        else:
+            a = np.ascontiguousarray(psi_km1, np.float64)
+            assert a.size == b.size
+            pa = _p(a)
+        self._check(self.L.mw3_upload_state_all(self.h, pa, _p(b), it), "mw3_upload_state_all")
 
     def state_all(self, out_km1=None, out_k=None):
         """Every wave's state at once, back to back in wave order."""
