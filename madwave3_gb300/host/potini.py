@@ -1,0 +1,361 @@
+"""pot.out: the pre-processing program that tabulates a surface for madwave3.
+
+Restates the parts of ``pot.out`` (SRC/main_potini.f:25-104) that the
+propagation reads, for a surface given as a ``potelebond(r1, r2, cos)``
+callable returning the diabatic matrix in hartree (the interface of the
+reference's pothead.f files):
+
+* ``radial_functions01_write`` (SRC/mod_baseYfunciones_01y2.f:553-836): the
+  reactant diatom's rovibrational levels on a 2000-point grid -- finite
+  difference eigenvalues as starting energies, Numerov-Cooley refinement
+  (``schr``, SRC/liboctdyn.f:405-587), spline interpolation onto the
+  propagation's r1 grid (SPLSET/SPLINQQ) and normalisation -- written to
+  ``func/bcwf`` and ``func/eref``;
+* ``pot1`` (SRC/mod_pot_01y2.f:147-341): the surface on the reactant Jacobi
+  grid, referred to ``eref``, kept where an adiabatic energy lies below Vcut,
+  written to ``pot/pot.NNN.dat`` and ``pot/cont.pot``.
+
+The finite-difference eigenvalues come from LAPACK's tridiagonal solver where
+the reference calls Numerical Recipes' TQLI (SRC/liboctdyn.f:233-296); they
+only seed the Numerov iterations, which converge to the same levels.
+"""
+import math
+import os
+
+import numpy as np
+from scipy.linalg import eigvalsh_tridiagonal
+
+from . import constants as C
+from . import namelist
+from .setup import Inputs, input_grid, pot0
+from .transcoor import splset
+
+NPUNT = 2000        # radial_functions01_write's grid
+
+
+def _sqrt(x):
+    return math.sqrt(x) if x >= 0.0 else float("nan")
+
+
+def schr(e0, rmin, rmax, n, maxit, eps, v):
+    """SCHR (SRC/liboctdyn.f:405-587): Numerov-Cooley eigenvalue refinement of
+    -p'' + v p = e p on n points of [rmin, rmax] (v and e in the units of
+    2 m E).  Inward integration from rmax to the matching point (the first
+    maximum of |p| coming in), outward from rmin, Cooley's energy correction,
+    repeated until the correction stops shrinking and is below eps.
+    Returns (e2, nodes, p) with p normalised to sum p^2 h = 1."""
+    h = (rmax - rmin) / float(n - 1)
+    h2 = h ** 2
+    hv = h2 / 12.0
+    e = e0
+    test = -1.0
+    de = 0.0
+    dold = 0.0
+    p = [0.0] * (n + 1)           # 1-based as the Fortran arrays
+    V = [0.0] + list(v)
+    df = 0.0
+    for _ in range(maxit):
+        # inward integration, first steps
+        p[n] = 1.0e-30
+        gn = V[n] - e
+        gi = V[n - 1] - e
+        if not gi >= 0.0:
+            e = V[n - 2]
+        apr = (rmax - h) * _sqrt(gi) - rmax * _sqrt(gn)
+        if apr > 50.0:
+            apr = 50.0
+        p[n - 1] = p[n] * math.exp(-apr) if apr == apr else float("nan")
+        y1 = (1.0 - hv * gn) * p[n]
+        y2 = (1.0 - hv * gi) * p[n - 1]
+        m = n - 2
+        while True:
+            y3 = y2 + ((y2 - y1) + h2 * gi * p[m + 1])
+            gi = V[m] - e
+            p[m] = y3 / (1.0 - hv * gi)
+            if not abs(p[m]) < 1.0e34:
+                if p[m] != p[m]:
+                    pass              # NaN: the reference carries it on
+                else:
+                    pm = p[m + 1]
+                    for j in range(m + 1, n + 1):
+                        p[j] = p[j] / pm
+                    y1, y2, y3 = y1 / pm, y2 / pm, y3 / pm
+                    gi = V[m + 1] - e
+                    continue
+            if abs(p[m]) <= abs(p[m + 1]) or m <= 2:
+                break
+            y1, y2 = y2, y3
+            m -= 1
+        pm = p[m]
+        yin = y2 / pm
+        for j in range(m, n + 1):
+            p[j] = p[j] / pm
+        # outward integration
+        p[1] = 1.0
+        y1 = 0.0
+        gi = V[1] - e
+        y2 = (1.0 - hv * gi) * p[1]
+        i = 2
+        while i <= m:
+            y3 = y2 + ((y2 - y1) + h2 * gi * p[i - 1])
+            gi = V[i] - e
+            p[i] = y3 / (1.0 - hv * gi)
+            if not abs(p[i]) < 1.0e34 and p[i] == p[i]:
+                i1 = i - 1
+                pm = p[i1]
+                for j in range(1, i1 + 1):
+                    p[j] = p[j] / pm
+                y1, y2, y3 = y1 / pm, y2 / pm, y3 / pm
+                gi = V[i1] - e
+                continue          # label 110: the same point again
+            y1, y2 = y2, y3
+            i += 1
+        pm = p[m]
+        if pm == 0.0:
+            # label 149 is reached before DOLD = DE: the old DOLD is kept
+            f = 9.99999e29
+            df = -f
+            de = abs(0.0001 * e)
+        else:
+            yout = y1 / pm
+            ym = y3 / pm
+            for j in range(1, m + 1):
+                p[j] = p[j] / pm
+            df = 0.0
+            for j in range(1, n + 1):
+                df = df - p[j] ** 2
+            f = (-yout - yin + 2.0 * ym) / h2 + (V[m] - e)
+            dold = de
+            if abs(f) < 1.0e37:
+                de = -f / df
+            else:
+                f = 9.99999e29
+                df = -f
+                de = abs(0.0001 * e)
+        eold = e
+        e = e + de
+        test = max(abs(dold) - abs(de), test)
+        if test < 0.0:
+            continue
+        if abs(e - eold) < eps:
+            break
+    # node count (labels 173-192)
+    kv = 0
+    for j in range(3, n - 1):
+        pj, pjm, pjp, pjm2 = p[j], p[j - 1], p[j + 1], p[j - 2]
+        if pj >= 0.0:
+            if pjm < 0.0 and pjp >= 0.0 and pjm2 < 0.0:
+                kv += 1
+        else:
+            if pjm > 0.0:
+                if pjp < 0.0 and pjm2 >= 0.0:
+                    kv += 1
+            elif pjm == 0.0:
+                if pjp < 0.0 and pjm2 > 0.0:
+                    kv += 1
+    sn = _sqrt(-h * df)
+    return e, kv, [x / sn for x in p[1:]]
+
+
+def splinqq_many(f, d, x, rr):
+    """SPLINQQ (SRC/liboctdyn.f:298-340) at increasing points rr: the cubic
+    Hermite piece of the first knot above r (searched from the second knot),
+    or the C6/r^6 + C8/r^8 tail at and beyond the last knot."""
+    rr = np.asarray(rr, np.float64)
+    nx = len(x)
+    out = np.empty(rr.size)
+    for k, r in enumerate(rr):
+        if r >= x[nx - 1]:
+            ro, yo, yp = x[nx - 1], f[nx - 1], d[nx - 1]
+            ain = yo + yp * ro / 6.0
+            c8 = -ain * 3.0 * ro ** 8
+            c6 = yo * ro ** 6 - c8 / ro / ro
+            out[k] = c6 / r ** 6 + c8 / r ** 8
+            continue
+        idol = max(1, int(np.searchsorted(x, r, side="right")))
+        hi = x[idol] - x[idol - 1]
+        xr = (r - x[idol - 1]) / hi
+        u1 = xr * xr * (-2.0 * xr + 3.0)
+        u3 = hi * xr * xr * (xr - 1.0)
+        u2 = 1.0 - u1
+        u4 = hi * xr * ((xr - 2.0) * xr + 1.0)
+        out[k] = u1 * f[idol] + u2 * f[idol - 1] + u3 * d[idol] + u4 * d[idol - 1]
+    return out
+
+
+def _inputs(path_or_groups):
+    groups = namelist.read(path_or_groups) if isinstance(path_or_groups, str) else path_or_groups
+    inp = Inputs.from_namelists(groups)
+    flat = {}
+    for g in groups.values():
+        flat.update(g)
+    return inp, flat
+
+
+class _Grid:
+    pass
+
+
+def _grid(inp):
+    g = _Grid()
+    g.inp = inp
+    input_grid(g)
+    pot0(g)
+    return g
+
+
+def radial_functions01_write(g, potelebond, r2inf=100.0, nelec=1, bound_test="margin"):
+    """Reactant (01) diatom levels and functions on the propagation's r1 grid
+    (SRC/mod_baseYfunciones_01y2.f:553-836).  Returns (nobc[nelec][nj],
+    ediat[nelec][nj][nv] in zot, fd[nelec][nj][nv][npun1], ediatref).
+
+    ``bound_test`` picks which levels count as bound.  "margin" is the shipped
+    source: E more than 0.01 hartree below V at the grid's end (:702), level
+    counts starting at nvini - 1 (:584) and the j loop ending at the first j
+    with at most one level whose last v failed (:758).  "below_asymptote" is
+    the earlier form the same routine has in SRC/mod_baseYfunciones_Renner_01y2.f
+    (:567, :684, :737) and in the comment at :701: E below V at the grid's
+    end, counts starting at 0 and the loop ending at a j whose count stayed 0;
+    the shipped H + HD run (EXAMPLES/HD+H_collision/J000-check) was made with
+    it (its log lists the j = 37..39 entries that only a count of 0 leaves)."""
+    if bound_test not in ("margin", "below_asymptote"):
+        raise ValueError("bound_test must be 'margin' or 'below_asymptote'")
+    inp = g.inp
+    n1 = inp.npun1
+    nj = inp.jmax - inp.jini + 1
+    nv = inp.nvmax - inp.nvini + 1
+    nobc = np.full((nelec, nj), inp.nvini - 1 if bound_test == "margin" else 0, np.int32)
+    ediat = np.zeros((nelec, nj, nv))
+    fd = np.zeros((nelec, nj, nv, n1))
+    rmis = inp.rmis1 / C.convl
+    rfin = (inp.rmis1 + float(n1 - 1) * g.ah1) / C.convl
+    ah = (rfin - rmis) / float(NPUNT - 1)
+    rg = r2inf / C.convl
+    xm = g.xm1reac * C.convm
+    xz = 0.5 / xm
+    r = rmis + np.arange(NPUNT, dtype=np.float64) * ah
+    r1grid = np.array([(inp.rmis1 + float(ir1) * g.ah1) / C.convl for ir1 in range(n1)])
+    for ie in range(nelec):
+        V = potelebond(r, np.full(NPUNT, rg), 1.0)[ie, ie]
+        irmin = 0
+        vmin = 1e10
+        for ir in range(NPUNT):
+            if V[ir] < vmin:
+                vmin = V[ir]
+                irmin = ir
+        if irmin == 0:
+            continue                       # repulsive state: no bound levels
+        for jj, j in enumerate(range(inp.jini, inp.jmax + 1)):
+            xl = 0.5 * float(j * (j + 1)) / xm
+            vv = V + xl / r / r
+            diag = -2.0 - 2.0 * xm * vv * ah * ah
+            lam = eigvalsh_tridiagonal(diag, np.ones(NPUNT - 1))
+            alpha = np.sort(-xz * lam / ah / ah)
+            ifail = -1
+            for iv in range(inp.nvini, inp.nvmax + 1):
+                ifail = -1
+                if (V[NPUNT - 1] - alpha[iv] > 1.0e-2) if bound_test == "margin" else (alpha[iv] < V[NPUNT - 1]):
+                    xz1 = 2.0 * xm
+                    e0 = alpha[iv] * xz1
+                    vvs = (vv * xz1).tolist()
+                    e2, _, p = schr(e0, rmis, rfin, NPUNT, 20, 1.0e-10, vvs)
+                    e2 = e2 / xz1
+                    ediat[ie, jj, iv - inp.nvini] = e2 / C.conve * C.conve1
+                    nobc[ie, jj] = iv
+                    ifail = 0
+                    ff = np.array(p) / math.sqrt(C.convl)
+                    d = splset(ff, r)
+                    vals = np.zeros(n1)
+                    inside = (r1grid >= r[0]) & (r1grid <= r[NPUNT - 1])
+                    vals[inside] = splinqq_many(ff, d, r, r1grid[inside])
+                    xnorm = float(np.sum(vals * vals)) * g.ah1
+                    fd[ie, jj, iv - inp.nvini] = vals * (math.sqrt(g.ah1) / math.sqrt(xnorm))
+            last = nobc[ie, jj] <= 0 if bound_test == "margin" else nobc[ie, jj] == 0
+            if last and ifail == -1:
+                break                      # no bound levels for higher j
+    ediatref = 0.0
+    if inp.iprod != 1 and n1 > 1:
+        if (inp.nvini <= inp.nvref <= inp.nvmax and inp.jref <= inp.jmax and inp.ielecref <= nelec):
+            ediatref = ediat[inp.ielecref - 1, inp.jref - inp.jini, inp.nvref - inp.nvini]
+        if inp.no_ref_energy == 0:
+            ediatref = 0.0
+    return nobc, ediat, fd, ediatref
+
+
+def write_func(outdir, inp, nobc, ediat, fd, ediatref, nelec=1):
+    """func/bcwf and func/eref (SRC/mod_baseYfunciones_01y2.f:785-808)."""
+    os.makedirs(os.path.join(outdir, "func"), exist_ok=True)
+    lines = []
+    for ie in range(nelec):
+        for jj, j in enumerate(range(inp.jini, inp.jmax + 1)):
+            lines.append("%d %d %d" % (ie + 1, j, nobc[ie, jj]))
+            for iv in range(inp.nvini, nobc[ie, jj] + 1):
+                lines.append("%d %r" % (iv, float(ediat[ie, jj, iv - inp.nvini])))
+                lines.extend(repr(float(x)) for x in fd[ie, jj, iv - inp.nvini])
+    with open(os.path.join(outdir, "func", "bcwf"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    with open(os.path.join(outdir, "func", "eref"), "w") as f:
+        f.write("%r\n" % float(ediatref))
+
+
+def pot1(g, potelebond, vref, outdir, nelec=1):
+    """SRC/mod_pot_01y2.f:147-341 for one electronic state: V on the grid in
+    zot minus vref, stored where it lies below Vcut (capped at Vcut otherwise);
+    pot/pot.NNN.dat rows 'ir1 ir2 V' with ir2 outer and ir1 inner, and
+    pot/cont.pot.  Returns (npunreal, vmin, vmaxtot)."""
+    if nelec != 1:
+        raise NotImplementedError("pot1 is restated for one electronic state")
+    inp = g.inp
+    os.makedirs(os.path.join(outdir, "pot"), exist_ok=True)
+    n1, n2 = inp.npun1, inp.npun2
+    vcut = g.vcutmax
+    r1 = inp.rmis1 + np.arange(n1, dtype=np.float64) * g.ah1
+    r2 = inp.rmis2 + np.arange(n2, dtype=np.float64) * g.ah2
+    rpeq = np.broadcast_to((r1 / C.convl)[None, :], (n2, n1))     # [ir2][ir1]
+    Rg = np.broadcast_to((r2 / C.convl)[:, None], (n2, n1))
+    gam = inp.xm1 / (inp.xm0 + inp.xm1)
+    vmin = 1e10
+    vmaxtot = vcut
+    npunreal = []
+    for iang in range(inp.nangu):
+        ctet = float(g.cgamma[iang])
+        X2 = np.sqrt(Rg * Rg + gam * gam * rpeq * rpeq + 2.0 * gam * Rg * rpeq * ctet)
+        calpha = (Rg * ctet + gam * rpeq) / X2
+        calpha = np.where(np.abs(calpha) > 1.0, calpha / np.abs(calpha), calpha)
+        with np.errstate(invalid="ignore"):
+            pm = potelebond(rpeq, X2, calpha)[0, 0]
+        v = pm / C.conve * C.conve1 - vref
+        v = np.where(v > vcut, vcut, v)
+        vmaxtot = max(vmaxtot, float(np.nanmax(v)))
+        vmin = min(vmin, float(np.nanmin(v)))
+        keep = v < vcut
+        i2, i1 = np.nonzero(keep)
+        vals = v[i2, i1]
+        with open(os.path.join(outdir, "pot", "pot.%03d.dat" % (iang + 1)), "w") as f:
+            f.write("".join("%d %d %r\n" % (a + 1, b + 1, float(x)) for a, b, x in zip(i1, i2, vals)))
+        npunreal.append(len(i1))
+    with open(os.path.join(outdir, "pot", "cont.pot"), "w") as f:
+        f.write("%d\n0 0 1.0 1.0\n" % nelec)
+        f.write("%r %d %r\n" % (vmin, sum(npunreal), vmaxtot))
+        f.write("%r %r %d\n" % (inp.rmis1, inp.rfin1, n1))
+        f.write("%r %r %d\n" % (inp.rmis2, inp.rfin2, n2))
+        f.write("%d %d\n" % (inp.nangu, inp.inc))
+        f.write(" ".join("%d" % n for n in npunreal) + "\n")
+    return np.array(npunreal, np.int32), vmin, vmaxtot
+
+
+def write_case(outdir, inputfile, potelebond, bound_test="margin"):
+    """pot.out for one input.dat and surface: func/ and pot/ beside a copy of
+    the input.  Returns a summary (levels, eref, points per angle, vmin)."""
+    inp, flat = _inputs(inputfile)
+    os.makedirs(outdir, exist_ok=True)
+    groups = namelist.read(inputfile)
+    with open(os.path.join(outdir, "input.dat"), "w") as f:
+        f.write(namelist.dumps(groups))
+    g = _grid(inp)
+    r2inf = float(flat.get("r2inf_radial_functions", 100.0))
+    nobc, ediat, fd, eref = radial_functions01_write(g, potelebond, r2inf=r2inf, bound_test=bound_test)
+    write_func(outdir, inp, nobc, ediat, fd, eref)
+    npunreal, vmin, vmaxtot = pot1(g, potelebond, eref, outdir)
+    return {"nobc": nobc, "ediat": ediat, "fd": fd, "ediatref": eref, "npunreal": npunreal,
+            "vmin": vmin, "vmaxtot": vmaxtot, "cgamma": g.cgamma}
