@@ -344,12 +344,13 @@ def pot1(g, potelebond, vref, outdir, nelec=1):
     return np.array(npunreal, np.int32), vmin, vmaxtot
 
 
-def write_case(outdir, inputfile, potelebond, bound_test="margin"):
-    """pot.out for one input.dat and surface: func/ and pot/ beside a copy of
-    the input.  Returns a summary (levels, eref, points per angle, vmin)."""
-    inp, flat = _inputs(inputfile)
+def write_case(outdir, inputfile, potelebond, bound_test="margin", input_text=None):
+    """pot.out for one input.dat (a path, or its text in ``input_text``) and a
+    surface: func/ and pot/ beside a copy of the input.  Returns a summary
+    (levels, eref, points per angle, vmin)."""
+    groups = namelist.parse(input_text) if input_text is not None else namelist.read(inputfile)
+    inp, flat = _inputs(groups)
     os.makedirs(outdir, exist_ok=True)
-    groups = namelist.read(inputfile)
     with open(os.path.join(outdir, "input.dat"), "w") as f:
         f.write(namelist.dumps(groups))
     g = _grid(inp)

@@ -52,3 +52,33 @@ def synthetic_product_tables(run, seed=20261203):
         rng.uniform(0.5, 1.5, run.ntot),
         rng.uniform(-1.0, 1.0, (run.ncan, nom, nang, n2p)),
         rng.standard_normal((nom, njp, nvp, run.nelec, nang, n2p)))
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="session")
+def example_pins():
+    import json
+    with open(os.path.join(GOLDEN, "example_pins.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def example_case(tmp_path_factory, example_pins):
+    """The reference's shipped H + HD example (EXAMPLES/HD+H_collision: J = 0,
+    256 r1 x 256 R x 140 angles, its neural-network H3 surface), tabulated by
+    the restated pot.out from the example's input file and the surface's
+    weights (tests/golden/).  Returns (case directory, pot.out summary)."""
+    from madwave3_gb300.host import h3nn, potini
+    d = str(tmp_path_factory.mktemp("example") / "HD+H")
+    nn = h3nn.H3NN(os.path.join(GOLDEN, "h3nn_weights.json"))
+    summary = potini.write_case(d, None, nn.potelebond, bound_test="below_asymptote",
+                                input_text=example_pins["input_dat"])
+    return d, summary
+
+
+@pytest.fixture(scope="session")
+def example_run(example_case):
+    from madwave3_gb300.host import setup
+    return setup.load(os.path.join(example_case[0], "input.dat"))

@@ -17,6 +17,7 @@ Sources (inside the reference):
 * J000-check/S2prod.v00.J000.k00008, the same run's probability file
   (its layout in reference_pins.json, every row in example_pins.json);
 * EXAMPLES/HD+H_collision/README.md (the 60-angle list of its pot.out run);
+* EXAMPLES/HD+H_collision/input.dat, the run's namelists (example_pins.json);
 * EXAMPLES/HD+H_collision/pes/FFmodules.f90: the weights and scalings of the
   example's neural-network surface, kept as their decimal text (h3nn_weights.json).
 """
@@ -105,9 +106,11 @@ def _table_after(sal, header, ncols):
     return rows
 
 
-def example_pins(sal, s2p):
-    """The numbers of the shipped run that depend on its neural-network surface."""
-    out = {"source": "EXAMPLES/HD+H_collision/J000-check/sal.000 and S2prod.v00.J000.k00008"}
+def example_pins(ref, sal, s2p):
+    """The numbers of the shipped run that depend on its neural-network surface,
+    and the run's input file."""
+    out = {"source": "EXAMPLES/HD+H_collision/J000-check/sal.000 and S2prod.v00.J000.k00008",
+           "input_dat": open(os.path.join(ref, "EXAMPLES/HD+H_collision/input.dat")).read()}
     # reactant (01) diatomic levels minus ediatref: ie, j, v, E(eV)
     out["reactant_levels_ev"] = _table_after(sal, "ie  j   v   E(eV)", 4)
     # product (02) diatomic levels minus ediatref: j, v, E(eV)
@@ -160,7 +163,7 @@ def main(ref):
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
         json.dump(pins, f, indent=1)
     with open(os.path.join(HERE, "example_pins.json"), "w") as f:
-        json.dump(example_pins(sal, s2p), f, separators=(",", ":"))
+        json.dump(example_pins(ref, sal, s2p), f, separators=(",", ":"))
     with open(os.path.join(HERE, "h3nn_weights.json"), "w") as f:
         json.dump(nn_weights(ref), f, indent=0)
 

@@ -1,0 +1,85 @@
+"""The GPU path against the reference's own run of its H + HD example.
+
+The case (EXAMPLES/HD+H_collision: J = 0, 256 x 256 x 140, its neural-network
+H3 surface, 704,278 stored points) is tabulated here by the restated pot.out,
+then propagated on the GB300 for the run's 4000 Chebyshev iterations.  The
+reference printed ||psi_k||^2 for k = 1..4001 at 17 digits (sal.000) and P(E)
+at 7 (S2prod.v00.J000.k00008, columns 2 and 3: the total reaction probability
+of totalflux and that plus the reactant-channel sum of printprob).
+
+The FP64 path reproduces the norm trace to 1e-10 relative (the north-star
+bar for the plain FP64 path) and P(E) to the file's print precision; the
+mixed path (FP32 transforms) reproduces P(E) to 1e-4 absolute, the bar of
+the mixed form."""
+import numpy as np
+import pytest
+
+from madwave3_gb300.host import constants as C
+
+pytestmark = pytest.mark.gpu
+
+
+def _print_close(a, b, digits=7):
+    """|a - b| within one unit of the last printed digit of b (E13.7: 7
+    significant digits), or both below the file's 1e-90 floor."""
+    a, b = np.asarray(a), np.asarray(b)
+    scale = np.where(b != 0.0, 10.0 ** (np.floor(np.log10(np.abs(np.where(b != 0.0, b, 1.0)))) + 1 - digits), 0.0)
+    return np.abs(a - b) <= np.maximum(scale, 1e-90)
+
+
+@pytest.fixture(scope="module")
+def fp64_run(example_run):
+    from madwave3_gb300 import Propagator
+    prop = Propagator(example_run, "fp64")
+    h = prop.hphi(example_run.psi0)
+    prop.start()
+    prop.run(4000)
+    out = {"h": h, "norms": prop.norms(), "pe": prop.totalflux()[0], "acc": prop.accumulators(),
+           "tables": prop.tables()}
+    prop.close()
+    return out
+
+
+def test_fp64_mean_energy(example_run, example_pins, fp64_run):
+    em = float(np.dot(example_run.psi0, fp64_run["h"])) / C.conve1 / 8065.5
+    assert abs(em - example_pins["mean_energy_ev"]) / example_pins["mean_energy_ev"] < 1e-13
+
+
+def test_fp64_norm_trace(example_pins, fp64_run):
+    ref = np.array(example_pins["norm_trace"])
+    got = fp64_run["norms"]
+    assert got.size == ref.size == 4001
+    rel = np.abs(got - ref) / ref
+    assert rel.max() < 1e-10, (int(np.argmax(rel)) + 1, float(rel.max()))
+
+
+def test_fp64_probabilities(example_run, example_pins, fp64_run):
+    """S2prod columns 1-3 after the 4000 iterations: E, P(E) and P(E) plus the
+    reactant channels' sum (printprob, SRC/main_madwave3.f:640-746)."""
+    from madwave3_gb300.printprob import s2_elements
+    rows = np.array(example_pins["s2prod_rows"])
+    t = fp64_run["tables"]
+    e_ev = t["etot"] / C.conve1 / C.eV2cm
+    assert np.all(_print_close(e_ev, rows[:, 0]))
+    pe = np.where(fp64_run["pe"] < 1e-90, 0.0, fp64_run["pe"])
+    ok = _print_close(pe, rows[:, 1])
+    assert ok.all(), np.nonzero(~ok)[0][:10]
+    s2reac = s2_elements(example_run, fp64_run["acc"]["zs2"], t["s2factor"]).sum(axis=(0, 1, 2))
+    ok3 = _print_close(pe + s2reac, rows[:, 2])
+    assert ok3.all(), np.nonzero(~ok3)[0][:10]
+
+
+def test_mixed_probabilities(example_run, example_pins):
+    """The mixed path's P(E) after the same 4000 iterations, against the
+    reference's printed P(E): within 1e-4 absolute."""
+    from madwave3_gb300 import Propagator
+    prop = Propagator(example_run, "mixed")
+    prop.start()
+    prop.run(4000)
+    pe = prop.totalflux()[0]
+    norms = prop.norms()
+    prop.close()
+    rows = np.array(example_pins["s2prod_rows"])
+    assert np.abs(pe - rows[:, 1]).max() <= 1e-4
+    ref = np.array(example_pins["norm_trace"])
+    assert np.max(np.abs(norms - ref)) / ref.max() < 1e-4
