@@ -149,6 +149,12 @@ module mw3gpu
        integer(c_int32_t), value :: wave_id
        complex(c_double_complex), intent(in) :: zcr(*), zcdr(*), zs2(*)
      end function
+     integer(c_int) function mw3_packet_energy_norm(ctx, wave_id, apaqini) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: wave_id
+       real(c_double) :: apaqini(*)
+     end function
      integer(c_int) function mw3_set_product_projection(ctx, wave_id, proj) bind(c)
        import
        type(c_ptr), value :: ctx

@@ -166,6 +166,12 @@ int mw3_upload_accumulators(mw3_ctx *ctx, int32_t wave_id, const double *zcr, co
 int mw3_tables(mw3_ctx *ctx, int32_t wave_id, int32_t *nopr1, double *etot, double *reacfct,
                double *s2factor, double *absfr1, double *absfr2);
 
+/* apaqini[netot]: the energy distribution |<packet|E>|^2 of the initial
+ * collision packet that Smatini_col computes (SRC/mod_flux_01y2.f:467-524) and
+ * the reference keeps in mod_flux for its normalisations -- ini_transcoor's
+ * S2prodfac (SRC/mod_coortrans01_02.f:121-145) among them. */
+int mw3_packet_energy_norm(mw3_ctx *ctx, int32_t wave_id, double *apaqini);
+
 /* Number of CUDA kernels this context has launched so far. */
 int mw3_kernel_launches(mw3_ctx *ctx, int64_t *count);
 

@@ -1186,6 +1186,14 @@ int mw3_tables(mw3_ctx *h, int32_t w, int32_t *nopr1, double *etot, double *reac
     return MW3_OK;
 }
 
+int mw3_packet_energy_norm(mw3_ctx *h, int32_t w, double *apaqini)
+{
+    if (!h || !apaqini || w < 0 || w >= (int)h->c.waves.size()) return MW3_ERR_ARG;
+    const WaveTables &t = h->c.waves[w];
+    std::copy(t.apaqini.begin(), t.apaqini.end(), apaqini);
+    return MW3_OK;
+}
+
 int mw3_kernel_launches(mw3_ctx *h, int64_t *count)
 {
     if (!h || !count) return MW3_ERR_ARG;

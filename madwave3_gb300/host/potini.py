@@ -282,6 +282,52 @@ def radial_functions01_write(g, potelebond, r2inf=100.0, nelec=1, bound_test="ma
     return nobc, ediat, fd, ediatref
 
 
+def product_radialf_write(g, potelebond, nviniprod, nvmaxprod, jiniprod, jmaxprod, n2prod1, r1inf=100.0,
+                          nelec=1):
+    """Product (02) diatom states on the R grid, the diabatic form of
+    product_radialf_write (SRC/mod_baseYfunciones_01y2.f:1065-1308 with
+    diabatic_prod_pot > 0): per j, the box DVR of bndbcele
+    (SRC/liboctdyn.f:1687-1814) on the npun2 points of [rmis2, rfin2], kinetic
+    matrix (-1)^(i-i') (1/(i-i')^2 + 1/(i+i')^2) / (ah^2 mu) off the diagonal
+    and (pi^2/6 + 1/(2i)^2) / (ah^2 mu) on it, the lowest nvmaxprod - nviniprod
+    + 1 levels kept (all of them, noBCprod = nvmaxprod).  The shipped H + HD run
+    took its product states from this form (its log's product levels agree with
+    it to 1e-13 eV).  Eigenvector signs are free; each state is made positive
+    at its largest component.  Returns (fdprod[njp][nvp][nelec][n2prod1],
+    ediatprod[njp][nvp] in zot, nobcprod[njp])."""
+    inp = g.inp
+    if nelec != 1:
+        raise NotImplementedError("product_radialf_write is restated for one electronic state")
+    npun = inp.npun2
+    rmis = inp.rmis2 / C.convl
+    rfin = inp.rfin2 / C.convl
+    ah = (rfin - rmis) / float(npun - 1)
+    rg = r1inf / C.convl
+    xmu = g.xm1prod * C.convm
+    r = rmis + np.arange(npun, dtype=np.float64) * ah
+    V = potelebond(np.full(npun, rg), r, 1.0)[0, 0]
+    i = np.arange(1, npun + 1)
+    menos = (i[:, None] - i[None, :]).astype(np.float64)
+    mas = (i[:, None] + i[None, :]).astype(np.float64)
+    sign = np.where((i[:, None] - i[None, :]) % 2 == 0, 1.0, -1.0)
+    x1 = np.where(menos == 0.0, math.pi * math.pi / 6.0, 1.0 / np.where(menos == 0.0, 1.0, menos * menos))
+    T = sign * (x1 + 1.0 / (mas * mas)) / (ah * ah) / xmu
+    njp, nvp = jmaxprod - jiniprod + 1, nvmaxprod - nviniprod + 1
+    fdprod = np.zeros((njp, nvp, nelec, n2prod1))
+    ediatprod = np.zeros((njp, nvp))
+    for jj, j in enumerate(range(jiniprod, jmaxprod + 1)):
+        xl = 0.5 * float(j * (j + 1)) / xmu
+        H = T + np.diag(xl / (r * r) + V)
+        w, vec = np.linalg.eigh(H)
+        for k, iv in enumerate(range(nviniprod, nvmaxprod + 1)):
+            c = vec[:, k]
+            if c[np.argmax(np.abs(c))] < 0:
+                c = -c
+            ediatprod[jj, k] = w[k] / C.conve * C.conve1
+            fdprod[jj, k, 0] = (c / math.sqrt(ah))[:n2prod1] * math.sqrt(g.ah2 / C.convl)
+    return fdprod, ediatprod, np.full(njp, nvmaxprod, np.int32)
+
+
 def write_func(outdir, inp, nobc, ediat, fd, ediatref, nelec=1):
     """func/bcwf and func/eref (SRC/mod_baseYfunciones_01y2.f:785-808)."""
     os.makedirs(os.path.join(outdir, "func"), exist_ok=True)
@@ -358,5 +404,12 @@ def write_case(outdir, inputfile, potelebond, bound_test="margin", input_text=No
     nobc, ediat, fd, eref = radial_functions01_write(g, potelebond, r2inf=r2inf, bound_test=bound_test)
     write_func(outdir, inp, nobc, ediat, fd, eref)
     npunreal, vmin, vmaxtot = pot1(g, potelebond, eref, outdir)
-    return {"nobc": nobc, "ediat": ediat, "fd": fd, "ediatref": eref, "npunreal": npunreal,
-            "vmin": vmin, "vmaxtot": vmaxtot, "cgamma": g.cgamma}
+    out = {"nobc": nobc, "ediat": ediat, "fd": fd, "ediatref": eref, "npunreal": npunreal,
+           "vmin": vmin, "vmaxtot": vmaxtot, "cgamma": g.cgamma}
+    prod = groups.get("inputprod", {})
+    if int(prod.get("iprod", 0)) == 2:
+        out["product"] = product_radialf_write(
+            g, potelebond, int(prod.get("nviniprod", 0)), int(prod.get("nvmaxprod", 0)),
+            int(prod.get("jiniprod", 0)), int(prod.get("jmaxprod", 0)), int(prod.get("n2prod1", inp.npun2)),
+            r1inf=float(flat.get("r1inf_radial_functions", 100.0)))
+    return out

@@ -30,7 +30,7 @@ import math
 
 import numpy as np
 
-from .wigner import dwigner
+from .wigner import dwigner, dwigner_vec
 
 
 # ---------------------------------------------------------------------------
@@ -115,6 +115,35 @@ def splinqq(f, d, x, r, iold=1):
     return u1 * f[idol] + u2 * f[idol - 1] + u3 * d[idol] + u4 * d[idol - 1]
 
 
+def splinqq_vec(f, d, x, rr):
+    """splinqq at many points at once (each searched from the second knot, as
+    the reference does for increasing points)."""
+    f = np.asarray(f, np.float64)
+    d = np.asarray(d, np.float64)
+    x = np.asarray(x, np.float64)
+    rr = np.asarray(rr, np.float64)
+    nx = len(x)
+    out = np.empty(rr.shape)
+    tail = rr >= x[nx - 1]
+    if tail.any():
+        ro, yo, yp = x[nx - 1], f[nx - 1], d[nx - 1]
+        ain = yo + yp * ro / 6.0
+        c8 = -ain * 3.0 * ro ** 8
+        c6 = yo * ro ** 6 - c8 / ro / ro
+        rt = rr[tail]
+        out[tail] = c6 / rt ** 6 + c8 / rt ** 8
+    r = rr[~tail]
+    idol = np.maximum(1, np.searchsorted(x, r, side="right"))
+    hi = x[idol] - x[idol - 1]
+    xr = (r - x[idol - 1]) / hi
+    u1 = xr * xr * (-2.0 * xr + 3.0)
+    u3 = hi * xr * xr * (xr - 1.0)
+    u2 = 1.0 - u1
+    u4 = hi * xr * ((xr - 2.0) * xr + 1.0)
+    out[~tail] = u1 * f[idol] + u2 * f[idol - 1] + u3 * d[idol] + u4 * d[idol - 1]
+    return out
+
+
 # ---------------------------------------------------------------------------
 # mass factors of the reactant -> product Jacobi change
 # ---------------------------------------------------------------------------
@@ -151,6 +180,7 @@ def trans_rg_jac(run, rbalinprod, nangproj0, nangproj1):
     r1 = inp.rmis1 + np.arange(n1) * ah1
     out = np.zeros(run.ntot)
     c0 = (xm0 + xm2) * rbalinprod / xm2
+    s1 = np.sin(np.outer(r1, xk))
     for iang in range(nangproj0, nangproj1 + 1):
         cg = run.cgamma[iang - 1]
         raux = np.zeros((n2, n1))
@@ -162,7 +192,7 @@ def trans_rg_jac(run, rbalinprod, nangproj0, nangproj1):
             r1inter = (r2 * cg + math.sqrt(c0 * c0 + x2)) / a
             if not (inp.rmis1 < r1inter < inp.rfin1):
                 continue
-            s = np.sin(np.outer(r1, xk)) @ np.sin(xk * r1inter)
+            s = s1 @ np.sin(xk * r1inter)
             jac1 = math.sqrt(x2 + (rbalinprod * (xm0 + xm2) / xm2) ** 2)
             jac = math.sqrt(rbalinprod * ((xm0 + xm2) / xm2) ** 2 / (a * jac1))
             raux[ir2] = s * 2.0 / (n1 + 1.0) * jac / math.sqrt(ah1)
@@ -215,6 +245,65 @@ def prod_functions(run, rbalinprod, fdprod, n2prod0, n2prod1, nangproj0, nangpro
                 a, _ = _ab(inp)
                 xjaco = rgb * ((xm0 + inp.xm2) / inp.xm2) ** 2 / (a * math.sqrt(xjac1))
                 out[ielec, ia, k] = fdiat * angpart * rga * rpa * math.sqrt(xjaco) / (rpb * rgb)
+    return out
+
+
+def prod_geometry(run, rbalinprod, n2prod0, n2prod1, nangproj0, nangproj1):
+    """The per-(angle, R) quantities of prodwftrans (:485-588) that do not depend
+    on the product state: [nang][n2p] arrays of rpa, rpb, beta, the factor
+    rga rpa sqrt(xjaco) / (rpb rgb) and a mask of the points that contribute
+    (real square root, |cos beta| <= 1)."""
+    inp = run.inp
+    a, bm = _ab(inp)
+    xm0, xm1, xm2 = inp.xm0, inp.xm1, inp.xm2
+    rgb = rbalinprod
+    cg = np.asarray(run.cgamma[nangproj0 - 1:nangproj1], np.float64)[:, None]
+    rga = (inp.rmis2 + np.arange(n2prod0 - 1, n2prod1) * run.ah2)[None, :]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        sqr = rga * rga * (cg * cg - 1.0) + (rgb * (xm0 + xm2) / xm2) ** 2
+        ok = sqr > 0.0
+        rpa = (rga * cg + np.sqrt(np.where(ok, sqr, 1.0))) / a
+        rpb = np.sqrt((rpa * xm1 / (xm0 + xm1)) ** 2 + rga * rga + 2.0 * rpa * rga * cg * xm1 / (xm0 + xm1))
+        angjac = (rgb * rgb + bm * bm * rpb * rpb - (rga * (xm0 + xm1) / xm1) ** 2) * 0.5 / (bm * rpb * rgb)
+        ok &= np.abs(angjac) <= 1.0
+        beta = np.arccos(np.clip(angjac, -1.0, 1.0))
+        xjac1 = rga ** 2 * (cg ** 2 - 1.0) + (rgb * (xm0 + xm2) / xm2) ** 2
+        xjaco = rgb * ((xm0 + xm2) / xm2) ** 2 / (a * np.sqrt(np.where(ok, xjac1, 1.0)))
+        fac = rga * rpa * np.sqrt(np.where(ok, xjaco, 0.0)) / (rpb * rgb)
+    return rpa, rpb, beta, np.where(ok, fac, 0.0), ok
+
+
+def prod_functions_omega(run, rbalinprod, fdprod, nobcprod, jiniprod, jmaxprod, nviniprod, n2prod0, n2prod1,
+                         nangproj0, nangproj1, iom):
+    """prodwftrans for every product state (j, v) of one Omega at once:
+    [njp][nvp][nelec][nang][n2p] (zero for j < Omega and v > noBCprod(j)).
+    Same arithmetic as prod_functions, vectorised over the (angle, R) points."""
+    inp = run.inp
+    lmax = (inp.nangu - 1) * inp.inc
+    jmax2 = lmax * 2
+    facnorm = 1.0 / math.sqrt(2.0) if inp.inc == 2 else 1.0
+    xx = inp.rmis2 + np.arange(n2prod1) * run.ah2
+    rpa, rpb, beta, fac, ok = prod_geometry(run, rbalinprod, n2prod0, n2prod1, nangproj0, nangproj1)
+    nang, n2p = ok.shape
+    w = np.asarray(run._weiprod[nangproj0 - 1:nangproj1], np.float64)[:, None]
+    inside = ok & (rpb >= inp.rmis2) & (rpb <= inp.rfin2)
+    njp = jmaxprod - jiniprod + 1
+    nvp = int(np.max(np.asarray(fdprod).shape[1])) if njp else 0
+    out = np.zeros((njp, nvp, run.nelec, nang, n2p))
+    for ielec in range(run.nelec):
+        pm = dwigner_vec(jmax2, 2 * (iom - int(run.iomatom[ielec])), 2 * int(run.iomdiat[ielec]),
+                         beta[ok]).T                                   # [jmax2+1][npts]
+        for j in range(max(jiniprod, iom), jmaxprod + 1):
+            jj = j - jiniprod
+            ang = np.zeros((nang, n2p))
+            ang[ok] = pm[2 * j] * math.sqrt((2.0 * j + 1.0) * 0.5)
+            ang = ang * np.sqrt(w) * facnorm
+            for iv in range(nviniprod, int(nobcprod[jj]) + 1):
+                ff = np.asarray(fdprod[jj][iv - nviniprod][ielec][:n2prod1], np.float64)
+                dd = splset(ff, xx)
+                fdiat = np.zeros((nang, n2p))
+                fdiat[inside] = splinqq_vec(ff, dd, xx, rpb[inside])
+                out[jj, iv - nviniprod, ielec] = np.where(ok, fdiat * ang * fac, 0.0)
     return out
 
 
@@ -295,11 +384,8 @@ def ini_transcoor(run, rbalinprod, n2prod0, n2prod1, nangproj0, nangproj1, iommi
     nang, n2p = nangproj1 - nangproj0 + 1, n2prod1 - n2prod0 + 1
     wf = np.zeros((nom, njp, nvp, run.nelec, nang, n2p))
     for o, iom in enumerate(range(iomminprod, iommaxprod + 1)):
-        for j in range(max(jiniprod, iom), jmaxprod + 1):
-            jj = j - jiniprod
-            for iv in range(nviniprod, int(nobcprod[jj]) + 1):
-                wf[o, jj, iv - nviniprod] = prod_functions(run, rbalinprod, fdprod[jj][iv - nviniprod], n2prod0,
-                                                           n2prod1, nangproj0, nangproj1, iom, j, iv)
+        wf[o] = prod_functions_omega(run, rbalinprod, fdprod, nobcprod, jiniprod, jmaxprod, nviniprod, n2prod0,
+                                     n2prod1, nangproj0, nangproj1, iom)
     return ProductProjection(
         n2prod0, n2prod1, nangproj0, nangproj1, iomminprod, iommaxprod, jiniprod, jmaxprod, nviniprod, nvmaxprod,
         np.asarray(nobcprod, np.int32), trans_rg_jac(run, rbalinprod, nangproj0, nangproj1),

@@ -66,7 +66,8 @@ HEADER_FUNCS = [
     "mw3_create", "mw3_add_wave", "mw3_wave_size", "mw3_hphi", "mw3_start", "mw3_upload_state",
     "mw3_run", "mw3_sync", "mw3_download_state", "mw3_upload_state_all", "mw3_download_state_all",
     "mw3_norms", "mw3_totalflux", "mw3_flux_count",
-    "mw3_download_accumulators", "mw3_tables", "mw3_kernel_launches", "mw3_path_flags", "mw3_get_stream",
+    "mw3_download_accumulators", "mw3_tables", "mw3_packet_energy_norm", "mw3_kernel_launches", "mw3_path_flags",
+    "mw3_get_stream",
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_set_product_projection", "mw3_download_product",
     "mw3_upload_accumulators", "mw3_upload_product",
@@ -114,6 +115,7 @@ def load_library(build_if_missing=True):
     L.mw3_flux_count.argtypes = [vp, ct.c_int32, I32P]
     L.mw3_download_accumulators.argtypes = [vp, ct.c_int32, F64P, F64P, F64P, F64P, F64P]
     L.mw3_tables.argtypes = [vp, ct.c_int32, I32P, F64P, F64P, F64P, F64P, F64P]
+    L.mw3_packet_energy_norm.argtypes = [vp, ct.c_int32, F64P]
     L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
     L.mw3_path_flags.argtypes = [vp, ct.POINTER(ct.c_int32)]
     L.mw3_get_stream.argtypes = [vp, ct.POINTER(ct.c_void_p)]
@@ -376,7 +378,9 @@ class Propagator:
         a1, a2 = np.empty(i.npun1), np.empty(i.npun2)
         self._check(self.L.mw3_tables(self.h, wave, _p(nopr1, ct.c_int32), _p(etot), _p(reac), _p(s2f), _p(a1),
                                       _p(a2)), "mw3_tables")
-        return dict(nopr1=nopr1, etot=etot, reacfct=reac, s2factor=s2f, absfr1=a1, absfr2=a2)
+        apaq = np.empty(i.netot)
+        self._check(self.L.mw3_packet_energy_norm(self.h, wave, _p(apaq)), "mw3_packet_energy_norm")
+        return dict(nopr1=nopr1, etot=etot, reacfct=reac, s2factor=s2f, absfr1=a1, absfr2=a2, apaqini=apaq)
 
     def kernel_launches(self):
         n = ct.c_int64()

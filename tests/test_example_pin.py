@@ -73,3 +73,42 @@ def test_oracle_mean_energy_and_norm_trace(example_run, example_pins):
     n = o.run_iters(20)
     ref = np.array(example_pins["norm_trace"][1:21])
     assert np.max(np.abs(n - ref) / ref) < 5e-12
+
+
+def _product_setup(example_case, example_run):
+    _, s = example_case
+    return s["product"]
+
+
+def test_product_levels(example_case, example_run, example_pins):
+    """ediatprod(v, j) - ediatref of the product diatom (sal.000:561-791): the
+    box DVR of the diabatic product branch, all 21 x 11 levels."""
+    fd, ed, nob = _product_setup(example_case, example_run)
+    ev = (ed - example_run.ediatref) / C.conve1 / C.eV2cm
+    rows = example_pins["product_levels_ev"]
+    assert len(rows) == 231 and np.all(nob == 10)
+    for j, v, e in rows:
+        assert abs(ev[j, v] - e) < 1e-12, (j, v, ev[j, v], e)
+
+
+def test_product_projection_tables(example_case, example_run, example_pins):
+    """ini_transcoor on the example: transRgjac's sum of squares over process
+    0's angles (the log's xt1, sal.000:1143), the sampled product distances
+    (rpbmin, rpbmax) and the norm of every product state's projection function
+    (sal.000:909-1139, printed to 7 digits)."""
+    from madwave3_gb300.host import transcoor
+    run = example_run
+    fd, ed, nob = _product_setup(example_case, example_run)
+    tr = transcoor.trans_rg_jac(run, 6.0, 1, run.inp.nangu)
+    _, ang, _, _ = run.point_table()
+    xt1 = float(np.sum(tr[ang % 7 == 0] ** 2))
+    assert abs(xt1 - 7372.9687214579890) / 7372.9687214579890 < 1e-13
+    _, rpb, _, _, ok = transcoor.prod_geometry(run, 6.0, 1, run.inp.npun2, 1, run.inp.nangu)
+    assert abs(rpb[ok].min() - 4.6465921805298308e-2) < 1e-15
+    assert abs(rpb[ok].max() - 24.752987568936842) < 1e-13
+    wf = transcoor.prod_functions_omega(run, 6.0, fd, nob, 0, 20, 0, 1, run.inp.npun2, 1, run.inp.nangu, 0)
+    rows = example_pins["product_wf_norms"]
+    assert len(rows) == 231
+    for iom, j, v, n in rows:
+        x = float(np.sum(wf[j, v] ** 2))
+        assert abs(x - n) <= 5e-7 * n, (j, v, x, n)

@@ -27,15 +27,26 @@ def _print_close(a, b, digits=7):
     return np.abs(a - b) <= np.maximum(scale, 1e-90)
 
 
+def _projection(example_case, run):
+    """ini_transcoor for the run's &inputprod (Rbalinprod = 6, all R and angles,
+    Omega' = 0, j' = 0..20, v' = 0..10) from the restated product states."""
+    from madwave3_gb300.host import transcoor
+    fd, ed, nob = example_case[1]["product"]
+    pp = transcoor.ini_transcoor(run, 6.0, 1, run.inp.npun2, 1, run.inp.nangu, 0, 0, 0, 20, 0, 10, nob, fd)
+    return pp, ed, nob
+
+
 @pytest.fixture(scope="module")
-def fp64_run(example_run):
+def fp64_run(example_case, example_run):
     from madwave3_gb300 import Propagator
+    pp, ed, nob = _projection(example_case, example_run)
     prop = Propagator(example_run, "fp64")
+    prop.set_product_projection(pp)
     h = prop.hphi(example_run.psi0)
     prop.start()
     prop.run(4000)
     out = {"h": h, "norms": prop.norms(), "pe": prop.totalflux()[0], "acc": prop.accumulators(),
-           "tables": prop.tables()}
+           "tables": prop.tables(), "product": prop.product(), "pp": pp, "ediatprod": ed, "nobcprod": nob}
     prop.close()
     return out
 
@@ -67,6 +78,26 @@ def test_fp64_probabilities(example_run, example_pins, fp64_run):
     s2reac = s2_elements(example_run, fp64_run["acc"]["zs2"], t["s2factor"]).sum(axis=(0, 1, 2))
     ok3 = _print_close(pe + s2reac, rows[:, 2])
     assert ok3.all(), np.nonzero(~ok3)[0][:10]
+
+
+def test_fp64_product_probabilities(example_run, example_pins, fp64_run):
+    """S2prod columns 4-15 (iprod = 2): the sum over the product states and the
+    v'-resolved product probabilities of the device projection (prodpaq /
+    prodcvj, printprob :669-684)."""
+    from madwave3_gb300.host import transcoor
+    from madwave3_gb300.printprob import s2prod_products
+    rows = np.array(example_pins["s2prod_rows"])
+    t = fp64_run["tables"]
+    fac = transcoor.s2prodfac(example_run, t["etot"], t["apaqini"], fp64_run["ediatprod"], fp64_run["nobcprod"],
+                              0, 10)
+    s2no, vib = s2prod_products(fp64_run["product"][0], fac, fp64_run["pp"])
+    s2no = np.where(s2no < 1e-90, 0.0, s2no)
+    vib = np.where(vib < 1e-90, 0.0, vib)
+    ok = _print_close(s2no, rows[:, 3])
+    assert ok.all(), np.nonzero(~ok)[0][:10]
+    for v in range(11):
+        okv = _print_close(vib[v], rows[:, 4 + v])
+        assert okv.all(), (v, np.nonzero(~okv)[0][:10])
 
 
 def test_mixed_probabilities(example_run, example_pins):

@@ -114,6 +114,22 @@ def test_product_functions(runs):
     assert np.all(transcoor.prod_functions(run, 1.5, f1, 3, 30, 2, 8, 2, 1, 0) == 0)
 
 
+def test_vectorised_product_functions_match_the_pointwise_ones(runs):
+    """ini_transcoor's prodwftrans over all (angle, R) points at once gives the
+    point-by-point restatement's numbers for every state of an Omega."""
+    run = runs["tiny_j3"]
+    jp0, jp1, vp0, vp1 = 0, 3, 0, 1
+    nob = np.array([1, 1, 0, 1], np.int32)
+    fd = _gauss_states(run, 30, jp1 - jp0 + 1, vp1 - vp0 + 1)
+    for iom in (0, 1, 2):
+        allv = transcoor.prod_functions_omega(run, 1.5, fd, nob, jp0, jp1, vp0, 3, 30, 2, 8, iom)
+        for j in range(jp0, jp1 + 1):
+            for iv in range(vp0, int(nob[j - jp0]) + 1):
+                one = transcoor.prod_functions(run, 1.5, fd[j - jp0][iv - vp0], 3, 30, 2, 8, iom, j, iv)
+                got = allv[j - jp0, iv - vp0]
+                assert np.allclose(got, one, rtol=0, atol=1e-14 * max(np.abs(one).max(), 1e-300)), (iom, j, iv)
+
+
 def test_ini_transcoor_feeds_the_oracle_projection(runs):
     from oracle.mw3ref import Oracle
 
