@@ -11,7 +11,10 @@ line reports max |Delta P(E)| for every J.
 Both runs start from the same packet and take the same number of Chebyshev
 iterations; P(E) is the total reaction probability of totalflux
 (SRC/mod_flux_01y2.f:778-816).  Prints one JSON line with max |Delta P|, the
-energy where it occurs, max P, the iterations and both paths' wall times.
+energy where it occurs, max P, the iterations and both paths' wall times, and
+the error of the state-resolved probabilities: P_vj(E) of every reactant
+channel (v, j), summed over the Omega blocks, as printprob forms them from
+zS2 (SRC/main_madwave3.f:640-652).
 """
 import argparse
 import json
@@ -20,6 +23,21 @@ import tempfile
 import time
 
 import numpy as np
+
+
+def state_probabilities(run, prop, wave=0):
+    """P[nj][nv][netot]: |S|^2 of every reactant channel (v, j) summed over the
+    wave's Omega/electronic blocks (printprob's S2 elements)."""
+    from .printprob import s2_elements
+    s2 = s2_elements(run, prop.accumulators(wave)["zs2"], prop.tables(wave)["s2factor"])
+    return s2.sum(axis=0)
+
+
+def _vj_error(run, a, b):
+    d = np.abs(a - b)
+    k = np.unravel_index(int(np.argmax(d)), d.shape)
+    return {"max_abs_dP_vj": float(d.max()), "at_j": int(k[0] + run.inp.jini), "at_v": int(k[1] + run.inp.nvini),
+            "max_P_vj": float(np.abs(a).max())}
 
 
 def run_gate(case, iterations, cases_dir=None, waves=None):
@@ -43,7 +61,9 @@ def run_gate(case, iterations, cases_dir=None, waves=None):
         out["seconds_" + prec] = time.time() - t
         res[prec] = p.totalflux()[0]
         res[prec + "_norm"] = p.norms()[-1]
+        res[prec + "_vj"] = state_probabilities(run, p)
         p.close()
+    out.update(_vj_error(run, res["fp64_vj"], res["mixed_vj"]))
     a, b = res["fp64"], res["mixed"]
     e = np.linspace(run.inp.ekinmin_ev, run.inp.ekinmax_ev, run.inp.netot)
     k = int(np.argmax(np.abs(a - b)))
@@ -75,13 +95,17 @@ def run_sweep_gate(case, js, iterations, cases_dir=None):
         p.sync()
         out["seconds_" + prec] = time.time() - t
         res[prec] = [p.totalflux(w)[0] for w in range(len(runs))]
+        res[prec + "_vj"] = [state_probabilities(runs[w], p, w) for w in range(len(runs))]
         p.close()
     per = []
     for w, J in enumerate(js):
         a, b = res["fp64"][w], res["mixed"][w]
-        per.append({"J": J, "max_abs_dP": float(np.abs(a - b).max()), "max_P": float(np.abs(a).max())})
+        row = {"J": J, "max_abs_dP": float(np.abs(a - b).max()), "max_P": float(np.abs(a).max())}
+        row.update(_vj_error(runs[w], res["fp64_vj"][w], res["mixed_vj"][w]))
+        per.append(row)
     out["per_J"] = per
     out["max_abs_dP"] = max(x["max_abs_dP"] for x in per)
+    out["max_abs_dP_vj"] = max(x["max_abs_dP_vj"] for x in per)
     out["pass_1e-4"] = bool(out["max_abs_dP"] <= 1e-4)
     return out
 

@@ -489,6 +489,25 @@ def set_colini(run):
     run.psi0 = psi
 
 
+def input_psie(run, inputfile):
+    """&inputPsiE (SRC/mod_PsiE_01y2.f:19-88): with iphoto > 0, nofe energies
+    (eV, one per line of file_resonancesE, relative to the input's directory)
+    at which funE accumulates psi(E); sets run.efe_zot (zot), empty when off."""
+    run.efe_zot = np.zeros(0)
+    if run.inp.iphoto <= 0 or not inputfile:
+        return
+    g = namelist.read(inputfile).get("inputpsie", {})
+    nofe = int(g.get("nofe", 0))
+    if nofe <= 0:
+        return
+    path = os.path.join(os.path.dirname(os.path.abspath(inputfile)), str(g.get("file_resonancese", "")))
+    with open(path) as f:
+        vals = [float(t.replace("D", "E").replace("d", "e")) for t in f.read().split()[:nofe]]
+    if len(vals) < nofe:
+        raise ValueError("%s holds fewer than nofe = %d energies" % (path, nofe))
+    run.efe_zot = np.array(vals) * C.eV2cm * C.conve1
+
+
 def load_sweep(inputfile, Js, overrides):
     """Partial waves that share one grid, potential and diatomic functions:
     the files are read once; ``overrides(J)`` gives the per-J namelist values
@@ -534,4 +553,5 @@ def load(inputfile, potdir=None, funcdir=None, inputs=None):
     pot2(run, potdir)
     if inp.iphoto == 0:
         set_colini(run)
+    input_psie(run, inputfile)
     return run

@@ -368,6 +368,19 @@ class Propagator:
         cx = lambda a: a[..., 0] + 1j * a[..., 1]
         return dict(zcr=cx(zcr), zcdr=cx(zcdr), zs2=cx(zs2), cvj=cvj)
 
+    def psi_e(self, wave=0):
+        """funE's zfe [nofe][ntot] complex: the energy-resolved wave functions
+        accumulated over the iterations (SRC/mod_PsiE_01y2.f:92-123)."""
+        r = self.runs[wave]
+        efe = getattr(r, "efe_zot", None)
+        nofe = 0 if efe is None else len(efe)
+        if nofe == 0:
+            raise Mw3Error("the wave has no funE energies (nofe = 0)")
+        z = np.empty((nofe, self.ntot[wave], 2))
+        self._check(self.L.mw3_download_accumulators(self.h, wave, None, None, None, None, _p(z)),
+                    "mw3_download_accumulators")
+        return z[..., 0] + 1j * z[..., 1]
+
     def tables(self, wave=0):
         r = self.runs[wave]
         i = r.inp
