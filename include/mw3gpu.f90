@@ -149,6 +149,19 @@ module mw3gpu
        integer(c_int32_t), value :: wave_id
        complex(c_double_complex), intent(in) :: zcr(*), zcdr(*), zs2(*)
      end function
+     integer(c_int) function mw3_cvj_history(ctx, capacity) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int64_t), value :: capacity
+     end function
+     integer(c_int) function mw3_download_cvj_history(ctx, wave_id, n, cvj, cvjprod, it_last) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: wave_id
+       integer(c_int64_t), value :: n
+       type(c_ptr), value :: cvj, cvjprod
+       integer(c_int64_t) :: it_last
+     end function
      integer(c_int) function mw3_packet_energy_norm(ctx, wave_id, apaqini) bind(c)
        import
        type(c_ptr), value :: ctx

@@ -166,6 +166,20 @@ int mw3_upload_accumulators(mw3_ctx *ctx, int32_t wave_id, const double *zcr, co
 int mw3_tables(mw3_ctx *ctx, int32_t wave_id, int32_t *nopr1, double *etot, double *reacfct,
                double *s2factor, double *absfr1, double *absfr2);
 
+/* Per-iteration Cvj and Cvjprod, the records the reference writes every
+ * iteration to Cvj.NNNN / Cvjprod.NNNN (write(15) it, Cvj and write(16) it,
+ * Cvjprod, SRC/main_madwave3.f:310-321, 354-364): mw3_cvj_history keeps them
+ * on the device in a ring of `capacity` iterations (0 turns it off), filled by
+ * every iteration of mw3_run since the last mw3_start / upload; the host
+ * drains it once per ntimes block.  mw3_download_cvj_history returns the last
+ * n recorded iterations, oldest first: cvj[n][ncan][nj][nv] (the wave's Cvj,
+ * Fortran Cvj(nvini:nvmax,jini:jmax,ncan)) and, for a wave with a product
+ * projection, cvjprod[n][nom][njp][nvp]; either may be NULL.  *it_last is the
+ * iteration of the newest record. */
+int mw3_cvj_history(mw3_ctx *ctx, int64_t capacity);
+int mw3_download_cvj_history(mw3_ctx *ctx, int32_t wave_id, int64_t n, double *cvj, double *cvjprod,
+                             int64_t *it_last);
+
 /* apaqini[netot]: the energy distribution |<packet|E>|^2 of the initial
  * collision packet that Smatini_col computes (SRC/mod_flux_01y2.f:467-524) and
  * the reference keeps in mod_flux for its normalisations -- ini_transcoor's

@@ -108,3 +108,29 @@ def read_cont(outdir, idproc=0, zs2_shape=None, flux_shape=None, prod_shape=None
             zp = np.frombuffer(read_record(f), np.complex128).copy()
         out["zs2prod"] = zp.reshape(prod_shape) if prod_shape else zp
     return out
+
+
+def write_cvj_file(path, iterations, cvj):
+    """Cvj.NNNN / Cvjprod.NNNN (SRC/main_madwave3.f:310-321, 354-364): one
+    unformatted record per iteration holding the iteration number (4-byte
+    integer) and the array (Cvj(nvini:nvmax, jini:jmax, ncan) or
+    Cvjprod(nviniprod:nvmaxprod, jiniprod:jmaxprod, iomminprod:iommaxprod), the
+    C order of mw3_download_cvj_history's rows)."""
+    with open(path, "wb") as f:
+        for it, row in zip(iterations, cvj):
+            write_record(f, struct.pack("<i", int(it)) + np.ascontiguousarray(row, "<f8").tobytes())
+
+
+def read_cvj_file(path, shape):
+    """The (iterations, arrays [n][shape]) of a Cvj.NNNN / Cvjprod.NNNN file."""
+    its, rows = [], []
+    with open(path, "rb") as f:
+        while True:
+            try:
+                b = read_record(f)
+            except EOFError:
+                break
+            its.append(struct.unpack("<i", b[:4])[0])
+            rows.append(np.frombuffer(b[4:], "<f8").reshape(shape))
+    return np.array(its), np.array(rows)
+

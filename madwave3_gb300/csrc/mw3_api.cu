@@ -155,6 +155,35 @@ int build_typed(Ctx &c)
     return MW3_OK;
 }
 
+// cudaFree one of the context's allocations and drop it from the list
+void dfree(Ctx &c, void *p)
+{
+    if (!p) return;
+    for (size_t i = 0; i < c.allocs.size(); i++)
+        if (c.allocs[i] == p) {
+            cudaFree(p);
+            c.allocs.erase(c.allocs.begin() + (long)i);
+            return;
+        }
+}
+
+// the Cvj / Cvjprod history ring for hist_cap iterations (none when 0)
+int alloc_history(Ctx &c)
+{
+    dfree(c, c.d_cvjh);
+    c.d_cvjh = nullptr;
+    for (auto &w : c.wdev) {
+        dfree(c, w.prod.cvjph);
+        w.prod.cvjph = nullptr;
+    }
+    c.hist_n = 0;
+    if (c.hist_cap <= 0) return MW3_OK;
+    if (c.n2 > 1) TRY(dalloc(c, &c.d_cvjh, (size_t)c.hist_cap * c.G * c.nj * c.nv));
+    for (auto &w : c.wdev)
+        if (w.prod.cvjprod) TRY(dalloc(c, &w.prod.cvjph, (size_t)c.hist_cap * w.prod.nrow));
+    return MW3_OK;
+}
+
 int build_device(Ctx &c)
 {
     if (c.built) return MW3_OK;
@@ -583,6 +612,7 @@ int build_device(Ctx &c)
     }
     int rc = c.fp64 ? build_typed<double>(c) : build_typed<float>(c);
     if (rc) return rc;
+    TRY(alloc_history(c));
     if (c.use_tc_dst2d) TRY(mw3::encode_tc_dst2d_xmap(c));
     if (c.d_dj32) mw3::build_cvj32(c);
     cudaError_t e = cudaStreamSynchronize(c.stream);
@@ -855,6 +885,7 @@ int mw3_start(mw3_ctx *h, const double *const *psi0s)
     mw3::launch_norms(c, 0);
     c.it = 1;
     c.norm_slot = 1;
+    c.hist_n = 0;
     c.started = true;
     return check_launch(c, "mw3_start");
 }
@@ -886,6 +917,7 @@ int mw3_upload_state(mw3_ctx *h, int32_t w, const double *psi_km1, const double 
     }
     c.it = it;
     c.norm_slot = 0;
+    c.hist_n = 0;
     c.started = true;
     rc = check_launch(c, "mw3_upload_state");
     if (rc) return rc;
@@ -907,6 +939,8 @@ void run_iteration(Ctx &c)
     std::swap(c.d_pk32, c.d_pkm1_32);
     mw3::launch_accumulators(c, it);
     mw3::launch_norms(c, c.norm_slot);
+    mw3::launch_cvj_keep(c, it, c.norm_slot);
+    if (c.hist_cap > 0) c.hist_n = std::min(c.hist_n + 1, c.hist_cap);
     if (c.prof && c.prof_n < c.prof_cap) {
         mw3::stage_mark(c, MW3_NSTAGES);
         c.prof_n++;
@@ -939,7 +973,7 @@ void capture_graph(Ctx &c, int par)
         }
         c.allocs.push_back(c.d_itbase);
     }
-    const int64_t it0 = c.it, slot0 = c.norm_slot, l0 = c.launches;
+    const int64_t it0 = c.it, slot0 = c.norm_slot, l0 = c.launches, h0 = c.hist_n;
     double *pk = c.d_pk, *pkm1 = c.d_pkm1;
     float *pk32 = c.d_pk32, *pkm1_32 = c.d_pkm1_32;
     cudaGraph_t g = nullptr;
@@ -956,6 +990,7 @@ void capture_graph(Ctx &c, int par)
     const int64_t launches = c.launches - l0;
     c.it = it0;
     c.norm_slot = slot0;
+    c.hist_n = h0;
     c.d_pk = pk;
     c.d_pkm1 = pkm1;
     c.d_pk32 = pk32;
@@ -1003,6 +1038,7 @@ int mw3_run(mw3_ctx *h, int64_t n)
                 c.launches += c.graph_launches[par];
                 c.it += mw3::kGraphIters;
                 c.norm_slot += mw3::kGraphIters;
+                if (c.hist_cap > 0) c.hist_n = std::min(c.hist_n + mw3::kGraphIters, c.hist_cap);
                 s += mw3::kGraphIters;
                 continue;
             }
@@ -1064,6 +1100,7 @@ int mw3_upload_state_all(mw3_ctx *h, const double *psi_km1, const double *psi_k,
     }
     c.it = it;
     c.norm_slot = 0;
+    c.hist_n = 0;
     c.started = true;
     rc = check_launch(c, "mw3_upload_state_all");
     if (rc) return rc;
@@ -1192,6 +1229,58 @@ int mw3_packet_energy_norm(mw3_ctx *h, int32_t w, double *apaqini)
     const WaveTables &t = h->c.waves[w];
     std::copy(t.apaqini.begin(), t.apaqini.end(), apaqini);
     return MW3_OK;
+}
+
+int mw3_cvj_history(mw3_ctx *h, int64_t capacity)
+{
+    if (!h || capacity < 0) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    for (int p = 0; p < 2; p++) {   // captured blocks must include (or drop) the record
+        if (c.graph_exec[p]) cudaGraphExecDestroy(c.graph_exec[p]);
+        c.graph_exec[p] = nullptr;
+        c.graph_launches[p] = 0;
+    }
+    c.hist_cap = capacity;
+    if (!c.built) return MW3_OK;
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    int rc = alloc_history(c);
+    if (rc) return rc;
+    return check_launch(c, "mw3_cvj_history");
+}
+
+int mw3_download_cvj_history(mw3_ctx *h, int32_t w, int64_t n, double *cvj, double *cvjprod, int64_t *it_last)
+{
+    if (!h || n < 0) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) return MW3_ERR_ARG;
+    if (!c.built || c.hist_cap <= 0) {
+        c.err = "mw3_download_cvj_history: no history enabled (mw3_cvj_history)";
+        return MW3_ERR_STATE;
+    }
+    if (n > c.hist_n) {
+        c.err = "mw3_download_cvj_history: " + std::to_string(n) + " iterations asked, " +
+                std::to_string(c.hist_n) + " recorded";
+        return MW3_ERR_ARG;
+    }
+    const WaveTables &t = c.waves[w];
+    const mw3::ProdDev &d = c.wdev[w].prod;
+    if (cvjprod && !d.cvjph) {
+        c.err = "mw3_download_cvj_history: the wave has no product projection";
+        return MW3_ERR_ARG;
+    }
+    const size_t R = (size_t)c.G * c.nj * c.nv, per = (size_t)t.ncan * c.nj * c.nv;
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t slot = ((c.norm_slot - n + k) % c.hist_cap + c.hist_cap) % c.hist_cap;
+        if (cvj && c.d_cvjh)
+            MW3_CUDA_TRY(cudaMemcpyAsync(cvj + (size_t)k * per, c.d_cvjh + (size_t)slot * R + (size_t)t.g0 * c.nj * c.nv,
+                                         sizeof(double) * per, cudaMemcpyDeviceToHost, c.stream));
+        if (cvjprod)
+            MW3_CUDA_TRY(cudaMemcpyAsync(cvjprod + (size_t)k * d.nrow, d.cvjph + (size_t)slot * d.nrow,
+                                         sizeof(double) * d.nrow, cudaMemcpyDeviceToHost, c.stream));
+    }
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    if (it_last) *it_last = c.it;
+    return check_device_flags(c, "mw3_download_cvj_history");
 }
 
 int mw3_kernel_launches(mw3_ctx *h, int64_t *count)

@@ -94,6 +94,7 @@ struct ProdDev {
     double *dtrans = nullptr, *prodwf = nullptr;
     int *nobcprod = nullptr, *blk_elec = nullptr;
     double *cvjprod = nullptr;                   // [nrow]
+    double *cvjph = nullptr;                     // [hist_cap][nrow]: Cvjprod of the recorded iterations
     double *zs2prod = nullptr;                   // [nrow][netot][2]
 };
 
@@ -136,6 +137,10 @@ struct Ctx {
     bool started = false;
     int64_t it = 0;                  // Chebyshev index of psi_k (all waves advance together)
     int64_t norm_slot = 0;           // iterations recorded since the last start/upload
+    // per-iteration Cvj / Cvjprod record (the Cvj.NNNN / Cvjprod.NNNN dumps): a ring
+    // of hist_cap iterations at slot norm_slot mod hist_cap, hist_n of them valid
+    int64_t hist_cap = 0, hist_n = 0;
+    double *d_cvjh = nullptr;        // [hist_cap][G nj nv]
 
     // host copies of the shared grid
     std::vector<int> npunreal, indr1, indr2;
@@ -361,6 +366,8 @@ void launch_norms(Ctx &c, int64_t slot);
 void launch_set_itbase(Ctx &c);
 // prodpaq + prodcvj of every wave that has a product projection
 void launch_product(Ctx &c);
+// the iteration's Cvj (and Cvjprod) into the history ring at slot mod hist_cap
+void launch_cvj_keep(Ctx &c, int64_t it, int64_t slot);
 constexpr int kGraphIters = 32;      // iterations per captured graph (one ring cycle)
 static_assert(kFluxRing == kGraphIters, "a captured block must cycle the Cvj ring exactly once");
 static_assert(kGraphIters % (kFluxSlots / 4) == 0, "flux slice flushes must repeat with the captured block");

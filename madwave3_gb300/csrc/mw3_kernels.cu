@@ -1684,6 +1684,39 @@ void launch_addv(Ctx &c, const double *psi, int g0, int g1)
 }
 
 // the iteration and norm-slot base of a graph replay
+// Cvj / Cvjprod of one iteration into its slot of the history ring (FP64 source,
+// or the mixed path's FP32 Cvj ring slot); graph replays add the block's first
+// slot from base[1] as k_norms does
+__global__ void k_cvj_keep(const double *__restrict__ src64, const float *__restrict__ src32, int n,
+                           double *__restrict__ dst, int64_t cap, int64_t slot, const int64_t *__restrict__ base)
+{
+    if (base) slot += base[1];
+    const int64_t s = slot % cap;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        dst[s * n + i] = src64 ? src64[i] : (double)src32[i];
+}
+
+void launch_cvj_keep(Ctx &c, int64_t it, int64_t slot)
+{
+    if (c.hist_cap <= 0) return;
+    const int64_t sarg = c.capturing ? slot - c.cap_slot0 : slot;
+    const int64_t *bp = c.capturing ? c.d_itbase : nullptr;
+    if (c.d_cvjh && c.n2 > 1) {
+        const int R = c.G * c.nj * c.nv;
+        const float *s32 = c.d_cvring ? c.d_cvring + (size_t)(it % kFluxRing) * R : nullptr;
+        k_cvj_keep<<<(R + 255) / 256, 256, 0, c.stream>>>(c.d_cvring ? nullptr : c.d_cvj, s32, R, c.d_cvjh,
+                                                           c.hist_cap, sarg, bp);
+        LAUNCH_CHECK(c);
+    }
+    for (size_t w = 0; w < c.wdev.size(); w++) {
+        const ProdDev &d = c.wdev[w].prod;
+        if (!d.cvjph || !d.cvjprod) continue;
+        k_cvj_keep<<<(d.nrow + 255) / 256, 256, 0, c.stream>>>(d.cvjprod, nullptr, d.nrow, d.cvjph, c.hist_cap, sarg,
+                                                               bp);
+        LAUNCH_CHECK(c);
+    }
+}
+
 __global__ void k_set_itbase(int64_t *base, int64_t it, int64_t slot)
 {
     base[0] = it;

@@ -70,6 +70,7 @@ HEADER_FUNCS = [
     "mw3_get_stream",
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_set_product_projection", "mw3_download_product",
+    "mw3_cvj_history", "mw3_download_cvj_history",
     "mw3_upload_accumulators", "mw3_upload_product",
     "mw3_last_error", "mw3_destroy",
 ]
@@ -116,6 +117,8 @@ def load_library(build_if_missing=True):
     L.mw3_download_accumulators.argtypes = [vp, ct.c_int32, F64P, F64P, F64P, F64P, F64P]
     L.mw3_tables.argtypes = [vp, ct.c_int32, I32P, F64P, F64P, F64P, F64P, F64P]
     L.mw3_packet_energy_norm.argtypes = [vp, ct.c_int32, F64P]
+    L.mw3_cvj_history.argtypes = [vp, ct.c_int64]
+    L.mw3_download_cvj_history.argtypes = [vp, ct.c_int32, ct.c_int64, F64P, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
     L.mw3_path_flags.argtypes = [vp, ct.POINTER(ct.c_int32)]
     L.mw3_get_stream.argtypes = [vp, ct.POINTER(ct.c_void_p)]
@@ -367,6 +370,24 @@ class Propagator:
                     "mw3_download_accumulators")
         cx = lambda a: a[..., 0] + 1j * a[..., 1]
         return dict(zcr=cx(zcr), zcdr=cx(zcdr), zs2=cx(zs2), cvj=cvj)
+
+    def cvj_history(self, capacity):
+        """Record Cvj (and Cvjprod) of every iteration in a device ring of
+        ``capacity`` iterations (0: off)."""
+        self._check(self.L.mw3_cvj_history(self.h, int(capacity)), "mw3_cvj_history")
+
+    def download_cvj_history(self, n, wave=0):
+        """(iterations [n], cvj [n][ncan][nj][nv], cvjprod [n][nom][njp][nvp] or
+        None) of the last n recorded iterations, oldest first."""
+        r = self.runs[wave]
+        i = r.inp
+        cvj = np.empty((n, r.ncan, i.jmax - i.jini + 1, i.nvmax - i.nvini + 1))
+        shp = getattr(self, "_prodshape", {}).get(wave)
+        cp = np.empty((n,) + shp) if shp is not None else None
+        last = ct.c_int64()
+        self._check(self.L.mw3_download_cvj_history(self.h, wave, n, _p(cvj), None if cp is None else _p(cp),
+                                                     ct.byref(last)), "mw3_download_cvj_history")
+        return np.arange(last.value - n + 1, last.value + 1), cvj, cp
 
     def psi_e(self, wave=0):
         """funE's zfe [nofe][ntot] complex: the energy-resolved wave functions
