@@ -180,6 +180,14 @@ int mw3_cvj_history(mw3_ctx *ctx, int64_t capacity);
 int mw3_download_cvj_history(mw3_ctx *ctx, int32_t wave_id, int64_t n, double *cvj, double *cvjprod,
                              int64_t *it_last);
 
+/* totalflux_k's energy test (SRC/mod_flux_01y2.f:640): with on != 0 (the
+ * default, as the shipped source) the flux through a point counts only at the
+ * energies above its potential; with on = 0 every energy takes every flux
+ * point, the earlier form of the routine with which the reference's shipped
+ * H + HD run (EXAMPLES/HD+H_collision/J000-check) was made.  Call before the
+ * context's device tables exist, else MW3_ERR_STATE. */
+int mw3_set_flux_gate(mw3_ctx *ctx, int32_t wave_id, int32_t on);
+
 /* apaqini[netot]: the energy distribution |<packet|E>|^2 of the initial
  * collision packet that Smatini_col computes (SRC/mod_flux_01y2.f:467-524) and
  * the reference keeps in mod_flux for its normalisations -- ini_transcoor's

@@ -421,7 +421,7 @@ int build_device(Ctx &c)
             WaveTables &t = c.waves[w];
             for (int f = 0; f < t.nflux; f++) {
                 fidx.push_back(t.flat0 + t.fl_idx[f]);
-                fpoti.push_back(t.potiflux[f]);
+                fpoti.push_back(t.flux_gate ? t.potiflux[f] : -1.0e300);
                 fdptr.push_back((int)fdidx.size());
                 for (int q = t.fl_dptr[f]; q < t.fl_dptr[f + 1]; q++) {
                     fdidx.push_back(t.flat0 + t.fl_didx[q]);
@@ -934,6 +934,7 @@ void run_iteration(Ctx &c)
 {
     int64_t it = c.it + 1;
     hphi_all(c, c.d_pk, 0, c.G);
+    if (c.nofemax > 0) mw3::launch_fe_coef(c, it);
     update(c, 0);
     std::swap(c.d_pk, c.d_pkm1);
     std::swap(c.d_pk32, c.d_pkm1_32);
@@ -1220,6 +1221,18 @@ int mw3_tables(mw3_ctx *h, int32_t w, int32_t *nopr1, double *etot, double *reac
     if (s2factor) std::copy(t.s2factor.begin(), t.s2factor.end(), s2factor);
     if (absfr1) std::copy(t.absfr1.begin(), t.absfr1.end(), absfr1);
     if (absfr2) std::copy(t.absfr2.begin(), t.absfr2.end(), absfr2);
+    return MW3_OK;
+}
+
+int mw3_set_flux_gate(mw3_ctx *h, int32_t w, int32_t on)
+{
+    if (!h || w < 0 || w >= (int)h->c.waves.size()) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (c.built) {
+        c.err = "mw3_set_flux_gate: call before the device tables exist";
+        return MW3_ERR_STATE;
+    }
+    c.waves[w].flux_gate = on != 0;
     return MW3_OK;
 }
 

@@ -61,6 +61,7 @@ struct WaveTables {
     std::vector<int64_t> fl_idx;            // flat index (wave-relative) of each flux point
     std::vector<int> fl_block;              // block of each flux point
     std::vector<double> potiflux;
+    bool flux_gate = true;                  // totalflux_k's E > V(flux point) test
     std::vector<int> fl_dptr;               // CSR over flux points of the r1-derivative terms
     std::vector<int64_t> fl_didx;           // wave-relative flat index of each term
     std::vector<int> fl_dir1;               // ir1 (0-based) of each term
@@ -366,6 +367,8 @@ void launch_norms(Ctx &c, int64_t slot);
 void launch_set_itbase(Ctx &c);
 // prodpaq + prodcvj of every wave that has a product projection
 void launch_product(Ctx &c);
+// funE's C_k(E) for iteration it (launched before the update that uses it)
+void launch_fe_coef(Ctx &c, int64_t it);
 // the iteration's Cvj (and Cvjprod) into the history ring at slot mod hist_cap
 void launch_cvj_keep(Ctx &c, int64_t it, int64_t slot);
 constexpr int kGraphIters = 32;      // iterations per captured graph (one ring cycle)

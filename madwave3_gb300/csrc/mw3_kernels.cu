@@ -1464,6 +1464,24 @@ static CvjArgs cvj_args(Ctx &c, bool gate)
     return a;
 }
 
+// C_k(E) at funE's energies for iteration it, before the update kernel adds
+// C_k(E) psi_k to zfe (funE follows the update, main_madwave3.f:350-352)
+void launch_fe_coef(Ctx &c, int64_t it)
+{
+    const int64_t itarg = c.capturing ? it - c.cap_it0 : it;
+    const int64_t *bp = c.capturing ? c.d_itbase : nullptr;
+    for (size_t w = 0; w < c.waves.size(); w++) {
+        WaveTables &t = c.waves[w];
+        if (t.nofe > 0) {
+            k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(c.wdev[w].efe, t.nofe, c.grid.emindlt,
+                                                                     c.grid.delta2, c.grid.hbr,
+                                                                     itarg, c.d_zcke + (size_t)w * c.nofemax * 2,
+                                                                     nullptr, 0, nullptr, bp);
+            LAUNCH_CHECK(c);
+        }
+    }
+}
+
 void launch_accumulators(Ctx &c, int64_t it)
 {
     stage_mark(c, 6);
@@ -1477,16 +1495,6 @@ void launch_accumulators(Ctx &c, int64_t it)
         c.d_etot, c.netot, c.grid.emindlt, c.grid.delta2, c.grid.hbr, itarg, c.d_zck, ring ? c.d_cring : nullptr,
         flux_on ? 0 : 1, c.d_cvcring ? c.d_cvcring + (size_t)(it % kFluxRing) * c.netot * 2 : nullptr, bp);
     LAUNCH_CHECK(c);
-    for (size_t w = 0; w < c.waves.size(); w++) {
-        WaveTables &t = c.waves[w];
-        if (t.nofe > 0) {
-            k_coefecheby<<<(t.nofe + 127) / 128, 128, 0, c.stream>>>(c.wdev[w].efe, t.nofe, c.grid.emindlt,
-                                                                     c.grid.delta2, c.grid.hbr,
-                                                                     itarg, c.d_zcke + (size_t)w * c.nofemax * 2,
-                                                                     nullptr, 0, nullptr, bp);
-            LAUNCH_CHECK(c);
-        }
-    }
     if (ring) {
         if (flux_on) {
             k_flux_deriv<<<(c.NF * 32 + 255) / 256, 256, 0, c.stream>>>(

@@ -350,6 +350,7 @@ struct mw3ref {
     int *fl_ang, *fl_can, *fl_r2;   /* flux points */
     int64_t *fl_idx;          /* flat index of each flux point */
     double *potiflux;
+    int flux_gate;            /* 1: flux only where E > V(flux point) */
     cplx *zcr, *zcdr;         /* [nflux][netot] */
     double *etot, *reacfct, *apaqini, *s2factor;  /* s2factor [nelec][nj][nv][netot] */
     cplx *zck;                /* [netot] */
@@ -720,6 +721,7 @@ mw3ref *mw3ref_create(const mw3ref_in *in, char *err, int errlen)
     for (int a = 0; a < in->nangu; a++)
         if (in->npunreal[a] <= 0) { set_err(err, errlen, "angle without stored points"); return NULL; }
     mw3ref *r = (mw3ref *)calloc(1, sizeof(mw3ref));
+    if (r) r->flux_gate = 1;
     r->in = *in;
     r->nthreads = 1;
     r->n1 = in->npun1; r->n2 = in->npun2; r->na = in->nangu; r->ne = in->nelec; r->nc = in->ncan;
@@ -789,6 +791,11 @@ void mw3ref_destroy(mw3ref *r)
 int64_t mw3ref_ntot(const mw3ref *r) { return r->ntot; }
 void mw3ref_set_threads(mw3ref *r, int n) { r->nthreads = n < 1 ? 1 : (n > 256 ? 256 : n); }
 void mw3ref_set_dst_mode(mw3ref *r, int mode) { r->dstmode = mode; }
+
+/* totalflux_k's energy test E > V(flux point) (mod_flux_01y2.f:640): on as in
+   the shipped source, or off as in the earlier form that made the shipped
+   H + HD run (every energy takes every flux point) */
+void mw3ref_set_flux_gate(mw3ref *r, int on) { r->flux_gate = on; }
 
 /* T, V and angular contributions of one source (block, angle) pair: the body of
    the jangp loop of difs (mod_Hphi_01y2.f:748-902).  hrec/hproc are the
@@ -1016,7 +1023,7 @@ static void totalflux_k(mw3ref *r, int64_t k)
         for (int ie = 0; ie < netot; ie++) {
             cplx ze = r->zck[ie];
             if (in->iphoto == 0 && in->iprod == 1 && k < in->kminelastic) { ze.re = 0; ze.im = 0; }
-            if (r->etot[ie] > r->potiflux[f]) {
+            if (!r->flux_gate || r->etot[ie] > r->potiflux[f]) {
                 cplx *c = &r->zcr[(size_t)f * netot + ie], *d = &r->zcdr[(size_t)f * netot + ie];
                 c->re = c->re + (ze.re * zr - ze.im * 0.0);
                 c->im = c->im + (ze.re * 0.0 + ze.im * zr);

@@ -71,6 +71,7 @@ def lib():
         L.mw3ref_ntot.argtypes = [ct.c_void_p]
         L.mw3ref_set_threads.argtypes = [ct.c_void_p, ct.c_int]
         L.mw3ref_set_dst_mode.argtypes = [ct.c_void_p, ct.c_int]
+        L.mw3ref_set_flux_gate.argtypes = [ct.c_void_p, ct.c_int]
         for name in ("mw3ref_hphi",):
             getattr(L, name).argtypes = [ct.c_void_p, F64P, F64P]
         L.mw3ref_start.argtypes = [ct.c_void_p, F64P]
@@ -146,7 +147,7 @@ def riccati(l, x):
 class Oracle:
     """One partial wave on the CPU oracle, built from a host ``setup.Run``."""
 
-    def __init__(self, run, nofe_energies_ev=None, threads=1, dst_mode=0):
+    def __init__(self, run, nofe_energies_ev=None, threads=1, dst_mode=0, flux_gate=True):
         i = run.inp
         self.run = run
         keep = {}
@@ -208,6 +209,7 @@ class Oracle:
         self.ntot = lib().mw3ref_ntot(h)
         lib().mw3ref_set_threads(h, threads)
         lib().mw3ref_set_dst_mode(h, dst_mode)
+        lib().mw3ref_set_flux_gate(h, 1 if flux_gate else 0)
         self.netot = i.netot
         self.nelec = run.nelec
         self.nj = i.jmax - i.jini + 1

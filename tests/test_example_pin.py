@@ -112,3 +112,36 @@ def test_product_projection_tables(example_case, example_run, example_pins):
     for iom, j, v, n in rows:
         x = float(np.sum(wf[j, v] ** 2))
         assert abs(x - n) <= 5e-7 * n, (j, v, x, n)
+
+
+def test_oracle_flux_gate_switch(runs):
+    """The oracle's totalflux_k with and without the E > V(flux point) test
+    (SRC/mod_flux_01y2.f:640): for each flux point and energy above the point's
+    potential the two forms hold the same sums; below it the gated form holds
+    0 and the gate-free form the point's contribution."""
+    from oracle.mw3ref import Oracle
+    run = runs["tiny_j0"]
+    i = run.inp
+    out = []
+    for gate in (True, False):
+        o = Oracle(run, flux_gate=gate)
+        o.start(run.psi0)
+        o.run_iters(30)
+        out.append(o.flux()[0])
+    etot = Oracle(run).flux_tables()["etot"]
+    poti = []                        # the flux points in the reference's order: angle, block, point
+    for iang in run.angle_order():
+        n = run.npunreal[iang - 1]
+        ir1 = run.indr1[iang - 1, :n]
+        r1 = i.rmis1 + (ir1 - 1) * run.ah1
+        ir1f = ir1[r1 <= i.r1flux_ang].max()
+        for b in range(run.ncan):
+            e = run.nelebas[b] - 1
+            poti.extend(run.vvv[e, e, iang - 1, :n][ir1 == ir1f])
+    poti = np.array(poti)
+    zg, zn = out
+    assert zg.shape == zn.shape == (poti.size, etot.size)
+    above = etot[None, :] > poti[:, None]
+    assert above.any() and (~above).any()
+    assert np.array_equal(zg[above], zn[above])
+    assert np.all(zg[~above] == 0) and np.any(zn[~above] != 0)

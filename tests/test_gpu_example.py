@@ -7,6 +7,11 @@ reference printed ||psi_k||^2 for k = 1..4001 at 17 digits (sal.000) and P(E)
 at 7 (S2prod.v00.J000.k00008, columns 2 and 3: the total reaction probability
 of totalflux and that plus the reactant-channel sum of printprob).
 
+The shipped run was made with the earlier form of totalflux_k, without the
+shipped source's test E > V(flux point) (with the test, P(E) comes out up to
+4e-3 lower near threshold; without it, within 5e-8 of the file), so the flux
+runs here with that test off (mw3_set_flux_gate).
+
 The FP64 path reproduces the norm trace to 1e-10 relative (the north-star
 bar for the plain FP64 path) and P(E) to the file's print precision; the
 mixed path (FP32 transforms) reproduces P(E) to 1e-4 absolute, the bar of
@@ -41,6 +46,7 @@ def fp64_run(example_case, example_run):
     from madwave3_gb300 import Propagator
     pp, ed, nob = _projection(example_case, example_run)
     prop = Propagator(example_run, "fp64")
+    prop.set_flux_gate(False)
     prop.set_product_projection(pp)
     h = prop.hphi(example_run.psi0)
     prop.start()
@@ -74,10 +80,12 @@ def test_fp64_probabilities(example_run, example_pins, fp64_run):
     assert np.all(_print_close(e_ev, rows[:, 0]))
     pe = np.where(fp64_run["pe"] < 1e-90, 0.0, fp64_run["pe"])
     ok = _print_close(pe, rows[:, 1])
-    assert ok.all(), np.nonzero(~ok)[0][:10]
+    bad = np.nonzero(~ok)[0][:5]
+    assert ok.all(), [(int(k), rows[k, 0], pe[k], rows[k, 1]) for k in bad]
     s2reac = s2_elements(example_run, fp64_run["acc"]["zs2"], t["s2factor"]).sum(axis=(0, 1, 2))
     ok3 = _print_close(pe + s2reac, rows[:, 2])
-    assert ok3.all(), np.nonzero(~ok3)[0][:10]
+    bad = np.nonzero(~ok3)[0][:5]
+    assert ok3.all(), [(int(k), rows[k, 0], pe[k] + s2reac[k], rows[k, 2]) for k in bad]
 
 
 def test_fp64_product_probabilities(example_run, example_pins, fp64_run):
@@ -94,10 +102,12 @@ def test_fp64_product_probabilities(example_run, example_pins, fp64_run):
     s2no = np.where(s2no < 1e-90, 0.0, s2no)
     vib = np.where(vib < 1e-90, 0.0, vib)
     ok = _print_close(s2no, rows[:, 3])
-    assert ok.all(), np.nonzero(~ok)[0][:10]
+    bad = np.nonzero(~ok)[0][:5]
+    assert ok.all(), [(int(k), rows[k, 0], s2no[k], rows[k, 3]) for k in bad]
     for v in range(11):
         okv = _print_close(vib[v], rows[:, 4 + v])
-        assert okv.all(), (v, np.nonzero(~okv)[0][:10])
+        bad = np.nonzero(~okv)[0][:5]
+        assert okv.all(), (v, [(int(k), rows[k, 0], vib[v][k], rows[k, 4 + v]) for k in bad])
 
 
 def test_mixed_probabilities(example_run, example_pins):
@@ -105,6 +115,7 @@ def test_mixed_probabilities(example_run, example_pins):
     reference's printed P(E): within 1e-4 absolute."""
     from madwave3_gb300 import Propagator
     prop = Propagator(example_run, "mixed")
+    prop.set_flux_gate(False)
     prop.start()
     prop.run(4000)
     pe = prop.totalflux()[0]

@@ -143,3 +143,22 @@ def test_wide_angle_grid_fp64_and_mixed(tmp_path):
     pmx = Propagator(run, "mixed")
     assert rel(pmx.hphi(psi), h64) < 1e-6
     pmx.close()
+
+
+@pytest.mark.parametrize("case", ["tiny_j0", "tiny_e2"])
+def test_flux_gate_off_fp64(runs, case):
+    """totalflux_k without the E > V(flux point) test (mw3_set_flux_gate 0)
+    against the oracle's gate-free form: flux accumulators and P(E)."""
+    run = runs[case]
+    prop = Propagator(run, "fp64")
+    prop.set_flux_gate(False)
+    ref = Oracle(run, flux_gate=False)
+    prop.start()
+    ref.start(run.psi0)
+    prop.run(NIT)
+    ref.run_iters(NIT)
+    acc = prop.accumulators()
+    zcr, zcdr = ref.flux()
+    assert rel(acc["zcr"], zcr) < 1e-10 and rel(acc["zcdr"], zcdr) < 1e-10
+    assert rel(prop.totalflux()[0], ref.totalflux()[0]) < 1e-10
+    prop.close()
