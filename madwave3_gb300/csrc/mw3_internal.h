@@ -275,6 +275,13 @@ struct Ctx {
     bool use_tc_dst2d = false;
     float *d_dst_planes = nullptr;   // S1 of every length: 128 x 128 TF32 hi/lo chunk planes
     float *d_dst_s2fold = nullptr;   // S2 split by column parity (DST-I symmetry), hi/lo chunk planes
+    // the split-FP16 form of the fused DST (default; MW3_DST_TF32=1 keeps the 3xTF32 one):
+    // the same planes as FP16 hi/lo x 2^12 in chunks of 32, each slab's largest |X|
+    bool dst_f16 = false;
+    void *d_dst_planes16 = nullptr, *d_dst_s2fold16 = nullptr;
+    int64_t *d_dst_s1off16 = nullptr;
+    unsigned *d_xmax = nullptr;      // [G na], written by the scatter and update kernels
+    int dst_fexp = 0;                // ceil(log2) of the largest F = min(p2, radcut) / (4 (nn+1)(n2+1))
     int64_t *d_dst_s1off = nullptr;  // [W][na] float offset of the slab's S1
     float *d_p2r1f = nullptr, *d_p2r2f = nullptr;      // FP32 copies of the momenta tables
     alignas(64) unsigned char dst_xmap[128] = {};       // TMA map of the rectangles (CUtensorMap)

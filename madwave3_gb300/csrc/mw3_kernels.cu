@@ -38,7 +38,7 @@ template <> __device__ __forceinline__ float rect_value<float>(double v) { retur
 // update reads for the potential term
 template <typename T>
 __global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict__ psi, float *__restrict__ psi32,
-                          int seg0)
+                          int seg0, unsigned *__restrict__ xmax)
 {
     int seg = seg0 + blockIdx.x;
     int a = seg % d.na;
@@ -46,12 +46,21 @@ __global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict
     int n = d.npunreal[a];
     int i0 = blockIdx.y * kPointChunk, i1 = min(n, i0 + kPointChunk);
     T *base = X + (size_t)seg * d.n1 * d.n2;
+    float m = 0.f;
     for (int ir = i0 + threadIdx.x; ir < i1; ir += blockDim.x) {
         int ir1 = d.indr1[(size_t)a * d.npt + ir] - 1;
         int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
         const double v = psi[off + ir];
-        base[(size_t)ir1 * d.n2 + ir2] = rect_value<T>(v);
+        const T x = rect_value<T>(v);
+        base[(size_t)ir1 * d.n2 + ir2] = x;
+        m = fmaxf(m, fabsf((float)x));
         if (psi32) psi32[off + ir] = rect_value<float>(v);
+    }
+    // the slab's largest |X| for the split-FP16 DST (its scale)
+    if (xmax) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(xmax + seg, __float_as_uint(m));
     }
 }
 
@@ -440,6 +449,7 @@ struct UpdArgs {
     const double *zcke;            // [W][nofe][2]
     double *const *zfe;            // per wave [nofe][ntot_w][2] (null when the wave has none)
     const int64_t *wflat0;         // [W+1]
+    unsigned *xmax;                // mixed path: bits of each slab's largest |X| (split-FP16 DST scale)
 };
 
 // funE: zfe[e][i] += zcke[w][e] psi_k+1(i) for the selected energies
@@ -503,7 +513,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
     int64_t wst = u.wflat0[w], wlen = u.wflat0[w + 1] - u.wflat0[w];
     constexpr int U = kPointChunk / 256;        // points per thread, loads issued together
     const int ir0 = chunk * kPointChunk + threadIdx.x;
-    float nrmf = 0.f;
+    float nrmf = 0.f, xmf = 0.f;
     if constexpr (sizeof(T) == 8) {
         int r1[U], r2[U];
         double hv[U], pk[U], p1[U];
@@ -593,9 +603,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
             rect[(size_t)r1[k] * n2 + r2[k]] = (T)nf;
             o32[ir] = nf;
             nrmf = fmaf(nf, nf, nrmf);
+            xmf = fmaxf(xmf, fabsf(nf));
             outp[ir] = nv;
             if (zf) upd_fe(u, zf, w, wst, wlen, off + ir, nv);
         }
+    }
+    if (sizeof(T) == 4 && u.xmax) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) xmf = fmaxf(xmf, __shfl_xor_sync(0xffffffffu, xmf, o));
+        if (lane == 0 && xmf > 0.f) atomicMax(u.xmax + seg, __float_as_uint(xmf));
     }
     // norm partial: fixed shuffle tree per warp, then the warps in order (deterministic);
     // the mixed path reduces its FP32 sums in FP32 up to the warp level
@@ -1260,7 +1276,8 @@ void launch_scatter(Ctx &c, const double *psi, float *psi32, int g_begin, int g_
 {
     int nseg = (g_end - g_begin) * c.na;
     if (nseg <= 0) return;
-    k_scatter<T><<<dim3(nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, psi32, g_begin * c.na);
+    k_scatter<T><<<dim3(nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, psi32, g_begin * c.na,
+                                                              sizeof(T) == 4 ? c.d_xmax : nullptr);
     LAUNCH_CHECK(c);
 }
 
@@ -1352,6 +1369,7 @@ template <typename T>
 void launch_update(Ctx &c, int first)
 {
     UpdArgs u;
+    u.xmax = sizeof(T) == 4 ? c.d_xmax : nullptr;
     u.H = c.d_h;
     u.pk = c.d_pk;
     u.pkm1 = c.d_pkm1;
@@ -1781,7 +1799,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     const double *P = psi - t.flat0;
     double *H = hpsi - t.flat0;
     DevGrid d = devgrid(c);
-    k_scatter<T><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, X, P, nullptr, g0 * na);
+    k_scatter<T><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, X, P, nullptr, g0 * na, nullptr);
     LAUNCH_CHECK(c);
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g0 * na * n1, nrows = (int64_t)ng * na * n1;

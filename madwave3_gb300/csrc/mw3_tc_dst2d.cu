@@ -22,6 +22,7 @@
 #include "mw3_tc.cuh"
 
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -457,6 +458,375 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
     if (warp == 0) tmem_dealloc(tb, 512);
 }
 
+// ===========================================================================
+// The same chain as split-FP16 products (kind::f16, FP32 accumulation).
+//
+// FP16 and TF32 carry the same 10-bit mantissa, so x ~= hi + lo with hi, lo in
+// FP16 keeps 22 bits like the TF32 split, and Ahi Bhi + Ahi Blo + Alo Bhi has the
+// error of the 3xTF32 form; kind::f16 runs at twice the kind::tf32 rate.  FP16's
+// exponent range is narrow, so every operand is scaled by a power of two that
+// brings its bound to 2^12..2^13 (an element's absolute error is then at most
+// 2^-25, the spacing of the FP16 subnormals, against an operand bound of 2^12:
+// 37 bits of range, of which the split needs 22):
+//   DST matrices    x 2^12 (entries 2 sin(.) are bounded by 2; host planes);
+//   Xs              x 2^(12 - e), xmax < 2^e the slab's largest |X|, which the
+//                   kernels that write X leave in xmax[slab] (atomicMax of the
+//                   bits; this kernel reads it and clears it);
+//   D1, D3          x 2^-20 (|D| <= 2^12 * 2^13 * 2 * 128 terms);
+//   D2 o F          x 2^(-20 - ceil log2 max F);
+// and H is D4 times the inverse of the product of the scales, again a power of
+// two.  A K chunk is 32 FP16 values, the same 64 bytes per row as the 16 TF32
+// values of the TF32 form, so operands and DST-matrix chunks keep their byte
+// layout while a slab takes half as many chunks (and MMA-warp waits); with the
+// X tile of a first-product chunk now 64 R columns (two 32-column tensor
+// copies), a stage is 64 KB and three stages fill the same 192 KB.
+constexpr int H_KC = 32;                                // FP16 values of K per chunk
+constexpr int H_NS = 3;                                 // stages
+constexpr uint32_t H_SBO = (H_KC / 8) * 128;            // 512 B between 8-row groups
+constexpr uint32_t H_SMALL = 2 * 128 * H_KC * 2;        // 16 KB: hi + lo, 128 rows
+constexpr uint32_t H_SMALL_LO = H_SMALL / 2;
+constexpr uint32_t H_BIG = 2 * 256 * H_KC * 2;          // 32 KB: hi + lo, 256 rows
+constexpr uint32_t H_XT = 16384;                        // one 128 x 32 FP32 X tile
+constexpr uint32_t H_STAGE = 65536;                     // big [0, 32K), X tiles [16K, 48K), small [48K, 64K)
+constexpr uint32_t H_SMALL_AT = 49152;
+constexpr uint32_t H_BYTES = H_NS * H_STAGE;            // 192 KB
+constexpr int H_NKH = 128 / H_KC;                       // K chunks of a 128-wide operand
+constexpr size_t H_CHUNK = H_SMALL / 2;                 // halves of one 128-row chunk (hi + lo)
+constexpr int H_S_EXP = 12;                             // the DST matrices' scale 2^12
+static_assert(H_SMALL == D2_SMALL && H_SBO == D2_SBO, "FP16 chunks keep the TF32 chunks' bytes");
+
+__device__ __forceinline__ uint32_t kmaj16_off(int r, int k)
+{
+    return (uint32_t)((r & 7) * 16 + (r >> 3) * H_SBO + (k & 7) * 2 + (k >> 3) * 128);
+}
+
+__device__ __forceinline__ uint32_t h_pack(float a, float b)
+{
+    return (uint32_t)__half_as_ushort(__float2half_rn(a)) | ((uint32_t)__half_as_ushort(__float2half_rn(b)) << 16);
+}
+
+// eight consecutive k values of one row (already scaled) into the hi plane at
+// off and the lo plane lo_off further: hi = fp16(x), lo = fp16(x - hi)
+__device__ __forceinline__ void h_split8(unsigned char *hi, uint32_t lo_off, uint32_t off, const float *v)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const __half a = __float2half_rn(v[2 * i]), b = __float2half_rn(v[2 * i + 1]);
+        h[i] = (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
+        l[i] = h_pack(v[2 * i] - __half2float(a), v[2 * i + 1] - __half2float(b));
+    }
+    *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(hi + lo_off + off) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// instruction descriptor of kind::f16 with FP16 A and B, FP32 accumulate, K-major
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, int accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :
+        : "r"(dtmem), "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+}
+
+// the chunk sequence as d2_for_chunks, with the stage s and its phase parity ph
+// carried along (three stages: no power of two)
+template <typename F>
+__device__ __forceinline__ void h_for_chunks(int nkh, int nkr, F &&f)
+{
+    int t = 0, s = 0, ph = 0;
+    auto step = [&](int gi, int par, int jc) {
+        f(t, s, ph, gi, par, jc);
+        t++;
+        if (++s == H_NS) {
+            s = 0;
+            ph ^= 1;
+        }
+    };
+    for (int jc = 0; jc < nkh; jc++)
+        for (int par = 0; par < 2; par++) step(0, par, jc);
+    for (int jc = 0; jc < nkr; jc++) step(1, 0, jc);
+    for (int jc = 0; jc < nkr; jc++) step(2, 0, jc);
+    for (int par = 0; par < 2; par++)
+        for (int jc = 0; jc < nkh; jc++) step(3, par, jc);
+}
+
+struct Dst2hArgs {
+    Dst2Args b;                   // the TF32 kernel's arguments (matrix planes unused)
+    const __half *s2fold;         // [parity][H_NKH][hi, lo] x 2^12
+    const __half *s1planes;       // S1 of each length, H_NKH chunks of 32 columns, x 2^12
+    unsigned *xmax;               // [G na]: bits of the slab's largest |X|, cleared here
+    int fexp;                     // ceil(log2(max F)) over the context
+};
+
+__global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, const __grid_constant__ CUtensorMap xmap)
+{
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char *sm = smraw + ((1024 - (smem_u32(smraw) & 1023)) & 1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + H_BYTES);
+    uint64_t *empty = full + H_NS;
+    uint64_t *xfull = empty + H_NS;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(xfull + H_NS);
+    float *s_p1f = reinterpret_cast<float *>(sm + H_BYTES + 128);
+    volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
+    const Dst2Args &p = P.b;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int na = p.na, n1 = p.n1, n2 = p.n2;
+    const int h = (n2 + 1) >> 1;
+    const int nkh = (h + H_KC - 1) / H_KC;
+    const int seg = p.seg0 + blockIdx.x;
+    if (warp == D2_COPY_WARP && lane == 0)
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&xmap)) : "memory");
+    if (warp == 0) tmem_alloc(slot, 512);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < H_NS; i++) {
+            mbar_init(&full[i], D2_FILL + 1);
+            mbar_init(&empty[i], 1);
+            mbar_init(&xfull[i], 1);
+        }
+        *fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tb = *slot;
+    const int NT = (n2 + 127) / 128;
+    const int RB = 128 * NT;
+    const uint32_t big_lo = (uint32_t)RB * H_KC * 2;    // lo plane of an RB-row operand
+    const int g = seg / na, a = seg % na, w = p.blk_wave[g];
+    const int nn = p.nopr1[w * na + a];
+    const int nnp = (nn + 15) & ~15;
+    const int nkr = (nn + H_KC - 1) / H_KC;
+    const int total = 4 * nkh + 2 * nkr;
+    const __half *S1p = P.s1planes + p.s1off[w * na + a];
+    int copies = 0;
+
+    if (warp == D2_COPY_WARP) {
+        if (lane == 0)
+            h_for_chunks(nkh, nkr, [&](int t, int s, int ph, int gi, int par, int jc) {
+                if (*fail) return;
+                if (t >= H_NS && !d2_wait(&empty[s], ph ^ 1, fail)) return;
+                unsigned char *st = sm + (size_t)s * H_STAGE;
+                const bool alongR = (gi == 0 || gi == 3);
+                const __half *src = alongR ? P.s2fold + (size_t)(par * H_NKH + jc) * H_CHUNK
+                                           : S1p + (size_t)jc * H_CHUNK;
+                if (gi == 0) {
+                    // the 64 R columns of this K chunk (both parities), two 32-column tiles
+                    // behind the S2 chunk; each parity's stage gets its own copy
+                    mbar_expect_tx(&xfull[s], 2 * H_XT);
+                    tma_load_2d(st + 16384, &xmap, 64 * jc, seg * n1, &xfull[s]);
+                    tma_load_2d(st + 32768, &xmap, 64 * jc + 32, seg * n1, &xfull[s]);
+                }
+                mbar_expect_tx(&full[s], H_SMALL);
+                bulk_g2s(alongR ? st : st + H_SMALL_AT, src, H_SMALL, &full[s]);
+                copies = t + 1;
+            });
+    } else if (warp == D2_MMA_WARP) {
+        if (lane == 0) {
+            const uint64_t k16 = 256 >> 4;                  // one K step of 16 (two core matrices)
+            const uint64_t d0 = sdesc(smem_u32(sm), 128, H_SBO);
+            const uint64_t stage16 = H_STAGE >> 4, small16 = H_SMALL_AT >> 4;
+            const uint64_t lo128 = H_SMALL_LO >> 4, loRB = big_lo >> 4, tile16 = (16 * H_SBO) >> 4;
+            const uint32_t id_nn = idesc_f16(128, nnp), id_rb = idesc_f16(128, RB), id_128 = idesc_f16(128, 128);
+            h_for_chunks(nkh, nkr, [&](int t, int s, int ph, int gi, int par, int jc) {
+                const bool ok = d2_wait(&full[s], ph, fail);
+                fence_after_sync();
+                if (ok) {
+                    const uint64_t bg = d0 + (uint64_t)s * stage16, sl = bg + small16;
+#pragma unroll
+                    for (int ks = 0; ks < H_KC / 16; ks++) {
+                        const uint64_t o = ks * k16;
+                        const int acc0 = (jc > 0 || ks > 0) ? 1 : 0;
+                        if (gi == 0) {
+                            const uint32_t d = tb + 128u * par;
+                            mma_f16(d, bg + o, sl + o, id_nn, acc0);
+                            mma_f16(d, bg + o, sl + lo128 + o, id_nn, 1);
+                            mma_f16(d, bg + lo128 + o, sl + o, id_nn, 1);
+                        } else if (gi == 1) {
+                            for (int tt = 0; tt < NT; tt++) {
+                                const uint64_t at = bg + tt * tile16;
+                                const uint32_t d = tb + 256u + 128u * tt;
+                                mma_f16(d, at + o, sl + o, id_nn, acc0);
+                                mma_f16(d, at + o, sl + lo128 + o, id_nn, 1);
+                                mma_f16(d, at + loRB + o, sl + o, id_nn, 1);
+                            }
+                        } else if (gi == 2) {
+                            mma_f16(tb, sl + o, bg + o, id_rb, acc0);
+                            mma_f16(tb, sl + o, bg + loRB + o, id_rb, 1);
+                            mma_f16(tb, sl + lo128 + o, bg + o, id_rb, 1);
+                        } else {
+                            const uint32_t d = tb + 256u + 128u * par;
+                            mma_f16(d, sl + o, bg + o, id_128, acc0);
+                            mma_f16(d, sl + o, bg + lo128 + o, id_128, 1);
+                            mma_f16(d, sl + lo128 + o, bg + o, id_128, 1);
+                        }
+                    }
+                }
+                mma_commit(&empty[s]);
+            });
+        }
+    } else {
+        const int q4 = warp & 3, sub = warp >> 2;
+        const int m = q4 * 32 + lane;
+        const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
+        const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
+        // the slab's scales (powers of two, see above)
+        const float xm = __uint_as_float(P.xmax[seg]);
+        int ex = 0;
+        if (xm > 0.f) frexpf(xm, &ex);                  // xm < 2^ex
+        const int sx_exp = min(100, max(-100, 12 - ex)), a2_exp = -20 - P.fexp;
+        const float sx = ldexpf(1.f, sx_exp), a1 = ldexpf(1.f, -20), a2 = ldexpf(1.f, a2_exp), a3 = a1;
+        const float hinv = ldexpf(1.f, -(4 * H_S_EXP + sx_exp - 20 + a2_exp - 20));
+        {
+            const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
+            if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
+            asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
+        }
+        const int rset = sub & 1, colq = sub >> 1;
+        const int rR = 128 * rset + m;
+        const float e2 = (rset < NT && rR < n2) ? p.p2r2f[((size_t)w * na + a) * n2 + rR] : 0.f;
+        const float radcut = p.radcut;
+        const bool on2 = rset == 0 ? (m < h) : (m < n2 - h);
+        const int R2 = rset == 0 ? m : n2 - 1 - m;
+        const float sg2 = rset == 0 ? 1.f : -1.f;
+        int pt = -1, pph = 0;                           // the previous chunk's stage and parity
+        h_for_chunks(nkh, nkr, [&](int t, int s, int ph, int gi, int par, int jc) {
+            unsigned char *st = sm + (size_t)s * H_STAGE, *big = st, *small = st + H_SMALL_AT;
+            if (jc == 0 && par == 0 && gi > 0) {
+                d2_wait(&empty[pt], pph, fail);
+                fence_after_sync();
+            }
+            if (t >= H_NS) d2_wait(&empty[s], ph ^ 1, fail);
+            const int k0 = jc * H_KC;
+            if (gi == 0) {
+                // B = Xs columns 2j + par, j in this chunk's 32 (rows r1): thread (row r, group kg
+                // of 8 j) reads 16 consecutive R columns of its row from one 32-column tile
+                d2_wait(&xfull[s], ph, fail);
+                const int e = threadIdx.x, rest = e >> 3, kg = rest & 3, r = (rest >> 2) * 8 + (e & 7);
+                const unsigned char *row = st + 16384 + (kg >> 1) * H_XT + r * 128;
+                const int q0 = (kg & 1) * 4;
+                float v[8];
+#pragma unroll
+                for (int qq = 0; qq < 4; qq++) {
+                    const float4 x = *reinterpret_cast<const float4 *>(row + (((q0 + qq) ^ (r & 7)) << 4));
+                    v[2 * qq] = (par == 0 ? x.x : x.y) * sx;
+                    v[2 * qq + 1] = (par == 0 ? x.z : x.w) * sx;
+                }
+                if (r >= nn) {
+#pragma unroll
+                    for (int i = 0; i < 8; i++) v[i] = 0.f;
+                }
+                h_split8(small, H_SMALL_LO, kmaj16_off(r, 8 * kg), v);
+            } else if (gi == 1) {
+                // A = D1 rows R (sum or difference rows) from 16 E and O columns of lane i
+                const int kc = k0 + 16 * colq;
+                float ev[16], ov[16];
+                tmem_ld16(lrow + (uint32_t)kc, ev);
+                tmem_ld16(lrow + 128u + (uint32_t)kc, ov);
+                if (on2) {
+                    const bool fullc = kc + 16 <= nn;
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        const float x = (ev[i] + sg2 * ov[i]) * a1;
+                        ev[i] = (fullc || kc + i < nn) ? x : 0.f;
+                    }
+                    h_split8(big, big_lo, kmaj16_off(R2, 16 * colq), ev);
+                    h_split8(big, big_lo, kmaj16_off(R2, 16 * colq + 8), ev + 8);
+                }
+            } else if (gi == 2) {
+                // B = (D2 o F^T) rows R, 16 columns of R tile rset
+                if (rset < NT) {
+                    const int kc = k0 + 16 * colq;
+                    float v[16];
+                    tmem_ld16(lrow + 256u + 128u * rset + (uint32_t)kc, v);
+                    const bool fullc = kc + 16 <= nn && rR < n2;
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        const float ek = fminf(s_p1f[kc + i] + e2, radcut);
+                        const float x = v[i] * ek * divi * a2;
+                        v[i] = (fullc || (kc + i < nn && rR < n2)) ? x : 0.f;
+                    }
+                    h_split8(big, big_lo, kmaj16_off(rR, 16 * colq), v);
+                    h_split8(big, big_lo, kmaj16_off(rR, 16 * colq + 8), v + 8);
+                }
+            } else {
+                // A = D3 columns 2j + par (rows r1): warp sub takes j in [k0 + 8 sub, +8)
+                float v16[16];
+                const int col0 = 2 * k0 + 16 * sub;
+                tmem_ld16(lrow + (uint32_t)col0, v16);
+                const bool fullc = col0 + 16 <= n2;
+                float v[8];
+#pragma unroll
+                for (int uu = 0; uu < 8; uu++) {
+                    const float x = (par == 0 ? v16[2 * uu] : v16[2 * uu + 1]) * a3;
+                    v[uu] = (fullc || col0 + 2 * uu + par < n2) ? x : 0.f;
+                }
+                h_split8(small, H_SMALL_LO, kmaj16_off(m, 8 * sub), v);
+            }
+            fence_async_smem();
+            fence_before_sync();
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&full[s]);
+            pt = s;
+            pph = ph;
+        });
+        const int *mT = p.mapT + (size_t)a * n2 * n1;
+        if (m < nn) {
+#pragma unroll 4
+            for (int uu = 0; uu < 32; uu++) {
+                int i = 32 * sub + uu;
+                if (i < h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)i * n1 + m));
+                if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
+            }
+        }
+        d2_wait(&empty[pt], pph, fail);
+        fence_after_sync();
+        if (!*fail) {
+            const int64_t fo = p.foff[seg];
+#pragma unroll
+            for (int cc = 0; cc < 2; cc++) {
+                const int i0 = 32 * sub + 16 * cc;
+                float e[16], o[16];
+                tmem_ld16(lrow + 256u + (uint32_t)i0, e);
+                tmem_ld16(lrow + 384u + (uint32_t)i0, o);
+                int is[16], id[16];
+#pragma unroll
+                for (int uu = 0; uu < 16; uu++) {
+                    int i = i0 + uu;
+                    is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
+                    id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
+                }
+#pragma unroll
+                for (int uu = 0; uu < 16; uu++) {
+                    if (is[uu] >= 0) p.H[fo + is[uu]] = (e[uu] + o[uu]) * hinv;
+                    if (id[uu] >= 0) p.H[fo + id[uu]] = (e[uu] - o[uu]) * hinv;
+                }
+            }
+        }
+    }
+    const int lt = total - 1, ls = lt % H_NS, lph = (lt / H_NS) & 1;
+    if (lane == 0 && warp == D2_COPY_WARP && copies > 0) {
+        const int c1 = copies - 1;
+        mbar_wait(&full[c1 % H_NS], (c1 / H_NS) & 1);
+    }
+    if (lane == 0 && warp == D2_MMA_WARP) mbar_wait(&empty[ls], lph);
+    fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (*fail) atomicExch(p.err, 1);
+        P.xmax[seg] = 0u;                               // the next writer of X starts from zero
+    }
+    if (warp == 0) tmem_dealloc(tb, 512);
+}
+
 }  // namespace tc
 
 namespace {
@@ -508,6 +878,39 @@ std::vector<float> s2_fold_planes(const std::vector<double> &S, int n)
     return out;
 }
 
+// the FP16 forms: x 2^12 split into hi = fp16(x) and lo = fp16(x - hi), chunks
+// of 128 rows x 32 k in the canonical K-major layout of 16-bit values
+inline void put16(std::vector<__half> &out, size_t base, int r, int k, double x)
+{
+    const double xs = x * (double)(1 << tc::H_S_EXP);
+    const __half h = __double2half(xs);
+    const __half l = __double2half(xs - (double)__half2float(h));
+    const int c = k / tc::H_KC, kk = k % tc::H_KC;
+    const size_t plane = (size_t)128 * tc::H_KC;
+    const size_t o = (size_t)((r & 7) * 16 + (r >> 3) * tc::H_SBO + (kk & 7) * 2 + (kk >> 3) * 128) / 2;
+    out[base + (size_t)c * 2 * plane + o] = h;
+    out[base + (size_t)c * 2 * plane + plane + o] = l;
+}
+
+void append_planes16(std::vector<__half> &out, const std::vector<double> &S, int n)
+{
+    size_t base = out.size();
+    out.resize(base + (size_t)tc::H_NKH * 2 * 128 * tc::H_KC, __float2half(0.f));
+    for (int r = 0; r < n; r++)
+        for (int k = 0; k < n; k++) put16(out, base, r, k, S[(size_t)r * n + k]);
+}
+
+std::vector<__half> s2_fold_planes16(const std::vector<double> &S, int n)
+{
+    const size_t per = (size_t)tc::H_NKH * 2 * 128 * tc::H_KC;
+    std::vector<__half> out(2 * per, __float2half(0.f));
+    const int h = (n + 1) / 2;
+    for (int par = 0; par < 2; par++)
+        for (int i = 0; i < h; i++)
+            for (int j = 0; 2 * j + par < n; j++) put16(out, (size_t)par * per, i, j, S[(size_t)i * n + 2 * j + par]);
+    return out;
+}
+
 template <typename V>
 int upload_vec(Ctx &c, V **dst, const std::vector<V> &v)
 {
@@ -542,10 +945,12 @@ int build_tc_dst2d(Ctx &c)
     for (auto &t : c.waves)
         for (int a = 0; a < na; a++)
             if (t.nopr1[a] > 128 || t.nopr1[a] < 1) return MW3_OK;
-    std::vector<float> fold = s2_fold_planes(dst_matrix(c.n2), c.n2);
+    std::vector<double> S2 = dst_matrix(c.n2);
+    std::vector<float> fold = s2_fold_planes(S2, c.n2);
+    std::vector<__half> fold16 = s2_fold_planes16(S2, c.n2), planes16;
     std::vector<float> planes;
-    std::map<int, int64_t> off;
-    std::vector<int64_t> s1off((size_t)W * na);
+    std::map<int, int64_t> off, off16;
+    std::vector<int64_t> s1off((size_t)W * na), s1off16((size_t)W * na);
     // the r1 momenta padded by one chunk: the kernel reads them 16 at a time
     std::vector<float> p1f((size_t)W * na * c.n1 + 16, 0.f), p2f((size_t)W * na * c.n2);
     for (int w = 0; w < W; w++) {
@@ -554,16 +959,36 @@ int build_tc_dst2d(Ctx &c)
             int nn = t.nopr1[a];
             auto it = off.find(nn);
             if (it == off.end()) {
+                std::vector<double> S1 = dst_matrix(nn);
                 int64_t o = (int64_t)planes.size();
-                append_planes(planes, dst_matrix(nn), nn);
+                append_planes(planes, S1, nn);
                 it = off.emplace(nn, o).first;
+                int64_t o16 = (int64_t)planes16.size();
+                append_planes16(planes16, S1, nn);
+                off16.emplace(nn, o16);
             }
             s1off[(size_t)w * na + a] = it->second;
+            s1off16[(size_t)w * na + a] = off16[nn];
         }
         for (size_t i = 0; i < t.p2r1.size(); i++) p1f[(size_t)w * na * c.n1 + i] = (float)t.p2r1[i];
         for (size_t i = 0; i < t.p2r2.size(); i++) p2f[(size_t)w * na * c.n2 + i] = (float)t.p2r2[i];
     }
     int rc;
+    const char *tf = std::getenv("MW3_DST_TF32");
+    c.dst_f16 = !(tf && tf[0] == '1');
+    {
+        // F <= radcut / (4 (nn+1)(n2+1)) with nn >= 1: a bound for every slab
+        int e = 0;
+        std::frexp(c.grid.radcutmax / (8.0 * (c.n2 + 1)), &e);
+        c.dst_fexp = e;
+    }
+    __half *p16 = nullptr, *f16 = nullptr;
+    if ((rc = upload_vec(c, &p16, planes16))) return rc;
+    if ((rc = upload_vec(c, &f16, fold16))) return rc;
+    c.d_dst_planes16 = p16;
+    c.d_dst_s2fold16 = f16;
+    if ((rc = upload_vec(c, &c.d_dst_s1off16, s1off16))) return rc;
+    if ((rc = upload_vec(c, &c.d_xmax, std::vector<unsigned>((size_t)c.G * na, 0u)))) return rc;
     if ((rc = upload_vec(c, &c.d_dst_planes, planes))) return rc;
     if ((rc = upload_vec(c, &c.d_dst_s2fold, fold))) return rc;
     if ((rc = upload_vec(c, &c.d_dst_s1off, s1off))) return rc;
@@ -604,8 +1029,10 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     using namespace tc;
     static bool attr = false;
     const size_t smem = D2_BYTES + 1024 + 1024;         // stages, barriers and momenta, alignment slack
+    static_assert(H_BYTES == D2_BYTES, "both forms take the same shared memory");
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_tc_dst2d_h, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr = true;
     }
     int nseg = (g_end - g_begin) * c.na;
@@ -619,7 +1046,18 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.err = c.d_tc_err;
     CUtensorMap xmap;
     std::memcpy(&xmap, c.dst_xmap, sizeof(xmap));
-    k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p, xmap);
+    if (c.dst_f16) {
+        Dst2hArgs P;
+        P.b = p;
+        P.s2fold = static_cast<const __half *>(c.d_dst_s2fold16);
+        P.s1planes = static_cast<const __half *>(c.d_dst_planes16);
+        P.b.s1off = c.d_dst_s1off16;
+        P.xmax = c.d_xmax;
+        P.fexp = c.dst_fexp;
+        k_tc_dst2d_h<<<nseg, D2_WARPS * 32, smem, c.stream>>>(P, xmap);
+    } else {
+        k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p, xmap);
+    }
     c.launches++;
 }
 

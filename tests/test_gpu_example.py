@@ -38,7 +38,8 @@ def _projection(example_case, run):
     from madwave3_gb300.host import transcoor
     fd, ed, nob = example_case[1]["product"]
     pp = transcoor.ini_transcoor(run, 6.0, 1, run.inp.npun2, 1, run.inp.nangu, 0, 0, 0, 20, 0, 10, nob, fd)
-    return pp, ed, nob
+    # product_radialf_read refers the product levels to ediatref, as the reactants'
+    return pp, ed - run.ediatref, nob
 
 
 @pytest.fixture(scope="module")
