@@ -123,6 +123,13 @@ module mw3gpu
        real(c_double) :: norms(*)
        integer(c_int64_t) :: n
      end function
+     integer(c_int) function mw3_autocorrelation(ctx, wave_id, autos, n) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: wave_id
+       real(c_double) :: autos(*)
+       integer(c_int64_t) :: n
+     end function
      integer(c_int) function mw3_totalflux(ctx, wave_id, s2prodtot, s2prodelec) bind(c)
        import
        type(c_ptr), value :: ctx

@@ -146,6 +146,12 @@ int mw3_norms(mw3_ctx *ctx, int32_t wave_id, double *norms, int64_t *n);
  * s2prodtot[netot], s2prodelec[nelec][netot] (may be NULL). */
 int mw3_totalflux(mw3_ctx *ctx, int32_t wave_id, double *s2prodtot, double *s2prodelec);
 
+/* check's autocorrelation for photodissociation waves (iphoto >= 1,
+ * SRC/main_madwave3.f:444-455, written to the auto.* file the spectra program
+ * reads): <psi0|psi_k> after each iteration since the last mw3_start, with
+ * psi0 the packet mw3_start received; same slots as mw3_norms. */
+int mw3_autocorrelation(mw3_ctx *ctx, int32_t wave_id, double *autos, int64_t *n);
+
 /* Raw accumulators, complex as (re,im) pairs: zcr/zcdr [nflux][netot],
  * zs2 [ncan][nj][nv][netot], cvj [ncan][nj][nv] of the last iteration,
  * zfe [nofe][ntot].  Any pointer may be NULL. */

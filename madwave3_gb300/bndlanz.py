@@ -229,12 +229,11 @@ def write_bnd(outdir, run, iv, energy_zot, vec, idproc=0):
             f.write("".join(" %7d" % x for x in (k + 1,) + tuple(lab[k])) + "\n")
 
 
-def initial_from_bound(run, outdir, iv, nelec_bnd=None, idproc=0):
-    """dip_bndgrid for iphoto = 2 (SRC/mod_photoini_01y2.f:509-717): the initial
-    packet from a bound state that write_bnd stored on the same radial and
-    angular grid, point by point through (ir1, ir2, gamma, Omega, electronic
-    state); points of the run outside the stored state's range stay 0.
-    Returns (psi0, energy in eV, norm of the mapped part)."""
+def read_bound_state(run, outdir, iv, idproc=0):
+    """A bound state write_bnd stored (bnd.ivNNN.ipNNN, grid.ipNNN), checked to
+    lie on the run's grid as dip_bndgrid checks it (SRC/mod_photoini_01y2.f:
+    537-650).  Returns ({(ir1, ir2, iang, Omega, ielec): value}, (nr1, nr2,
+    nang, Omega max, electronic states), energy in eV)."""
     import os
     i = run.inp
     with open(os.path.join(outdir, "grid.ip%03d" % idproc)) as f:
@@ -255,9 +254,19 @@ def initial_from_bound(run, outdir, iv, nelec_bnd=None, idproc=0):
     # columns: i, icanp, ielec, iom, iangp, ir, ir1, ir2, iang
     for row, x in zip(lab, val):
         key[(row[6], row[7], row[8], row[3], row[2])] = x     # ir1, ir2, iang, iom, ielec
-    nr1, nr2, nang = lab[:, 6].max(), lab[:, 7].max(), lab[:, 8].max()
-    omax = lab[:, 3].max()
-    nel = lab[:, 2].max() if nelec_bnd is None else nelec_bnd
+    dims = (lab[:, 6].max(), lab[:, 7].max(), lab[:, 8].max(), lab[:, 3].max(), lab[:, 2].max())
+    return key, dims, e_ev
+
+
+def initial_from_bound(run, outdir, iv, nelec_bnd=None, idproc=0):
+    """dip_bndgrid for iphoto = 2 (SRC/mod_photoini_01y2.f:509-717): the initial
+    packet from a bound state that write_bnd stored on the same radial and
+    angular grid, point by point through (ir1, ir2, gamma, Omega, electronic
+    state); points of the run outside the stored state's range stay 0.
+    Returns (psi0, energy in eV, norm of the mapped part).  The dipole-weighted
+    form (iphoto = 1) is madwave3_gb300.photo.initial_packet."""
+    key, (nr1, nr2, nang, omax, nel0), e_ev = read_bound_state(run, outdir, iv, idproc)
+    nel = nel0 if nelec_bnd is None else nelec_bnd
     me = _point_labels(run)
     psi0 = np.zeros(run.ntot)
     for k in range(run.ntot):

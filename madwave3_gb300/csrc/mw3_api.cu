@@ -513,6 +513,7 @@ int build_device(Ctx &c)
     }
     c.wdev.assign(W, WaveDev());
     c.nofemax = 0;
+    c.auto_nb = 0;
     for (auto &t : c.waves) c.nofemax = std::max(c.nofemax, t.nofe);
     TRY(dalloc(c, &c.d_zcke, (size_t)W * std::max(c.nofemax, 1) * 2));
     std::vector<double *> zfeptr(W, nullptr), normptr(W, nullptr);
@@ -537,11 +538,16 @@ int build_device(Ctx &c)
                 zfeptr[w] = d.zfe;
             }
             d.norms_cap = 1024;
-            TRY(dalloc(c, &d.norms, (size_t)d.norms_cap));
+            TRY(dalloc(c, &d.norms, (size_t)2 * d.norms_cap));
+            if (t.iphoto >= 1) {
+                TRY(dalloc(c, &d.psi0, (size_t)t.ntot));
+                c.auto_nb = std::max(c.auto_nb, (int)((t.ntot + 2047) / 2048));
+            }
             normptr[w] = d.norms;
             normcap[w] = d.norms_cap;
         }
     }
+    if (c.auto_nb > 0) TRY(dalloc(c, &c.d_autopart, (size_t)c.auto_nb));
     TRY(dupload(c, &c.d_zfe_ptrs, zfeptr));
     TRY(dupload(c, &c.d_norm_ptrs, normptr));
     TRY(dupload(c, &c.d_norm_cap, normcap));
@@ -637,9 +643,11 @@ int grow_norms(Ctx &c, int64_t need)
         if (need > d.norms_cap) {
             int64_t nc = std::max(need, 2 * d.norms_cap);
             double *p;
-            TRY(dalloc(c, &p, (size_t)nc));
+            TRY(dalloc(c, &p, (size_t)2 * nc));      // norm trace, then the autocorrelation
             MW3_CUDA_TRY(cudaMemcpyAsync(p, d.norms, sizeof(double) * d.norms_cap, cudaMemcpyDeviceToDevice,
                                          c.stream));
+            MW3_CUDA_TRY(cudaMemcpyAsync(p + nc, d.norms + d.norms_cap, sizeof(double) * d.norms_cap,
+                                         cudaMemcpyDeviceToDevice, c.stream));
             d.norms = p;
             d.norms_cap = nc;
             changed = true;
@@ -875,6 +883,10 @@ int mw3_start(mw3_ctx *h, const double *const *psi0s)
                                      c.stream));
     }
     MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, c.d_pk, sizeof(double) * c.NT, cudaMemcpyDeviceToDevice, c.stream));
+    for (size_t w = 0; w < c.waves.size(); w++)   // check's rpaq0 of the photodissociation waves
+        if (c.wdev[w].psi0)
+            MW3_CUDA_TRY(cudaMemcpyAsync(c.wdev[w].psi0, c.d_pk + c.waves[w].flat0, sizeof(double) * c.waves[w].ntot,
+                                         cudaMemcpyDeviceToDevice, c.stream));
     rc = reset_accumulators(c);
     if (rc) return rc;
     scatter(c, c.d_pk, 0, c.G);
@@ -883,6 +895,7 @@ int mw3_start(mw3_ctx *h, const double *const *psi0s)
     std::swap(c.d_pk, c.d_pkm1);
     std::swap(c.d_pk32, c.d_pkm1_32);
     mw3::launch_norms(c, 0);
+    if (c.auto_nb > 0) mw3::launch_autocorr(c, 0);
     c.it = 1;
     c.norm_slot = 1;
     c.hist_n = 0;
@@ -940,6 +953,7 @@ void run_iteration(Ctx &c)
     std::swap(c.d_pk32, c.d_pkm1_32);
     mw3::launch_accumulators(c, it);
     mw3::launch_norms(c, c.norm_slot);
+    if (c.auto_nb > 0) mw3::launch_autocorr(c, c.norm_slot);
     mw3::launch_cvj_keep(c, it, c.norm_slot);
     if (c.hist_cap > 0) c.hist_n = std::min(c.hist_n + 1, c.hist_cap);
     if (c.prof && c.prof_n < c.prof_cap) {
@@ -1132,6 +1146,24 @@ int mw3_norms(mw3_ctx *h, int32_t w, double *norms, int64_t *n)
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
     *n = m;
     return MW3_OK;
+}
+
+int mw3_autocorrelation(mw3_ctx *h, int32_t w, double *autos, int64_t *n)
+{
+    if (!h || !n) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size() || !c.started) return MW3_ERR_STATE;
+    if (!c.wdev[w].psi0) {
+        c.err = "mw3_autocorrelation: the wave is not a photodissociation (iphoto >= 1)";
+        return MW3_ERR_STATE;
+    }
+    int64_t m = std::min(*n, c.norm_slot);
+    if (autos && m > 0)
+        MW3_CUDA_TRY(cudaMemcpyAsync(autos, c.wdev[w].norms + c.wdev[w].norms_cap, sizeof(double) * m,
+                                     cudaMemcpyDeviceToHost, c.stream));
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    *n = m;
+    return check_device_flags(c, "mw3_autocorrelation");
 }
 
 int mw3_totalflux(mw3_ctx *h, int32_t w, double *tot, double *elec)

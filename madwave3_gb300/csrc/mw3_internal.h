@@ -112,6 +112,7 @@ struct WaveDev {
     int *nobc = nullptr, *r2abs_map = nullptr;
     double *djmmp = nullptr;                     // wave's Djmmp
     double *efe = nullptr, *zfe = nullptr;       // PsiE
+    double *psi0 = nullptr;                      // photodissociation (iphoto >= 1): the initial packet
     ProdDev prod;                                // product-state projection, if set
 };
 
@@ -178,7 +179,9 @@ struct Ctx {
     // per-wave device tables
     int64_t *d_wflat0 = nullptr;     // [W+1]
     int *d_wseg0 = nullptr, *d_wseg1 = nullptr;      // segment range of each wave
-    double **d_norm_ptrs = nullptr;  // [W]
+    double **d_norm_ptrs = nullptr;  // [W]: norm trace [cap], then <psi0|psi_k> [cap] (photodissociation)
+    double *d_autopart = nullptr;    // block partial sums of <psi0|psi_k>
+    int auto_nb = 0;                 // their count for the largest photodissociation wave
     int64_t *d_norm_cap = nullptr;   // [W]
     double **d_zfe_ptrs = nullptr;   // [W]
     double *d_zcke = nullptr;        // [W][nofemax][2]
@@ -374,6 +377,8 @@ void launch_norms(Ctx &c, int64_t slot);
 void launch_set_itbase(Ctx &c);
 // prodpaq + prodcvj of every wave that has a product projection
 void launch_product(Ctx &c);
+// check's autocorrelation <psi0|psi_k> of every photodissociation wave into slot
+void launch_autocorr(Ctx &c, int64_t slot);
 // funE's C_k(E) for iteration it (launched before the update that uses it)
 void launch_fe_coef(Ctx &c, int64_t it);
 // the iteration's Cvj (and Cvjprod) into the history ring at slot mod hist_cap

@@ -1710,6 +1710,64 @@ void launch_addv(Ctx &c, const double *psi, int g0, int g1)
 }
 
 // the iteration and norm-slot base of a graph replay
+// check's autocorrelation (main_madwave3.f:444-455) for iphoto >= 1:
+// <psi0|psi_k> over a wave's points, block partial sums in a fixed order, then
+// one block sums the partials in order (deterministic, as the norm trace)
+constexpr int kAutoPer = 8;          // points per thread
+__global__ void __launch_bounds__(256) k_auto_part(const double *__restrict__ psi0, const double *__restrict__ pk,
+                                                   int64_t n, double *__restrict__ part)
+{
+    __shared__ double red[8];
+    const int64_t i0 = (int64_t)blockIdx.x * 256 * kAutoPer + threadIdx.x;
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < kAutoPer; k++) {
+        const int64_t i = i0 + 256 * k;
+        if (i < n) s = fma(psi0[i], pk[i], s);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int wv = 0; wv < 8; wv++) t += red[wv];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_auto_reduce(const double *__restrict__ part, int nb, double *const *norms_out,
+                                                     const int64_t *__restrict__ cap, int w, int64_t slot,
+                                                     const int64_t *__restrict__ base)
+{
+    if (base) slot += base[1];
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += 256) s += part[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && slot >= 0 && slot < cap[w]) norms_out[w][cap[w] + slot] = red[0];
+}
+
+void launch_autocorr(Ctx &c, int64_t slot)
+{
+    const int64_t sarg = c.capturing ? slot - c.cap_slot0 : slot;
+    const int64_t *bp = c.capturing ? c.d_itbase : nullptr;
+    for (size_t w = 0; w < c.waves.size(); w++) {
+        const WaveTables &t = c.waves[w];
+        if (t.iphoto < 1 || !c.wdev[w].psi0) continue;
+        const int nb = (int)((t.ntot + 256 * kAutoPer - 1) / (256 * kAutoPer));
+        k_auto_part<<<nb, 256, 0, c.stream>>>(c.wdev[w].psi0, c.d_pk + t.flat0, t.ntot, c.d_autopart);
+        LAUNCH_CHECK(c);
+        k_auto_reduce<<<1, 256, 0, c.stream>>>(c.d_autopart, nb, c.d_norm_ptrs, c.d_norm_cap, (int)w, sarg, bp);
+        LAUNCH_CHECK(c);
+    }
+}
+
 // Cvj / Cvjprod of one iteration into its slot of the history ring (FP64 source,
 // or the mixed path's FP32 Cvj ring slot); graph replays add the block's first
 // slot from base[1] as k_norms does

@@ -203,8 +203,8 @@ int build_wave_tables(Ctx &c, const mw3_wave &w, WaveTables &t, std::string &err
         err = "Proj_j2_up != 0 reads Wigner values the reference never sets; not supported";
         return MW3_ERR_UNSUPPORTED;
     }
-    if (w.iphoto != 0) {
-        err = "only collisions (iphoto=0) are supported";
+    if (w.iphoto < 0 || w.iphoto > 2) {
+        err = "iphoto must be 0 (collision), 1 (dipole transition) or 2 (bright approximation)";
         return MW3_ERR_UNSUPPORTED;
     }
     if (w.iprod == 1) {
@@ -481,6 +481,24 @@ int build_wave_tables(Ctx &c, const mw3_wave &w, WaveTables &t, std::string &err
     }
     int netot = w.netot;
     double estep = (w.ekinmax - w.ekinmin) / (double)(netot - 1);
+    if (w.iphoto >= 1) {
+        // Smatini_photo (SRC/mod_flux_01y2.f:526-581): no collision packet to divide
+        // by; the normalisation of the initial packet (photonorm) is the host's
+        t.etot.assign(netot, 0.0);
+        t.reacfct.assign(netot, 0.25 / kPi / w.xm1reac);
+        t.apaqini.assign(netot, 0.0);
+        t.s2factor.assign((size_t)ne * t.nj * t.nv * netot, 0.0);
+        for (int ie = 0; ie < netot; ie++) {
+            t.etot[ie] = w.ekinmin + (double)ie * estep;
+            for (int e = 0; e < ne; e++)
+                for (int jj = 0; jj < t.nj; jj++)
+                    for (int iv = 0; iv < t.nv; iv++) {
+                        double ekf = t.etot[ie] - t.ediat[((size_t)e * t.nj + jj) * t.nv + iv];
+                        double pfin = ekf > 0.0 ? sqrt(ekf * w.xm2reac * 2.0 / gr.hbr / gr.hbr) : 0.0;
+                        t.s2factor[(((size_t)e * t.nj + jj) * t.nv + iv) * netot + ie] = 4.0 * pfin / (kPi * w.xm2reac);
+                    }
+        }
+    } else {
     const int npunt = 1000;
     std::vector<double> rg(npunt);
     double ahgauss = (gr.rfin2 - gr.rmis2) / (double)(npunt - 1);
@@ -529,6 +547,7 @@ int build_wave_tables(Ctx &c, const mw3_wave &w, WaveTables &t, std::string &err
         t.reacfct[ie] =
             (paqini < 1e-10) ? 0.0 : gr.hbr * gr.hbr * pini / paqini / w.xmasa0 / w.xm1reac / 4.0 / kPi / kPi;
     }
+    }   // collision (Smatini_col)
 
     // ---- Cvjflux_k: point at (ir1, ir2abs) for every angle ----
     t.r2abs_map.assign((size_t)na * n1, -1);

@@ -3,8 +3,10 @@ SRC/main_madwave3.f:555-844) from the library's accumulators, in the
 reference's formats, so the post-processing programs of
 SRC/AUXILIARy-CODES (sigmaFromS2prod, CRP-fast, ...) read them unchanged.
 
-Written for the collision workloads (iphoto = 0, photonorm = 1,
-mod_flux_01y2.f:416) with a diatom (xm2 > 1e-3) and iprod = 0, 1 or 2:
+Written for a diatom (xm2 > 1e-3) and iprod = 0, 1 or 2; every probability
+is multiplied by photonorm, 1 for collisions (mod_flux_01y2.f:416) and the
+norm |d.e psi|^2 of the initial packet for photodissociation (dip_bnd,
+SRC/mod_photoini_01y2.f:384-386):
 
 * ``S2prod.vVV.JJJJ.kKKKKK``, one line per energy, format (501(1x,e17.7e3)):
   iprod = 0: E (eV), P(E) (S2prodtot), P(E) + S2reac, reacfct(E)
@@ -87,11 +89,13 @@ def s2prod_products(zs2prod, s2prodfac, pp):
 
 
 def write_s2prod(outdir, run, iloop, s2prodtot, s2prodelec, zs2, etot, reacfct, s2factor, nvmaxprod=None,
-                 iprod=None, product=None):
+                 iprod=None, product=None, photonorm=1.0):
     """Writes S2prod.vVV.JJJJ.kKKKKK and S2prodelec for one loop; returns the
     S2prod path.  Arguments as the library returns them (``Propagator.totalflux``,
     ``.accumulators()['zs2']``, ``.tables()``); iprod defaults to the run's,
-    and iprod = 2 takes product = (zs2prod, s2prodfac, ProductProjection)."""
+    and iprod = 2 takes product = (zs2prod, s2prodfac, ProductProjection).
+    photonorm scales every probability (1 for collisions; |d.e psi|^2 of
+    the photodissociation start, madwave3_gb300.photo.initial_packet)."""
     i = run.inp
     iprod = run.inp.iprod if iprod is None else iprod
     if iprod not in (0, 1, 2):
@@ -120,6 +124,14 @@ def write_s2prod(outdir, run, iloop, s2prodtot, s2prodelec, zs2, etot, reacfct, 
         vib[vib < 1e-90] = 0.0
     tot = np.where(np.asarray(s2prodtot) < 1e-90, 0.0, s2prodtot)
     s2reac = np.where(s2reac < 1e-90, 0.0, s2reac)
+    pn = float(photonorm)
+    if pn != 1.0:
+        tot, s2reac = tot * pn, s2reac * pn
+        s2prodelec = [np.asarray(x) * pn for x in s2prodelec]
+        if vib is not None:
+            vib = vib * pn
+        if iprod == 2:
+            s2no = s2no * pn
     name = os.path.join(outdir, "S2prod.v%02d.J%03d.k%05d" % (i.nvref, i.Jtot, iloop))
     e_ev = np.asarray(etot) / conve1 / eV2cm
     with open(name, "w") as f, open(os.path.join(outdir, "S2prodelec"), "w") as fe:

@@ -70,7 +70,7 @@ HEADER_FUNCS = [
     "mw3_get_stream",
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_set_product_projection", "mw3_download_product",
-    "mw3_cvj_history", "mw3_download_cvj_history", "mw3_set_flux_gate",
+    "mw3_cvj_history", "mw3_download_cvj_history", "mw3_set_flux_gate", "mw3_autocorrelation",
     "mw3_upload_accumulators", "mw3_upload_product",
     "mw3_last_error", "mw3_destroy",
 ]
@@ -118,6 +118,7 @@ def load_library(build_if_missing=True):
     L.mw3_tables.argtypes = [vp, ct.c_int32, I32P, F64P, F64P, F64P, F64P, F64P]
     L.mw3_packet_energy_norm.argtypes = [vp, ct.c_int32, F64P]
     L.mw3_cvj_history.argtypes = [vp, ct.c_int64]
+    L.mw3_autocorrelation.argtypes = [vp, ct.c_int32, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_set_flux_gate.argtypes = [vp, ct.c_int32, ct.c_int32]
     L.mw3_download_cvj_history.argtypes = [vp, ct.c_int32, ct.c_int64, F64P, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
@@ -342,6 +343,13 @@ class Propagator:
         buf = np.empty(cap)
         n = ct.c_int64(cap)
         self._check(self.L.mw3_norms(self.h, wave, _p(buf), ct.byref(n)), "mw3_norms")
+        return buf[: n.value].copy()
+
+    def autocorrelation(self, wave=0, cap=1 << 22):
+        """<psi0|psi_k>, k = 1, 2, ... of a photodissociation wave (check)."""
+        buf = np.empty(cap)
+        n = ct.c_int64(cap)
+        self._check(self.L.mw3_autocorrelation(self.h, wave, _p(buf), ct.byref(n)), "mw3_autocorrelation")
         return buf[: n.value].copy()
 
     def totalflux(self, wave=0):

@@ -351,6 +351,8 @@ struct mw3ref {
     int64_t *fl_idx;          /* flat index of each flux point */
     double *potiflux;
     int flux_gate;            /* 1: flux only where E > V(flux point) */
+    double *psi0;             /* photodissociation: the initial packet (check's rpaq0) */
+    double autocor;           /* <psi0|psi_k> of the last iteration */
     cplx *zcr, *zcdr;         /* [nflux][netot] */
     double *etot, *reacfct, *apaqini, *s2factor;  /* s2factor [nelec][nj][nv][netot] */
     cplx *zck;                /* [netot] */
@@ -657,11 +659,28 @@ static int ini_flux(mw3ref *r, char *err, int errlen)
     for (int b = 0; b < nc; b++)
         if (in->nelebas[b] == in->ielecref && in->iombas[b] == abs(in->iomref)) r->icanref = b;
     if (r->icanref < 0) { set_err(err, errlen, "icanref can not be set"); return -1; }
-    if (in->iphoto != 0) { set_err(err, errlen, "only collisions (iphoto=0) are restated"); return -1; }
-    /* Smatini_col */
+    if (in->iphoto < 0 || in->iphoto > 2) { set_err(err, errlen, "iphoto must be 0, 1 or 2"); return -1; }
     int netot = in->netot;
     double etotmin = in->ekinmin, etotmax = in->ekinmax;
     double estep = (etotmax - etotmin) / (double)(netot - 1);
+    if (in->iphoto >= 1) {
+        /* Smatini_photo (mod_flux_01y2.f:526-581) */
+        for (int ie = 0; ie < netot; ie++) {
+            r->etot[ie] = etotmin + (double)ie * estep;
+            r->apaqini[ie] = 0.0;
+            r->reacfct[ie] = 0.25 / MW3_PI / in->xm1reac;
+            for (int e = 0; e < in->nelec; e++)
+                for (int jj = 0; jj < r->nj; jj++)
+                    for (int iv = 0; iv < r->nv; iv++) {
+                        double ekinfin = r->etot[ie] - in->ediat[((size_t)e * r->nj + jj) * r->nv + iv];
+                        double pfin = ekinfin > 0.0 ? sqrt(ekinfin * in->xm2reac * 2.0 / in->hbr / in->hbr) : 0.0;
+                        r->s2factor[(((size_t)e * r->nj + jj) * r->nv + iv) * netot + ie] =
+                            4.0 * pfin / (MW3_PI * in->xm2reac);
+                    }
+        }
+        return 0;
+    }
+    /* Smatini_col */
     const int npunt = 1000;
     double *rg = (double *)malloc(sizeof(double) * npunt);
     double ahgauss = (in->rfin2 - in->rmis2) / (double)(npunt - 1);
@@ -778,6 +797,7 @@ void mw3ref_destroy(mw3ref *r)
     free(r->aorder); free(r->offs); free(r->nopr1); free(r->nopr2); free(r->p2r1); free(r->p2r2);
     free(r->xj2); free(r->xl2p); free(r->absfr1); free(r->absfr2);
     free(r->psi_km1); free(r->psi_k); free(r->hpsi); free(r->hproc);
+    free(r->psi0);
     free(r->zar1flux); free(r->ir1flux); free(r->fl_ang); free(r->fl_can); free(r->fl_r2); free(r->fl_idx); free(r->potiflux);
     free(r->zcr); free(r->zcdr); free(r->etot); free(r->reacfct); free(r->apaqini); free(r->s2factor);
     free(r->zck); free(r->zs2); free(r->cvj); free(r->zfe);
@@ -1253,6 +1273,10 @@ int mw3ref_get_product(const mw3ref *r, double *zs2prod, double *cvjprod)
 
 int mw3ref_start(mw3ref *r, const double *psi0)
 {
+    if (r->in.iphoto >= 1) {        /* check's rpaq0 (main_madwave3.f:444-455) */
+        if (!r->psi0) r->psi0 = (double *)malloc(sizeof(double) * r->ntot);
+        memcpy(r->psi0, psi0, sizeof(double) * r->ntot);
+    }
     int64_t n = r->ntot;
     memcpy(r->psi_km1, psi0, sizeof(double) * n);
     memcpy(r->psi_k, psi0, sizeof(double) * n);
@@ -1300,11 +1324,18 @@ int mw3ref_run(mw3ref *r, int nit, double *norms)
             for (int64_t i = 0; i < r->ntot; i++) x = x + r->psi_k[i] * r->psi_k[i];
             norms[s] = x;
         }
+        if (r->psi0) {
+            double x = 0.0;
+            for (int64_t i = 0; i < r->ntot; i++) x = x + r->psi0[i] * r->psi_k[i];
+            r->autocor = x;
+        }
         if (in->nofe > 0) fune(r, it);
         r->it = it;
     }
     return 0;
 }
+
+double mw3ref_autocorrelation(const mw3ref *r) { return r->autocor; }
 
 int mw3ref_get_state(const mw3ref *r, double *psi_km1, double *psi_k, int64_t *it)
 {

@@ -84,6 +84,7 @@ int64_t mw3ref_ntot(const mw3ref *r);
 void mw3ref_set_threads(mw3ref *r, int nthreads);
 void mw3ref_set_dst_mode(mw3ref *r, int mode);      /* 0 = FFT, 1 = direct sum */
 void mw3ref_set_flux_gate(mw3ref *r, int on);       /* totalflux_k's E > V(flux point) test, default on */
+double mw3ref_autocorrelation(const mw3ref *r);     /* iphoto >= 1: <psi0|psi_k> of the last iteration */
 
 /* difs: hpsi = H psi (flat reference layout) */
 int mw3ref_hphi(mw3ref *r, const double *psi, double *hpsi);

@@ -72,6 +72,8 @@ def lib():
         L.mw3ref_set_threads.argtypes = [ct.c_void_p, ct.c_int]
         L.mw3ref_set_dst_mode.argtypes = [ct.c_void_p, ct.c_int]
         L.mw3ref_set_flux_gate.argtypes = [ct.c_void_p, ct.c_int]
+        L.mw3ref_autocorrelation.argtypes = [ct.c_void_p]
+        L.mw3ref_autocorrelation.restype = ct.c_double
         for name in ("mw3ref_hphi",):
             getattr(L, name).argtypes = [ct.c_void_p, F64P, F64P]
         L.mw3ref_start.argtypes = [ct.c_void_p, F64P]
@@ -238,6 +240,14 @@ class Oracle:
         norms = np.zeros(n)
         lib().mw3ref_run(self.h, n, _p(norms, ct.c_double))
         return norms
+
+    def run_autocorrelation(self, n):
+        """n iterations one by one: (norms, <psi0|psi_k>) after each (iphoto >= 1)."""
+        norms, autos = np.zeros(n), np.zeros(n)
+        for k in range(n):
+            norms[k] = self.run_iters(1)[0]
+            autos[k] = lib().mw3ref_autocorrelation(self.h)
+        return norms, autos
 
     def state(self):
         a, b = np.zeros(self.ntot), np.zeros(self.ntot)
