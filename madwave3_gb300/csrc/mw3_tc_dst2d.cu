@@ -500,25 +500,35 @@ __device__ __forceinline__ uint32_t kmaj16_off(int r, int k)
     return (uint32_t)((r & 7) * 16 + (r >> 3) * H_SBO + (k & 7) * 2 + (k >> 3) * 128);
 }
 
-__device__ __forceinline__ uint32_t h_pack(float a, float b)
+// eight consecutive k values of one row (already scaled) into the hi plane at
+// off and the lo plane lo_off further: hi = fp16(x), lo = fp16(x - hi)
+__device__ __forceinline__ uint32_t h2_bits(__half2 x) { return *reinterpret_cast<const uint32_t *>(&x); }
+
+// hi and lo of two values, packed (two values per cvt, the lower k in the low half)
+__device__ __forceinline__ void h_split2(float a, float b, uint32_t &h, uint32_t &l)
 {
-    return (uint32_t)__half_as_ushort(__float2half_rn(a)) | ((uint32_t)__half_as_ushort(__float2half_rn(b)) << 16);
+    const __half2 hh = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(hh);
+    h = h2_bits(hh);
+    l = h2_bits(__floats2half2_rn(a - hf.x, b - hf.y));
 }
 
 // eight consecutive k values of one row (already scaled) into the hi plane at
 // off and the lo plane lo_off further: hi = fp16(x), lo = fp16(x - hi)
-__device__ __forceinline__ void h_split8(unsigned char *hi, uint32_t lo_off, uint32_t off, const float *v)
+__device__ __forceinline__ void h_split8(unsigned char *hi, uint32_t lo_off, uint32_t off, float v0, float v1,
+                                         float v2, float v3, float v4, float v5, float v6, float v7)
 {
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const __half a = __float2half_rn(v[2 * i]), b = __float2half_rn(v[2 * i + 1]);
-        h[i] = (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
-        l[i] = h_pack(v[2 * i] - __half2float(a), v[2 * i + 1] - __half2float(b));
-    }
-    *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4 *>(hi + lo_off + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    uint32_t h0, h1, h2, h3, l0, l1, l2, l3;
+    h_split2(v0, v1, h0, l0);
+    h_split2(v2, v3, h1, l1);
+    h_split2(v4, v5, h2, l2);
+    h_split2(v6, v7, h3, l3);
+    *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h0, h1, h2, h3);
+    *reinterpret_cast<uint4 *>(hi + lo_off + off) = make_uint4(l0, l1, l2, l3);
 }
+
+#define H_SPLIT8(dst, lo, off, v, o) \
+    h_split8(dst, lo, off, v[o], v[o + 1], v[o + 2], v[o + 3], v[o + 4], v[o + 5], v[o + 6], v[o + 7])
 
 // instruction descriptor of kind::f16 with FP16 A and B, FP32 accumulate, K-major
 __host__ __device__ constexpr uint32_t idesc_f16(int M, int N)
@@ -683,8 +693,10 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
         int ex = 0;
         if (xm > 0.f) frexpf(xm, &ex);                  // xm < 2^ex
         const int sx_exp = min(100, max(-100, 12 - ex)), a2_exp = -20 - P.fexp;
-        const float sx = ldexpf(1.f, sx_exp), a1 = ldexpf(1.f, -20), a2 = ldexpf(1.f, a2_exp), a3 = a1;
-        const float hinv = ldexpf(1.f, -(4 * H_S_EXP + sx_exp - 20 + a2_exp - 20));
+        const float sx = ldexpf(1.f, sx_exp);
+        constexpr float a1 = 1.f / 1048576.f, a3 = a1;  // 2^-20
+        const float fa2 = divi * ldexpf(1.f, a2_exp);    // F's normalisation and the operand scale
+        const int h_exp = -(4 * H_S_EXP + sx_exp - 20 + a2_exp - 20);
         {
             const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
             if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
@@ -724,7 +736,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
 #pragma unroll
                     for (int i = 0; i < 8; i++) v[i] = 0.f;
                 }
-                h_split8(small, H_SMALL_LO, kmaj16_off(r, 8 * kg), v);
+                H_SPLIT8(small, H_SMALL_LO, kmaj16_off(r, 8 * kg), v, 0);
             } else if (gi == 1) {
                 // A = D1 rows R (sum or difference rows) from 16 E and O columns of lane i
                 const int kc = k0 + 16 * colq;
@@ -738,8 +750,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                         const float x = (ev[i] + sg2 * ov[i]) * a1;
                         ev[i] = (fullc || kc + i < nn) ? x : 0.f;
                     }
-                    h_split8(big, big_lo, kmaj16_off(R2, 16 * colq), ev);
-                    h_split8(big, big_lo, kmaj16_off(R2, 16 * colq + 8), ev + 8);
+                    H_SPLIT8(big, big_lo, kmaj16_off(R2, 16 * colq), ev, 0);
+                    H_SPLIT8(big, big_lo, kmaj16_off(R2, 16 * colq + 8), ev, 8);
                 }
             } else if (gi == 2) {
                 // B = (D2 o F^T) rows R, 16 columns of R tile rset
@@ -751,11 +763,11 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
 #pragma unroll
                     for (int i = 0; i < 16; i++) {
                         const float ek = fminf(s_p1f[kc + i] + e2, radcut);
-                        const float x = v[i] * ek * divi * a2;
+                        const float x = v[i] * ek * fa2;
                         v[i] = (fullc || (kc + i < nn && rR < n2)) ? x : 0.f;
                     }
-                    h_split8(big, big_lo, kmaj16_off(rR, 16 * colq), v);
-                    h_split8(big, big_lo, kmaj16_off(rR, 16 * colq + 8), v + 8);
+                    H_SPLIT8(big, big_lo, kmaj16_off(rR, 16 * colq), v, 0);
+                    H_SPLIT8(big, big_lo, kmaj16_off(rR, 16 * colq + 8), v, 8);
                 }
             } else {
                 // A = D3 columns 2j + par (rows r1): warp sub takes j in [k0 + 8 sub, +8)
@@ -769,7 +781,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                     const float x = (par == 0 ? v16[2 * uu] : v16[2 * uu + 1]) * a3;
                     v[uu] = (fullc || col0 + 2 * uu + par < n2) ? x : 0.f;
                 }
-                h_split8(small, H_SMALL_LO, kmaj16_off(m, 8 * sub), v);
+                H_SPLIT8(small, H_SMALL_LO, kmaj16_off(m, 8 * sub), v, 0);
             }
             fence_async_smem();
             fence_before_sync();
@@ -791,21 +803,22 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
         fence_after_sync();
         if (!*fail) {
             const int64_t fo = p.foff[seg];
+            const float hinv = ldexpf(1.f, h_exp);
 #pragma unroll
-            for (int cc = 0; cc < 2; cc++) {
-                const int i0 = 32 * sub + 16 * cc;
-                float e[16], o[16];
-                tmem_ld16(lrow + 256u + (uint32_t)i0, e);
-                tmem_ld16(lrow + 384u + (uint32_t)i0, o);
-                int is[16], id[16];
+            for (int cc = 0; cc < 4; cc++) {
+                const int i0 = 32 * sub + 8 * cc;
+                float e[8], o[8];
+                tmem_ld8(lrow + 256u + (uint32_t)i0, e);
+                tmem_ld8(lrow + 384u + (uint32_t)i0, o);
+                int is[8], id[8];
 #pragma unroll
-                for (int uu = 0; uu < 16; uu++) {
+                for (int uu = 0; uu < 8; uu++) {
                     int i = i0 + uu;
                     is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
                     id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
                 }
 #pragma unroll
-                for (int uu = 0; uu < 16; uu++) {
+                for (int uu = 0; uu < 8; uu++) {
                     if (is[uu] >= 0) p.H[fo + is[uu]] = (e[uu] + o[uu]) * hinv;
                     if (id[uu] >= 0) p.H[fo + id[uu]] = (e[uu] - o[uu]) * hinv;
                 }
