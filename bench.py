@@ -46,6 +46,9 @@ WORKLOADS = {
     "j0_256x128x60": dict(case="j0_256x128x60", sweep=None),
     # J=0 at 512 R x 256 r x 120 angles
     "j0_512x256x120": dict(case="j0_512x256x120", sweep=None),
+    # three diabatic states, J=2 with Omega=0..2, 384 R x 192 r x 80 angles, started from the
+    # lowest J=1 bound state of the ground surface times a constant transition dipole of 1 a.u.
+    "e3_384x192x80_photo": dict(case="e3_384x192x80", sweep=None, photo=True),
 }
 DEFAULT_WORKLOAD = "jsweep0-40_256x128x60"
 
@@ -74,6 +77,9 @@ def case_runs(workload, rank):
     from madwave3_gb300.host import generator, setup
     w = WORKLOADS[workload]
     base = os.environ.get("MW3_CASES", os.path.join(tempfile.gettempdir(), "mw3_cases_r%d" % rank))
+    if w.get("photo"):
+        from madwave3_gb300 import workloads
+        return [workloads.photodissociation(base, w["case"])[0]]
     d = os.path.join(base, w["case"])
     if not os.path.exists(os.path.join(d, "pot", "cont.pot")):
         generator.write_case(d, **generator.CASES[w["case"]])

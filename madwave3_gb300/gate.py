@@ -41,19 +41,29 @@ def _vj_error(run, a, b):
 
 
 def run_gate(case, iterations, cases_dir=None, waves=None):
-    from . import Propagator
     from .host import generator, setup
 
     base = cases_dir or os.path.join(tempfile.gettempdir(), "mw3_gate_cases")
-    d = os.path.join(base, case)
-    if not os.path.exists(os.path.join(d, "pot", "cont.pot")):
-        generator.write_case(d, **generator.CASES[case])
-    run = setup.load(os.path.join(d, "input.dat"))
+    if case.endswith("_photo"):
+        from . import workloads
+        run, summary = workloads.photodissociation(base, case[: -len("_photo")])
+    else:
+        d = os.path.join(base, case)
+        if not os.path.exists(os.path.join(d, "pot", "cont.pot")):
+            generator.write_case(d, **generator.CASES[case])
+        run = setup.load(os.path.join(d, "input.dat"))
+    return run_gate_run(run, iterations, case)
+
+
+def run_gate_run(run, iterations, case=""):
+    """The gate on one prepared wave (its packet in run.psi0)."""
+    from . import Propagator
+
     out = {"case": case, "iterations": iterations, "stored_points": int(run.ntot)}
     res = {}
     for prec in ("fp64", "mixed"):
         p = Propagator(run, prec)
-        p.start()
+        p.start([run.psi0])
         p.sync()
         t = time.time()
         p.run(iterations - 1)

@@ -102,6 +102,7 @@ DEFAULT = dict(
     ntimes=500, nloop=3, kminelastic=0,
     shifts_ev=(0.0, 0.8, 1.5), coupling_ev=0.05, coupling_width_bohr=0.5,
     absorb_strength=10.0,
+    iphoto=0,
 )
 
 
@@ -130,7 +131,7 @@ def make_inputs(**over):
             nvini=p["nvini"], nvmax=p["nvmax"], nvref=p["nvref"], jref=p["jref"],
             iomref=p["iomref"], ielecref=p["ielecref"]),
         "inputprod": dict(iprod=0),
-        "inputprocess": dict(iphoto=0),
+        "inputprocess": dict(iphoto=p["iphoto"]),
         "inputpotmass": dict(system="H+DH LEPS", xm0=xm0, xm1=xm1, xm2=xm2,
                              vcutmaxev=p["vcutmaxev"], radcutmaxev=p["radcutmaxev"],
                              rotcutmaxev=p["rotcutmaxev"]),
