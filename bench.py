@@ -17,6 +17,7 @@ are independent, so each rank propagates its own replica of the workload
 ("replicas only": the path has no exchange step on one node).
 """
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -97,49 +98,70 @@ def sample_waves(runs, n=5):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms from before
+    the warm-up; the summary keeps the samples whose timestamps fall inside the
+    timed region (marked by start() and end(), 100 ms of slack each side)."""
 
     def __init__(self, gpu_index):
         self.path = os.path.join(tempfile.gettempdir(), "mw3_clocks_%d_%d.csv" % (os.getpid(), gpu_index))
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        self.t0 = self.t1 = None
         try:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 
+    def wait_first(self, timeout=5.0):
+        """Until the first sample is written (nvidia-smi takes a moment to start)."""
+        t = time.time()
+        while self.p is not None and time.time() - t < timeout:
+            if os.path.getsize(self.path) > 0:
+                return
+            time.sleep(0.05)
+
+    def start(self):
+        self.t0 = datetime.datetime.now()
+
+    def end(self):
+        self.t1 = datetime.datetime.now()
+
     def stop(self):
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
         self.p.terminate()
         try:
             self.p.wait(timeout=5)
         except Exception:
             self.p.kill()
         self.f.close()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         with open(self.path) as f:
             for line in f:
                 parts = [x.strip() for x in line.split(",")]
-                if len(parts) < 9:
+                if len(parts) < 10:
                     continue
                 try:
-                    sm.append(float(parts[1]))
-                    smax.append(float(parts[2]))
+                    ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                    rows.append((ts, float(parts[2]), float(parts[3]), parts[6:10]))
                 except ValueError:
                     continue
-                for n, v in zip(names, parts[5:9]):
-                    if v.lower() == "active":
-                        reasons.add(n)
         os.unlink(self.path)
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": float(max(smax)) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        slack = datetime.timedelta(seconds=0.1)
+        inside = [r for r in rows if self.t0 is not None and self.t1 is not None
+                  and self.t0 - slack <= r[0] <= self.t1 + slack]
+        use = inside or rows
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in use for n, v in zip(names, r[3]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[1] for r in use])) if use else None,
+                "sm_max_mhz": float(max(r[2] for r in use)) if use else None,
+                "reasons": reasons, "samples": len(use),
+                "window": "timed region" if inside else "whole run (no sample inside the timed region)"}
 
 
 def stage_model(runs, prop, stages=None):
@@ -224,6 +246,8 @@ def run_gpu(args, rank, world, local):
     working_set = nsto * 8 * 4
     flush = working_set < 2 * L2_BYTES
     nwarm = warmup_count(1, args.warmup, args.steps) if not flush else args.warmup
+    clocks = ClockSampler(local)
+    clocks.wait_first()
     prop.run(nwarm)
     prop.sync()
     it0 = 1 + nwarm
@@ -233,7 +257,7 @@ def run_gpu(args, rank, world, local):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = prop.kernel_launches()
-    clocks = ClockSampler(local)
+    clocks.start()
     if flush:
         # a small workload: L2 flushed before every step, each step timed alone
         evs = []
@@ -260,6 +284,7 @@ def run_gpu(args, rank, world, local):
         prop.sync()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+    clocks.end()
     clk = clocks.stop()
     launches = prop.kernel_launches() - launches0
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
@@ -317,7 +342,9 @@ def run_gpu(args, rank, world, local):
         roof = {"bound": "tensor", "achieved": achieved, "peak": tf, "unit": "TFLOP/s",
                 "frac": achieved / tf, "traffic": traffic, "kernel": dom, "peak_source": src,
                 "work": "algorithmic DST flops (4 nopr1 npun2^2 + 4 nopr1^2 npun2 per slab); the kernel issues "
-                        "3 TF32 products per flop (3xTF32), and the peak is the dense bf16 one"}
+                        + ("3 FP16 products per flop (split FP16, kind::f16 at the bf16 rate)" if kin.get("dst_f16")
+                           else "3 TF32 products per flop (3xTF32, kind::tf32 at half the bf16 rate)")
+                        + ", and the peak is the dense bf16 one"}
     else:
         achieved = work / t_launch / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",

@@ -206,12 +206,14 @@ int mw3_kernel_launches(mw3_ctx *ctx, int64_t *count);
 /* Which kernels the context runs, valid once its device tables exist (after
  * mw3_start, mw3_upload_state or mw3_hphi): MW3_PATH_TC_DST when the radial
  * DSTs run on the tensor cores (with MW3_PATH_TC_DST_FUSED when as one fused
- * kernel), MW3_PATH_TC_ANG when the angular terms run as the factorised
- * tensor-core contraction (all mixed precision only).  No
+ * kernel, and MW3_PATH_DST_F16 when that kernel takes split-FP16 products
+ * rather than 3xTF32), MW3_PATH_TC_ANG when the angular terms run as the
+ * factorised tensor-core contraction (all mixed precision only).  No
  * reference counterpart: the reference has a single code path. */
 #define MW3_PATH_TC_DST 1
 #define MW3_PATH_TC_ANG 2
 #define MW3_PATH_TC_DST_FUSED 4   /* the whole radial DST chain in one kernel per (block, angle) */
+#define MW3_PATH_DST_F16 8        /* the fused chain as split-FP16 products (MW3_DST_TF32=1 selects 3xTF32) */
 int mw3_path_flags(mw3_ctx *ctx, int32_t *flags);
 
 /* The CUDA stream (cudaStream_t) all device work of the context runs on, for

@@ -284,7 +284,6 @@ struct Ctx {
     void *d_dst_planes16 = nullptr, *d_dst_s2fold16 = nullptr;
     int64_t *d_dst_s1off16 = nullptr;
     unsigned *d_xmax = nullptr;      // [G na], written by the scatter and update kernels
-    int dst_fexp = 0;                // ceil(log2) of the largest F = min(p2, radcut) / (4 (nn+1)(n2+1))
     int64_t *d_dst_s1off = nullptr;  // [W][na] float offset of the slab's S1
     float *d_p2r1f = nullptr, *d_p2r2f = nullptr;      // FP32 copies of the momenta tables
     alignas(64) unsigned char dst_xmap[128] = {};       // TMA map of the rectangles (CUtensorMap)

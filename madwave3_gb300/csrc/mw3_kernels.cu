@@ -68,10 +68,19 @@ __global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict
 // row DST: C[r][:] = A[r][:] x S2 for the rows r = (g, a, ir1) with ir1 < nopr1
 // register-tiled GEMM; epilogue either stores C or gathers it into H
 // ---------------------------------------------------------------------------
+// The DST-I matrices are symmetric and S[n-1-i][k] = (-1)^k S[i][k], so with
+// E_i and O_i the sums over even and odd k, y_i = E_i + O_i and
+// y_{n-1-i} = E_i - O_i: both transforms compute only the first ceil(n/2)
+// outputs, from two accumulators, and mirror them (the first radix-2 level of
+// an FFT of the odd extension; the rest stays dense because n + 1 is prime or
+// has large factors for the grid lengths in use).  Half the multiply-adds of
+// the dense product; the sums run in the same k order within each parity.
 template <typename T> struct RowCfg;
 template <> struct RowCfg<double> { enum { BM = 64, BN = 64, BK = 16, TM = 4, TN = 4 }; };
-template <> struct RowCfg<float> { enum { BM = 128, BN = 128, BK = 8, TM = 8, TN = 8 }; };
+template <> struct RowCfg<float> { enum { BM = 128, BN = 64, BK = 16, TM = 8, TN = 4 }; };
 
+// C[r][i] = sum_k A[r][k] S[k][i] over rows r of every slab (DST along R); grid.y
+// covers the first ceil(n2/2) output columns, each CTA writing both mirrors
 template <typename T, bool GATHER>
 __global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict__ A, const T *__restrict__ S,
                                                   T *__restrict__ C, double *__restrict__ H,
@@ -81,9 +90,10 @@ __global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict
     constexpr int TM = RowCfg<T>::TM, TN = RowCfg<T>::TN;
     constexpr int TX = BN / TN, TY = BM / TM;
     static_assert(TX * TY == 256, "256 threads");
+    static_assert(BK % 2 == 0, "chunks start at even k");
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN];
-    const int n1 = d.n1, n2 = d.n2, na = d.na;
+    const int n1 = d.n1, n2 = d.n2, na = d.na, h = (n2 + 1) / 2;
     int64_t rbase = row0 + (int64_t)blockIdx.x * BM;     // row tiles on x: no 65535 limit
     int cbase = blockIdx.y * BN;
     int tid = threadIdx.x;
@@ -103,11 +113,11 @@ __global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict
     __syncthreads();
     if (!any) return;
     int tx = tid % TX, ty = tid / TX;
-    T acc[TM][TN];
+    T ae[TM][TN], ao[TM][TN];
 #pragma unroll
     for (int m = 0; m < TM; m++)
 #pragma unroll
-        for (int n = 0; n < TN; n++) acc[m][n] = (T)0;
+        for (int n = 0; n < TN; n++) ae[m][n] = ao[m][n] = (T)0;
     for (int k0 = 0; k0 < n2; k0 += BK) {
         for (int e = tid; e < BM * BK; e += 256) {
             int i = e / BK, kk = e % BK;
@@ -119,21 +129,30 @@ __global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict
         for (int e = tid; e < BK * BN; e += 256) {
             int kk = e / BN, j = e % BN;
             T v = 0;
-            if (k0 + kk < n2 && cbase + j < n2) v = S[(size_t)(k0 + kk) * n2 + cbase + j];
+            if (k0 + kk < n2 && cbase + j < h) v = S[(size_t)(k0 + kk) * n2 + cbase + j];
             Bs[kk][j] = v;
         }
         __syncthreads();
 #pragma unroll
-        for (int kk = 0; kk < BK; kk++) {
-            T av[TM], bv[TN];
+        for (int kk = 0; kk < BK; kk += 2) {
+            T av[TM], bv[TN], aw[TM], bw[TN];
 #pragma unroll
-            for (int m = 0; m < TM; m++) av[m] = As[kk][ty + m * TY];
+            for (int m = 0; m < TM; m++) {
+                av[m] = As[kk][ty + m * TY];
+                aw[m] = As[kk + 1][ty + m * TY];
+            }
 #pragma unroll
-            for (int n = 0; n < TN; n++) bv[n] = Bs[kk][tx + n * TX];
+            for (int n = 0; n < TN; n++) {
+                bv[n] = Bs[kk][tx + n * TX];
+                bw[n] = Bs[kk + 1][tx + n * TX];
+            }
 #pragma unroll
             for (int m = 0; m < TM; m++)
 #pragma unroll
-                for (int n = 0; n < TN; n++) acc[m][n] += av[m] * bv[n];
+                for (int n = 0; n < TN; n++) {
+                    ae[m][n] += av[m] * bv[n];
+                    ao[m][n] += aw[m] * bw[n];
+                }
         }
         __syncthreads();
     }
@@ -148,12 +167,17 @@ __global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict
 #pragma unroll
         for (int n = 0; n < TN; n++) {
             int col = cbase + tx + n * TX;
-            if (col >= n2) continue;
+            if (col >= h) continue;
+            const int mir = n2 - 1 - col;
+            const T y0 = ae[m][n] + ao[m][n], y1 = ae[m][n] - ao[m][n];
             if (GATHER) {
-                int idx = d.map[((size_t)a * n1 + ir1) * n2 + col];
-                if (idx >= 0) H[d.foff[ga] + idx] = (double)acc[m][n];
+                const int *mp = d.map + ((size_t)a * n1 + ir1) * n2;
+                int idx = mp[col];
+                if (idx >= 0) H[d.foff[ga] + idx] = (double)y0;
+                if (mir != col && (idx = mp[mir]) >= 0) H[d.foff[ga] + idx] = (double)y1;
             } else {
-                C[r * n2 + col] = acc[m][n];
+                C[r * n2 + col] = y0;
+                if (mir != col) C[r * n2 + mir] = y1;
             }
         }
     }
@@ -162,10 +186,11 @@ __global__ void __launch_bounds__(256) k_dst_rows(DevGrid d, const T *__restrict
 // ---------------------------------------------------------------------------
 // column DSTs: for one (block, angle) and a tile of W columns,
 // Y[0:nn][cols] <- S1 ( E o (S1 Y[0:nn][cols]) ),  E = min(p2r1+p2r2, radcut)/(4(nn+1)(n2+1))
+// each thread sums rows i < ceil(nn/2) by parity of k and writes rows i and nn-1-i
 // ---------------------------------------------------------------------------
 constexpr int COL_W = 32;
 constexpr int COL_KC = 32;
-constexpr int COL_RMAX = 32;   // rows per thread (n1 <= 256)
+constexpr int COL_RMAX = 16;   // folded rows per thread (n1 <= 256)
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, const T *__restrict__ S1all,
@@ -180,6 +205,7 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
     int g = seg / d.na, a = seg % d.na;
     int w = d.blk_wave[g];
     int nn = nopr1[w * d.na + a];
+    const int hn = (nn + 1) / 2;
     const T *S1 = S1all + s1off[w * d.na + a];
     int n1 = d.n1, n2 = d.n2;
     int c0 = blockIdx.y * COL_W;
@@ -193,24 +219,28 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
     const double *p2 = p2r2 + ((size_t)w * d.na + a) * n2;
     const T divi = (T)(1.0 / (4.0 * (double)(nn + 1) * (double)(n2 + 1)));
     const T rcut = (T)radcut;
-    T acc[COL_RMAX];
+    T ae[COL_RMAX], ao[COL_RMAX];
     for (int pass = 0; pass < 2; pass++) {
 #pragma unroll
-        for (int r = 0; r < COL_RMAX; r++) acc[r] = (T)0;
+        for (int r = 0; r < COL_RMAX; r++) ae[r] = ao[r] = (T)0;
         for (int kc = 0; kc < nn; kc += COL_KC) {
             __syncthreads();
-            for (int e = threadIdx.x; e < nn * COL_KC; e += 256) {
+            for (int e = threadIdx.x; e < hn * COL_KC; e += 256) {
                 int i = e / COL_KC, kk = e % COL_KC;
                 Sc[i * COL_KC + kk] = (kc + kk < nn) ? S1[(size_t)i * nn + kc + kk] : (T)0;
             }
             __syncthreads();
             int kmax = min(COL_KC, nn - kc);
-            for (int kk = 0; kk < kmax; kk++) {
-                T y = Yt[(kc + kk) * COL_W + tx];
+            for (int kk = 0; kk < kmax; kk += 2) {
+                T y0 = Yt[(kc + kk) * COL_W + tx];
+                T y1 = kk + 1 < kmax ? Yt[(kc + kk + 1) * COL_W + tx] : (T)0;
 #pragma unroll
                 for (int r = 0; r < COL_RMAX; r++) {
                     int i = ty + 8 * r;
-                    if (i < nn) acc[r] += Sc[i * COL_KC + kk] * y;
+                    if (i < hn) {
+                        ae[r] += Sc[i * COL_KC + kk] * y0;
+                        ao[r] += Sc[i * COL_KC + kk + 1] * y1;
+                    }
                 }
             }
         }
@@ -220,12 +250,20 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
 #pragma unroll
             for (int r = 0; r < COL_RMAX; r++) {
                 int i = ty + 8 * r;
-                if (i < nn && col < n2) {
+                if (i >= hn) continue;
+                const int im = nn - 1 - i;
+                if (col < n2) {
                     T ek = (T)p1[i] + (T)p2[col];
                     if (ek > rcut) ek = rcut;
-                    Yt[i * COL_W + tx] = acc[r] * ek * divi;
-                } else if (i < nn) {
+                    Yt[i * COL_W + tx] = (ae[r] + ao[r]) * ek * divi;
+                    if (im != i) {
+                        T em = (T)p1[im] + (T)p2[col];
+                        if (em > rcut) em = rcut;
+                        Yt[im * COL_W + tx] = (ae[r] - ao[r]) * em * divi;
+                    }
+                } else {
                     Yt[i * COL_W + tx] = (T)0;
+                    Yt[im * COL_W + tx] = (T)0;
                 }
             }
         }
@@ -235,7 +273,10 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
 #pragma unroll
         for (int r = 0; r < COL_RMAX; r++) {
             int i = ty + 8 * r;
-            if (i < nn) base[(size_t)i * n2 + col] = acc[r];
+            if (i >= hn) continue;
+            const int im = nn - 1 - i;
+            base[(size_t)i * n2 + col] = ae[r] + ao[r];
+            if (im != i) base[(size_t)im * n2 + col] = ae[r] - ao[r];
         }
 }
 
@@ -1276,8 +1317,12 @@ void launch_scatter(Ctx &c, const double *psi, float *psi32, int g_begin, int g_
 {
     int nseg = (g_end - g_begin) * c.na;
     if (nseg <= 0) return;
+    unsigned *xmax = sizeof(T) == 4 ? c.d_xmax : nullptr;
+    // the scattered rectangle replaces whatever the update left: its slabs' largest
+    // |X| start from zero, so a restart scales X exactly as the uninterrupted run
+    if (xmax) cudaMemsetAsync(xmax + (size_t)g_begin * c.na, 0, (size_t)nseg * sizeof(unsigned), c.stream);
     k_scatter<T><<<dim3(nseg, c.nchunk), 256, 0, c.stream>>>(devgrid(c), (T *)c.d_X, psi, psi32, g_begin * c.na,
-                                                              sizeof(T) == 4 ? c.d_xmax : nullptr);
+                                                              xmax);
     LAUNCH_CHECK(c);
 }
 
@@ -1301,7 +1346,7 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g_begin * c.na * c.n1;
     int64_t nrows = (int64_t)ng * c.na * c.n1;
-    dim3 gr((unsigned)((nrows + BM - 1) / BM), (c.n2 + BN - 1) / BN);
+    dim3 gr((unsigned)((nrows + BM - 1) / BM), ((c.n2 + 1) / 2 + BN - 1) / BN);   // folded: ceil(n2/2) columns
     if (sizeof(T) == 4 && c.use_tc_dst2d) {
         // mixed path: the whole DST chain of each slab in one tensor-core kernel, H in FP32
         stage_mark(c, 0);
@@ -1861,7 +1906,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     LAUNCH_CHECK(c);
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g0 * na * n1, nrows = (int64_t)ng * na * n1;
-    dim3 gr((unsigned)((nrows + BM - 1) / BM), (n2 + BN - 1) / BN);
+    dim3 gr((unsigned)((nrows + BM - 1) / BM), ((n2 + 1) / 2 + BN - 1) / BN);
     k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, X, (const T *)c.d_S2, Y, nullptr, c.d_nopr1, row0, nrows);
     LAUNCH_CHECK(c);
     dim3 gc(ng * na, (n2 + COL_W - 1) / COL_W);

@@ -465,15 +465,21 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
 // FP16 keeps 22 bits like the TF32 split, and Ahi Bhi + Ahi Blo + Alo Bhi has the
 // error of the 3xTF32 form; kind::f16 runs at twice the kind::tf32 rate.  FP16's
 // exponent range is narrow, so every operand is scaled by a power of two that
-// brings its bound to 2^12..2^13 (an element's absolute error is then at most
-// 2^-25, the spacing of the FP16 subnormals, against an operand bound of 2^12:
-// 37 bits of range, of which the split needs 22):
+// puts its largest element in [2^11, 2^12): the lo part of an element within
+// 2^-11 of that maximum then stays a normal FP16 number, and the absolute error
+// of any element is at most 2^-25 (half the spacing of the FP16 subnormals)
+// against a maximum of 2^11, so the split keeps 22 bits of every element that
+// matters to the product:
 //   DST matrices    x 2^12 (entries 2 sin(.) are bounded by 2; host planes);
 //   Xs              x 2^(12 - e), xmax < 2^e the slab's largest |X|, which the
 //                   kernels that write X leave in xmax[slab] (atomicMax of the
 //                   bits; this kernel reads it and clears it);
-//   D1, D3          x 2^-20 (|D| <= 2^12 * 2^13 * 2 * 128 terms);
-//   D2 o F          x 2^(-20 - ceil log2 max F);
+//   D1, D2 o F, D3  x 2^(12 - e) with e from the slab's largest |element| of that
+//                   operand, which the fill warps read out of tensor memory when
+//                   the product before it completes and reduce across the CTA
+//                   (a bound fixed in advance left the operand of a smooth packet
+//                   up to 2^16 below it, where the lo parts fall into FP16
+//                   subnormals: 1e-4 relative error in H psi);
 // and H is D4 times the inverse of the product of the scales, again a power of
 // two.  A K chunk is 32 FP16 values, the same 64 bytes per row as the 16 TF32
 // values of the TF32 form, so operands and DST-matrix chunks keep their byte
@@ -573,7 +579,6 @@ struct Dst2hArgs {
     const __half *s2fold;         // [parity][H_NKH][hi, lo] x 2^12
     const __half *s1planes;       // S1 of each length, H_NKH chunks of 32 columns, x 2^12
     unsigned *xmax;               // [G na]: bits of the slab's largest |X|, cleared here
-    int fexp;                     // ceil(log2(max F)) over the context
 };
 
 __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, const __grid_constant__ CUtensorMap xmap)
@@ -585,6 +590,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
     uint64_t *xfull = empty + H_NS;
     uint32_t *slot = reinterpret_cast<uint32_t *>(xfull + H_NS);
     float *s_p1f = reinterpret_cast<float *>(sm + H_BYTES + 128);
+    unsigned *s_red = reinterpret_cast<unsigned *>(sm + H_BYTES + 640);    // largest |D1|, |D2 o F|, |D3|
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const Dst2Args &p = P.b;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -602,6 +608,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
             mbar_init(&xfull[i], 1);
         }
         *fail = 0;
+        s_red[0] = s_red[1] = s_red[2] = s_red[3] = 0u;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before_sync();
@@ -692,11 +699,10 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
         const float xm = __uint_as_float(P.xmax[seg]);
         int ex = 0;
         if (xm > 0.f) frexpf(xm, &ex);                  // xm < 2^ex
-        const int sx_exp = min(100, max(-100, 12 - ex)), a2_exp = -20 - P.fexp;
+        const int sx_exp = min(100, max(-100, 12 - ex));
         const float sx = ldexpf(1.f, sx_exp);
-        constexpr float a1 = 1.f / 1048576.f, a3 = a1;  // 2^-20
-        const float fa2 = divi * ldexpf(1.f, a2_exp);    // F's normalisation and the operand scale
-        const int h_exp = -(4 * H_S_EXP + sx_exp - 20 + a2_exp - 20);
+        int s_exp = sx_exp;                             // sum of the operand scales' exponents so far
+        float sc = 1.f;                                 // the scale of the current product's operand
         {
             const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
             if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
@@ -715,6 +721,51 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
             if (jc == 0 && par == 0 && gi > 0) {
                 d2_wait(&empty[pt], pph, fail);
                 fence_after_sync();
+                // the previous product is complete: the largest |element| this thread will
+                // write, over the chunks below (loads warp-uniform, values masked by lane)
+                float mx = 0.f;
+                if (gi == 1) {
+                    for (int j = 0; j < nkr; j++) {
+                        const int kc = j * H_KC + 16 * colq;
+                        float ev[16], ov[16];
+                        tmem_ld16(lrow + (uint32_t)kc, ev);
+                        tmem_ld16(lrow + 128u + (uint32_t)kc, ov);
+#pragma unroll
+                        for (int i = 0; i < 16; i++)
+                            if (on2 && kc + i < nn) mx = fmaxf(mx, fabsf(ev[i] + sg2 * ov[i]));
+                    }
+                } else if (gi == 2) {
+                    if (rset < NT)
+                        for (int j = 0; j < nkr; j++) {
+                            const int kc = j * H_KC + 16 * colq;
+                            float v[16];
+                            tmem_ld16(lrow + 256u + 128u * rset + (uint32_t)kc, v);
+#pragma unroll
+                            for (int i = 0; i < 16; i++) {
+                                const float ek = fminf(s_p1f[kc + i] + e2, radcut);
+                                if (kc + i < nn && rR < n2) mx = fmaxf(mx, fabsf(v[i] * ek * divi));
+                            }
+                        }
+                } else {
+                    for (int j = 0; j < nkh; j++) {
+                        const int col0 = 2 * j * H_KC + 16 * sub;
+                        float v16[16];
+                        tmem_ld16(lrow + (uint32_t)col0, v16);
+#pragma unroll
+                        for (int i = 0; i < 16; i++)
+                            if (col0 + i < n2) mx = fmaxf(mx, fabsf(v16[i]));
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                if (lane == 0) atomicMax(&s_red[gi], __float_as_uint(mx));
+                asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
+                const float gm = __uint_as_float(s_red[gi]);
+                int e = 0;
+                if (gm > 0.f) frexpf(gm, &e);           // gm < 2^e
+                const int se = min(100, max(-100, 12 - e));
+                sc = ldexpf(1.f, se);
+                s_exp += se;
             }
             if (t >= H_NS) d2_wait(&empty[s], ph ^ 1, fail);
             const int k0 = jc * H_KC;
@@ -747,7 +798,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                     const bool fullc = kc + 16 <= nn;
 #pragma unroll
                     for (int i = 0; i < 16; i++) {
-                        const float x = (ev[i] + sg2 * ov[i]) * a1;
+                        const float x = (ev[i] + sg2 * ov[i]) * sc;
                         ev[i] = (fullc || kc + i < nn) ? x : 0.f;
                     }
                     H_SPLIT8(big, big_lo, kmaj16_off(R2, 16 * colq), ev, 0);
@@ -763,7 +814,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
 #pragma unroll
                     for (int i = 0; i < 16; i++) {
                         const float ek = fminf(s_p1f[kc + i] + e2, radcut);
-                        const float x = v[i] * ek * fa2;
+                        const float x = v[i] * ek * divi * sc;
                         v[i] = (fullc || (kc + i < nn && rR < n2)) ? x : 0.f;
                     }
                     H_SPLIT8(big, big_lo, kmaj16_off(rR, 16 * colq), v, 0);
@@ -778,7 +829,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                 float v[8];
 #pragma unroll
                 for (int uu = 0; uu < 8; uu++) {
-                    const float x = (par == 0 ? v16[2 * uu] : v16[2 * uu + 1]) * a3;
+                    const float x = (par == 0 ? v16[2 * uu] : v16[2 * uu + 1]) * sc;
                     v[uu] = (fullc || col0 + 2 * uu + par < n2) ? x : 0.f;
                 }
                 H_SPLIT8(small, H_SMALL_LO, kmaj16_off(m, 8 * sub), v, 0);
@@ -803,7 +854,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
         fence_after_sync();
         if (!*fail) {
             const int64_t fo = p.foff[seg];
-            const float hinv = ldexpf(1.f, h_exp);
+            const float hinv = ldexpf(1.f, -(4 * H_S_EXP + s_exp));
 #pragma unroll
             for (int cc = 0; cc < 4; cc++) {
                 const int i0 = 32 * sub + 8 * cc;
@@ -989,12 +1040,6 @@ int build_tc_dst2d(Ctx &c)
     int rc;
     const char *tf = std::getenv("MW3_DST_TF32");
     c.dst_f16 = !(tf && tf[0] == '1');
-    {
-        // F <= radcut / (4 (nn+1)(n2+1)) with nn >= 1: a bound for every slab
-        int e = 0;
-        std::frexp(c.grid.radcutmax / (8.0 * (c.n2 + 1)), &e);
-        c.dst_fexp = e;
-    }
     __half *p16 = nullptr, *f16 = nullptr;
     if ((rc = upload_vec(c, &p16, planes16))) return rc;
     if ((rc = upload_vec(c, &f16, fold16))) return rc;
@@ -1066,7 +1111,6 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
         P.s1planes = static_cast<const __half *>(c.d_dst_planes16);
         P.b.s1off = c.d_dst_s1off16;
         P.xmax = c.d_xmax;
-        P.fexp = c.dst_fexp;
         k_tc_dst2d_h<<<nseg, D2_WARPS * 32, smem, c.stream>>>(P, xmap);
     } else {
         k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p, xmap);

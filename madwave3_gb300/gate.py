@@ -14,7 +14,9 @@ iterations; P(E) is the total reaction probability of totalflux
 energy where it occurs, max P, the iterations and both paths' wall times, and
 the error of the state-resolved probabilities: P_vj(E) of every reactant
 channel (v, j), summed over the Omega blocks, as printprob forms them from
-zS2 (SRC/main_madwave3.f:640-652).
+zS2 (SRC/main_madwave3.f:640-652), over the energies where the packet's
+amplitude |a(E)|^2 is at least 1e-3 of its largest value (S2factor divides by
+it, so outside that window both paths' P_vj are rounding over a tiny number).
 """
 import argparse
 import json
@@ -33,11 +35,31 @@ def state_probabilities(run, prop, wave=0):
     return s2.sum(axis=0)
 
 
-def _vj_error(run, a, b):
+# P_vj(E) carries S2factor's 1/|a(E)|^2 (Smatini_col): where the packet has almost
+# no amplitude both paths divide their rounding by a tiny number, so the
+# state-resolved comparison covers the energies where |a(E)|^2 is at least this
+# fraction of its largest value
+VJ_AMPLITUDE_FRACTION = 1e-3
+
+
+def energy_window(apaqini):
+    a = np.asarray(apaqini, np.float64)
+    return a >= VJ_AMPLITUDE_FRACTION * a.max() if a.size and a.max() > 0 else np.ones(a.shape, bool)
+
+
+def _vj_error(run, a, b, window=None):
     d = np.abs(a - b)
+    pa = np.abs(a)
+    if window is not None:
+        d = d * window
+        pa = pa * window
     k = np.unravel_index(int(np.argmax(d)), d.shape)
-    return {"max_abs_dP_vj": float(d.max()), "at_j": int(k[0] + run.inp.jini), "at_v": int(k[1] + run.inp.nvini),
-            "max_P_vj": float(np.abs(a).max())}
+    e = np.linspace(run.inp.ekinmin_ev, run.inp.ekinmax_ev, run.inp.netot)
+    out = {"max_abs_dP_vj": float(d.max()), "at_j": int(k[0] + run.inp.jini), "at_v": int(k[1] + run.inp.nvini),
+           "at_energy_ev_vj": float(e[k[2]]), "max_P_vj": float(pa.max())}
+    if window is not None:
+        out["vj_window_ev"] = [float(e[window].min()), float(e[window].max())] if window.any() else None
+    return out
 
 
 def run_gate(case, iterations, cases_dir=None, waves=None):
@@ -72,8 +94,9 @@ def run_gate_run(run, iterations, case=""):
         res[prec] = p.totalflux()[0]
         res[prec + "_norm"] = p.norms()[-1]
         res[prec + "_vj"] = state_probabilities(run, p)
+        res["window"] = energy_window(p.tables()["apaqini"])
         p.close()
-    out.update(_vj_error(run, res["fp64_vj"], res["mixed_vj"]))
+    out.update(_vj_error(run, res["fp64_vj"], res["mixed_vj"], res["window"]))
     a, b = res["fp64"], res["mixed"]
     e = np.linspace(run.inp.ekinmin_ev, run.inp.ekinmax_ev, run.inp.netot)
     k = int(np.argmax(np.abs(a - b)))
@@ -106,12 +129,13 @@ def run_sweep_gate(case, js, iterations, cases_dir=None):
         out["seconds_" + prec] = time.time() - t
         res[prec] = [p.totalflux(w)[0] for w in range(len(runs))]
         res[prec + "_vj"] = [state_probabilities(runs[w], p, w) for w in range(len(runs))]
+        res["window"] = [energy_window(p.tables(w)["apaqini"]) for w in range(len(runs))]
         p.close()
     per = []
     for w, J in enumerate(js):
         a, b = res["fp64"][w], res["mixed"][w]
         row = {"J": J, "max_abs_dP": float(np.abs(a - b).max()), "max_P": float(np.abs(a).max())}
-        row.update(_vj_error(runs[w], res["fp64_vj"][w], res["mixed_vj"][w]))
+        row.update(_vj_error(runs[w], res["fp64_vj"][w], res["mixed_vj"][w], res["window"][w]))
         per.append(row)
     out["per_J"] = per
     out["max_abs_dP"] = max(x["max_abs_dP"] for x in per)

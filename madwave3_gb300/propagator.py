@@ -437,10 +437,12 @@ class Propagator:
 
     def path(self):
         """Kernels in use (after start): tensor-core radial DSTs, fused into one
-        kernel per slab or not, and the tensor-core angular contraction."""
+        kernel per slab or not (as split-FP16 or 3xTF32 products), and the
+        tensor-core angular contraction."""
         f = ct.c_int32()
         self._check(self.L.mw3_path_flags(self.h, ct.byref(f)), "mw3_path_flags")
-        return {"tc_dst": bool(f.value & 1), "tc_dst_fused": bool(f.value & 4), "tc_angular": bool(f.value & 2)}
+        return {"tc_dst": bool(f.value & 1), "tc_dst_fused": bool(f.value & 4), "tc_angular": bool(f.value & 2),
+                "dst_f16": bool(f.value & 8)}
 
     def stream(self):
         """cudaStream_t of the context, as an integer handle."""

@@ -73,7 +73,8 @@ def _mixed_vs_fp64(runs, waves):
         psi = rng.uniform(-1, 1, runs[w].ntot)
         assert rel(pmx.hphi(psi, w), p64.hphi(psi, w)) < 5e-6
         assert rel(pmx.hphi(runs[w].psi0, w), p64.hphi(runs[w].psi0, w)) < 5e-6
-    assert pmx.path() == {"tc_dst": True, "tc_dst_fused": True, "tc_angular": True}
+    path = pmx.path()
+    assert path["tc_dst"] and path["tc_dst_fused"] and path["tc_angular"], path
     pmx.close()
     p64.close()
 
