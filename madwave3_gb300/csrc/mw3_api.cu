@@ -213,6 +213,34 @@ int build_device(Ctx &c)
                 for (int i2 = 0; i2 < n2; i2++)
                     mapT[((size_t)a * n2 + i2) * n1 + i1] = map[((size_t)a * n1 + i1) * n2 + i2];
         TRY(dupload(c, &c.d_mapT, mapT));
+        // each (angle, R) row's stored points by r1 word w < 4 (r1 < 128, the fused DST's
+        // range): the bits of the stored r1 and the index of the row's first point at or
+        // after r1 = 32 w, so a point's index is that plus the bits below it; an angle
+        // qualifies when every row's indices run consecutively in r1 order (points
+        // stored R outer, r1 inner)
+        std::vector<int> rows((size_t)na * n2 * 4 * 2, 0), rows_ok(na, 1);
+        for (int a = 0; a < na; a++)
+            for (int i2 = 0; i2 < n2; i2++) {
+                int base = -1, k = 0;
+                for (int i1 = 0; i1 < n1; i1++) {
+                    const int idx = map[((size_t)a * n1 + i1) * n2 + i2];
+                    if (idx < 0) continue;
+                    if (base < 0) base = idx;
+                    if (idx != base + k) rows_ok[a] = 0;
+                    k++;
+                }
+                int before = base < 0 ? 0 : base;
+                for (int w = 0; w < 4; w++) {
+                    unsigned bits = 0u;
+                    for (int b = 0; b < 32 && 32 * w + b < n1; b++)
+                        if (map[((size_t)a * n1 + 32 * w + b) * n2 + i2] >= 0) bits |= 1u << b;
+                    rows[(((size_t)a * n2 + i2) * 4 + w) * 2] = (int)bits;
+                    rows[(((size_t)a * n2 + i2) * 4 + w) * 2 + 1] = before;
+                    before += __builtin_popcount(bits);
+                }
+            }
+        TRY(dupload(c, &c.d_rows, rows));
+        TRY(dupload(c, &c.d_rows_ok, rows_ok));
     }
     // ---- layout of the wave set ----
     int G = 0;

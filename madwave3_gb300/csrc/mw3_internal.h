@@ -162,6 +162,8 @@ struct Ctx {
     double *d_vvv = nullptr;
     int *d_map = nullptr;            // [na][n1][n2] local point index, -1 = not stored
     int *d_mapT = nullptr;           // [na][n2][n1] the same, r1 fastest (stored points are r1-major runs)
+    int *d_rows = nullptr;           // [na][n2][4][2]: stored-r1 bits of word w, index of the first point in it
+    int *d_rows_ok = nullptr;        // [na]: 1 when every R row's indices run consecutively in r1
     // block tables
     int *d_blk_wave = nullptr, *d_blk_elec = nullptr, *d_blk_om = nullptr;
     int64_t *d_foff = nullptr;       // [G][na] context-wide flat start of (block, angle)

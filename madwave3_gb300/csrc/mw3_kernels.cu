@@ -220,6 +220,7 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
     const T divi = (T)(1.0 / (4.0 * (double)(nn + 1) * (double)(n2 + 1)));
     const T rcut = (T)radcut;
     T ae[COL_RMAX], ao[COL_RMAX];
+    const int nr = ty < hn ? (hn - 1 - ty) / 8 + 1 : 0;    // rows ty + 8 r < hn of this warp
     for (int pass = 0; pass < 2; pass++) {
 #pragma unroll
         for (int r = 0; r < COL_RMAX; r++) ae[r] = ao[r] = (T)0;
@@ -234,13 +235,13 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
             for (int kk = 0; kk < kmax; kk += 2) {
                 T y0 = Yt[(kc + kk) * COL_W + tx];
                 T y1 = kk + 1 < kmax ? Yt[(kc + kk + 1) * COL_W + tx] : (T)0;
+                // a warp's rows end at nr (uniform): leave instead of issuing masked FMAs
 #pragma unroll
                 for (int r = 0; r < COL_RMAX; r++) {
-                    int i = ty + 8 * r;
-                    if (i < hn) {
-                        ae[r] += Sc[i * COL_KC + kk] * y0;
-                        ao[r] += Sc[i * COL_KC + kk + 1] * y1;
-                    }
+                    if (r >= nr) break;
+                    const T *sr = Sc + (ty + 8 * r) * COL_KC + kk;
+                    ae[r] += sr[0] * y0;
+                    ao[r] += sr[1] * y1;
                 }
             }
         }

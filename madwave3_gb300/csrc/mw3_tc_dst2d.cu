@@ -65,11 +65,89 @@ struct Dst2Args {
     const float *p2r1f, *p2r2f;   // [W][na][n1], [W][na][n2]
     float radcut;
     const int *mapT;              // [na][n2][n1]
+    const int2 *rows;             // [na][n2][4]: stored-r1 bits of word w, index of its first stored point
+    const int *rows_ok;           // [na]: every R row's indices run consecutively in r1
+    int wave;                     // CTAs resident at once (one per SM): the next wave's slab is seg + wave
     const int64_t *foff;
     const int *blk_wave;
     int na, n1, n2, seg0;
     int *err;
 };
+
+// H at the stored points of one slab from D4 (E in tensor-memory columns 256 + i,
+// O in 384 + i of lane m = r1 = 32 q + l): R = i takes E + O and R = n2-1-i takes
+// E - O, for the 32 i of warp group sub.  When the angle's rows store their points
+// consecutively in r1 order, a point's index is the row's count before word q plus
+// the stored bits below l: srow, the angle's (bits, count) table staged in shared
+// memory (8 KB), gives both in one broadcast read per row.  Otherwise (srow null)
+// through the [R][r1] map: a coalesced 128-byte line per R, 128 KB per slab,
+// prefetched into L1 while the last products run.
+__device__ __forceinline__ void d2_prefetch_map(const Dst2Args &p, int a, int m, int nn, int h, int sub)
+{
+    const int n1 = p.n1, n2 = p.n2;
+    const int *mT = p.mapT + (size_t)a * n2 * n1;
+    if (m < nn) {
+#pragma unroll 4
+        for (int uu = 0; uu < 32; uu++) {
+            int i = 32 * sub + uu;
+            if (i < h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)i * n1 + m));
+            if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
+        }
+    }
+}
+
+// the angle's row table into shared memory (fill warps; visible after their next barrier)
+__device__ __forceinline__ void d2_stage_rows(const Dst2Args &p, int a, int2 *srow, int nthreads)
+{
+    const int4 *src = reinterpret_cast<const int4 *>(p.rows + (size_t)a * p.n2 * 4);
+    int4 *dst = reinterpret_cast<int4 *>(srow);
+    for (int e = threadIdx.x; e < 2 * p.n2; e += nthreads) dst[e] = __ldg(src + e);
+}
+
+__device__ __forceinline__ void d2_store_h(const Dst2Args &p, int a, int64_t fo, int m, int nn, int h, int sub,
+                                           uint32_t lrow, float hinv, const int2 *srow)
+{
+    const int n1 = p.n1, n2 = p.n2;
+    const int q = m >> 5;
+    const unsigned below = (1u << (m & 31)) - 1u, me = 1u << (m & 31);
+    const int *mT = p.mapT + (size_t)a * n2 * n1;
+#pragma unroll 1
+    for (int cc = 0; cc < 4; cc++) {
+        const int i0 = 32 * sub + 8 * cc;
+        float e[8], o[8];
+        tmem_ld8(lrow + 256u + (uint32_t)i0, e);
+        tmem_ld8(lrow + 384u + (uint32_t)i0, o);
+        if (srow) {
+            if (m < nn) {
+#pragma unroll
+                for (int uu = 0; uu < 8; uu++) {
+                    const int i = i0 + uu;
+                    if (i < h) {
+                        const int2 r = srow[i * 4 + q];
+                        if (r.x & me) p.H[fo + r.y + __popc(r.x & below)] = (e[uu] + o[uu]) * hinv;
+                    }
+                    if (i < n2 - h) {
+                        const int2 r = srow[(n2 - 1 - i) * 4 + q];
+                        if (r.x & me) p.H[fo + r.y + __popc(r.x & below)] = (e[uu] - o[uu]) * hinv;
+                    }
+                }
+            }
+        } else {
+            int is[8], id[8];
+#pragma unroll
+            for (int uu = 0; uu < 8; uu++) {
+                const int i = i0 + uu;
+                is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
+                id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
+            }
+#pragma unroll
+            for (int uu = 0; uu < 8; uu++) {
+                if (is[uu] >= 0) p.H[fo + is[uu]] = (e[uu] + o[uu]) * hinv;
+                if (id[uu] >= 0) p.H[fo + id[uu]] = (e[uu] - o[uu]) * hinv;
+            }
+        }
+    }
+}
 
 // four values of one row into the hi plane at off and the lo plane lo_off further
 __device__ __forceinline__ void d2_split4(unsigned char *hi, uint32_t lo_off, uint32_t off, float a, float b,
@@ -109,6 +187,16 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
         :
         : "r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(mbar))
         : "memory");
+}
+
+// L2 prefetch of one 2-D tile (no shared memory, no completion): the first
+// product's X tiles start streaming from DRAM while the slab sets up
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap *map, int x, int y)
+{
+    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];"
+                 :
+                 : "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y)
+                 : "memory");
 }
 
 // Tensor memory (512 columns):
@@ -200,6 +288,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
     uint64_t *xfull = empty + D2_NS;                    // the X tile of a first-product chunk landed
     uint32_t *slot = reinterpret_cast<uint32_t *>(xfull + D2_NS);
     float *s_p1f = reinterpret_cast<float *>(sm + D2_BYTES + 128);   // the slab's r1 momenta
+    int2 *s_rows = reinterpret_cast<int2 *>(sm + D2_BYTES + 1024);   // the angle's row table [n2][4]
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int na = p.na, n1 = p.n1, n2 = p.n2;
@@ -312,9 +401,11 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
         const uint32_t lrow = tb + ((uint32_t)(q4 * 32) << 16);
         const float divi = 1.0f / (4.0f * (float)(nn + 1) * (float)(n2 + 1));
         {
-            // the r1 momenta of the slab into shared memory (read 8 at a time by the third product)
+            // the r1 momenta of the slab into shared memory (read 8 at a time by the third
+            // product) and, when the angle has one, its row table (read by the H write)
             const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
             if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
+            if (p.rows_ok[a]) d2_stage_rows(p, a, s_rows, D2_FILL * 32);
             asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
         }
         // second and third products: sub & 1 picks the row set, sub >> 1 the 8-column half
@@ -410,40 +501,11 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
             if (lane == 0) mbar_arrive1(&full[s]);
         });
         // ---- H at the stored points: lane r1; R = i takes E + O, R = n2-1-i takes E - O ----
-        const int *mT = p.mapT + (size_t)a * n2 * n1;
-        if (m < nn) {
-            // the map entries this thread reads, into L1 while the last MMAs run
-#pragma unroll 4
-            for (int uu = 0; uu < 32; uu++) {
-                int i = 32 * sub + uu;
-                if (i < h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)i * n1 + m));
-                if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
-            }
-        }
+        const int2 *srow = p.rows_ok[a] ? s_rows : nullptr;
+        if (!srow) d2_prefetch_map(p, a, m, nn, h, sub);
         d2_wait(&empty[(total - 1) & (D2_NS - 1)], ((total - 1) >> 2) & 1, fail);
         fence_after_sync();
-        if (!*fail) {
-            const int64_t fo = p.foff[seg];
-#pragma unroll
-            for (int cc = 0; cc < 2; cc++) {
-                const int i0 = 32 * sub + 16 * cc;
-                float e[16], o[16];
-                tmem_ld16(lrow + 256u + (uint32_t)i0, e);
-                tmem_ld16(lrow + 384u + (uint32_t)i0, o);
-                int is[16], id[16];
-#pragma unroll
-                for (int uu = 0; uu < 16; uu++) {
-                    int i = i0 + uu;
-                    is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
-                    id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
-                }
-#pragma unroll
-                for (int uu = 0; uu < 16; uu++) {
-                    if (is[uu] >= 0) p.H[fo + is[uu]] = e[uu] + o[uu];
-                    if (id[uu] >= 0) p.H[fo + id[uu]] = e[uu] - o[uu];
-                }
-            }
-        }
+        if (!*fail) d2_store_h(p, a, p.foff[seg], m, nn, h, sub, lrow, 1.f, srow);
     }
     // before shared and tensor memory are released, the async work this CTA issued
     // must be done: the copy warp waits for its last copy, the MMA warp for its
@@ -474,11 +536,17 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d(Dst2Args p, const
 //   Xs              x 2^(12 - e), xmax < 2^e the slab's largest |X|, which the
 //                   kernels that write X leave in xmax[slab] (atomicMax of the
 //                   bits; this kernel reads it and clears it);
-//   D1, D2 o F, D3  x 2^(12 - e) with e from the slab's largest |element| of that
-//                   operand, which the fill warps read out of tensor memory when
-//                   the product before it completes and reduce across the CTA
-//                   (a bound fixed in advance left the operand of a smooth packet
-//                   up to 2^16 below it, where the lo parts fall into FP16
+//   D1, D3          x 2^-20: |D1| <= 2^12 * 2^13 * 256 terms, and |D3| the same
+//                   with the normalised D2 o F below; the largest element of
+//                   either is at least that of one 2 sin(.) x 2^12 term times the
+//                   largest operand element (2^25 -> 2^5), so an element within
+//                   2^-8 of it keeps a normal lo part;
+//   D2 o F          x 2^(12 - e) with e from the slab's largest |element|, which
+//                   the fill warps read out of tensor memory when the second
+//                   product completes and reduce across the CTA (F's bound,
+//                   radcut / (4 (nn+1)(n2+1)), sits up to 2^10 above the F of a
+//                   smooth packet's spectrum, and with D2's own slack a fixed
+//                   scale left this operand up to 2^16 low, its lo parts in FP16
 //                   subnormals: 1e-4 relative error in H psi);
 // and H is D4 times the inverse of the product of the scales, again a power of
 // two.  A K chunk is 32 FP16 values, the same 64 bytes per row as the 16 TF32
@@ -590,7 +658,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
     uint64_t *xfull = empty + H_NS;
     uint32_t *slot = reinterpret_cast<uint32_t *>(xfull + H_NS);
     float *s_p1f = reinterpret_cast<float *>(sm + H_BYTES + 128);
-    unsigned *s_red = reinterpret_cast<unsigned *>(sm + H_BYTES + 640);    // largest |D1|, |D2 o F|, |D3|
+    unsigned *s_red = reinterpret_cast<unsigned *>(sm + H_BYTES + 640);    // largest |D2 o F|
+    int2 *s_rows = reinterpret_cast<int2 *>(sm + H_BYTES + 1024);          // the angle's row table [n2][4]
     volatile int *fail = reinterpret_cast<volatile int *>(slot + 1);
     const Dst2Args &p = P.b;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -627,6 +696,10 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
     int copies = 0;
 
     if (warp == D2_COPY_WARP) {
+        // once this slab's X copies are issued, the X of the slab the next wave of CTAs
+        // takes (one CTA per SM, issued in order) streams into L2, so that slab's first
+        // product finds its tiles there instead of waiting on DRAM chunk by chunk
+        const int nxt = (int)blockIdx.x + p.wave;
         if (lane == 0)
             h_for_chunks(nkh, nkr, [&](int t, int s, int ph, int gi, int par, int jc) {
                 if (*fail) return;
@@ -645,6 +718,8 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                 mbar_expect_tx(&full[s], H_SMALL);
                 bulk_g2s(alongR ? st : st + H_SMALL_AT, src, H_SMALL, &full[s]);
                 copies = t + 1;
+                if (t == 2 * nkh - 1 && nxt < (int)gridDim.x)
+                    for (int j = 0; j < 2 * nkh; j++) tma_prefetch_2d(&xmap, 32 * j, (seg + p.wave) * n1);
             });
     } else if (warp == D2_MMA_WARP) {
         if (lane == 0) {
@@ -701,11 +776,13 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
         if (xm > 0.f) frexpf(xm, &ex);                  // xm < 2^ex
         const int sx_exp = min(100, max(-100, 12 - ex));
         const float sx = ldexpf(1.f, sx_exp);
-        int s_exp = sx_exp;                             // sum of the operand scales' exponents so far
-        float sc = 1.f;                                 // the scale of the current product's operand
+        int s_exp = sx_exp - 40;                        // sum of the operand scales' exponents (D1, D3: -20)
+        constexpr float a13 = 1.f / 1048576.f;          // 2^-20
+        float sc2 = 1.f;                                // D2 o F's scale, set when the second product completes
         {
             const float *p1f = p.p2r1f + ((size_t)w * na + a) * n1;
             if (threadIdx.x < 128) s_p1f[threadIdx.x] = threadIdx.x < nn ? p1f[threadIdx.x] : 0.f;
+            if (p.rows_ok[a]) d2_stage_rows(p, a, s_rows, D2_FILL * 32);
             asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
         }
         const int rset = sub & 1, colq = sub >> 1;
@@ -721,51 +798,59 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
             if (jc == 0 && par == 0 && gi > 0) {
                 d2_wait(&empty[pt], pph, fail);
                 fence_after_sync();
-                // the previous product is complete: the largest |element| this thread will
+                // the second product is complete: the largest |D2 o F| this thread will
                 // write, over the chunks below (loads warp-uniform, values masked by lane)
-                float mx = 0.f;
-                if (gi == 1) {
-                    for (int j = 0; j < nkr; j++) {
-                        const int kc = j * H_KC + 16 * colq;
-                        float ev[16], ov[16];
-                        tmem_ld16(lrow + (uint32_t)kc, ev);
-                        tmem_ld16(lrow + 128u + (uint32_t)kc, ov);
-#pragma unroll
-                        for (int i = 0; i < 16; i++)
-                            if (on2 && kc + i < nn) mx = fmaxf(mx, fabsf(ev[i] + sg2 * ov[i]));
-                    }
-                } else if (gi == 2) {
+                if (gi == 2) {
+                    // max |v ek| first, times divi after the reduction: rounding is monotone,
+                    // so this is the largest of the rounded products the fills below write
+                    float mx = 0.f;
                     if (rset < NT)
-                        for (int j = 0; j < nkr; j++) {
+                        for (int j = 0; j < nkr; j += 2) {
                             const int kc = j * H_KC + 16 * colq;
-                            float v[16];
-                            tmem_ld16(lrow + 256u + 128u * rset + (uint32_t)kc, v);
+                            uint32_t v[32];
+                            const bool two = j + 1 < nkr;     // uniform over the CTA
+                            tmem_ld16_nw(lrow + 256u + 128u * rset + (uint32_t)kc, v);
+                            if (two) tmem_ld16_nw(lrow + 256u + 128u * rset + (uint32_t)(kc + H_KC), v + 16);
 #pragma unroll
-                            for (int i = 0; i < 16; i++) {
-                                const float ek = fminf(s_p1f[kc + i] + e2, radcut);
-                                if (kc + i < nn && rR < n2) mx = fmaxf(mx, fabsf(v[i] * ek * divi));
+                            for (int i = 16; i < 32; i++)
+                                if (!two) v[i] = 0u;
+                            tmem_wait16(v);
+                            tmem_regs16(v + 16);
+#pragma unroll
+                            for (int g = 0; g < 2; g++) {
+                                const int k0g = kc + g * H_KC;
+                                const float4 *pq = reinterpret_cast<const float4 *>(s_p1f + (k0g & 127));
+                                float q[16];
+#pragma unroll
+                                for (int u = 0; u < 4; u++) {
+                                    const float4 f = pq[u];
+                                    q[4 * u] = f.x, q[4 * u + 1] = f.y, q[4 * u + 2] = f.z, q[4 * u + 3] = f.w;
+                                }
+                                if (k0g + 16 <= nn) {
+#pragma unroll
+                                    for (int i = 0; i < 16; i++)
+                                        mx = fmaxf(mx, fabsf(__uint_as_float(v[16 * g + i]) * fminf(q[i] + e2, radcut)));
+                                } else {
+#pragma unroll
+                                    for (int i = 0; i < 16; i++)
+                                        if (k0g + i < nn)
+                                            mx = fmaxf(mx, fabsf(__uint_as_float(v[16 * g + i]) * fminf(q[i] + e2, radcut)));
+                                }
                             }
                         }
-                } else {
-                    for (int j = 0; j < nkh; j++) {
-                        const int col0 = 2 * j * H_KC + 16 * sub;
-                        float v16[16];
-                        tmem_ld16(lrow + (uint32_t)col0, v16);
+                    if (rR >= n2) mx = 0.f;
+                    mx *= divi;
 #pragma unroll
-                        for (int i = 0; i < 16; i++)
-                            if (col0 + i < n2) mx = fmaxf(mx, fabsf(v16[i]));
-                    }
+                    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                    if (lane == 0) atomicMax(&s_red[0], __float_as_uint(mx));
+                    asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
+                    const float gm = __uint_as_float(s_red[0]);
+                    int e = 0;
+                    if (gm > 0.f) frexpf(gm, &e);       // gm < 2^e
+                    const int se = min(100, max(-100, 12 - e));
+                    sc2 = ldexpf(1.f, se);
+                    s_exp += se;
                 }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-                if (lane == 0) atomicMax(&s_red[gi], __float_as_uint(mx));
-                asm volatile("bar.sync 1, %0;" ::"n"(D2_FILL * 32) : "memory");
-                const float gm = __uint_as_float(s_red[gi]);
-                int e = 0;
-                if (gm > 0.f) frexpf(gm, &e);           // gm < 2^e
-                const int se = min(100, max(-100, 12 - e));
-                sc = ldexpf(1.f, se);
-                s_exp += se;
             }
             if (t >= H_NS) d2_wait(&empty[s], ph ^ 1, fail);
             const int k0 = jc * H_KC;
@@ -798,7 +883,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                     const bool fullc = kc + 16 <= nn;
 #pragma unroll
                     for (int i = 0; i < 16; i++) {
-                        const float x = (ev[i] + sg2 * ov[i]) * sc;
+                        const float x = (ev[i] + sg2 * ov[i]) * a13;
                         ev[i] = (fullc || kc + i < nn) ? x : 0.f;
                     }
                     H_SPLIT8(big, big_lo, kmaj16_off(R2, 16 * colq), ev, 0);
@@ -814,7 +899,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
 #pragma unroll
                     for (int i = 0; i < 16; i++) {
                         const float ek = fminf(s_p1f[kc + i] + e2, radcut);
-                        const float x = v[i] * ek * divi * sc;
+                        const float x = v[i] * ek * divi * sc2;
                         v[i] = (fullc || (kc + i < nn && rR < n2)) ? x : 0.f;
                     }
                     H_SPLIT8(big, big_lo, kmaj16_off(rR, 16 * colq), v, 0);
@@ -829,7 +914,7 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                 float v[8];
 #pragma unroll
                 for (int uu = 0; uu < 8; uu++) {
-                    const float x = (par == 0 ? v16[2 * uu] : v16[2 * uu + 1]) * sc;
+                    const float x = (par == 0 ? v16[2 * uu] : v16[2 * uu + 1]) * a13;
                     v[uu] = (fullc || col0 + 2 * uu + par < n2) ? x : 0.f;
                 }
                 H_SPLIT8(small, H_SMALL_LO, kmaj16_off(m, 8 * sub), v, 0);
@@ -841,40 +926,11 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
             pt = s;
             pph = ph;
         });
-        const int *mT = p.mapT + (size_t)a * n2 * n1;
-        if (m < nn) {
-#pragma unroll 4
-            for (int uu = 0; uu < 32; uu++) {
-                int i = 32 * sub + uu;
-                if (i < h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)i * n1 + m));
-                if (i < n2 - h) asm volatile("prefetch.global.L1 [%0];" ::"l"(mT + (size_t)(n2 - 1 - i) * n1 + m));
-            }
-        }
+        const int2 *srow = p.rows_ok[a] ? s_rows : nullptr;
+        if (!srow) d2_prefetch_map(p, a, m, nn, h, sub);
         d2_wait(&empty[pt], pph, fail);
         fence_after_sync();
-        if (!*fail) {
-            const int64_t fo = p.foff[seg];
-            const float hinv = ldexpf(1.f, -(4 * H_S_EXP + s_exp));
-#pragma unroll
-            for (int cc = 0; cc < 4; cc++) {
-                const int i0 = 32 * sub + 8 * cc;
-                float e[8], o[8];
-                tmem_ld8(lrow + 256u + (uint32_t)i0, e);
-                tmem_ld8(lrow + 384u + (uint32_t)i0, o);
-                int is[8], id[8];
-#pragma unroll
-                for (int uu = 0; uu < 8; uu++) {
-                    int i = i0 + uu;
-                    is[uu] = (m < nn && i < h) ? __ldg(mT + (size_t)i * n1 + m) : -1;
-                    id[uu] = (m < nn && i < n2 - h) ? __ldg(mT + (size_t)(n2 - 1 - i) * n1 + m) : -1;
-                }
-#pragma unroll
-                for (int uu = 0; uu < 8; uu++) {
-                    if (is[uu] >= 0) p.H[fo + is[uu]] = (e[uu] + o[uu]) * hinv;
-                    if (id[uu] >= 0) p.H[fo + id[uu]] = (e[uu] - o[uu]) * hinv;
-                }
-            }
-        }
+        if (!*fail) d2_store_h(p, a, p.foff[seg], m, nn, h, sub, lrow, ldexpf(1.f, -(4 * H_S_EXP + s_exp)), srow);
     }
     const int lt = total - 1, ls = lt % H_NS, lph = (lt / H_NS) & 1;
     if (lane == 0 && warp == D2_COPY_WARP && copies > 0) {
@@ -1086,7 +1142,8 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
 {
     using namespace tc;
     static bool attr = false;
-    const size_t smem = D2_BYTES + 1024 + 1024;         // stages, barriers and momenta, alignment slack
+    // stages, barriers and momenta, the row table (n2 <= 256), alignment slack
+    const size_t smem = D2_BYTES + 1024 + 8192 + 1024;
     static_assert(H_BYTES == D2_BYTES, "both forms take the same shared memory");
     if (!attr) {
         cudaFuncSetAttribute(k_tc_dst2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1100,6 +1157,15 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
     p.s2fold = c.d_dst_s2fold; p.s1planes = c.d_dst_planes; p.s1off = c.d_dst_s1off; p.nopr1 = c.d_nopr1;
     p.p2r1f = c.d_p2r1f; p.p2r2f = c.d_p2r2f; p.radcut = (float)c.grid.radcutmax;
     p.mapT = c.d_mapT; p.foff = c.d_foff; p.blk_wave = c.d_blk_wave;
+    p.rows = reinterpret_cast<const int2 *>(c.d_rows); p.rows_ok = c.d_rows_ok;
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+    p.wave = nsm;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.seg0 = g_begin * c.na;
     p.err = c.d_tc_err;
     CUtensorMap xmap;

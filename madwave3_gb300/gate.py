@@ -62,6 +62,20 @@ def _vj_error(run, a, b, window=None):
     return out
 
 
+def channel_table(run, a, b, window=None, floor=1e-8):
+    """One row per reactant channel (v, j) whose P_vj(E) reaches ``floor``
+    inside the window: [v, j, max |P_a - P_b|, max P_a] over the energies."""
+    w = np.ones(a.shape[-1], bool) if window is None else window
+    rows = []
+    for jj in range(a.shape[0]):
+        for vv in range(a.shape[1]):
+            pa, pb = a[jj, vv][w], b[jj, vv][w]
+            if pa.size and np.abs(pa).max() >= floor:
+                rows.append([int(vv + run.inp.nvini), int(jj + run.inp.jini), float(np.abs(pa - pb).max()),
+                             float(np.abs(pa).max())])
+    return rows
+
+
 def run_gate(case, iterations, cases_dir=None, waves=None):
     from .host import generator, setup
 
@@ -107,7 +121,7 @@ def run_gate_run(run, iterations, case=""):
     return out, e, a, b
 
 
-def run_sweep_gate(case, js, iterations, cases_dir=None):
+def run_sweep_gate(case, js, iterations, cases_dir=None, channels=False):
     from . import Propagator
     from .host import generator, setup
 
@@ -136,11 +150,14 @@ def run_sweep_gate(case, js, iterations, cases_dir=None):
         a, b = res["fp64"][w], res["mixed"][w]
         row = {"J": J, "max_abs_dP": float(np.abs(a - b).max()), "max_P": float(np.abs(a).max())}
         row.update(_vj_error(runs[w], res["fp64_vj"][w], res["mixed_vj"][w], res["window"][w]))
+        if channels:
+            row["channels"] = channel_table(runs[w], res["fp64_vj"][w], res["mixed_vj"][w], res["window"][w])
         per.append(row)
     out["per_J"] = per
     out["max_abs_dP"] = max(x["max_abs_dP"] for x in per)
     out["max_abs_dP_vj"] = max(x["max_abs_dP_vj"] for x in per)
     out["pass_1e-4"] = bool(out["max_abs_dP"] <= 1e-4)
+    out["dst_form"] = "split FP16" if os.environ.get("MW3_DST_TF32", "") != "1" else "3xTF32"
     return out
 
 
@@ -150,9 +167,12 @@ def main():
     ap.add_argument("--iterations", type=int, default=2000)
     ap.add_argument("--out", default=None, help="also write E, P_fp64, P_mixed as text")
     ap.add_argument("--sweep", default=None, help="comma-separated J of a batched partial-wave gate")
+    ap.add_argument("--channels", action="store_true",
+                    help="with --sweep: every reactant channel's max |dP_vj(E)| and max P_vj(E) per J")
     args = ap.parse_args()
     if args.sweep:
-        print(json.dumps(run_sweep_gate(args.case, [int(x) for x in args.sweep.split(",")], args.iterations)))
+        print(json.dumps(run_sweep_gate(args.case, [int(x) for x in args.sweep.split(",")], args.iterations,
+                                        channels=args.channels)))
         return
     out, e, a, b = run_gate(args.case, args.iterations)
     if args.out:
