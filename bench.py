@@ -36,7 +36,7 @@ L2_BYTES = 129 * 1024 * 1024
 # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the J=0..4
 # sweep; the per-block structure of the full sweep is the same, so the traffic
 # scales with the stored points (profiles/k_*_jsweep0-4_256x128x60_mixed.md)
-TRAFFIC_PER_POINT = {"dst_R": 17.1, "angular": 16.7, "update": 27.7}
+TRAFFIC_PER_POINT = {"dst_R": 16.0, "angular": 16.6, "update": 27.9}
 
 WORKLOADS = {
     # partial-wave sweep J=0..40, Omega=0..min(J,6): 266 blocks on 256 R x 128 r x 60 angles
