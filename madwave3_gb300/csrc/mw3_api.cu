@@ -332,6 +332,44 @@ int build_device(Ctx &c)
         }
     }
     TRY(dupload(c, &c.d_nopr1, nopr1));
+    {
+        // the rows each segment transforms (ir1 < nopr1), as a prefix over segments
+        std::vector<int64_t> pre((size_t)G * na + 1, 0);
+        for (int s = 0; s < G * na; s++) pre[s + 1] = pre[s] + nopr1[(size_t)bw[s / na] * na + s % na];
+        TRY(dupload(c, &c.d_rowpre, pre));
+    }
+    if (n2 == 256) {
+        // Rader's tables for the 257-point transform behind the FP64 DST along R: with g = 3
+        // a primitive root of 257, W_{g^-p} = sum_q a_q d_{p-q}, a_q = w_{g^q}, d_m =
+        // exp(-2 pi i g^-m / 257), a 256-point cyclic convolution; d's FFT / 256 in long double
+        const int NP = 257, M = 256;
+        std::vector<int> perm(M);
+        for (int q = 0, v = 1; q < M; q++, v = (v * 3) % NP) perm[q] = v;
+        std::vector<short> col(M);
+        std::vector<int> outc(M);
+        for (int q = 0; q < M; q++) col[q] = (short)(perm[q] - 1);
+        for (int p = 0; p < M; p++) {
+            const int j = perm[(M - p) % M];            // W_j lands at convolution index p
+            outc[p] = j <= 128 ? 2 * j - 1 : (2 * j - 258) | (1 << 16);
+        }
+        const long double twopi = 6.283185307179586476925286766559005768L;
+        std::vector<double2> tw(M), ch(M);
+        for (int k = 0; k < M; k++) {
+            const long double th = twopi * (long double)k / M;
+            tw[k] = make_double2((double)cosl(th), (double)-sinl(th));
+            long double re = 0.0L, im = 0.0L;
+            for (int m = 0; m < M; m++) {
+                const long double ph = twopi * ((long double)perm[(M - m) % M] / NP + (long double)((m * k) % M) / M);
+                re += cosl(ph);
+                im -= sinl(ph);
+            }
+            ch[k] = make_double2((double)(re / M), (double)(im / M));
+        }
+        TRY(dupload(c, &c.d_rd_tw, tw));
+        TRY(dupload(c, &c.d_rd_ch, ch));
+        TRY(dupload(c, &c.d_rd_col, col));
+        TRY(dupload(c, &c.d_rd_out, outc));
+    }
     TRY(dupload(c, &c.d_p2r1, p2r1));
     TRY(dupload(c, &c.d_p2r2, p2r2));
     TRY(dupload(c, &c.d_absfr1, a1));

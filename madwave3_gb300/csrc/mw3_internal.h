@@ -192,6 +192,12 @@ struct Ctx {
     void *d_X = nullptr, *d_Y = nullptr;
     // DST matrices (type T): S2 [n2][n2]; S1 of every (wave, angle) length, packed
     void *d_S2 = nullptr, *d_S1 = nullptr;
+    // FP64 DST along R by Rader's algorithm (npun2 = 256, npun2 + 1 = 257 prime, root 3)
+    double2 *d_rd_tw = nullptr;      // W_256^k
+    double2 *d_rd_ch = nullptr;      // FFT_256 of the Rader kernel exp(-2 pi i 3^-m / 257), / 256
+    short *d_rd_col = nullptr;       // q -> input column 3^q mod 257 - 1
+    int *d_rd_out = nullptr;         // p -> output column | (odd output) << 16
+    int64_t *d_rowpre = nullptr;     // [G na + 1]: rows ir1 < nopr1 before each segment
     int64_t *d_S1off = nullptr;      // [W][na]
     // explicit angular kinetic matrices (type T)
     void *d_xj2 = nullptr;           // [G][n1][na][na]

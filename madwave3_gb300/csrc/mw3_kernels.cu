@@ -281,6 +281,167 @@ __global__ void __launch_bounds__(256) k_dst_cols(DevGrid d, T *__restrict__ Y, 
         }
 }
 
+// ---------------------------------------------------------------------------
+// FP64 DST along R for npun2 = 256 as a 257-point transform by Rader's algorithm.
+// y_i = sum_k 2 sin(pi i k / 257) x_k (i, k = 1..256) is read off the 257-point DFT W
+// of w_k = x_k + i (-1)^k x_k: y_2j = Im W_{257-j} - Im W_j (j <= 128) and
+// y_{2j-257} = Re W_j - Re W_{257-j} (j >= 129).  257 is prime with primitive root 3,
+// so W_{3^-p} = sum_q w_{3^q} d_{p-q} (indices mod 256, d_m = exp(-2 pi i 3^-m / 257)),
+// a 256-point cyclic convolution: FFT, product with d's FFT (a table, / 256), and the
+// inverse as conj(FFT(conj(.))); W_{257-j} sits 128 places from W_j (3^128 = -1).  The
+// FFTs are radix-4 Stockham passes in shared memory (natural order, no bit reversal).
+// About 14 k FP64 operations a row, against 33 k multiply-adds for the folded dense
+// product, and only the rows ir1 < nopr1 are transformed (the dense kernel computes
+// whole 64-row tiles).  Four rows per CTA batch, one per 64-thread group.
+// ---------------------------------------------------------------------------
+constexpr int RD_M = 256, RD_ROWS = 4;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// forward FFT of a[256] (in place through b), radix-4 Stockham, 64 threads a row
+__device__ __forceinline__ void rd_fft256(double2 *a, double2 *b, const double2 *tw, int t)
+{
+    double2 *in = a, *out = b;
+#pragma unroll
+    for (int ns = 1; ns < RD_M; ns *= 4) {
+        double2 v[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) v[r] = in[t + 64 * r];
+        if (ns > 1) {
+            const int jm = t % ns, st = 64 / ns;
+#pragma unroll
+            for (int r = 1; r < 4; r++) v[r] = cmul(v[r], tw[jm * r * st]);
+        }
+        const double2 a0 = make_double2(v[0].x + v[2].x, v[0].y + v[2].y);
+        const double2 a1 = make_double2(v[0].x - v[2].x, v[0].y - v[2].y);
+        const double2 a2 = make_double2(v[1].x + v[3].x, v[1].y + v[3].y);
+        const double2 a3 = make_double2(v[1].x - v[3].x, v[1].y - v[3].y);
+        const int d0 = (t / ns) * ns * 4 + t % ns;
+        out[d0] = make_double2(a0.x + a2.x, a0.y + a2.y);
+        out[d0 + ns] = make_double2(a1.x + a3.y, a1.y - a3.x);        // a1 - i a3
+        out[d0 + 2 * ns] = make_double2(a0.x - a2.x, a0.y - a2.y);
+        out[d0 + 3 * ns] = make_double2(a1.x - a3.y, a1.y + a3.x);    // a1 + i a3
+        __syncthreads();
+        double2 *tmp = in;
+        in = out;
+        out = tmp;
+    }
+}
+
+struct RaderTab {
+    const double2 *tw, *ch;
+    const short *col;
+    const int *out;
+    const int64_t *rowpre;
+};
+
+template <bool GATHER>
+__global__ void __launch_bounds__(256) k_dst_rows_rader(DevGrid d, const double *__restrict__ A,
+                                                        double *__restrict__ C, double *__restrict__ H, RaderTab rt,
+                                                        int seg0, int nseg)
+{
+    __shared__ double2 s_tw[RD_M], s_ch[RD_M];
+    __shared__ short s_col[RD_M];
+    __shared__ int s_out[RD_M];
+    __shared__ double2 s_buf[RD_ROWS][2][RD_M];
+    const int tid = threadIdx.x, grp = tid >> 6, t = tid & 63;
+    s_tw[tid] = rt.tw[tid];
+    s_ch[tid] = rt.ch[tid];
+    s_col[tid] = rt.col[tid];
+    s_out[tid] = rt.out[tid];
+    const int64_t v1 = rt.rowpre[seg0 + nseg];
+    const int n1 = d.n1, na = d.na;
+    double2 *a = s_buf[grp][0], *b = s_buf[grp][1];
+    double *xs = reinterpret_cast<double *>(b);
+    for (int64_t vb = rt.rowpre[seg0] + (int64_t)blockIdx.x * RD_ROWS; vb < v1;
+         vb += (int64_t)gridDim.x * RD_ROWS) {
+        const int64_t v = vb + grp;
+        const bool live = v < v1;
+        int seg = seg0, ir1 = 0;
+        if (live) {
+            // the segment holding transformed row v: the last with rowpre[seg] <= v
+            int lo = seg0, hi = seg0 + nseg - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (rt.rowpre[mid] <= v) lo = mid;
+                else hi = mid - 1;
+            }
+            seg = lo;
+            ir1 = (int)(v - rt.rowpre[seg]);
+        }
+        const int64_t row = (int64_t)seg * n1 + ir1;
+        __syncthreads();                    // the tables, and the previous batch's reads of b
+        if (live)
+#pragma unroll
+            for (int k = 0; k < 4; k++) xs[t + 64 * k] = A[row * RD_M + t + 64 * k];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int q = t + 64 * k, c = s_col[q];
+            const double x = live ? xs[c] : 0.0;
+            a[q] = make_double2(x, (c & 1) ? x : -x);   // k = c + 1: (-1)^k x
+        }
+        __syncthreads();
+        rd_fft256(a, b, s_tw, t);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int q = t + 64 * k;
+            const double2 z = cmul(a[q], s_ch[q]);
+            a[q] = make_double2(z.x, -z.y);
+        }
+        __syncthreads();
+        rd_fft256(a, b, s_tw, t);            // a = FFT(conj(.)): W_{3^-p} = conj(a[p])
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int p = t + 64 * k, q = (p + 128) & (RD_M - 1), o = s_out[p];
+            const double y = (o >> 16) ? a[p].x - a[q].x : a[p].y - a[q].y;
+            xs[o & 0xffff] = y;
+        }
+        __syncthreads();
+        if (live) {
+            if (GATHER) {
+                const int ang = seg % na;
+                const int *mp = d.map + ((size_t)ang * n1 + ir1) * RD_M;
+                const int64_t fo = d.foff[seg];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int col = t + 64 * k, idx = mp[col];
+                    if (idx >= 0) H[fo + idx] = xs[col];
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) C[row * RD_M + t + 64 * k] = xs[t + 64 * k];
+            }
+        }
+    }
+}
+
+static int rd_grid()
+{
+    static int g = 0;
+    if (!g) {
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        g = (nsm > 0 ? nsm : 1) * 5;        // 41.5 KB of shared memory a CTA: five per SM
+    }
+    return g;
+}
+
+static RaderTab rd_tab(const Ctx &c)
+{
+    RaderTab r;
+    r.tw = c.d_rd_tw;
+    r.ch = c.d_rd_ch;
+    r.col = c.d_rd_col;
+    r.out = c.d_rd_out;
+    r.rowpre = c.d_rowpre;
+    return r;
+}
+
 // double -> float, round to nearest even, with integer instructions only (the
 // F2F conversion issues on the FP64 pipe); magnitudes below FLT_MIN go to a
 // signed zero, above FLT_MAX to infinity
@@ -1371,8 +1532,13 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     } else {
         // 1. DST along R
         stage_mark(c, 0);
-        k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_S2, (T *)c.d_Y, nullptr,
-                                                        c.d_nopr1, row0, nrows);
+        const bool rader = sizeof(T) == 8 && c.d_rd_tw;
+        if (rader)
+            k_dst_rows_rader<false><<<rd_grid(), 256, 0, c.stream>>>(d, (const double *)c.d_X, (double *)c.d_Y,
+                                                                     nullptr, rd_tab(c), g_begin * c.na, ng * c.na);
+        else
+            k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_X, (const T *)c.d_S2, (T *)c.d_Y,
+                                                            nullptr, c.d_nopr1, row0, nrows);
         LAUNCH_CHECK(c);
         // 2. DST along r, k-space scaling, DST along r
         stage_mark(c, 1);
@@ -1383,8 +1549,12 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
         LAUNCH_CHECK(c);
         // 3. DST along R, gathered into H at the stored points
         stage_mark(c, 2);
-        k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_Y, (const T *)c.d_S2, nullptr, c.d_h,
-                                                       c.d_nopr1, row0, nrows);
+        if (rader)
+            k_dst_rows_rader<true><<<rd_grid(), 256, 0, c.stream>>>(d, (const double *)c.d_Y, nullptr, c.d_h,
+                                                                    rd_tab(c), g_begin * c.na, ng * c.na);
+        else
+            k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, (const T *)c.d_Y, (const T *)c.d_S2, nullptr, c.d_h,
+                                                           c.d_nopr1, row0, nrows);
         LAUNCH_CHECK(c);
     }
     // points beyond the r1 DST length keep psi
@@ -1908,13 +2078,22 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
     int64_t row0 = (int64_t)g0 * na * n1, nrows = (int64_t)ng * na * n1;
     dim3 gr((unsigned)((nrows + BM - 1) / BM), ((n2 + 1) / 2 + BN - 1) / BN);
-    k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, X, (const T *)c.d_S2, Y, nullptr, c.d_nopr1, row0, nrows);
+    const bool rader = sizeof(T) == 8 && c.d_rd_tw;
+    if (rader)
+        k_dst_rows_rader<false><<<rd_grid(), 256, 0, c.stream>>>(d, (const double *)X, (double *)Y, nullptr,
+                                                                 rd_tab(c), g0 * na, ng * na);
+    else
+        k_dst_rows<T, false><<<gr, 256, 0, c.stream>>>(d, X, (const T *)c.d_S2, Y, nullptr, c.d_nopr1, row0, nrows);
     LAUNCH_CHECK(c);
     dim3 gc(ng * na, (n2 + COL_W - 1) / COL_W);
     k_dst_cols<T><<<gc, 256, col_smem(c, sizeof(T)), c.stream>>>(d, Y, (const T *)c.d_S1, c.d_S1off, c.d_nopr1,
                                                                   c.d_p2r1, c.d_p2r2, c.grid.radcutmax, g0 * na);
     LAUNCH_CHECK(c);
-    k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, Y, (const T *)c.d_S2, nullptr, H, c.d_nopr1, row0, nrows);
+    if (rader)
+        k_dst_rows_rader<true><<<rd_grid(), 256, 0, c.stream>>>(d, (const double *)Y, nullptr, H, rd_tab(c), g0 * na,
+                                                                ng * na);
+    else
+        k_dst_rows<T, true><<<gr, 256, 0, c.stream>>>(d, Y, (const T *)c.d_S2, nullptr, H, c.d_nopr1, row0, nrows);
     LAUNCH_CHECK(c);
     k_quirk<double><<<ng * na, 128, 0, c.stream>>>(d, P, H, c.d_quirk_ptr, c.d_quirk, g0 * na);
     LAUNCH_CHECK(c);
