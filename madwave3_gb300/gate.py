@@ -167,14 +167,15 @@ def main():
     ap.add_argument("--iterations", type=int, default=2000)
     ap.add_argument("--out", default=None, help="also write E, P_fp64, P_mixed as text")
     ap.add_argument("--sweep", default=None, help="comma-separated J of a batched partial-wave gate")
+    ap.add_argument("--cases-dir", default=None, help="where the generated input cases live (default: a temp dir)")
     ap.add_argument("--channels", action="store_true",
                     help="with --sweep: every reactant channel's max |dP_vj(E)| and max P_vj(E) per J")
     args = ap.parse_args()
     if args.sweep:
         print(json.dumps(run_sweep_gate(args.case, [int(x) for x in args.sweep.split(",")], args.iterations,
-                                        channels=args.channels)))
+                                        cases_dir=args.cases_dir, channels=args.channels)))
         return
-    out, e, a, b = run_gate(args.case, args.iterations)
+    out, e, a, b = run_gate(args.case, args.iterations, cases_dir=args.cases_dir)
     if args.out:
         np.savetxt(args.out, np.stack([e, a, b], 1), header="E(eV) P_fp64 P_mixed")
     print(json.dumps(out))
