@@ -222,6 +222,64 @@ def warmup_count(it_now, warmup, steps):
     return w
 
 
+# contexts (one CUDA stream each, one host thread each) the end-to-end leg splits
+# the waves over, so that copies and kernels of different contexts overlap
+E2E_CONTEXTS = 4
+
+
+def run_e2e(runs, precision, nctx, steps):
+    """End to end through the C-ABI with host buffers: the host owns every wave's
+    psi_k (pinned) and each step hands it in, runs one iteration and reads the
+    new psi_k back (psi_k-1 stays the device's own).  The waves are split over
+    nctx contexts, each driven by its own host thread (the library's calls
+    release the interpreter lock and wait on their own stream), so one context's
+    copies overlap the other contexts' kernels and the two directions of the
+    host link overlap each other.  Host wall time over the steps of all
+    contexts; returns (ms per step, contexts)."""
+    import threading
+    import torch
+    from madwave3_gb300 import Propagator, replicas
+
+    parts = replicas.partition([float(r.ntot) for r in runs], nctx) if nctx > 1 else [list(range(len(runs)))]
+    props, bufs, its = [], [], []
+    for part in parts:
+        if not part:
+            continue
+        p = Propagator([runs[i] for i in part], precision)
+        p.start()
+        p.run(RING)
+        _, k, it = p.state_all()
+        props.append(p)
+        bufs.append([torch.from_numpy(k).pin_memory(), torch.empty(k.size, dtype=torch.float64).pin_memory()])
+        its.append(it)
+    errors = []
+
+    def drive(i):
+        try:
+            p, (a, b) = props[i], bufs[i]
+            for s in range(steps):
+                p.upload_state_all(None, a.numpy(), its[i] + s)
+                p.run(1)
+                p.state_k_all(b.numpy())
+                a, b = b, a
+        except Exception as e:      # re-raised on the main thread
+            errors.append(e)
+
+    torch.cuda.synchronize()
+    threads = [threading.Thread(target=drive, args=(i,)) for i in range(len(props))]
+    t0 = time.perf_counter()
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    for p in props:
+        p.close()
+    if errors:
+        raise errors[0]
+    return ms, len(props)
+
+
 def run_gpu(args, rank, world, local):
     import torch
     from madwave3_gb300 import Propagator, replicas
@@ -302,25 +360,11 @@ def run_gpu(args, rank, world, local):
     stages, nrec = prop.stage_times()
     prop.profile(False)
 
-    # end to end through the C-ABI with host buffers (all waves back to back,
-    # pinned): every step hands psi_k in from the host, runs one iteration and
-    # reads the new psi_k back; psi_k-1 is the device's own (the psi_k it held)
+    # the host link is shared with the rest of the node, so the leg runs three times
+    # and the median is reported (all three are in the line)
     e2e_steps = max(1, min(args.steps, 10))
-    _, k, it = prop.state_all()
-    bufs = [torch.from_numpy(k).pin_memory(), torch.empty(k.size, dtype=torch.float64).pin_memory()]
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for s in range(e2e_steps):
-        a, b = bufs
-        prop.upload_state_all(None, a.numpy(), it + s)
-        prop.run(1)
-        prop.state_k_all(b.numpy())
-        bufs = [b, a]
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_runs = [run_e2e(runs, args.precision, min(E2E_CONTEXTS, len(runs)), e2e_steps) for _ in range(3)]
+    e2e_ms, e2e_ctx = sorted(e2e_runs)[1]
     if world > 1:
         te = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
@@ -365,7 +409,11 @@ def run_gpu(args, rank, world, local):
                               "graph_blocks": (not flush) and args.steps % RING == 0},
                    "parallelism": parallelism},
         "e2e": {"value": e2e_value, "unit": "grid-pt*iter/s",
-                "h2d_bytes_per_step": int(8 * nsto), "d2h_bytes_per_step": int(8 * nsto)},
+                "h2d_bytes_per_step": int(8 * nsto), "d2h_bytes_per_step": int(8 * nsto),
+                "ms_per_step": e2e_ms, "contexts": e2e_ctx, "ms_per_step_runs": [r[0] for r in e2e_runs],
+                "how": "host-owned psi_k (pinned) in and psi_k+1 out every step through mw3_upload_state_all / "
+                       "mw3_run / mw3_download_state_all; waves split over the contexts, one host thread and "
+                       "CUDA stream each, host wall time; median of three runs of the steps"},
         "gpu_launches": launches,
         "stages_ms_per_step": {k: v / max(nrec, 1) for k, v in stages.items()},
         "roofline": roof,

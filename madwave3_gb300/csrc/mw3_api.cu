@@ -773,16 +773,30 @@ int check_launch(Ctx &c, const char *where)
 }
 
 // after a synchronisation: did a tensor-core kernel give up waiting for its MMAs?
+// The flag is copied in the context's own stream into a pinned word (ordered after
+// the context's kernels); a synchronous copy would go through the default stream
+// and could wait behind other contexts' transfers on a shared copy engine.
+int enqueue_device_flags(Ctx &c)
+{
+    if (!c.d_tc_err || !c.h_flag) return MW3_OK;
+    MW3_CUDA_TRY(cudaMemcpyAsync(c.h_flag, c.d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    return MW3_OK;
+}
+
+// after enqueue_device_flags and a synchronisation of the context's stream
+int device_flags_result(Ctx &c, const char *where)
+{
+    if (!c.d_tc_err || !c.h_flag || !*c.h_flag) return MW3_OK;
+    c.err = std::string(where) + ": a tensor-core kernel timed out waiting for its MMAs";
+    return MW3_ERR_CUDA;
+}
+
 int check_device_flags(Ctx &c, const char *where)
 {
-    if (!c.d_tc_err) return MW3_OK;
-    int h = 0;
-    MW3_CUDA_TRY(cudaMemcpy(&h, c.d_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h) {
-        c.err = std::string(where) + ": a tensor-core kernel timed out waiting for its MMAs";
-        return MW3_ERR_CUDA;
-    }
-    return MW3_OK;
+    int rc = enqueue_device_flags(c);
+    if (rc) return rc;
+    MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return device_flags_result(c, where);
 }
 
 int reset_accumulators(Ctx &c)
@@ -866,6 +880,11 @@ int mw3_create(mw3_ctx **out, const mw3_grid *g, const int32_t *npunreal, const 
         }
     }
     cudaError_t e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        e = cudaHostAlloc((void **)&c.h_flag, sizeof(int), cudaHostAllocDefault);
+        if (e == cudaSuccess) *c.h_flag = 0;
+        else cudaStreamDestroy(c.stream);
+    }
     if (e != cudaSuccess) {
         delete h;
         return MW3_ERR_CUDA;
@@ -877,6 +896,7 @@ int mw3_create(mw3_ctx **out, const mw3_grid *g, const int32_t *npunreal, const 
         // explicit angular kernels narrow their column chunk for large angle counts)
         if (!mw3::fit_smem(c, prop.sharedMemPerBlockOptin)) {
             cudaStreamDestroy(c.stream);
+            cudaFreeHost(c.h_flag);
             delete h;
             return MW3_ERR_UNSUPPORTED;
         }
@@ -1196,9 +1216,11 @@ int mw3_download_state_all(mw3_ctx *h, double *km1, double *k, int64_t *it)
     if (!c.started) return MW3_ERR_STATE;
     if (km1) MW3_CUDA_TRY(cudaMemcpyAsync(km1, c.d_pkm1, sizeof(double) * c.NT, cudaMemcpyDeviceToHost, c.stream));
     if (k) MW3_CUDA_TRY(cudaMemcpyAsync(k, c.d_pk, sizeof(double) * c.NT, cudaMemcpyDeviceToHost, c.stream));
+    int rc = enqueue_device_flags(c);
+    if (rc) return rc;
     MW3_CUDA_TRY(cudaStreamSynchronize(c.stream));
     if (it) *it = c.it;
-    return check_device_flags(c, "mw3_download_state_all");
+    return device_flags_result(c, "mw3_download_state_all");
 }
 
 int mw3_norms(mw3_ctx *h, int32_t w, double *norms, int64_t *n)
@@ -1536,6 +1558,7 @@ int mw3_destroy(mw3_ctx *h)
     for (cudaEvent_t e : c.prof_ev) cudaEventDestroy(e);
     free_device(c);
     if (c.stream) cudaStreamDestroy(c.stream);
+    if (c.h_flag) cudaFreeHost(c.h_flag);
     delete h;
     return MW3_OK;
 }

@@ -302,6 +302,7 @@ struct Ctx {
     float *d_vr32 = nullptr;         // like vvv, FP32 (mixed update)
     float *d_pk32 = nullptr, *d_pkm1_32 = nullptr;   // FP32 copies of psi_k and of the next psi (mixed update)
     int *d_tc_err = nullptr;         // set by a tensor-core kernel whose mbarrier wait ran out
+    int *h_flag = nullptr;           // pinned copy of it, read in the context's stream
     // optional per-stage event timing (mw3_profile)
     bool prof = false;
     std::vector<cudaEvent_t> prof_ev;    // (MW3_NSTAGES+1) events per recorded iteration
