@@ -393,6 +393,20 @@ def run_gpu(args, rank, world, local):
         achieved = work / t_launch / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic, "kernel": dom, "peak_source": src}
+    # the whole iteration against HBM (the fused ideal's bytes: psi_k-1 and psi_k
+    # read, psi_k+1 written, the V rows a state's Omega blocks share) and the angular
+    # DVR <-> basis transforms as tensor work (dense contractions over the rectangles,
+    # split products counted once), as the hot-path scope defines them
+    b_iter = sum(r.ntot * 8.0 * (3.0 + r.nelec / max(1.0, r.ncan / r.nelec)) for r in runs)
+    i0 = runs[0].inp
+    f_ang = 4.0 * sum(r.ncan for r in runs) * i0.npun1 * i0.npun2 * float(i0.nangu) ** 2
+    t_ang = (stages.get("angular", 0.0) + stages.get("angular_l2", 0.0)) / max(nrec, 1) * 1e-3
+    scope = {
+        "iteration_hbm": {"bytes": b_iter, "achieved": b_iter / (ms_step * 1e-3) / 1e9, "peak": hbm,
+                          "unit": "GB/s", "frac": b_iter / (ms_step * 1e-3) / 1e9 / hbm},
+        "angular_tensor": {"flop": f_ang, "achieved": f_ang / t_ang / 1e12 if t_ang > 0 else None, "peak": tf,
+                           "unit": "TFLOP/s", "frac": f_ang / t_ang / 1e12 / tf if t_ang > 0 else None},
+    }
     out = {
         "metric": metric_name(), "value": value, "unit": "grid-pt*iter/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -417,6 +431,7 @@ def run_gpu(args, rank, world, local):
         "gpu_launches": launches,
         "stages_ms_per_step": {k: v / max(nrec, 1) for k, v in stages.items()},
         "roofline": roof,
+        "scope_rooflines": scope,
         "clocks": clk,
     }
     out["config"]["kernels"] = out_kernels
