@@ -214,6 +214,7 @@ int mw3_kernel_launches(mw3_ctx *ctx, int64_t *count);
 #define MW3_PATH_TC_ANG 2
 #define MW3_PATH_TC_DST_FUSED 4   /* the whole radial DST chain in one kernel per (block, angle) */
 #define MW3_PATH_DST_F16 8        /* the fused chain as split-FP16 products (MW3_DST_TF32=1 selects 3xTF32) */
+#define MW3_PATH_X_T 16           /* the FP32 rectangle stored [R][r1] (MW3_X_T=1; default [r1][R]) */
 int mw3_path_flags(mw3_ctx *ctx, int32_t *flags);
 
 /* The CUDA stream (cudaStream_t) all device work of the context runs on, for

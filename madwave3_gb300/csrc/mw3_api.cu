@@ -1433,7 +1433,7 @@ int mw3_path_flags(mw3_ctx *h, int32_t *flags)
     }
     *flags = ((mw3::tc_dst_supported(c) || c.use_tc_dst2d) ? MW3_PATH_TC_DST : 0) |
              (c.use_tc_dst2d ? MW3_PATH_TC_DST_FUSED : 0) | (c.use_tc_ang ? MW3_PATH_TC_ANG : 0) |
-             ((c.use_tc_dst2d && c.dst_f16) ? MW3_PATH_DST_F16 : 0);
+             ((c.use_tc_dst2d && c.dst_f16) ? MW3_PATH_DST_F16 : 0) | (c.x_t ? MW3_PATH_X_T : 0);
     return MW3_OK;
 }
 

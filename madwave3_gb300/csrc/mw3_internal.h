@@ -289,6 +289,10 @@ struct Ctx {
     // the split-FP16 form of the fused DST (default; MW3_DST_TF32=1 keeps the 3xTF32 one):
     // the same planes as FP16 hi/lo x 2^12 in chunks of 32, each slab's largest |X|
     bool dst_f16 = false;
+    // the mixed rectangle transposed, [G][na][n2][n1] (r1 fastest): the update and the
+    // scatter then store it along the stored points' r1 runs (coalesced); only with
+    // the split-FP16 fused DST and the factorised angular contraction, on request
+    bool x_t = false;
     void *d_dst_planes16 = nullptr, *d_dst_s2fold16 = nullptr;
     int64_t *d_dst_s1off16 = nullptr;
     unsigned *d_xmax = nullptr;      // [G na], written by the scatter and update kernels
@@ -319,6 +323,7 @@ struct DevGrid {
     const int *mapT;
     const int64_t *foff;
     const int *blk_wave, *blk_elec, *blk_om;
+    int xt;                          // rectangle layout: 0 [..][r1][R], 1 [..][R][r1]
 };
 
 inline DevGrid devgrid(Ctx &c)
@@ -328,6 +333,7 @@ inline DevGrid devgrid(Ctx &c)
     d.indr1 = c.d_indr1; d.indr2 = c.d_indr2; d.npunreal = c.d_npunreal; d.vvv = c.d_vvv;
     d.map = c.d_map; d.mapT = c.d_mapT; d.foff = c.d_foff;
     d.blk_wave = c.d_blk_wave; d.blk_elec = c.d_blk_elec; d.blk_om = c.d_blk_om;
+    d.xt = c.x_t ? 1 : 0;
     return d;
 }
 
@@ -336,8 +342,8 @@ bool tc_dst_supported(Ctx &c);
 void launch_tc_dst(Ctx &c, const float *X, float *Y, double *H, int g_begin, int g_end, int stage_base);
 // tensor-core angular terms of the mixed path (mw3_tc_ang.cu); sets c.use_tc_ang
 int build_tc_ang(Ctx &c);
-void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end);
-void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end);
+void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end, bool xt);
+void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end, bool xt);
 // fused tensor-core radial DSTs of the mixed path (mw3_tc_dst2d.cu); sets c.use_tc_dst2d
 int build_tc_dst2d(Ctx &c);
 // true when the environment asks for the general (indexed) tables even where the

@@ -52,7 +52,7 @@ __global__ void k_scatter(DevGrid d, T *__restrict__ X, const double *__restrict
         int ir2 = d.indr2[(size_t)a * d.npt + ir] - 1;
         const double v = psi[off + ir];
         const T x = rect_value<T>(v);
-        base[(size_t)ir1 * d.n2 + ir2] = x;
+        base[d.xt ? (size_t)ir2 * d.n1 + ir1 : (size_t)ir1 * d.n2 + ir2] = x;
         m = fmaxf(m, fabsf((float)x));
         if (psi32) psi32[off + ir] = rect_value<float>(v);
     }
@@ -751,7 +751,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
                 double rhn = (hv[k] - emin * pk[k]) / u.delta2;
                 nv = (2.0 * rhn - fab * p1[k]) * fab;
             }
-            rect[(size_t)r1[k] * n2 + r2[k]] = (T)nv;
+            rect[d.xt ? (size_t)r2[k] * n1 + r1[k] : (size_t)r1[k] * n2 + r2[k]] = (T)nv;
             nrm += nv * nv;
             outp[ir] = nv;
             if (zf) upd_fe(u, zf, w, wst, wlen, off + ir, nv);
@@ -803,7 +803,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
                 }
             }
             float nf = f64_to_f32_int(nv);
-            rect[(size_t)r1[k] * n2 + r2[k]] = (T)nf;
+            // with the transposed rectangle a warp's points (an r1 run) store contiguously
+            rect[d.xt ? (size_t)r2[k] * n1 + r1[k] : (size_t)r1[k] * n2 + r2[k]] = (T)nf;
             o32[ir] = nf;
             nrmf = fmaf(nf, nf, nrmf);
             xmf = fmaxf(xmf, fabsf(nf));
@@ -1519,7 +1520,7 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
         LAUNCH_CHECK(c);
         stage_mark(c, 3);
         if (c.use_tc_ang) {
-            launch_tc_ang(c, (const float *)c.d_X, c.d_h32, g_begin, g_end);
+            launch_tc_ang(c, (const float *)c.d_X, c.d_h32, g_begin, g_end, c.x_t);
             stage_mark(c, 4);
             return;
         }
@@ -1566,7 +1567,7 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
     // 4. angular kinetic terms
     if (sizeof(T) == 4 && c.use_tc_ang) {
         // mixed path: j^2 + l^2 + Coriolis in one factorised tensor-core contraction
-        launch_tc_ang(c, (const float *)c.d_X, c.d_h, g_begin, g_end);
+        launch_tc_ang(c, (const float *)c.d_X, c.d_h, g_begin, g_end, c.x_t);
         stage_mark(c, 4);
     } else if (c.na > 1) {
         dim3 gj(c.ncj, c.n1, ng);
@@ -2073,6 +2074,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     const double *P = psi - t.flat0;
     double *H = hpsi - t.flat0;
     DevGrid d = devgrid(c);
+    d.xt = 0;                                  // the scratch rectangle keeps [r1][R]
     k_scatter<T><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, X, P, nullptr, g0 * na, nullptr);
     LAUNCH_CHECK(c);
     constexpr int BM = RowCfg<T>::BM, BN = RowCfg<T>::BN;
@@ -2098,7 +2100,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
     k_quirk<double><<<ng * na, 128, 0, c.stream>>>(d, P, H, c.d_quirk_ptr, c.d_quirk, g0 * na);
     LAUNCH_CHECK(c);
     if (sizeof(T) == 4 && c.use_tc_ang) {
-        launch_tc_ang(c, (const float *)X, H, g0, g1);
+        launch_tc_ang(c, (const float *)X, H, g0, g1, false);   // its own scratch, [r1][R]
     } else if (na > 1) {
         dim3 gj(c.ncj, n1, ng);
         k_ang_j<T><<<gj, 256, angj_smem(c, sizeof(T)), c.stream>>>(d, X, (const T *)c.d_xj2, H, c.d_tj_ptr, c.d_tj,

@@ -55,6 +55,7 @@ struct AngArgs {
     const int *blk_om, *map;
     const int64_t *foff;
     int na, n1, n2, chain0;
+    int xt;                      // rectangle layout: 0 [g][a][r1][R], 1 [g][a][R][r1]
     int *err;
 };
 
@@ -62,8 +63,21 @@ struct AngArgs {
 // The tile arrives by asynchronous 4-byte copies straight into the lo plane at
 // each element's operand position (zero outside the grid and beyond the angles),
 // issued as soon as the operand space is free; later each thread splits its own
-// elements into the hi and lo planes in place.  A quarter warp takes 8
-// consecutive R of one r1 row: one 32-byte sector per angle in global memory.
+// elements into the hi and lo planes in place.  In the [r1][R] layout a quarter
+// warp takes 8 consecutive R of one r1 row (one 32-byte sector per angle), in the
+// [R][r1] layout a half warp takes the 16 r1 of one R row (64 bytes per angle).
+__device__ __forceinline__ void ang_elem(int e, int xt, int &r1o, int &r2o, int &kg)
+{
+    if (xt) {
+        r1o = e & 15;
+        r2o = (e >> 4) & 7;
+    } else {
+        r2o = e & 7;
+        r1o = (e >> 3) & 15;
+    }
+    kg = e >> 7;
+}
+
 template <typename HT>
 __device__ __forceinline__ void ang_copy_x(const AngArgs<HT> &p, int g, int r1_0, int r2_0, unsigned char *lo)
 {
@@ -72,7 +86,8 @@ __device__ __forceinline__ void ang_copy_x(const AngArgs<HT> &p, int g, int r1_0
 #pragma unroll
     for (int it = 0; it < 8; it++) {
         const int e = threadIdx.x + 256 * it;
-        const int r2o = e & 7, r1o = (e >> 3) & 15, kg = e >> 7;
+        int r1o, r2o, kg;
+        ang_elem(e, p.xt, r1o, r2o, kg);
         const int gr1 = r1_0 + r1o, gr2 = r2_0 + r2o;
         const bool in = gr1 < p.n1 && gr2 < p.n2;
         const uint32_t dst = lo_s + kmaj_off(r1o * 8 + r2o, kg * 4, AG_K);
@@ -80,7 +95,8 @@ __device__ __forceinline__ void ang_copy_x(const AngArgs<HT> &p, int g, int r1_0
         for (int c = 0; c < 4; c++) {
             const int a = kg * 4 + c;
             const bool ok = in && a < p.na;
-            const float *src = ok ? Xg + ((size_t)a * p.n1 + gr1) * p.n2 + gr2 : Xg;
+            const size_t at = p.xt ? ((size_t)a * p.n2 + gr2) * p.n1 + gr1 : ((size_t)a * p.n1 + gr1) * p.n2 + gr2;
+            const float *src = ok ? Xg + at : Xg;
             asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst + 4 * c), "l"(src), "r"(ok ? 4 : 0)
                          : "memory");
         }
@@ -88,14 +104,17 @@ __device__ __forceinline__ void ang_copy_x(const AngArgs<HT> &p, int g, int r1_0
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-// this thread's elements of the copied tile: wait for its copies, split in place
-__device__ __forceinline__ void ang_split_x(unsigned char *hi, unsigned char *lo)
+// this thread's elements of the copied tile (the same assignment as ang_copy_x):
+// wait for its copies, split in place
+__device__ __forceinline__ void ang_split_x(unsigned char *hi, unsigned char *lo, int xt)
 {
     asm volatile("cp.async.wait_all;" ::: "memory");
 #pragma unroll
     for (int it = 0; it < 8; it++) {
         const int e = threadIdx.x + 256 * it;
-        const int m = ((e >> 3) & 15) * 8 + (e & 7), kg = e >> 7;
+        int r1o, r2o, kg;
+        ang_elem(e, xt, r1o, r2o, kg);
+        const int m = r1o * 8 + r2o;
         const uint32_t off = kmaj_off(m, kg * 4, AG_K);
         const float4 x = *reinterpret_cast<const float4 *>(lo + off);
         const float4 h = make_float4(tf32_hi(x.x), tf32_hi(x.y), tf32_hi(x.z), tf32_hi(x.w));
@@ -171,9 +190,17 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
         // row), and this block's j-basis rows into L1 for the scaling below
         if (pos + 2 < L) {
             const float *Xn = p.X + (size_t)p.chain[cb + pos + 2] * na * n1 * n2;
-            for (int e = threadIdx.x; e < na * AG_R1; e += blockDim.x) {
-                int a = e >> 4, gr1 = r1_0 + (e & 15);
-                if (gr1 < n1) asm volatile("prefetch.global.L2 [%0];" ::"l"(Xn + ((size_t)a * n1 + gr1) * n2 + r2_0));
+            if (p.xt) {
+                for (int e = threadIdx.x; e < na * AG_R2; e += blockDim.x) {
+                    int a = e >> 3, gr2 = r2_0 + (e & 7);
+                    if (gr2 < n2) asm volatile("prefetch.global.L2 [%0];" ::"l"(Xn + ((size_t)a * n2 + gr2) * n1 + r1_0));
+                }
+            } else {
+                for (int e = threadIdx.x; e < na * AG_R1; e += blockDim.x) {
+                    int a = e >> 4, gr1 = r1_0 + (e & 15);
+                    if (gr1 < n1)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(Xn + ((size_t)a * n1 + gr1) * n2 + r2_0));
+                }
             }
         }
         if (pos >= 0) {
@@ -196,7 +223,7 @@ __global__ void __launch_bounds__(256, 2) k_tc_ang(AngArgs<HT> p)
                 bulk_g2s(DS, p.dfw + (size_t)gn * 2 * 64 * AG_K, 2 * AG_DPLANE, &bars[0]);
                 copy_out = true;
             }
-            ang_split_x(AS, AS + AG_APLANE);
+            ang_split_x(AS, AS + AG_APLANE, p.xt);
             fence_async_smem();
             fence_before_sync();
             if (__syncthreads_or(bad)) break;
@@ -491,7 +518,7 @@ int build_tc_ang(Ctx &c)
 
 // blocks [g_begin, g_end) must be whole waves
 template <typename HT>
-static void tc_ang_launch(Ctx &c, const float *X, HT *H, int g_begin, int g_end)
+static void tc_ang_launch(Ctx &c, const float *X, HT *H, int g_begin, int g_end, bool xt)
 {
     using namespace tc;
     static bool attr = false;
@@ -517,19 +544,20 @@ static void tc_ang_launch(Ctx &c, const float *X, HT *H, int g_begin, int g_end)
     p.chain_ptr = c.d_ang_chain_ptr; p.chain = c.d_ang_chain; p.tiles = c.d_ang_tiles;
     p.blk_om = c.d_blk_om; p.map = c.d_map; p.foff = c.d_foff;
     p.na = c.na; p.n1 = c.n1; p.n2 = c.n2; p.chain0 = ch0;
+    p.xt = xt ? 1 : 0;
     p.err = c.d_tc_err;
     k_tc_ang<HT><<<dim3(c.ang_ntiles, nch), 256, smem, c.stream>>>(p);
     c.launches++;
 }
 
-void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end)
+void launch_tc_ang(Ctx &c, const float *X, double *H, int g_begin, int g_end, bool xt)
 {
-    tc_ang_launch<double>(c, X, H, g_begin, g_end);
+    tc_ang_launch<double>(c, X, H, g_begin, g_end, xt);
 }
 
-void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end)
+void launch_tc_ang(Ctx &c, const float *X, float *H, int g_begin, int g_end, bool xt)
 {
-    tc_ang_launch<float>(c, X, H, g_begin, g_end);
+    tc_ang_launch<float>(c, X, H, g_begin, g_end, xt);
 }
 
 }  // namespace mw3

@@ -647,6 +647,7 @@ struct Dst2hArgs {
     const __half *s2fold;         // [parity][H_NKH][hi, lo] x 2^12
     const __half *s1planes;       // S1 of each length, H_NKH chunks of 32 columns, x 2^12
     unsigned *xmax;               // [G na]: bits of the slab's largest |X|, cleared here
+    int xt;                       // rectangle layout: 0 [..][r1][R], 1 [..][R][r1] (the tensor map's)
 };
 
 __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, const __grid_constant__ CUtensorMap xmap)
@@ -709,17 +710,30 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                 const __half *src = alongR ? P.s2fold + (size_t)(par * H_NKH + jc) * H_CHUNK
                                            : S1p + (size_t)jc * H_CHUNK;
                 if (gi == 0) {
-                    // the 64 R columns of this K chunk (both parities), two 32-column tiles
-                    // behind the S2 chunk; each parity's stage gets its own copy
+                    // the 64 R of this K chunk (both parities) behind the S2 chunk: two
+                    // 32-R x 128-r1 tiles, or with the transposed rectangle four 32-r1 x
+                    // 64-R tiles; each parity's stage gets its own copy
                     mbar_expect_tx(&xfull[s], 2 * H_XT);
-                    tma_load_2d(st + 16384, &xmap, 64 * jc, seg * n1, &xfull[s]);
-                    tma_load_2d(st + 32768, &xmap, 64 * jc + 32, seg * n1, &xfull[s]);
+                    if (P.xt) {
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            tma_load_2d(st + 16384 + q * 8192, &xmap, 32 * q, seg * n2 + 64 * jc, &xfull[s]);
+                    } else {
+                        tma_load_2d(st + 16384, &xmap, 64 * jc, seg * n1, &xfull[s]);
+                        tma_load_2d(st + 32768, &xmap, 64 * jc + 32, seg * n1, &xfull[s]);
+                    }
                 }
                 mbar_expect_tx(&full[s], H_SMALL);
                 bulk_g2s(alongR ? st : st + H_SMALL_AT, src, H_SMALL, &full[s]);
                 copies = t + 1;
-                if (t == 2 * nkh - 1 && nxt < (int)gridDim.x)
-                    for (int j = 0; j < 2 * nkh; j++) tma_prefetch_2d(&xmap, 32 * j, (seg + p.wave) * n1);
+                if (t == 2 * nkh - 1 && nxt < (int)gridDim.x) {
+                    if (P.xt) {
+                        for (int j = 0; j < nkh; j++)
+                            for (int q = 0; q < 4; q++) tma_prefetch_2d(&xmap, 32 * q, (seg + p.wave) * n2 + 64 * j);
+                    } else {
+                        for (int j = 0; j < 2 * nkh; j++) tma_prefetch_2d(&xmap, 32 * j, (seg + p.wave) * n1);
+                    }
+                }
             });
     } else if (warp == D2_MMA_WARP) {
         if (lane == 0) {
@@ -859,14 +873,29 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                 // of 8 j) reads 16 consecutive R columns of its row from one 32-column tile
                 d2_wait(&xfull[s], ph, fail);
                 const int e = threadIdx.x, rest = e >> 3, kg = rest & 3, r = (rest >> 2) * 8 + (e & 7);
-                const unsigned char *row = st + 16384 + (kg >> 1) * H_XT + r * 128;
-                const int q0 = (kg & 1) * 4;
                 float v[8];
+                if (P.xt) {
+                    // tile q = r / 32 holds rows R' < 64 of the chunk, column r % 32, under the
+                    // 128-byte swizzle (16-byte granule ^ row % 8); R past npun2 (the next
+                    // slab's rows, or the tensor's end) is zero
+                    const unsigned char *tile = st + 16384 + (r >> 5) * 8192;
+                    const int c = r & 31;
 #pragma unroll
-                for (int qq = 0; qq < 4; qq++) {
-                    const float4 x = *reinterpret_cast<const float4 *>(row + (((q0 + qq) ^ (r & 7)) << 4));
-                    v[2 * qq] = (par == 0 ? x.x : x.y) * sx;
-                    v[2 * qq + 1] = (par == 0 ? x.z : x.w) * sx;
+                    for (int i = 0; i < 8; i++) {
+                        const int R = 16 * kg + 2 * i + par;
+                        const float x = *reinterpret_cast<const float *>(
+                            tile + R * 128 + ((((c >> 2) ^ (R & 7)) << 4) | ((c & 3) << 2)));
+                        v[i] = 64 * jc + R < n2 ? x * sx : 0.f;
+                    }
+                } else {
+                    const unsigned char *row = st + 16384 + (kg >> 1) * H_XT + r * 128;
+                    const int q0 = (kg & 1) * 4;
+#pragma unroll
+                    for (int qq = 0; qq < 4; qq++) {
+                        const float4 x = *reinterpret_cast<const float4 *>(row + (((q0 + qq) ^ (r & 7)) << 4));
+                        v[2 * qq] = (par == 0 ? x.x : x.y) * sx;
+                        v[2 * qq + 1] = (par == 0 ? x.z : x.w) * sx;
+                    }
                 }
                 if (r >= nn) {
 #pragma unroll
@@ -1122,10 +1151,19 @@ int encode_tc_dst2d_xmap(Ctx &c)
         c.err = "cuTensorMapEncodeTiled is not available";
         return MW3_ERR_CUDA;
     }
-    // rows: every r1 line of every slab, [G * na * n1]; columns: R, [n2]; box 32 x 128
-    const cuuint64_t dims[2] = {(cuuint64_t)c.n2, (cuuint64_t)c.G * c.na * c.n1};
-    const cuuint64_t strides[1] = {(cuuint64_t)c.n2 * sizeof(float)};
-    const cuuint32_t box[2] = {32, 128}, es[2] = {1, 1};
+    // [..][r1][R]: rows every r1 line of every slab, [G * na * n1], columns R, [n2], box
+    // 32 x 128; transposed [..][R][r1] (MW3_X_T=1): rows every R line, [G * na * n2],
+    // columns r1, [n1], box 32 x 64 (the first product's 64 R of a K chunk, 32 r1 a
+    // box).  The transposed layout coalesces the update's rectangle stores (1.47 ->
+    // 1.26 ms on the J = 0..40 sweep) but the angular kernel's tile copies, with the
+    // lanes along r1, land 16 lanes on one shared-memory bank (2.05 -> 3.15 ms), so it
+    // is not the default
+    const char *xt = std::getenv("MW3_X_T");
+    c.x_t = c.dst_f16 && c.use_tc_ang && c.n1 % 4 == 0 && c.n1 >= 32 && xt && xt[0] == '1';
+    const cuuint64_t dims[2] = {(cuuint64_t)(c.x_t ? c.n1 : c.n2),
+                                (cuuint64_t)c.G * c.na * (c.x_t ? c.n2 : c.n1)};
+    const cuuint64_t strides[1] = {(cuuint64_t)(c.x_t ? c.n1 : c.n2) * sizeof(float)};
+    const cuuint32_t box[2] = {32, c.x_t ? 64u : 128u}, es[2] = {1, 1};
     CUtensorMap m;
     CUresult r = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn)(
         &m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, c.d_X, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -1177,6 +1215,7 @@ void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end)
         P.s1planes = static_cast<const __half *>(c.d_dst_planes16);
         P.b.s1off = c.d_dst_s1off16;
         P.xmax = c.d_xmax;
+        P.xt = c.x_t ? 1 : 0;
         k_tc_dst2d_h<<<nseg, D2_WARPS * 32, smem, c.stream>>>(P, xmap);
     } else {
         k_tc_dst2d<<<nseg, D2_WARPS * 32, smem, c.stream>>>(p, xmap);

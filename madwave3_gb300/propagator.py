@@ -442,7 +442,7 @@ class Propagator:
         f = ct.c_int32()
         self._check(self.L.mw3_path_flags(self.h, ct.byref(f)), "mw3_path_flags")
         return {"tc_dst": bool(f.value & 1), "tc_dst_fused": bool(f.value & 4), "tc_angular": bool(f.value & 2),
-                "dst_f16": bool(f.value & 8)}
+                "dst_f16": bool(f.value & 8), "x_transposed": bool(f.value & 16)}
 
     def stream(self):
         """cudaStream_t of the context, as an integer handle."""

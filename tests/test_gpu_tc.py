@@ -139,3 +139,34 @@ def test_state_all_round_trip(runs):
     p.run(7)
     assert np.array_equal(p.state_all()[1], ref)
     p.close()
+
+
+def test_transposed_rectangle_bit_identical(tmp_path, monkeypatch):
+    """The FP32 rectangle stored [R][r1] (MW3_X_T=1: the update's stores coalesced
+    along the stored points' r1 runs; the fused DST and the angular kernel read it
+    that way) propagates bit for bit like the default [r1][R] layout: the same
+    values reach the same operand positions."""
+    import os
+    from madwave3_gb300 import Propagator
+    from madwave3_gb300.host import generator, setup
+
+    d = str(tmp_path / "xt")
+    generator.write_case(d, npun2=64, npun1=48, nangu=12, jmax=8, nvmax=2, netot=32, npun1min=8,
+                         Jtot=2, iommax=2)
+    run = setup.load(os.path.join(d, "input.dat"))
+    out = {}
+    for rect in ("0", "1"):
+        monkeypatch.setenv("MW3_X_T", rect)
+        p = Propagator(run, "mixed")
+        p.start()
+        path = p.path()
+        assert path["tc_dst_fused"] and path["tc_angular"], path
+        assert path["x_transposed"] == (rect == "1"), path
+        p.run(40)
+        out[rect] = (p.state()[1].copy(), p.norms().copy())
+        psi = np.random.default_rng(48).uniform(-1.0, 1.0, run.ntot)
+        out[rect + "h"] = p.hphi(psi)
+        p.close()
+    assert np.array_equal(out["0"][0], out["1"][0])
+    assert np.array_equal(out["0"][1], out["1"][1])
+    assert np.array_equal(out["0h"], out["1h"])
