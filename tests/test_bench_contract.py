@@ -43,3 +43,70 @@ def test_timed_window_alignment():
                 assert (it0 + steps) % 32 == 31
             # the window holds an iteration that is 31 mod 32
             assert any((it0 + j) % 32 == 31 for j in range(1, steps + 1))
+
+
+def test_end_to_end_leg_drives_every_context(monkeypatch):
+    """run_e2e splits the waves over the contexts (every wave exactly once), each
+    context's thread uploads psi_k, runs one iteration and downloads psi_k+1
+    every step with the iteration counting on, and an error in a context's
+    thread reaches the caller (a fake binding: no GPU)."""
+    import threading
+    import types
+
+    import numpy as np
+    import pytest
+
+    sys.path.insert(0, ROOT)
+    import bench
+    import madwave3_gb300
+
+    torch = pytest.importorskip("torch")
+    monkeypatch.setattr(torch.Tensor, "pin_memory", lambda self: self)
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda: None)
+    log, lock = [], threading.Lock()
+
+    class FakeProp:
+        fail_on = None
+
+        def __init__(self, runs, precision):
+            self.waves = [r.name for r in runs]
+            self.n = sum(r.ntot for r in runs)
+            self.it = 1
+
+        def start(self):
+            pass
+
+        def run(self, n):
+            if FakeProp.fail_on in self.waves and n == 1:      # inside the timed loop's thread
+                raise RuntimeError("context of %s failed" % FakeProp.fail_on)
+            self.it += n
+            with lock:
+                log.append(("run", tuple(self.waves), n))
+
+        def state_all(self):
+            return np.zeros(self.n), np.full(self.n, float(self.it)), self.it
+
+        def upload_state_all(self, km1, k, it):
+            assert km1 is None and k.shape == (self.n,) and it == self.it
+            with lock:
+                log.append(("up", tuple(self.waves), it))
+
+        def state_k_all(self, out):
+            out[:] = self.it
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(madwave3_gb300, "Propagator", FakeProp)
+    runs = [types.SimpleNamespace(name="J%d" % j, ntot=100 + 10 * j) for j in range(10)]
+    ms, n = bench.run_e2e(runs, "mixed", 4, 3)
+    assert n == 4 and ms > 0
+    ups = [e for e in log if e[0] == "up"]
+    groups = {e[1] for e in ups}
+    assert sorted(w for g in groups for w in g) == sorted(r.name for r in runs)
+    for g in groups:
+        its = [e[2] for e in ups if e[1] == g]
+        assert its == [its[0], its[0] + 1, its[0] + 2]
+    FakeProp.fail_on = "J3"
+    with pytest.raises(RuntimeError, match="J3"):
+        bench.run_e2e(runs, "mixed", 4, 2)
