@@ -378,6 +378,26 @@ int build_device(Ctx &c)
         std::vector<float> f1(a1.begin(), a1.end()), f2(a2.begin(), a2.end());
         TRY(dupload(c, &c.d_absfr1f, f1));
         TRY(dupload(c, &c.d_absfr2f, f2));
+        // where each wave's absorbers start: the points before both starts have factor
+        // 1 exactly, so the update need not read the tables there; an absorber that is
+        // not a suffix of its axis gets start 0 (always read)
+        const int nw = (int)c.waves.size();
+        std::vector<int> st((size_t)nw * 2, 0);
+        for (int w = 0; w < nw; w++)
+            for (int ax = 0; ax < 2; ax++) {
+                const std::vector<float> &f = ax == 0 ? f1 : f2;
+                const int n = ax == 0 ? n1 : n2;
+                int first = n;
+                for (int i = 0; i < n; i++)
+                    if (f[(size_t)w * n + i] != 1.0f) {
+                        first = i;
+                        break;
+                    }
+                bool suffix = true;
+                for (int i = first; i < n; i++) suffix = suffix && f[(size_t)w * n + i] != 1.0f;
+                st[(size_t)w * 2 + ax] = suffix ? first : 0;
+            }
+        TRY(dupload(c, &c.d_abs_start, st));
     }
     TRY(dupload(c, &c.d_djall, djall));
     TRY(dupload(c, &c.d_djoff, djoff));

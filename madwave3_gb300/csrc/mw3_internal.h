@@ -173,6 +173,7 @@ struct Ctx {
     double *d_p2r1 = nullptr, *d_p2r2 = nullptr;     // [W][na][n1], [W][na][n2]
     double *d_absfr1 = nullptr, *d_absfr2 = nullptr; // [W][n1], [W][n2]
     float *d_absfr1f = nullptr, *d_absfr2f = nullptr; // FP32 copies (mixed update)
+    int *d_abs_start = nullptr;      // [W][2]: first r1 / R index whose FP32 factor is not 1 (0: not a suffix)
     // recursion vectors (context-wide flat layout), H accumulator, norm partials
     double *d_psiA = nullptr, *d_psiB = nullptr;
     double *d_pk = nullptr, *d_pkm1 = nullptr;       // aliases, swapped every iteration

@@ -638,6 +638,7 @@ struct UpdArgs {
     const int *vsrc;               // [G][ne]
     const double *absfr1, *absfr2; // [W][n1], [W][n2]
     const float *absfr1f, *absfr2f; // FP32 copies (mixed path)
+    const int *abs_start;           // [W][2]: first r1 / R index inside an absorber (mixed path)
     double emindlt, delta2;
     double rdelta, r2delta;        // 1/delta2 and 2/delta2 (mixed path)
     const float *vr32;             // mixed path: V 2/delta2 - [same state] emindlt 2/delta2, layout of vvv
@@ -769,6 +770,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
         // written beside the FP64 vectors, the conversions done with integer
         // instructions, the norm in FP32
         const float *vr0 = nsrc > 0 ? u.vr32 + cd.voff : nullptr, *pr0 = nsrc > 0 ? u.pk32 + cd.poff : nullptr;
+        const int as1 = u.abs_start[2 * w], as2 = u.abs_start[2 * w + 1];
         float *__restrict__ o32 = u.out32 + off;
         int r1[U], r2[U];
         float hr[U], v0[U], q0[U];
@@ -796,10 +798,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 3) k_update(DevGrid 
                 nv = f32_to_f64_int(0.5f * t32);
             } else {
                 nv = f32_to_f64_int(t32) - p1[k];
-                const float a1 = u.absfr1f[(size_t)w * n1 + r1[k]], a2 = u.absfr2f[(size_t)w * n2 + r2[k]];
-                if (!(__float_as_uint(a1) == 0x3F800000u && __float_as_uint(a2) == 0x3F800000u)) {
-                    const float f = a1 * a2, p1f = f64_to_f32_int(p1[k]);
-                    nv += f32_to_f64_int(fmaf(f - 1.f, t32, (1.f - f * f) * p1f));
+                // the absorption factors only where a point can be inside an absorber
+                if (r1[k] >= as1 || r2[k] >= as2) {
+                    const float a1 = u.absfr1f[(size_t)w * n1 + r1[k]], a2 = u.absfr2f[(size_t)w * n2 + r2[k]];
+                    if (!(__float_as_uint(a1) == 0x3F800000u && __float_as_uint(a2) == 0x3F800000u)) {
+                        const float f = a1 * a2, p1f = f64_to_f32_int(p1[k]);
+                        nv += f32_to_f64_int(fmaf(f - 1.f, t32, (1.f - f * f) * p1f));
+                    }
                 }
             }
             float nf = f64_to_f32_int(nv);
@@ -1595,6 +1600,7 @@ void launch_update(Ctx &c, int first)
     u.absfr1 = c.d_absfr1;
     u.absfr2 = c.d_absfr2;
     u.absfr1f = c.d_absfr1f;
+    u.abs_start = c.d_abs_start;
     u.absfr2f = c.d_absfr2f;
     u.emindlt = c.grid.emindlt;
     u.delta2 = c.grid.delta2;
