@@ -103,6 +103,7 @@ DEFAULT = dict(
     shifts_ev=(0.0, 0.8, 1.5), coupling_ev=0.05, coupling_width_bohr=0.5,
     absorb_strength=10.0,
     iphoto=0,
+    lambdas=None,        # Omega_diatom (Lambda) of each electronic state; None: all 0
 )
 
 
@@ -302,8 +303,9 @@ def write_pot(outdir, p):
         maxpoint += len(i1)
     with open(os.path.join(outdir, "pot", "cont.pot"), "w") as f:
         f.write("%d\n" % ne)
+        lam = p.get("lambdas") or (0,) * ne
         for e in range(ne):
-            f.write("0 0 1.0 1.0\n")
+            f.write("%d 0 1.0 1.0\n" % lam[e])
         f.write("%r %d %r\n" % (vmin, maxpoint, vmaxtot))
         f.write("%r %r %d\n" % (p["rmis1"], p["rfin1"], n1))
         f.write("%r %r %d\n" % (p["rmis2"], p["rfin2"], n2))
@@ -329,6 +331,11 @@ CASES = {
     "tiny_e2": dict(npun2=36, npun1=20, nangu=8, jmax=5, nvmax=2, netot=48, npun1min=8,
                     nelecmax=2, Jtot=1, iommax=1, iparity=-1, alpha0_bohr=1.2, shifts_ev=(0.0, 0.3), coupling_ev=0.2,
                     coupling_width_bohr=1.5),
+    # two coupled states with Lambda = 0 and 1 (same sigma), J = 2, Omega = 0..2: the
+    # channels of equal Omega couple through the electronic Coriolis term
+    "tiny_ecor": dict(npun2=36, npun1=20, nangu=8, jmax=5, nvmax=2, netot=48, npun1min=8,
+                      nelecmax=2, lambdas=(0, 1), Jtot=2, iommax=2, iparity=1, alpha0_bohr=1.2,
+                      shifts_ev=(0.0, 0.3), coupling_ev=0.2, coupling_width_bohr=1.5),
 }
 
 

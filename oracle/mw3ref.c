@@ -336,6 +336,8 @@ struct mw3ref {
     /* kinetic tables */
     double *xj2;              /* [ncan][jang][iang][npun1] */
     double *xl2p;             /* [3][ncan][jang][iang][npun2]   (q+1) */
+    int ecor;                 /* electronic Coriolis variant (mod_Hphi_eCoriolis_01y2.f) */
+    double *xj2e;             /* [ncan src][ncan dst][jang][iang][npun1], ecor only */
     /* absorption */
     double *absfr1, *absfr2;
     int ir1abs, ir2abs;
@@ -454,6 +456,70 @@ static void angkinj2(mw3ref *r)
                 }
             }
         }
+    }
+}
+
+/* The channel-pair j^2 matrices of the electronic Coriolis variant: angkinj2 of
+   mod_Hphi_eCoriolis_01y2.f:186-324 fills xj2(ir1,i,jp,icanp,jcanp) for every
+   pair of channels; the diagonal pairs equal the plain xj2 above, and difs reads
+   the off-diagonal ones only for equal Omega and |Lambda - Lambda'| = 1
+   (:901-911).  Those come from the second branch of its xkinj (:249-258):
+   same j at the same basis index k, same sigma, |Lambda - Lambda'| = 1,
+   xkinj(k,k) = sqrt(L^2 + L'^2) sqrt(j(j+1) - |L L'|) hbar^2, times sqrt(2)
+   when either Lambda is 0; transformed with the source channel's Djmmp on
+   both sides (:270-285).  Its third branch (different sigma, equal Lambda)
+   fills pairs difs never reads and is not restated. */
+static void angkinj2_ecor(mw3ref *r)
+{
+    const mw3ref_in *in = &r->in;
+    int na = r->na, n1 = r->n1, nc = r->nc;
+    memset(r->xj2e, 0, sizeof(double) * (size_t)nc * nc * na * na * n1);
+    if (na <= 1) return;
+    int jjjmax = (na - 1) * in->inc;
+    for (int bd = 0; bd < nc; bd++) {                 /* jcanp */
+        int jelec = in->nelebas[bd], jom = in->iombas[bd];
+        int jomdi = in->iomdiat[jelec - 1];
+        for (int b = 0; b < nc; b++) {                /* icanp */
+            if (b == bd) continue;
+            int ielec = in->nelebas[b], iom = in->iombas[b];
+            int iomdi = in->iomdiat[ielec - 1];
+            if (iom != jom || in->sigdiat[ielec - 1] != in->sigdiat[jelec - 1]) continue;
+            if (abs(jomdi - iomdi) != 1) continue;
+            const int32_t *jb = in->jbas + (size_t)b * na, *jbd = in->jbas + (size_t)bd * na;
+            int nk = in->nojbas[b] < in->nojbas[bd] ? in->nojbas[b] : in->nojbas[bd];
+            for (int ir1 = 1; ir1 <= n1; ir1++) {
+                double r1 = in->rmis1 + (double)(ir1 - 1) * in->ah1;
+                for (int k = 0; k < nk; k++) {
+                    if (jb[k] != jbd[k] || jb[k] > jjjmax) continue;
+                    double xj = (double)jb[k];
+                    double xlam = sqrt((double)(iomdi * iomdi) + (double)(jomdi * jomdi));
+                    double xom = sqrt(xj * (xj + 1) - (double)abs(jomdi * iomdi));
+                    double xkinj = xlam * xom * in->hbr * in->hbr;
+                    if (jomdi == 0 || iomdi == 0) xkinj = xkinj * sqrt(2.0);
+                    double yyy = xkinj / (in->xm1red * r1 * r1);
+                    if (yyy > in->rotcutmax) yyy = in->rotcutmax;
+                    for (int i = 1; i <= na; i++) {
+                        double x1 = DJV(r, iom, ielec, jb[k], i);
+                        for (int jang = 1; jang <= na; jang++) {
+                            double x2 = DJV(r, iom, ielec, jb[k], jang);
+                            size_t o = ((((size_t)b * nc + bd) * na + (jang - 1)) * na + (i - 1)) * n1 + (ir1 - 1);
+                            r->xj2e[o] = r->xj2e[o] + yyy * x1 * x2;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+void mw3ref_set_ecoriolis(mw3ref *r, int on)
+{
+    r->ecor = on != 0;
+    free(r->xj2e);
+    r->xj2e = NULL;
+    if (r->ecor) {
+        r->xj2e = (double *)malloc(sizeof(double) * (size_t)r->nc * r->nc * r->na * r->na * r->n1);
+        angkinj2_ecor(r);
     }
 }
 
@@ -795,7 +861,7 @@ void mw3ref_destroy(mw3ref *r)
     if (!r) return;
     if (r->caches) { for (int t = 0; t < 256; t++) plan_free(r->caches[t].plans); free(r->caches); }
     free(r->aorder); free(r->offs); free(r->nopr1); free(r->nopr2); free(r->p2r1); free(r->p2r2);
-    free(r->xj2); free(r->xl2p); free(r->absfr1); free(r->absfr2);
+    free(r->xj2); free(r->xl2p); free(r->xj2e); free(r->absfr1); free(r->absfr2);
     free(r->psi_km1); free(r->psi_k); free(r->hpsi); free(r->hproc);
     free(r->psi0);
     free(r->zar1flux); free(r->ir1flux); free(r->fl_ang); free(r->fl_can); free(r->fl_r2); free(r->fl_idx); free(r->potiflux);
@@ -917,8 +983,18 @@ static void difs_source(mw3ref *r, int b, int jang, const double *psi, double *h
         const int32_t *t2 = in->indr2 + (size_t)(iang - 1) * in->npuntot;
         for (int b2 = 0; b2 < nc; b2++) {
             int iom2 = in->iombas[b2], ielec2 = in->nelebas[b2];
-            if (ielec != ielec2) continue;
             int64_t j0 = r->offs[(size_t)(iang - 1) * nc + b2];
+            if (ielec != ielec2) {
+                /* electronic Coriolis coupling (mod_Hphi_eCoriolis_01y2.f:901-911) */
+                if (r->ecor && iom == iom2 && abs(in->iomdiat[ielec - 1] - in->iomdiat[ielec2 - 1]) == 1) {
+                    const double *xj = r->xj2e + ((((size_t)b * nc + b2) * na + (jang - 1)) * na + (iang - 1)) * n1;
+                    for (int ir = 0; ir < npi; ir++) {
+                        int ir1 = t1[ir], ir2 = t2[ir];
+                        hproc[j0 + ir] = hproc[j0 + ir] + rphi0[(size_t)(ir1 - 1) * n2 + (ir2 - 1)] * xj[ir1 - 1];
+                    }
+                }
+                continue;
+            }
             if (iom == iom2) {
                 const double *xj = r->xj2 + (((size_t)b * na + (jang - 1)) * na + (iang - 1)) * n1;
                 const double *xl = r->xl2p + ((((size_t)1 * nc + b) * na + (jang - 1)) * na + (iang - 1)) * n2;

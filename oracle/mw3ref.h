@@ -11,6 +11,8 @@
  *   Tradial            SRC/mod_Hphi_01y2.f:487-620 (noptFFT liboctdyn.f:1033-1117,
  *                      sinmom liboctdyn.f:1004-1031, fftmom liboctdyn.f:1119-1152)
  *   angkinj2           SRC/mod_Hphi_01y2.f:166-311   -> explicit xj2
+ *   angkinj2 (eCoriolis) SRC/mod_Hphi_eCoriolis_01y2.f:186-324 -> channel-pair xj2,
+ *                      applied as in its difs :901-911 (mw3ref_set_ecoriolis)
  *   bfgridl2mat        SRC/mod_Hphi_01y2.f:315-484   -> explicit xl2p (l2mat liboctdyn.f:1944-1990)
  *   difs               SRC/mod_Hphi_01y2.f:623-943   (T, V and j^2+l^2 parts, single process)
  *   ini_absorcion      SRC/mod_absorcion_01y2.f:28-107
@@ -84,6 +86,7 @@ int64_t mw3ref_ntot(const mw3ref *r);
 void mw3ref_set_threads(mw3ref *r, int nthreads);
 void mw3ref_set_dst_mode(mw3ref *r, int mode);      /* 0 = FFT, 1 = direct sum */
 void mw3ref_set_flux_gate(mw3ref *r, int on);       /* totalflux_k's E > V(flux point) test, default on */
+void mw3ref_set_ecoriolis(mw3ref *r, int on);      /* the electronic Coriolis H (mod_Hphi_eCoriolis_01y2.f), default off */
 double mw3ref_autocorrelation(const mw3ref *r);     /* iphoto >= 1: <psi0|psi_k> of the last iteration */
 
 /* difs: hpsi = H psi (flat reference layout) */

@@ -72,6 +72,7 @@ def lib():
         L.mw3ref_set_threads.argtypes = [ct.c_void_p, ct.c_int]
         L.mw3ref_set_dst_mode.argtypes = [ct.c_void_p, ct.c_int]
         L.mw3ref_set_flux_gate.argtypes = [ct.c_void_p, ct.c_int]
+        L.mw3ref_set_ecoriolis.argtypes = [ct.c_void_p, ct.c_int]
         L.mw3ref_autocorrelation.argtypes = [ct.c_void_p]
         L.mw3ref_autocorrelation.restype = ct.c_double
         for name in ("mw3ref_hphi",):
@@ -149,7 +150,7 @@ def riccati(l, x):
 class Oracle:
     """One partial wave on the CPU oracle, built from a host ``setup.Run``."""
 
-    def __init__(self, run, nofe_energies_ev=None, threads=1, dst_mode=0, flux_gate=True):
+    def __init__(self, run, nofe_energies_ev=None, threads=1, dst_mode=0, flux_gate=True, ecoriolis=False):
         i = run.inp
         self.run = run
         keep = {}
@@ -212,6 +213,8 @@ class Oracle:
         lib().mw3ref_set_threads(h, threads)
         lib().mw3ref_set_dst_mode(h, dst_mode)
         lib().mw3ref_set_flux_gate(h, 1 if flux_gate else 0)
+        if ecoriolis:
+            lib().mw3ref_set_ecoriolis(h, 1)
         self.netot = i.netot
         self.nelec = run.nelec
         self.nj = i.jmax - i.jini + 1
