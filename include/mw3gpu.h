@@ -194,6 +194,16 @@ int mw3_download_cvj_history(mw3_ctx *ctx, int32_t wave_id, int64_t n, double *c
  * context's device tables exist, else MW3_ERR_STATE. */
 int mw3_set_flux_gate(mw3_ctx *ctx, int32_t wave_id, int32_t on);
 
+/* The electronic Coriolis Hamiltonian of the reference's mad3renner build
+ * (SRC/mod_Hphi_eCoriolis_01y2.f, linked in place of mod_Hphi_01y2.f): with
+ * on != 0 the wave's H psi adds the j^2-type coupling between channels of
+ * equal Omega and sigma whose diatomic Lambda (iomdiat) differ by one
+ * (angkinj2 :226-285, difs :901-911); off (the default) is the plain difs.
+ * Replaces linking the eCoriolis module: the same mw3_hphi / mw3_run calls
+ * then apply it.  Call before the context's device tables exist, else
+ * MW3_ERR_STATE. */
+int mw3_set_ecoriolis(mw3_ctx *ctx, int32_t wave_id, int32_t on);
+
 /* apaqini[netot]: the energy distribution |<packet|E>|^2 of the initial
  * collision packet that Smatini_col computes (SRC/mod_flux_01y2.f:467-524) and
  * the reference keeps in mod_flux for its normalisations -- ini_transcoor's

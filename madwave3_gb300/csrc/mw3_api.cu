@@ -143,9 +143,19 @@ int build_typed(Ctx &c)
     TRY(dalloc(c, &y, rect));
     c.d_X = x;
     c.d_Y = y;
+    // channel-pair j^2 matrices of the electronic Coriolis variant (every path)
+    c.d_xj2e = nullptr;
+    if (c.ec_pairs > 0) {
+        T *xe;
+        TRY(dalloc(c, &xe, (size_t)c.ec_pairs * n1 * na * na));
+        c.d_xj2e = xe;
+    }
     // explicit angular matrices (not needed when the factorised contraction runs)
     c.d_xj2 = c.d_xl2p = nullptr;
-    if (c.use_tc_ang) return MW3_OK;
+    if (c.use_tc_ang) {
+        mw3::launch_build_kinetic<T>(c);
+        return MW3_OK;
+    }
     T *xj2, *xl2p;
     TRY(dalloc(c, &xj2, (size_t)c.G * n1 * na * na));
     TRY(dalloc(c, &xl2p, (size_t)c.G * 3 * n2 * na * na));
@@ -301,6 +311,49 @@ int build_device(Ctx &c)
     TRY(dupload(c, &c.d_wflat0, wflat0));
     TRY(dupload(c, &c.d_wseg0, wseg0));
     TRY(dupload(c, &c.d_wseg1, wseg1));
+    // ---- electronic Coriolis pairs (waves with the variant on) ----
+    {
+        std::vector<int> tg, psrc;
+        std::vector<std::vector<std::pair<int, int>>> srcs;   // per target: (source block, pair)
+        std::vector<double> yall;
+        for (int w = 0; w < W; w++) {
+            const WaveTables &t = c.waves[w];
+            std::vector<int> s, d;
+            std::vector<double> y;
+            ecor_pairs(c, t, s, d, y);
+            for (size_t p = 0; p < s.size(); p++) {
+                int gs = t.g0 + s[p], gd = t.g0 + d[p];
+                if (tg.empty() || tg.back() != gd) {
+                    tg.push_back(gd);
+                    srcs.emplace_back();
+                }
+                srcs.back().emplace_back(gs, (int)psrc.size());
+                psrc.push_back(gs);
+            }
+            yall.insert(yall.end(), y.begin(), y.end());
+        }
+        int slots = 0;
+        for (auto &v : srcs) slots = std::max(slots, (int)v.size());
+        c.ec_nt = (int)tg.size();
+        c.ec_slots = slots;
+        c.ec_pairs = (int)psrc.size();
+        c.h_ec_tgt = tg;
+        c.h_ec_psrc = psrc;
+        c.d_ec_tgt = c.d_ec_src = c.d_ec_mat = nullptr;
+        c.d_ec_y = nullptr;
+        if (c.ec_nt > 0) {
+            std::vector<int> es((size_t)c.ec_nt * slots, -1), em((size_t)c.ec_nt * slots, -1);
+            for (int q = 0; q < c.ec_nt; q++)
+                for (size_t k = 0; k < srcs[q].size(); k++) {
+                    es[(size_t)q * slots + k] = srcs[q][k].first;
+                    em[(size_t)q * slots + k] = srcs[q][k].second;
+                }
+            TRY(dupload(c, &c.d_ec_tgt, tg));
+            TRY(dupload(c, &c.d_ec_src, es));
+            TRY(dupload(c, &c.d_ec_mat, em));
+            TRY(dupload(c, &c.d_ec_y, yall));
+        }
+    }
     // ---- per-wave tables concatenated ----
     std::vector<int> nopr1((size_t)W * na);
     std::vector<double> p2r1((size_t)W * na * n1), p2r2((size_t)W * na * n2), a1((size_t)W * n1),
@@ -1361,6 +1414,22 @@ int mw3_tables(mw3_ctx *h, int32_t w, int32_t *nopr1, double *etot, double *reac
     if (s2factor) std::copy(t.s2factor.begin(), t.s2factor.end(), s2factor);
     if (absfr1) std::copy(t.absfr1.begin(), t.absfr1.end(), absfr1);
     if (absfr2) std::copy(t.absfr2.begin(), t.absfr2.end(), absfr2);
+    return MW3_OK;
+}
+
+int mw3_set_ecoriolis(mw3_ctx *h, int32_t w, int32_t on)
+{
+    if (!h) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (w < 0 || w >= (int)c.waves.size()) {
+        c.err = "mw3_set_ecoriolis: no such wave";
+        return MW3_ERR_ARG;
+    }
+    if (c.built) {
+        c.err = "mw3_set_ecoriolis: call before the device tables exist";
+        return MW3_ERR_STATE;
+    }
+    c.waves[w].ecor = on != 0;
     return MW3_OK;
 }
 

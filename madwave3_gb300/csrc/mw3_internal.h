@@ -62,6 +62,7 @@ struct WaveTables {
     std::vector<int> fl_block;              // block of each flux point
     std::vector<double> potiflux;
     bool flux_gate = true;                  // totalflux_k's E > V(flux point) test
+    bool ecor = false;                      // electronic Coriolis H (mod_Hphi_eCoriolis_01y2.f)
     std::vector<int> fl_dptr;               // CSR over flux points of the r1-derivative terms
     std::vector<int64_t> fl_didx;           // wave-relative flat index of each term
     std::vector<int> fl_dir1;               // ir1 (0-based) of each term
@@ -204,6 +205,15 @@ struct Ctx {
     void *d_xj2 = nullptr;           // [G][n1][na][na]
     void *d_xl2p = nullptr;          // [G][3][n2][na][na]
     std::vector<char> h_slot_used;   // [G][3]
+    // electronic Coriolis coupling of the waves that enable it: the target blocks
+    // (ascending), per target up to ec_slots source blocks (-1: none) and the index of
+    // each source's channel-pair matrix
+    int ec_nt = 0, ec_slots = 0, ec_pairs = 0;
+    std::vector<int> h_ec_tgt;       // [ec_nt]
+    std::vector<int> h_ec_psrc;      // [ec_pairs] source block of each pair
+    int *d_ec_tgt = nullptr, *d_ec_src = nullptr, *d_ec_mat = nullptr;   // [ec_nt], [ec_nt][ec_slots] x2
+    double *d_ec_y = nullptr;        // [ec_pairs][n1][na] j-basis scalars
+    void *d_xj2e = nullptr;          // [ec_pairs][n1][na][na] channel-pair j^2 matrices
     // inputs of the device-side assembly of xj2/xl2p
     int *d_blk_nojb = nullptr, *d_blk_jbas = nullptr;
     double *d_blk_yj2 = nullptr;
@@ -363,6 +373,8 @@ std::vector<double> dst_matrix(int n);
 // setup (mw3_setup.cu)
 // ---------------------------------------------------------------------------
 int build_wave_tables(Ctx &c, const mw3_wave &w, WaveTables &t, std::string &err);
+void ecor_pairs(const Ctx &c, const WaveTables &t, std::vector<int> &src, std::vector<int> &dst,
+                std::vector<double> &y);
 int noptfft(int nin, int ntot);
 void riccati_fg(int l, double x, double *f, double *g);
 

@@ -16,6 +16,7 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "mw3_internal.h"
@@ -580,6 +581,55 @@ __global__ void __launch_bounds__(256) k_ang_j(DevGrid d, const T *__restrict__ 
         for (int j = 0; j < na; j++) acc += Xs[j * ANG_CW + col] * row[j];
         H[t_o[q]] += (double)acc;
     }
+}
+
+// electronic Coriolis coupling (mod_Hphi_eCoriolis_01y2.f:901-911): for each target
+// block t of the list, H(t, a, r1, r2) += sum_s sum_j' X(s, j', r1, r2) xj2e(m, r1, a, j')
+// over its source blocks s (equal Omega, Lambda one apart) with m the pair's matrix;
+// one CTA per (R chunk, r1, target) sums every source before its single update of H
+template <typename T, typename HT>
+__global__ void __launch_bounds__(256) k_ang_je(DevGrid d, const T *__restrict__ X, const T *__restrict__ xj2e,
+                                                HT *__restrict__ H, const int *__restrict__ tptr,
+                                                const int *__restrict__ tlist, int ncj, const int *__restrict__ tgt,
+                                                const int *__restrict__ esrc, const int *__restrict__ emat,
+                                                int nslot, int ANG_CW)
+{
+    extern __shared__ unsigned char smraw[];
+    int chunk = blockIdx.x, ir1 = blockIdx.y, z = blockIdx.z;
+    int b = tptr[ir1 * ncj + chunk], e = tptr[ir1 * ncj + chunk + 1];
+    if (b == e) return;
+    int na = d.na, n1 = d.n1, n2 = d.n2, g = tgt[z];
+    T *acc = reinterpret_cast<T *>(smraw);                     // [e-b]
+    T *Xs = reinterpret_cast<T *>(acc + (na * ANG_CW));         // [na][ANG_CW]
+    T *xs = Xs + (size_t)na * ANG_CW;                           // [na][na+1]
+    int *t_a = reinterpret_cast<int *>(xs + (size_t)na * (na + 1));
+    int *t_c = t_a + na * ANG_CW;
+    long long *t_o = reinterpret_cast<long long *>(t_c + na * ANG_CW);
+    int c0 = chunk * ANG_CW;
+    int nt = e - b;
+    for (int q = threadIdx.x; q < nt; q += blockDim.x) acc[q] = (T)0;
+    stage_targets(d, tlist + b, nt, d.indr2, c0, (size_t)g * na, t_a, t_c, t_o);
+    for (int slot = 0; slot < nslot; slot++) {
+        int s = esrc[z * nslot + slot], m = emat[z * nslot + slot];
+        if (s < 0) continue;
+        __syncthreads();
+        for (int i = threadIdx.x; i < na * ANG_CW; i += blockDim.x) {
+            int j = i / ANG_CW, cc = i % ANG_CW;
+            Xs[i] = (c0 + cc < n2) ? X[(((size_t)s * na + j) * n1 + ir1) * n2 + c0 + cc] : (T)0;
+        }
+        const T *xm = xj2e + ((size_t)m * n1 + ir1) * na * na;
+        for (int i = threadIdx.x; i < na * na; i += blockDim.x) xs[(i / na) * (na + 1) + (i % na)] = xm[i];
+        __syncthreads();
+        for (int q = threadIdx.x; q < nt; q += blockDim.x) {
+            int col = t_c[q];
+            T s_ = (T)0;
+            const T *row = xs + (size_t)t_a[q] * (na + 1);
+            for (int j = 0; j < na; j++) s_ += Xs[j * ANG_CW + col] * row[j];
+            acc[q] += s_;
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nt; q += blockDim.x) H[t_o[q]] += (HT)acc[q];
 }
 
 // l^2 with Omega coupling: H(t, a, r1, r2) += sum_(s,q) sum_j' X(s, j', r1, r2) xl2p(s, q, r2, a, j')
@@ -1430,13 +1480,16 @@ __device__ inline double djget(const KinBuildArgs &k, int w, int iom, int ielec,
     return k.djmmp[k.djoff[w] + (((size_t)iom * k.ne + (ielec - 1)) * (k.wnangu2[w] + 1) + j) * k.na + a];
 }
 
+// xj2[ir1][i][j] = sum_k yj2[ir1][k] D_g(i, j_k) D_g(j, j_k) with block g's basis and
+// Djmmp: the block's own j^2 matrix, or a channel-pair matrix of the electronic
+// Coriolis variant with g its source channel (yj2 then holds the pair's scalars)
 template <typename T>
-__global__ void k_build_xj2(KinBuildArgs k, T *__restrict__ xj2, int g)
+__global__ void k_build_xj2(KinBuildArgs k, const double *__restrict__ yj2, T *__restrict__ xj2, int g)
 {
     int na = k.na;
     int ir1 = blockIdx.x;
     int w = k.blk_wave[g], e = k.blk_elec[g], om = k.blk_om[g];
-    const double *yy = k.yj2 + ((size_t)g * k.n1 + ir1) * na;
+    const double *yy = yj2 + (size_t)ir1 * na;
     for (int ij = threadIdx.x; ij < na * na; ij += blockDim.x) {
         int i = ij / na, j = ij % na;
         double acc = 0.0;
@@ -1445,7 +1498,7 @@ __global__ void k_build_xj2(KinBuildArgs k, T *__restrict__ xj2, int g)
             double x1 = djget(k, w, om, e, jb, i), x2 = djget(k, w, om, e, jb, j);
             acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(yy[q], x1), x2));
         }
-        xj2[((size_t)g * k.n1 + ir1) * na * na + ij] = (T)acc;
+        xj2[(size_t)ir1 * na * na + ij] = (T)acc;
     }
 }
 
@@ -1505,6 +1558,21 @@ static size_t angl_smem(Ctx &c, size_t tsz)
     return tsz * ((size_t)c.na * c.ang_cw + (size_t)c.na * c.ang_cw + (size_t)c.na * (c.na + 1)) + ang_desc(c);
 }
 
+// the electronic Coriolis targets among blocks [g_begin, g_end)
+template <typename T, typename HT>
+static void launch_ecor(Ctx &c, const DevGrid &d, const T *X, HT *H, int g_begin, int g_end)
+{
+    if (c.ec_nt == 0 || !c.d_xj2e || c.na <= 1) return;
+    const long lo = std::lower_bound(c.h_ec_tgt.begin(), c.h_ec_tgt.end(), g_begin) - c.h_ec_tgt.begin();
+    const long hi = std::lower_bound(c.h_ec_tgt.begin(), c.h_ec_tgt.end(), g_end) - c.h_ec_tgt.begin();
+    if (hi <= lo) return;
+    dim3 grid(c.ncj, c.n1, (unsigned)(hi - lo));
+    k_ang_je<T, HT><<<grid, 256, angl_smem(c, sizeof(T)), c.stream>>>(
+        d, X, (const T *)c.d_xj2e, H, c.d_tj_ptr, c.d_tj, c.ncj, c.d_ec_tgt + lo, c.d_ec_src + lo * c.ec_slots,
+        c.d_ec_mat + lo * c.ec_slots, c.ec_slots, c.ang_cw);
+    LAUNCH_CHECK(c);
+}
+
 template <typename T>
 void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
 {
@@ -1526,6 +1594,7 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
         stage_mark(c, 3);
         if (c.use_tc_ang) {
             launch_tc_ang(c, (const float *)c.d_X, c.d_h32, g_begin, g_end, c.x_t);
+            launch_ecor<float, float>(c, d, (const float *)c.d_X, c.d_h32, g_begin, g_end);
             stage_mark(c, 4);
             return;
         }
@@ -1585,6 +1654,7 @@ void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end)
                                                                     c.d_tl_ptr, c.d_tl, c.d_cpl, c.ncl, g_begin, c.ang_cw);
         LAUNCH_CHECK(c);
     }
+    launch_ecor<T, double>(c, d, (const T *)c.d_X, c.d_h, g_begin, g_end);
 }
 
 template <typename T>
@@ -1639,8 +1709,16 @@ void launch_build_kinetic(Ctx &c)
     k.wnangu2 = c.d_wnangu2; k.wj0 = c.d_wj0; k.winc = c.d_winc; k.wiommin = c.d_wiommin;
     k.wiommax = c.d_wiommax; k.wnom = c.d_wnom; k.wnj2 = c.d_wnj2;
     k.l2tab = c.d_l2all; k.l2off = c.d_l2off; k.l2used = c.d_l2used; k.l2uoff = c.d_l2uoff;
+    const size_t mat = (size_t)c.n1 * c.na * c.na;
+    for (int p = 0; p < c.ec_pairs && c.d_xj2e; p++) {
+        k_build_xj2<T><<<c.n1, 256, 0, c.stream>>>(k, c.d_ec_y + (size_t)p * c.n1 * c.na, (T *)c.d_xj2e + p * mat,
+                                                    c.h_ec_psrc[p]);
+        LAUNCH_CHECK(c);
+    }
+    if (!c.d_xj2) return;
     for (int g = 0; g < c.G; g++) {
-        k_build_xj2<T><<<c.n1, 256, 0, c.stream>>>(k, (T *)c.d_xj2, g);
+        k_build_xj2<T><<<c.n1, 256, 0, c.stream>>>(k, c.d_blk_yj2 + (size_t)g * c.n1 * c.na, (T *)c.d_xj2 + g * mat,
+                                                    g);
         LAUNCH_CHECK(c);
         for (int slot = 0; slot < 3; slot++) {
             if (!c.h_slot_used[(size_t)g * 3 + slot]) continue;
@@ -1659,6 +1737,10 @@ void set_kernel_attributes(Ctx &c)
     cudaFuncSetAttribute(k_ang_j<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angj_smem(c, 4));
     cudaFuncSetAttribute(k_ang_l<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 8));
     cudaFuncSetAttribute(k_ang_l<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 4));
+    cudaFuncSetAttribute(k_ang_je<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)angl_smem(c, 8));
+    cudaFuncSetAttribute(k_ang_je<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 4));
+    cudaFuncSetAttribute(k_ang_je<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)angl_smem(c, 4));
 }
 
 bool fit_smem(Ctx &c, size_t optin)
@@ -2117,6 +2199,7 @@ static void noalloc_hphi(Ctx &c, const WaveTables &t, unsigned char *scratch, co
                                                                     c.d_cpl, c.ncl, g0, c.ang_cw);
         LAUNCH_CHECK(c);
     }
+    launch_ecor<T, double>(c, d, (const T *)X, H, g0, g1);
     k_addv<double><<<dim3(ng * na, c.nchunk), 256, 0, c.stream>>>(d, P, H, H, c.d_vsrc, g0 * na);
     LAUNCH_CHECK(c);
     (void)g1;

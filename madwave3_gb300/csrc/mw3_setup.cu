@@ -561,4 +561,53 @@ int build_wave_tables(Ctx &c, const mw3_wave &w, WaveTables &t, std::string &err
     return MW3_OK;
 }
 
+// Channel pairs of the electronic Coriolis variant and their j-basis scalars
+// (angkinj2 of mod_Hphi_eCoriolis_01y2.f:226-285): a source channel b couples to a
+// target b2 of equal Omega and sigma whose diatomic Lambda differs by one, through
+// the basis indices k at which both hold the same j:
+//   y(r1, k) = min(sqrt(L^2 + L'^2) sqrt(j(j+1) - |L L'|) hbar^2 [x sqrt 2 if L or L' is 0]
+//                  / (mu r1^2), rotcutmax),
+// later transformed with the source's Djmmp on both sides.  Pairs are listed
+// target-major; src/dst are wave-local channels, y is [pair][npun1][nangu].
+void ecor_pairs(const Ctx &c, const WaveTables &t, std::vector<int> &src, std::vector<int> &dst,
+                std::vector<double> &y)
+{
+    const mw3_grid &gr = c.grid;
+    int n1 = c.n1, na = c.na, nc = t.ncan;
+    double ah1 = (gr.rfin1 - gr.rmis1) / (double)(n1 - 1);
+    int jjjmax = (na - 1) * t.inc;
+    src.clear();
+    dst.clear();
+    y.clear();
+    if (!t.ecor || na <= 1) return;
+    for (int bd = 0; bd < nc; bd++) {
+        int jelec = t.nelebas[bd], jomdi = t.iomdiat[jelec - 1];
+        for (int b = 0; b < nc; b++) {
+            int ielec = t.nelebas[b], iomdi = t.iomdiat[ielec - 1];
+            if (b == bd || t.iombas[b] != t.iombas[bd]) continue;
+            if (t.sigdiat[ielec - 1] != t.sigdiat[jelec - 1] || std::abs(jomdi - iomdi) != 1) continue;
+            src.push_back(b);
+            dst.push_back(bd);
+            size_t p0 = y.size();
+            y.resize(p0 + (size_t)n1 * na, 0.0);
+            int nk = std::min(t.nojbas[b], t.nojbas[bd]);
+            for (int ir1 = 1; ir1 <= n1; ir1++) {
+                double r1 = gr.rmis1 + (double)(ir1 - 1) * ah1;
+                for (int k = 0; k < nk; k++) {
+                    int jb = t.jbas[(size_t)b * na + k];
+                    if (jb != t.jbas[(size_t)bd * na + k] || jb > jjjmax) continue;
+                    double xj = (double)jb;
+                    double xlam = sqrt((double)(iomdi * iomdi) + (double)(jomdi * jomdi));
+                    double xom = sqrt(xj * (xj + 1) - (double)std::abs(jomdi * iomdi));
+                    double xkinj = xlam * xom * gr.hbr * gr.hbr;
+                    if (jomdi == 0 || iomdi == 0) xkinj = xkinj * sqrt(2.0);
+                    double yyy = xkinj / (gr.xm1red * r1 * r1);
+                    if (yyy > gr.rotcutmax) yyy = gr.rotcutmax;
+                    y[p0 + (size_t)(ir1 - 1) * na + k] = yyy;
+                }
+            }
+        }
+    }
+}
+
 }  // namespace mw3

@@ -1159,7 +1159,7 @@ int encode_tc_dst2d_xmap(Ctx &c)
     // lanes along r1, land 16 lanes on one shared-memory bank (2.05 -> 3.15 ms), so it
     // is not the default
     const char *xt = std::getenv("MW3_X_T");
-    c.x_t = c.dst_f16 && c.use_tc_ang && c.n1 % 4 == 0 && c.n1 >= 32 && xt && xt[0] == '1';
+    c.x_t = c.dst_f16 && c.use_tc_ang && c.ec_nt == 0 && c.n1 % 4 == 0 && c.n1 >= 32 && xt && xt[0] == '1';
     const cuuint64_t dims[2] = {(cuuint64_t)(c.x_t ? c.n1 : c.n2),
                                 (cuuint64_t)c.G * c.na * (c.x_t ? c.n2 : c.n1)};
     const cuuint64_t strides[1] = {(cuuint64_t)(c.x_t ? c.n1 : c.n2) * sizeof(float)};

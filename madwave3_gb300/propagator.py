@@ -70,7 +70,7 @@ HEADER_FUNCS = [
     "mw3_get_stream",
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_set_product_projection", "mw3_download_product",
-    "mw3_cvj_history", "mw3_download_cvj_history", "mw3_set_flux_gate", "mw3_autocorrelation",
+    "mw3_cvj_history", "mw3_download_cvj_history", "mw3_set_flux_gate", "mw3_set_ecoriolis", "mw3_autocorrelation",
     "mw3_upload_accumulators", "mw3_upload_product",
     "mw3_last_error", "mw3_destroy",
 ]
@@ -120,6 +120,7 @@ def load_library(build_if_missing=True):
     L.mw3_cvj_history.argtypes = [vp, ct.c_int64]
     L.mw3_autocorrelation.argtypes = [vp, ct.c_int32, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_set_flux_gate.argtypes = [vp, ct.c_int32, ct.c_int32]
+    L.mw3_set_ecoriolis.argtypes = [vp, ct.c_int32, ct.c_int32]
     L.mw3_download_cvj_history.argtypes = [vp, ct.c_int32, ct.c_int64, F64P, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
     L.mw3_path_flags.argtypes = [vp, ct.POINTER(ct.c_int32)]
@@ -384,6 +385,12 @@ class Propagator:
         """totalflux_k's E > V(flux point) test for the wave (default on; off is
         the earlier form of the routine).  Before the first hphi/start."""
         self._check(self.L.mw3_set_flux_gate(self.h, wave, 1 if on else 0), "mw3_set_flux_gate")
+
+    def set_ecoriolis(self, on, wave=0):
+        """The electronic Coriolis Hamiltonian (mod_Hphi_eCoriolis_01y2.f) for the
+        wave: channels of equal Omega whose Lambda differ by one couple through
+        j^2.  Default off.  Before the first hphi/start."""
+        self._check(self.L.mw3_set_ecoriolis(self.h, wave, 1 if on else 0), "mw3_set_ecoriolis")
 
     def cvj_history(self, capacity):
         """Record Cvj (and Cvjprod) of every iteration in a device ring of

@@ -7,21 +7,17 @@ channels of equal Omega whose diatomic Lambda differ by one (angkinj2
 sigma, J = 2, Omega = 0..2.
 """
 import math
-import os
 
 import numpy as np
 import pytest
 
 from madwave3_gb300.host import constants as C
-from madwave3_gb300.host import generator, setup
 from oracle.mw3ref import Oracle
 
 
 @pytest.fixture(scope="module")
-def ecor_run(tmp_path_factory):
-    d = str(tmp_path_factory.mktemp("ecor") / "tiny_ecor")
-    generator.write_case(d, **generator.CASES["tiny_ecor"])
-    return setup.load(os.path.join(d, "input.dat"))
+def ecor_run(runs):
+    return runs["tiny_ecor"]
 
 
 def ecor_pairs(run):
