@@ -174,6 +174,11 @@ module mw3gpu
        type(c_ptr), value :: ctx
        integer(c_int32_t), value :: wave_id, on
      end function
+     integer(c_int) function mw3_set_ecoriolis(ctx, wave_id, on) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: wave_id, on
+     end function
      integer(c_int) function mw3_packet_energy_norm(ctx, wave_id, apaqini) bind(c)
        import
        type(c_ptr), value :: ctx
