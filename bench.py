@@ -230,7 +230,7 @@ def warmup_count(it_now, warmup, steps):
 E2E_CONTEXTS = (4, 8)
 
 
-def run_e2e(runs, precision, nctx, steps):
+def run_e2e(runs, precision, nctx, steps, choices=None):
     """End to end through the C-ABI with host buffers: the host owns every wave's
     psi_k (pinned) and each step hands it in, runs one iteration and reads the
     new psi_k back (psi_k-1 stays the device's own).  The waves are split over
@@ -249,6 +249,8 @@ def run_e2e(runs, precision, nctx, steps):
         if not part:
             continue
         p = Propagator([runs[i] for i in part], precision)
+        if choices:
+            p.set_choices(choices)
         p.start()
         p.run(RING)
         _, k, it = p.state_all()
@@ -303,6 +305,14 @@ def run_gpu(args, rank, world, local):
         nsto_job = world * nsto_job
     nsto = sum(r.ntot for r in runs)
     prop = Propagator(runs, args.precision)
+    tune = None
+    if args.autotune != "none":
+        # the project's autotuner: every distinct path of the scope timed over 64
+        # synthetic iterations of this workload, the fastest kept (before the start)
+        t0 = time.perf_counter()
+        choice, ms_tuned = prop.autotune(iterations=64, scope=args.autotune)
+        tune = {"scope": args.autotune, "choice": choice, "ms_per_iteration": ms_tuned,
+                "seconds": time.perf_counter() - t0}
     prop.start()
     working_set = nsto * 8 * 4
     flush = working_set < 2 * L2_BYTES
@@ -430,6 +440,8 @@ def run_gpu(args, rank, world, local):
         "clocks": clk,
     }
     out["config"]["kernels"] = out_kernels
+    if tune:
+        out["config"]["autotune"] = tune
     prop.close()
     del prop
 
@@ -439,7 +451,7 @@ def run_gpu(args, rank, world, local):
     e2e_steps = max(1, min(args.steps, 10))
     e2e_runs = {}
     for n in sorted({min(k, len(runs)) for k in E2E_CONTEXTS}):
-        e2e_runs[n] = [run_e2e(runs, args.precision, n, e2e_steps)[0] for _ in range(3)]
+        e2e_runs[n] = [run_e2e(runs, args.precision, n, e2e_steps, tune and tune["choice"])[0] for _ in range(3)]
     e2e_ctx = min(e2e_runs, key=lambda n: sorted(e2e_runs[n])[1])
     e2e_ms = sorted(e2e_runs[e2e_ctx])[1]
     if world > 1:
@@ -574,6 +586,8 @@ def main():
                     help="timed steps of the plain FP64 path on the same workload (0: skip)")
     ap.add_argument("--gate-iterations", type=int, default=2000,
                     help="iterations of the |dP(E)| gate of the mixed path against FP64 on the J=0 wave (0: skip)")
+    ap.add_argument("--autotune", default="none", choices=["none", "layout", "form", "all"],
+                    help="run the library's autotuner over this scope before the timed context starts")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -179,6 +179,23 @@ module mw3gpu
        type(c_ptr), value :: ctx
        integer(c_int32_t), value :: wave_id, on
      end function
+     integer(c_int) function mw3_set_choices(ctx, choice) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), intent(in) :: choice(4)
+     end function
+     integer(c_int) function mw3_get_choices(ctx, choice) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), intent(out) :: choice(4)
+     end function
+     integer(c_int) function mw3_autotune(ctx, iterations, scope, choice, ms_best) bind(c)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t), value :: iterations, scope
+       integer(c_int32_t), intent(out) :: choice(4)
+       real(c_double), intent(out) :: ms_best
+     end function
      integer(c_int) function mw3_packet_energy_norm(ctx, wave_id, apaqini) bind(c)
        import
        type(c_ptr), value :: ctx

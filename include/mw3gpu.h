@@ -204,6 +204,30 @@ int mw3_set_flux_gate(mw3_ctx *ctx, int32_t wave_id, int32_t on);
  * MW3_ERR_STATE. */
 int mw3_set_ecoriolis(mw3_ctx *ctx, int32_t wave_id, int32_t on);
 
+/* Path choices and the autotuner (no counterpart in the reference, whose
+ * single CPU code path has none).  choice[4]:
+ *   [0] radial DST form -- mixed: 0 fused split-FP16 tcgen05 chain, 1 fused
+ *       3xTF32 chain, 2 three-kernel tensor-core DST, 3 CUDA-core FP32 DST;
+ *       FP64: 0 folded dense DST-I, 1 Rader FFT along R (npun2 = 256);
+ *   [1] FP32 rectangle stored [R][r1]: 0 no, 1 yes (where eligible);
+ *   [2] mixed angular terms: 0 explicit kernels, 1 factorised tensor-core kernel;
+ *   [3] R-column chunk of the explicit angular kernels: 8..64, a power of two;
+ * -1 (0 for [3]) keeps the built-in rule, and a form the shape does not admit
+ * falls back to the next one that it does.  Call before mw3_start. */
+int mw3_set_choices(mw3_ctx *ctx, const int32_t *choice);
+int mw3_get_choices(mw3_ctx *ctx, int32_t *choice);
+
+#define MW3_TUNE_LAYOUT 1   /* rectangle layout, angular column chunk: results unchanged bit for bit */
+#define MW3_TUNE_FORM 2     /* DST factorisation and angular form: results change at the rounding level */
+/* Times `iterations` (rounded up to a multiple of 64) propagation iterations
+ * of the context's waves from a synthetic state for every distinct path the
+ * choices in `scope` allow, each after a warm-up that captures the iteration
+ * graphs, and keeps the fastest: the context is left built with it and not
+ * started, its choices in choice[4], its time per iteration in *ms_best
+ * (either may be NULL).  Call after mw3_add_wave (and any mw3_set_*), before
+ * mw3_start; the device tables are rebuilt once per candidate. */
+int mw3_autotune(mw3_ctx *ctx, int32_t iterations, int32_t scope, int32_t *choice, double *ms_best);
+
 /* apaqini[netot]: the energy distribution |<packet|E>|^2 of the initial
  * collision packet that Smatini_col computes (SRC/mod_flux_01y2.f:467-524) and
  * the reference keeps in mod_flux for its normalisations -- ini_transcoor's
@@ -225,6 +249,7 @@ int mw3_kernel_launches(mw3_ctx *ctx, int64_t *count);
 #define MW3_PATH_TC_DST_FUSED 4   /* the whole radial DST chain in one kernel per (block, angle) */
 #define MW3_PATH_DST_F16 8        /* the fused chain as split-FP16 products (MW3_DST_TF32=1 selects 3xTF32) */
 #define MW3_PATH_X_T 16           /* the FP32 rectangle stored [R][r1] (MW3_X_T=1; default [r1][R]) */
+#define MW3_PATH_RADER 32         /* FP64: the DST along R by Rader's FFT (npun2 = 256) */
 int mw3_path_flags(mw3_ctx *ctx, int32_t *flags);
 
 /* The CUDA stream (cudaStream_t) all device work of the context runs on, for

@@ -204,6 +204,7 @@ int build_device(Ctx &c)
     free_device(c);
     int na = c.na, n1 = c.n1, n2 = c.n2, ne = c.ne;
     int W = (int)c.waves.size();
+    c.ang_cw = c.k_cw > 0 ? c.k_cw : c.ang_cw_fit;
     // ---- shared grid ----
     TRY(dupload(c, &c.d_indr1, c.indr1));
     TRY(dupload(c, &c.d_indr2, c.indr2));
@@ -391,7 +392,10 @@ int build_device(Ctx &c)
         for (int s = 0; s < G * na; s++) pre[s + 1] = pre[s] + nopr1[(size_t)bw[s / na] * na + s % na];
         TRY(dupload(c, &c.d_rowpre, pre));
     }
-    if (n2 == 256) {
+    c.d_rd_tw = c.d_rd_ch = nullptr;
+    c.d_rd_col = nullptr;
+    c.d_rd_out = nullptr;
+    if (n2 == 256 && !(c.fp64 && c.k_dst == 0)) {
         // Rader's tables for the 257-point transform behind the FP64 DST along R: with g = 3
         // a primitive root of 257, W_{g^-p} = sum_q a_q d_{p-q}, a_q = w_{g^q}, d_m =
         // exp(-2 pi i g^-m / 257), a 256-point cyclic convolution; d's FFT / 256 in long double
@@ -908,6 +912,8 @@ int api_check_launch(Ctx &c, const char *where) { return check_launch(c, where);
 int api_check_device_flags(Ctx &c, const char *where) { return check_device_flags(c, where); }
 }  // namespace mw3
 
+static int start_device(Ctx &c);
+
 // ===========================================================================
 // C-ABI
 // ===========================================================================
@@ -974,6 +980,7 @@ int mw3_create(mw3_ctx **out, const mw3_grid *g, const int32_t *npunreal, const 
             return MW3_ERR_UNSUPPORTED;
         }
     }
+    c.ang_cw_fit = c.ang_cw;
     *out = h;
     return MW3_OK;
 }
@@ -1041,6 +1048,14 @@ int mw3_start(mw3_ctx *h, const double *const *psi0s)
         MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pk + t.flat0, psi0s[w], sizeof(double) * t.ntot, cudaMemcpyHostToDevice,
                                      c.stream));
     }
+    return start_device(c);
+}
+}  // extern "C"
+
+// the first Chebyshev step from the packets already in c.d_pk (main_madwave3.f:238-250)
+static int start_device(Ctx &c)
+{
+    int rc;
     MW3_CUDA_TRY(cudaMemcpyAsync(c.d_pkm1, c.d_pk, sizeof(double) * c.NT, cudaMemcpyDeviceToDevice, c.stream));
     for (size_t w = 0; w < c.waves.size(); w++)   // check's rpaq0 of the photodissociation waves
         if (c.wdev[w].psi0)
@@ -1061,6 +1076,8 @@ int mw3_start(mw3_ctx *h, const double *const *psi0s)
     c.started = true;
     return check_launch(c, "mw3_start");
 }
+
+extern "C" {
 
 int mw3_upload_state(mw3_ctx *h, int32_t w, const double *psi_km1, const double *psi_k, int64_t it)
 {
@@ -1522,7 +1539,8 @@ int mw3_path_flags(mw3_ctx *h, int32_t *flags)
     }
     *flags = ((mw3::tc_dst_supported(c) || c.use_tc_dst2d) ? MW3_PATH_TC_DST : 0) |
              (c.use_tc_dst2d ? MW3_PATH_TC_DST_FUSED : 0) | (c.use_tc_ang ? MW3_PATH_TC_ANG : 0) |
-             ((c.use_tc_dst2d && c.dst_f16) ? MW3_PATH_DST_F16 : 0) | (c.x_t ? MW3_PATH_X_T : 0);
+             ((c.use_tc_dst2d && c.dst_f16) ? MW3_PATH_DST_F16 : 0) | (c.x_t ? MW3_PATH_X_T : 0) |
+             ((c.fp64 && c.d_rd_tw) ? MW3_PATH_RADER : 0);
     return MW3_OK;
 }
 
@@ -1652,4 +1670,157 @@ int mw3_destroy(mw3_ctx *h)
     return MW3_OK;
 }
 
+int mw3_set_choices(mw3_ctx *h, const int32_t *choice)
+{
+    if (!h || !choice) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    const int dst = choice[0], xt = choice[1], ang = choice[2], cw = choice[3];
+    const bool cw_ok = cw == 0 || (cw >= 8 && cw <= c.ang_cw_fit && (cw & (cw - 1)) == 0);
+    if (dst < -1 || dst > (c.fp64 ? 1 : 3) || xt < -1 || xt > 1 || ang < -1 || ang > 1 || !cw_ok) {
+        c.err = "mw3_set_choices: choice out of range";
+        return MW3_ERR_ARG;
+    }
+    if (c.started) {
+        c.err = "mw3_set_choices: call before mw3_start";
+        return MW3_ERR_STATE;
+    }
+    c.k_dst = dst;
+    c.k_xt = xt;
+    c.k_ang = ang;
+    c.k_cw = cw;
+    c.built = false;
+    return MW3_OK;
+}
+
+int mw3_get_choices(mw3_ctx *h, int32_t *choice)
+{
+    if (!h || !choice) return MW3_ERR_ARG;
+    const Ctx &c = h->c;
+    choice[0] = c.k_dst;
+    choice[1] = c.k_xt;
+    choice[2] = c.k_ang;
+    choice[3] = c.k_cw;
+    return MW3_OK;
+}
 }  // extern "C"
+
+namespace {
+// what a build with the current choices runs: two builds with one signature run
+// the same kernels with the same launch shapes
+std::vector<int> path_signature(const Ctx &c)
+{
+    const bool explicit_ang = c.na > 1 && (c.fp64 || !c.use_tc_ang);
+    const bool tc3 = !c.fp64 && !c.use_tc_dst2d && mw3::tc_dst_supported(const_cast<Ctx &>(c));
+    return {(int)c.use_tc_dst2d, c.use_tc_dst2d ? (int)c.dst_f16 : -1, (int)tc3, (int)c.use_tc_ang, (int)c.x_t,
+            (int)(c.fp64 && c.d_rd_tw != nullptr), explicit_ang ? c.ang_cw : 0};
+}
+
+// time n iterations of the propagation from a synthetic state after the warm-up that
+// captures both graphs; ms per iteration
+int time_candidate(mw3_ctx *h, int n, double *ms)
+{
+    Ctx &c = h->c;
+    mw3::launch_fill_pattern(c, c.d_pk, c.NT);
+    int rc = start_device(c);
+    if (rc) return rc;
+    rc = mw3_run(h, (mw3::kGraphIters - 1) + 2 * mw3::kGraphIters);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    MW3_CUDA_TRY(cudaEventCreate(&e0));
+    MW3_CUDA_TRY(cudaEventCreate(&e1));
+    cudaEventRecord(e0, c.stream);
+    rc = mw3_run(h, n);
+    cudaEventRecord(e1, c.stream);
+    if (!rc) rc = check_device_flags(c, "mw3_autotune");
+    float t = 0.f;
+    if (!rc && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) rc = MW3_ERR_CUDA;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = (double)t / n;
+    return rc;
+}
+}  // namespace
+
+extern "C" int mw3_autotune(mw3_ctx *h, int32_t iterations, int32_t scope, int32_t *choice, double *ms_best)
+{
+    if (!h || iterations < 1 || scope < 1 || (scope & ~(MW3_TUNE_LAYOUT | MW3_TUNE_FORM))) return MW3_ERR_ARG;
+    Ctx &c = h->c;
+    if (c.waves.empty()) {
+        c.err = "mw3_autotune: no partial wave added";
+        return MW3_ERR_STATE;
+    }
+    if (c.started) {
+        c.err = "mw3_autotune: call before mw3_start";
+        return MW3_ERR_STATE;
+    }
+    const int per = 2 * mw3::kGraphIters;
+    const int n = (int)(((int64_t)iterations + per - 1) / per) * per;
+    const int k0[4] = {c.k_dst, c.k_xt, c.k_ang, c.k_cw};
+    std::vector<int> dsts{k0[0]}, angs{k0[2]};
+    if (scope & MW3_TUNE_FORM) {
+        if (c.fp64) {
+            if (c.n2 == 256) dsts = {1, 0};
+        } else {
+            dsts = {0, 1, 2, 3};
+            if (c.na > 1) angs = {1, 0};
+        }
+    }
+    std::vector<std::vector<int>> seen;
+    double best = 0.0;
+    int bk[4] = {k0[0], k0[1], k0[2], k0[3]};
+    bool have = false;
+    int rc = MW3_OK;
+    for (int d : dsts)
+        for (int a : angs) {
+            // the layouts this form admits, from a build with the first of them
+            c.k_dst = d;
+            c.k_ang = a;
+            c.k_xt = (scope & MW3_TUNE_LAYOUT) ? 0 : k0[1];
+            c.k_cw = (scope & MW3_TUNE_LAYOUT) ? 0 : k0[3];
+            c.built = false;
+            if ((rc = build_device(c))) goto done;
+            std::vector<int> xts{c.k_xt}, cws{c.k_cw};
+            if (scope & MW3_TUNE_LAYOUT) {
+                if (mw3::xt_eligible(c)) xts = {0, 1};
+                if (c.na > 1 && (c.fp64 || !c.use_tc_ang)) {
+                    cws.clear();
+                    for (int w = c.ang_cw_fit; w >= 8; w /= 2) cws.push_back(w);
+                }
+            }
+            for (int x : xts)
+                for (int w : cws) {
+                    const bool probe = x == c.k_xt && (w == c.k_cw || (c.k_cw == 0 && w == c.ang_cw_fit));
+                    c.k_xt = x;
+                    c.k_cw = w;
+                    if (!probe) {
+                        c.built = false;
+                        if ((rc = build_device(c))) goto done;
+                    }
+                    std::vector<int> sig = path_signature(c);
+                    if (std::find(seen.begin(), seen.end(), sig) != seen.end()) continue;
+                    seen.push_back(sig);
+                    double t = 0.0;
+                    if ((rc = time_candidate(h, n, &t))) goto done;
+                    if (!have || t < best) {
+                        best = t;
+                        bk[0] = d; bk[1] = x; bk[2] = a; bk[3] = w;
+                        have = true;
+                    }
+                }
+        }
+done:
+    c.k_dst = rc ? k0[0] : bk[0];
+    c.k_xt = rc ? k0[1] : bk[1];
+    c.k_ang = rc ? k0[2] : bk[2];
+    c.k_cw = rc ? k0[3] : bk[3];
+    c.built = false;
+    c.started = false;
+    if (rc) return rc;
+    rc = build_device(c);
+    if (rc) return rc;
+    if (choice) {
+        for (int i = 0; i < 4; i++) choice[i] = bk[i];
+    }
+    if (ms_best) *ms_best = best;
+    return MW3_OK;
+}

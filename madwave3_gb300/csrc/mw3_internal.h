@@ -230,6 +230,13 @@ struct Ctx {
     int *d_quirk_ptr = nullptr, *d_quirk = nullptr;  // per (wave, angle): local points with ir1 > nopr1
     int ncj = 0, ncl = 0;
     int ang_cw = 64;                 // column chunk of the explicit angular kernels (fit_smem)
+    int ang_cw_fit = 64;             // the widest chunk whose shared memory fits (set at create)
+    // path choices (mw3_set_choices, mw3_autotune); -1 (0 for k_cw) keeps the built-in rule
+    int k_dst = -1;                  // radial DST: mixed 0 fused split-FP16, 1 fused 3xTF32, 2 three-kernel
+                                     // tensor-core, 3 CUDA-core FP32; FP64 0 folded dense, 1 Rader FFT (npun2 = 256)
+    int k_xt = -1;                   // FP32 rectangle stored [R][r1]: 0 no, 1 yes where eligible
+    int k_ang = -1;                  // mixed angular terms: 0 explicit kernels, 1 factorised tensor-core kernel
+    int k_cw = 0;                    // column chunk of the explicit angular kernels (8..ang_cw_fit, power of 2)
     // scratch for mw3_hphi
     double *d_tmp = nullptr;
     int64_t tmp_cap = 0;
@@ -366,6 +373,9 @@ inline bool general_tables()
 }
 // the TMA tensor map of the rectangles (after they are allocated)
 int encode_tc_dst2d_xmap(Ctx &c);
+// the [R][r1] rectangle is possible: fused split-FP16 DST and factorised angular kernel,
+// no electronic Coriolis coupling, n1 a multiple of 4 and at least 32
+bool xt_eligible(const Ctx &c);
 void launch_tc_dst2d(Ctx &c, const float *X, float *H, int g_begin, int g_end);
 std::vector<double> dst_matrix(int n);
 
@@ -385,6 +395,7 @@ template <typename T>
 void launch_scatter(Ctx &c, const double *psi, float *psi32, int g_begin, int g_end);
 template <typename T>
 void launch_hphi(Ctx &c, const double *psi, int g_begin, int g_end);
+void launch_fill_pattern(Ctx &c, double *p, int64_t n);
 // records the boundary event of a stage when per-stage timing is on
 void stage_mark(Ctx &c, int stage);
 template <typename T>

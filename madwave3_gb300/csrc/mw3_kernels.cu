@@ -2137,6 +2137,22 @@ void launch_totalflux(Ctx &c, int w, double *d_out, double *d_outelec)
     LAUNCH_CHECK(c);
 }
 
+// a deterministic bounded pattern (|p| <= 5e-4) for timing runs that need no physics
+__global__ void k_fill_pattern(double *__restrict__ p, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t h = (uint32_t)i * 2654435761u;
+        h ^= h >> 15;
+        p[i] = 1e-3 * ((double)(h & 0xFFFFu) / 65536.0 - 0.5);
+    }
+}
+
+void launch_fill_pattern(Ctx &c, double *p, int64_t n)
+{
+    k_fill_pattern<<<1024, 256, 0, c.stream>>>(p, n);
+    LAUNCH_CHECK(c);
+}
+
 // ---------------------------------------------------------------------------
 // H psi without allocation (mw3_hphi_noalloc): the same kernels as launch_hphi,
 // with the two scratch rectangles taken from one static device array.

@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(128) k_tc_dst_cols(DevGrid d, float *__restric
 
 bool tc_dst_supported(Ctx &c)
 {
-    if (c.fp64 || !c.use_tc) return false;
+    if (c.fp64 || !c.use_tc || c.k_dst == 3) return false;
     for (auto &t : c.waves)
         for (int a = 0; a < c.na; a++)
             if (t.nopr1[a] > 128) return false;

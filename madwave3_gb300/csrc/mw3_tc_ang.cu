@@ -417,7 +417,7 @@ int build_tc_ang(Ctx &c)
 {
     using tc::AG_K;
     c.use_tc_ang = false;
-    if (c.fp64 || !c.use_tc || c.na < 2 || c.na > AG_K) return MW3_OK;
+    if (c.fp64 || !c.use_tc || c.k_ang == 0 || c.na < 2 || c.na > AG_K) return MW3_OK;
     if (c.npt >= 0xFFFF) return MW3_OK;                // the tile map holds 16-bit point indices
     const int na = c.na, n1 = c.n1, n2 = c.n2, G = c.G;
     std::vector<float> dfw((size_t)G * 2 * 64 * AG_K, 0.f), dbk((size_t)G * 2 * 64 * AG_K, 0.f);

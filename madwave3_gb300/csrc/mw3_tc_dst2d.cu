@@ -1087,9 +1087,10 @@ std::vector<double> dst_matrix(int n);
 int build_tc_dst2d(Ctx &c)
 {
     c.use_tc_dst2d = false;
+    c.x_t = false;
     // n1 a multiple of 4: the kernel reads the r1 momenta as float4
     // n2 a multiple of 4: the rectangles' rows are a 16-byte multiple for the tensor copies
-    if (c.fp64 || !c.use_tc || c.n2 > 256 || (c.n1 & 3) != 0 || (c.n2 & 3) != 0) return MW3_OK;
+    if (c.fp64 || !c.use_tc || c.k_dst >= 2 || c.n2 > 256 || (c.n1 & 3) != 0 || (c.n2 & 3) != 0) return MW3_OK;
     const int na = c.na, W = (int)c.waves.size();
     for (auto &t : c.waves)
         for (int a = 0; a < na; a++)
@@ -1124,7 +1125,7 @@ int build_tc_dst2d(Ctx &c)
     }
     int rc;
     const char *tf = std::getenv("MW3_DST_TF32");
-    c.dst_f16 = !(tf && tf[0] == '1');
+    c.dst_f16 = c.k_dst == 0 ? true : c.k_dst == 1 ? false : !(tf && tf[0] == '1');
     __half *p16 = nullptr, *f16 = nullptr;
     if ((rc = upload_vec(c, &p16, planes16))) return rc;
     if ((rc = upload_vec(c, &f16, fold16))) return rc;
@@ -1139,6 +1140,11 @@ int build_tc_dst2d(Ctx &c)
     if ((rc = upload_vec(c, &c.d_p2r2f, p2f))) return rc;
     c.use_tc_dst2d = true;
     return MW3_OK;
+}
+
+bool xt_eligible(const Ctx &c)
+{
+    return c.use_tc_dst2d && c.dst_f16 && c.use_tc_ang && c.ec_nt == 0 && c.n1 % 4 == 0 && c.n1 >= 32;
 }
 
 int encode_tc_dst2d_xmap(Ctx &c)
@@ -1159,7 +1165,7 @@ int encode_tc_dst2d_xmap(Ctx &c)
     // lanes along r1, land 16 lanes on one shared-memory bank (2.05 -> 3.15 ms), so it
     // is not the default
     const char *xt = std::getenv("MW3_X_T");
-    c.x_t = c.dst_f16 && c.use_tc_ang && c.ec_nt == 0 && c.n1 % 4 == 0 && c.n1 >= 32 && xt && xt[0] == '1';
+    c.x_t = xt_eligible(c) && (c.k_xt == 1 || (c.k_xt < 0 && xt && xt[0] == '1'));
     const cuuint64_t dims[2] = {(cuuint64_t)(c.x_t ? c.n1 : c.n2),
                                 (cuuint64_t)c.G * c.na * (c.x_t ? c.n2 : c.n1)};
     const cuuint64_t strides[1] = {(cuuint64_t)(c.x_t ? c.n1 : c.n2) * sizeof(float)};

@@ -70,7 +70,8 @@ HEADER_FUNCS = [
     "mw3_get_stream",
     "mw3_profile",
     "mw3_stage_times", "mw3_hphi_noalloc", "mw3_set_product_projection", "mw3_download_product",
-    "mw3_cvj_history", "mw3_download_cvj_history", "mw3_set_flux_gate", "mw3_set_ecoriolis", "mw3_autocorrelation",
+    "mw3_cvj_history", "mw3_download_cvj_history", "mw3_set_flux_gate", "mw3_set_ecoriolis", "mw3_set_choices",
+    "mw3_get_choices", "mw3_autotune", "mw3_autocorrelation",
     "mw3_upload_accumulators", "mw3_upload_product",
     "mw3_last_error", "mw3_destroy",
 ]
@@ -121,6 +122,9 @@ def load_library(build_if_missing=True):
     L.mw3_autocorrelation.argtypes = [vp, ct.c_int32, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_set_flux_gate.argtypes = [vp, ct.c_int32, ct.c_int32]
     L.mw3_set_ecoriolis.argtypes = [vp, ct.c_int32, ct.c_int32]
+    L.mw3_set_choices.argtypes = [vp, ct.POINTER(ct.c_int32)]
+    L.mw3_get_choices.argtypes = [vp, ct.POINTER(ct.c_int32)]
+    L.mw3_autotune.argtypes = [vp, ct.c_int32, ct.c_int32, ct.POINTER(ct.c_int32), ct.POINTER(ct.c_double)]
     L.mw3_download_cvj_history.argtypes = [vp, ct.c_int32, ct.c_int64, F64P, F64P, ct.POINTER(ct.c_int64)]
     L.mw3_kernel_launches.argtypes = [vp, ct.POINTER(ct.c_int64)]
     L.mw3_path_flags.argtypes = [vp, ct.POINTER(ct.c_int32)]
@@ -392,6 +396,31 @@ class Propagator:
         j^2.  Default off.  Before the first hphi/start."""
         self._check(self.L.mw3_set_ecoriolis(self.h, wave, 1 if on else 0), "mw3_set_ecoriolis")
 
+    CHOICES = ("dst", "x_transposed", "angular", "angular_chunk")
+    TUNE_SCOPES = {"layout": 1, "form": 2, "all": 3}
+
+    def set_choices(self, choices):
+        """Pin path choices (mw3_set_choices): a dict over CHOICES, missing keys
+        keep the built-in rule.  Before start."""
+        c = (ct.c_int32 * 4)(*[int(choices.get(k, 0 if k == "angular_chunk" else -1)) for k in self.CHOICES])
+        self._check(self.L.mw3_set_choices(self.h, c), "mw3_set_choices")
+
+    def choices(self):
+        c = (ct.c_int32 * 4)()
+        self._check(self.L.mw3_get_choices(self.h, c), "mw3_get_choices")
+        return dict(zip(self.CHOICES, [int(v) for v in c]))
+
+    def autotune(self, iterations=64, scope="layout"):
+        """Time every distinct path the scope allows ("layout": bit-identical
+        choices; "form": DST factorisation and angular form; "all") over
+        `iterations` synthetic propagation iterations and keep the fastest.
+        Before start; returns (choices, ms per iteration)."""
+        c = (ct.c_int32 * 4)()
+        ms = ct.c_double()
+        self._check(self.L.mw3_autotune(self.h, int(iterations), self.TUNE_SCOPES[scope], c, ct.byref(ms)),
+                    "mw3_autotune")
+        return dict(zip(self.CHOICES, [int(v) for v in c])), ms.value
+
     def cvj_history(self, capacity):
         """Record Cvj (and Cvjprod) of every iteration in a device ring of
         ``capacity`` iterations (0: off)."""
@@ -449,7 +478,7 @@ class Propagator:
         f = ct.c_int32()
         self._check(self.L.mw3_path_flags(self.h, ct.byref(f)), "mw3_path_flags")
         return {"tc_dst": bool(f.value & 1), "tc_dst_fused": bool(f.value & 4), "tc_angular": bool(f.value & 2),
-                "dst_f16": bool(f.value & 8), "x_transposed": bool(f.value & 16)}
+                "dst_f16": bool(f.value & 8), "x_transposed": bool(f.value & 16), "rader": bool(f.value & 32)}
 
     def stream(self):
         """cudaStream_t of the context, as an integer handle."""
