@@ -32,6 +32,8 @@ sys.path.insert(0, HERE)
 
 L2_BYTES = 129 * 1024 * 1024
 FP64_NOMINAL_TFLOPS = 1.25
+# FP32 CUDA-core rate at the maximum SM clock: 152 SMs x 128 lanes x 2 flop x 2.07 GHz
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 # DRAM bytes per stored point and launch of the mixed path's top kernels, from
 # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the J=0..4
@@ -48,6 +50,8 @@ WORKLOADS = {
     "j0_256x128x60": dict(case="j0_256x128x60", sweep=None),
     # J=0 at 512 R x 256 r x 120 angles
     "j0_512x256x120": dict(case="j0_512x256x120", sweep=None),
+    # J=10 with Omega=0..10 Coriolis-coupled: 11 blocks on 256 R x 128 r x 60 angles
+    "j10_256x128x60": dict(case="j10_256x128x60", sweep=None),
     # three diabatic states, J=2 with Omega=0..2, 384 R x 192 r x 80 angles, started from the
     # lowest J=1 bound state of the ground surface times a constant transition dipole of 1 a.u.
     "e3_384x192x80_photo": dict(case="e3_384x192x80", sweep=None, photo=True),
@@ -165,13 +169,13 @@ class ClockSampler:
                 "window": "timed region" if inside else "whole run (no sample inside the timed region)"}
 
 
-def stage_model(runs, prop, stages=None):
+def stage_model(runs, prop, kin):
     """Algorithmic work of each stage of one iteration (flops or bytes).
 
     The angular stage is counted as bytes when the mixed path runs it as the
-    fused tensor-core contraction (the l^2 stage then measures ~0): psi read at
-    every stored point in FP32 and H read and written in FP64, 20 bytes per
-    stored point.  The explicit form is counted in flops."""
+    factorised tensor-core contraction (kin["tc_angular"]; the l^2 stage then
+    measures ~0): psi read at every stored point in FP32 and H read and written,
+    20 bytes per stored point.  The explicit form is counted in flops."""
     r0 = runs[0]
     i = r0.inp
     n1, n2, na = i.npun1, i.npun2, i.nangu
@@ -185,8 +189,7 @@ def stage_model(runs, prop, stages=None):
         rows_sq += r.ncan * int((nopr1 ** 2).sum())
         nsto += r.ntot
     ne = r0.nelec
-    fused = bool(stages) and stages.get("angular_l2", 0.0) < 0.01 * max(stages.get("angular", 0.0), 1e-30)
-    kin = prop.path()
+    fused = prop.precision != "fp64" and kin["tc_angular"]
     return {
         # the fused radial kernel does all four DST products in stage 0
         "dst_R": ("flop", 4.0 * rows * n2 * n2 + 4.0 * rows_sq * n2) if kin["tc_dst_fused"]
@@ -373,13 +376,14 @@ def run_gpu(args, rank, world, local):
     stages, nrec = prop.stage_times()
     prop.profile(False)
 
-    # roofline of the dominant stage
+    # roofline of the dominant stage, against the unit that executes it
     hbm, tf, src = load_peaks()
-    model = stage_model(runs, prop, stages)
+    kin = out_kernels = prop.path()
+    model = stage_model(runs, prop, kin)
     dom = max(stages, key=lambda k: stages[k])
     kind, work = model[dom]
     t_launch = stages[dom] / max(nrec, 1) * 1e-3
-    kin = out_kernels = prop.path()
+    on_tensor = dom.startswith("dst") and kin["tc_dst"]
     traffic = None
     if args.precision == "mixed" and kin["tc_dst_fused"] and kin["tc_angular"] and dom in TRAFFIC_PER_POINT:
         traffic = TRAFFIC_PER_POINT[dom] * nsto
@@ -390,8 +394,18 @@ def run_gpu(args, rank, world, local):
         roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
                 "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": traffic, "kernel": dom,
                 "peak_source": "nominal GB300 FP64 rate (not measured)",
-                "work": "algorithmic DST flops of the dense transforms (the R transform runs as a Rader FFT "
-                        "with fewer flops when npun2 = 256)"}
+                "work": "algorithmic flops of the stage's dense products (DST along R: 2 nopr1 npun2^2 per "
+                        "slab, run as a Rader FFT with fewer flops when npun2 = 256; r1 pair: 4 nopr1^2 npun2; "
+                        "explicit angular: 2 nangu per stored point, the l^2 stage for up to three coupled blocks)"}
+    elif kind == "flop" and not on_tensor:
+        # mixed path, a stage on the FP32 CUDA cores (CUDA-core DSTs, explicit angular kernels)
+        achieved = work / t_launch / 1e12
+        roof = {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": traffic, "kernel": dom,
+                "peak_source": "nominal GB300 FP32 CUDA-core rate at 2070 MHz (not measured)",
+                "work": "algorithmic flops of the stage's dense products (DST along R: 2 nopr1 npun2^2 per "
+                        "slab; r1 pair: 4 nopr1^2 npun2; explicit angular: 2 nangu per stored point, the "
+                        "l^2 stage for up to three coupled blocks)"}
     elif kind == "flop":
         achieved = work / t_launch / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": tf, "unit": "TFLOP/s",
