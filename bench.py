@@ -207,6 +207,50 @@ def stage_model(runs, prop, kin):
     }
 
 
+def dominant_roofline(stages, nrec, model, kin, precision, nsto, peaks):
+    """Roofline of the stage that takes the most time per iteration, against the
+    unit that executes it: the FP64 pipe (FP64 path), the tensor cores (mixed-path
+    DSTs on tcgen05), the FP32 CUDA cores (mixed-path CUDA-core DSTs and explicit
+    angular kernels) or HBM (stages counted in bytes).  stages: total ms per
+    stage over nrec iterations; model: stage_model's (kind, work) per stage."""
+    hbm, tf, src = peaks
+    dom = max(stages, key=lambda k: stages[k])
+    kind, work = model[dom]
+    t_launch = stages[dom] / max(nrec, 1) * 1e-3
+    on_tensor = dom.startswith("dst") and kin["tc_dst"]
+    traffic = None
+    if precision == "mixed" and kin["tc_dst_fused"] and kin["tc_angular"] and dom in TRAFFIC_PER_POINT:
+        traffic = TRAFFIC_PER_POINT[dom] * nsto
+    flops = ("algorithmic flops of the stage's dense products (DST along R: 2 nopr1 npun2^2 per slab%s; "
+             "r1 pair: 4 nopr1^2 npun2; explicit angular: 2 nangu per stored point, the l^2 stage for up "
+             "to three coupled blocks)")
+    if kind == "flop" and precision == "fp64":
+        # the FP64 path's transforms run on the FP64 pipe: against its nominal rate
+        # (the measured peaks hold no FP64 figure)
+        achieved = work / t_launch / 1e12
+        return {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": traffic, "kernel": dom,
+                "peak_source": "nominal GB300 FP64 rate (not measured)",
+                "work": flops % ", run as a Rader FFT with fewer flops when npun2 = 256"}
+    if kind == "flop" and not on_tensor:
+        achieved = work / t_launch / 1e12
+        return {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": traffic, "kernel": dom,
+                "peak_source": "nominal GB300 FP32 CUDA-core rate at 2070 MHz (not measured)",
+                "work": flops % ""}
+    if kind == "flop":
+        achieved = work / t_launch / 1e12
+        return {"bound": "tensor", "achieved": achieved, "peak": tf, "unit": "TFLOP/s",
+                "frac": achieved / tf, "traffic": traffic, "kernel": dom, "peak_source": src,
+                "work": "algorithmic DST flops (4 nopr1 npun2^2 + 4 nopr1^2 npun2 per slab); the kernel issues "
+                        + ("3 FP16 products per flop (split FP16, kind::f16 at the bf16 rate)" if kin.get("dst_f16")
+                           else "3 TF32 products per flop (3xTF32, kind::tf32 at half the bf16 rate)")
+                        + ", and the peak is the dense bf16 one"}
+    achieved = work / t_launch / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": traffic, "kernel": dom, "peak_source": src}
+
+
 RING = 32   # iterations in one cycle of the Cvj ring and in one captured CUDA-graph block
 
 
@@ -379,45 +423,8 @@ def run_gpu(args, rank, world, local):
     # roofline of the dominant stage, against the unit that executes it
     hbm, tf, src = load_peaks()
     kin = out_kernels = prop.path()
-    model = stage_model(runs, prop, kin)
-    dom = max(stages, key=lambda k: stages[k])
-    kind, work = model[dom]
-    t_launch = stages[dom] / max(nrec, 1) * 1e-3
-    on_tensor = dom.startswith("dst") and kin["tc_dst"]
-    traffic = None
-    if args.precision == "mixed" and kin["tc_dst_fused"] and kin["tc_angular"] and dom in TRAFFIC_PER_POINT:
-        traffic = TRAFFIC_PER_POINT[dom] * nsto
-    if kind == "flop" and args.precision == "fp64":
-        # the FP64 path's transforms run on the FP64 pipe: against its nominal rate
-        # (the measured peaks hold no FP64 figure)
-        achieved = work / t_launch / 1e12
-        roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": traffic, "kernel": dom,
-                "peak_source": "nominal GB300 FP64 rate (not measured)",
-                "work": "algorithmic flops of the stage's dense products (DST along R: 2 nopr1 npun2^2 per "
-                        "slab, run as a Rader FFT with fewer flops when npun2 = 256; r1 pair: 4 nopr1^2 npun2; "
-                        "explicit angular: 2 nangu per stored point, the l^2 stage for up to three coupled blocks)"}
-    elif kind == "flop" and not on_tensor:
-        # mixed path, a stage on the FP32 CUDA cores (CUDA-core DSTs, explicit angular kernels)
-        achieved = work / t_launch / 1e12
-        roof = {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": traffic, "kernel": dom,
-                "peak_source": "nominal GB300 FP32 CUDA-core rate at 2070 MHz (not measured)",
-                "work": "algorithmic flops of the stage's dense products (DST along R: 2 nopr1 npun2^2 per "
-                        "slab; r1 pair: 4 nopr1^2 npun2; explicit angular: 2 nangu per stored point, the "
-                        "l^2 stage for up to three coupled blocks)"}
-    elif kind == "flop":
-        achieved = work / t_launch / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": tf, "unit": "TFLOP/s",
-                "frac": achieved / tf, "traffic": traffic, "kernel": dom, "peak_source": src,
-                "work": "algorithmic DST flops (4 nopr1 npun2^2 + 4 nopr1^2 npun2 per slab); the kernel issues "
-                        + ("3 FP16 products per flop (split FP16, kind::f16 at the bf16 rate)" if kin.get("dst_f16")
-                           else "3 TF32 products per flop (3xTF32, kind::tf32 at half the bf16 rate)")
-                        + ", and the peak is the dense bf16 one"}
-    else:
-        achieved = work / t_launch / 1e9
-        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": traffic, "kernel": dom, "peak_source": src}
+    roof = dominant_roofline(stages, nrec, stage_model(runs, prop, kin), kin, args.precision, nsto,
+                             (hbm, tf, src))
     # the whole iteration against HBM (the fused ideal's bytes: psi_k-1 and psi_k
     # read, psi_k+1 written, the V rows a state's Omega blocks share) and the angular
     # DVR <-> basis transforms as tensor work (dense contractions over the rectangles,

@@ -110,3 +110,32 @@ def test_end_to_end_leg_drives_every_context(monkeypatch):
     FakeProp.fail_on = "J3"
     with pytest.raises(RuntimeError, match="J3"):
         bench.run_e2e(runs, "mixed", 4, 2)
+
+
+def test_roofline_charges_the_executing_unit():
+    """The dominant stage's roofline is taken against the unit that runs it."""
+    sys.path.insert(0, ROOT)
+    import bench
+    peaks = (6677.8, 1908.8, "of measured")
+    model = {"dst_R": ("flop", 6.0e11), "dst_r_pair": ("flop", 1.0e11), "angular": ("byte", 3.0e9),
+             "angular_l2": ("flop", 1.0e10), "update": ("byte", 4.0e9)}
+    fused = {"tc_dst": True, "tc_dst_fused": True, "tc_angular": True, "dst_f16": True}
+    cuda_core = {"tc_dst": False, "tc_dst_fused": False, "tc_angular": False, "dst_f16": False}
+    # 10 iterations; the fused DST dominates: tensor cores at the measured bf16 peak
+    r = bench.dominant_roofline({"dst_R": 26.0, "angular": 20.0, "update": 14.0}, 10, model, fused, "mixed",
+                                1e8, peaks)
+    assert r["bound"] == "tensor" and r["kernel"] == "dst_R" and r["peak"] == 1908.8
+    assert abs(r["achieved"] - 6.0e11 / 2.6e-3 / 1e12) < 1e-9 and r["traffic"] == 16.0 * 1e8
+    # the factorised angular stage dominates: bytes against HBM
+    r = bench.dominant_roofline({"dst_R": 10.0, "angular": 20.0}, 10, model, fused, "mixed", 1e8, peaks)
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and abs(r["achieved"] - 3.0e9 / 2e-3 / 1e9) < 1e-9
+    # CUDA-core DSTs and explicit angular kernels: FP32 CUDA cores at the nominal rate
+    for dom in ("dst_r_pair", "angular_l2"):
+        st = {"dst_R": 1.0, "dst_r_pair": 2.0, "angular_l2": 2.0}
+        st[dom] = 5.0
+        r = bench.dominant_roofline(st, 10, model, cuda_core, "mixed", 1e8, peaks)
+        assert r["bound"] == "fp32" and r["kernel"] == dom
+        assert abs(r["peak"] - 152 * 128 * 2 * 2.07e9 / 1e12) < 1e-9 and r["traffic"] is None
+    # FP64 path: the FP64 pipe at its nominal rate
+    r = bench.dominant_roofline({"dst_r_pair": 5.0}, 10, model, cuda_core, "fp64", 1e8, peaks)
+    assert r["bound"] == "fp64" and r["peak"] == bench.FP64_NOMINAL_TFLOPS
