@@ -709,10 +709,10 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                 const bool alongR = (gi == 0 || gi == 3);
                 const __half *src = alongR ? P.s2fold + (size_t)(par * H_NKH + jc) * H_CHUNK
                                            : S1p + (size_t)jc * H_CHUNK;
-                if (gi == 0) {
-                    // the 64 R of this K chunk (both parities) behind the S2 chunk: two
+                if (gi == 0 && par == 0) {
+                    // the 64 R of this K chunk (both parities) behind the par 0 S2 chunk: two
                     // 32-R x 128-r1 tiles, or with the transposed rectangle four 32-r1 x
-                    // 64-R tiles; each parity's stage gets its own copy
+                    // 64-R tiles; the fill splits both parities from them
                     mbar_expect_tx(&xfull[s], 2 * H_XT);
                     if (P.xt) {
 #pragma unroll
@@ -868,12 +868,20 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
             }
             if (t >= H_NS) d2_wait(&empty[s], ph ^ 1, fail);
             const int k0 = jc * H_KC;
-            if (gi == 0) {
-                // B = Xs columns 2j + par, j in this chunk's 32 (rows r1): thread (row r, group kg
-                // of 8 j) reads 16 consecutive R columns of its row from one 32-column tile
-                d2_wait(&xfull[s], ph, fail);
+            if (gi == 0 && par == 0) {
+                // B = Xs columns 2j + par, j in this chunk's 32 (rows r1), for both parities at
+                // once: the chunk's 64 R columns are read once, the even columns split into
+                // this stage's B and the odd ones into the next stage's (the par 1 chunk,
+                // whose fill then only arrives), once the products that last read that stage
+                // are complete.  Thread (row r, group kg of 8 j) reads 16 consecutive R
+                // columns of its row from one 32-column tile
+                const int s1 = s + 1 == H_NS ? 0 : s + 1, ph1 = s + 1 == H_NS ? ph ^ 1 : ph;
+                if (t + 1 >= H_NS) d2_wait(&empty[s1], ph1 ^ 1, fail);
+                // X tiles come with the par 0 chunks (t even) only: stage t % 3 took them
+                // before at t - 6, t - 12, ..., so this is its phase t / 6
+                d2_wait(&xfull[s], (t / 6) & 1, fail);
                 const int e = threadIdx.x, rest = e >> 3, kg = rest & 3, r = (rest >> 2) * 8 + (e & 7);
-                float v[8];
+                float v[8], v1[8];
                 if (P.xt) {
                     // tile q = r / 32 holds rows R' < 64 of the chunk, column r % 32, under the
                     // 128-byte swizzle (16-byte granule ^ row % 8); R past npun2 (the next
@@ -882,10 +890,13 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
                     const int c = r & 31;
 #pragma unroll
                     for (int i = 0; i < 8; i++) {
-                        const int R = 16 * kg + 2 * i + par;
+                        const int R = 16 * kg + 2 * i, R1 = R + 1;
                         const float x = *reinterpret_cast<const float *>(
                             tile + R * 128 + ((((c >> 2) ^ (R & 7)) << 4) | ((c & 3) << 2)));
+                        const float x1 = *reinterpret_cast<const float *>(
+                            tile + R1 * 128 + ((((c >> 2) ^ (R1 & 7)) << 4) | ((c & 3) << 2)));
                         v[i] = 64 * jc + R < n2 ? x * sx : 0.f;
+                        v1[i] = 64 * jc + R1 < n2 ? x1 * sx : 0.f;
                     }
                 } else {
                     const unsigned char *row = st + 16384 + (kg >> 1) * H_XT + r * 128;
@@ -893,15 +904,20 @@ __global__ void __launch_bounds__(D2_WARPS * 32, 1) k_tc_dst2d_h(Dst2hArgs P, co
 #pragma unroll
                     for (int qq = 0; qq < 4; qq++) {
                         const float4 x = *reinterpret_cast<const float4 *>(row + (((q0 + qq) ^ (r & 7)) << 4));
-                        v[2 * qq] = (par == 0 ? x.x : x.y) * sx;
-                        v[2 * qq + 1] = (par == 0 ? x.z : x.w) * sx;
+                        v[2 * qq] = x.x * sx;
+                        v[2 * qq + 1] = x.z * sx;
+                        v1[2 * qq] = x.y * sx;
+                        v1[2 * qq + 1] = x.w * sx;
                     }
                 }
                 if (r >= nn) {
 #pragma unroll
-                    for (int i = 0; i < 8; i++) v[i] = 0.f;
+                    for (int i = 0; i < 8; i++) v[i] = v1[i] = 0.f;
                 }
                 H_SPLIT8(small, H_SMALL_LO, kmaj16_off(r, 8 * kg), v, 0);
+                H_SPLIT8(sm + (size_t)s1 * H_STAGE + H_SMALL_AT, H_SMALL_LO, kmaj16_off(r, 8 * kg), v1, 0);
+            } else if (gi == 0) {
+                // par 1: its B was split with the par 0 chunk (the fence below covers it)
             } else if (gi == 1) {
                 // A = D1 rows R (sum or difference rows) from 16 E and O columns of lane i
                 const int kc = k0 + 16 * colq;
