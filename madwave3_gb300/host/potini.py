@@ -344,6 +344,30 @@ def write_func(outdir, inp, nobc, ediat, fd, ediatref, nelec=1):
         f.write("%r\n" % float(ediatref))
 
 
+def write_prodwf(outdir, jiniprod, nviniprod, fdprod, ediatprod, nobcprod, elecprodmax=None, vibelecprod=None):
+    """func/prodwf (SRC/mod_baseYfunciones_01y2.f:1267-1281): per product j the
+    line 'j noBCprod(j) n2prod1 nelec', then per v in nviniprod..noBCprod(j)
+    the line 'v E(v,j) elecprodmax vibelecprod' (E in zot, unshifted) and
+    n2prod1 lines of fdprod(ir2, v, j, 1..nelec).  fdprod is
+    [njp][nvp][nelec][n2prod1], ediatprod [njp][nvp]; elecprodmax and
+    vibelecprod default to state 1 and v itself (diabatic products)."""
+    os.makedirs(os.path.join(outdir, "func"), exist_ok=True)
+    njp, nvp, nelec, n2p = fdprod.shape
+    lines = []
+    for jj in range(njp):
+        nob = int(nobcprod[jj])
+        lines.append("%d %d %d %d" % (jiniprod + jj, nob, n2p, nelec))
+        for iv in range(nviniprod, nob + 1):
+            k = iv - nviniprod
+            em = 1 if elecprodmax is None else int(elecprodmax[jj, k])
+            vb = iv if vibelecprod is None else int(vibelecprod[jj, k])
+            lines.append("%d %r %d %d" % (iv, float(ediatprod[jj, k]), em, vb))
+            for ir2 in range(n2p):
+                lines.append(" ".join(repr(float(fdprod[jj, k, e, ir2])) for e in range(nelec)))
+    with open(os.path.join(outdir, "func", "prodwf"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def pot1(g, potelebond, vref, outdir, nelec=1):
     """SRC/mod_pot_01y2.f:147-341 for one electronic state: V on the grid in
     zot minus vref, stored where it lies below Vcut (capped at Vcut otherwise);

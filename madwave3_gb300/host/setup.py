@@ -399,6 +399,47 @@ def radial_functions01_read(run, funcdir):
                 run.ediat[ielec, j - i.jini, iv - i.nvini] -= run.ediatref
 
 
+def product_radialf_read(path, jiniprod, jmaxprod, nviniprod, nvmaxprod, n2prod1, eref=None):
+    """func/prodwf as the main program reads it (product_radialf_read,
+    SRC/mod_baseYfunciones_01y2.f:1310-1400): per j its noBCprod (at most
+    nvmaxprod) and n2prod1 (must be the input's), per v the energy,
+    elecprodmax and vibelecprod and the n2prod1 x nelec function values.
+    Energies are returned as stored, or less eref when it is given (the
+    program subtracts func/eref).  Returns (fdprod[njp][nvp][nelec][n2prod1],
+    ediatprod[njp][nvp], nobcprod[njp], elecprodmax[njp][nvp], vibelecprod[njp][nvp])."""
+    njp, nvp = jmaxprod - jiniprod + 1, nvmaxprod - nviniprod + 1
+    with open(path) as f:
+        toks = f.read().split()
+    p = 0
+    fdprod = ediatprod = None
+    nobcprod = np.zeros(njp, np.int32)
+    elecprodmax = np.zeros((njp, nvp), np.int32)
+    vibelecprod = np.zeros((njp, nvp), np.int32)
+    for jj in range(njp):
+        nob, nn2, nnelec = int(toks[p + 1]), int(toks[p + 2]), int(toks[p + 3])
+        p += 4
+        if nob > nvmaxprod:
+            raise ValueError("noBCprod(%d) = %d exceeds nvmaxprod = %d" % (jiniprod + jj, nob, nvmaxprod))
+        if nn2 != n2prod1:
+            raise ValueError("n2prod1 = %d in func/prodwf but %d in the input" % (nn2, n2prod1))
+        if fdprod is None:
+            fdprod = np.zeros((njp, nvp, nnelec, n2prod1))
+            ediatprod = np.zeros((njp, nvp))
+        nobcprod[jj] = nob
+        for iv in range(nviniprod, nob + 1):
+            k = iv - nviniprod
+            ediatprod[jj, k] = float(toks[p + 1].replace("D", "E"))
+            elecprodmax[jj, k] = int(toks[p + 2])
+            vibelecprod[jj, k] = int(float(toks[p + 3].replace("D", "E")))
+            p += 4
+            vals = [float(t.replace("D", "E")) for t in toks[p:p + n2prod1 * nnelec]]
+            p += n2prod1 * nnelec
+            fdprod[jj, k] = np.array(vals).reshape(n2prod1, nnelec).T
+            if eref is not None:
+                ediatprod[jj, k] -= eref
+    return fdprod, ediatprod, nobcprod, elecprodmax, vibelecprod
+
+
 def pot2(run, potdir):
     """Compressed grid, flat index and potential matrix; Chebyshev interval
     (mod_pot_01y2.f:344-533; interval :502-505)."""
