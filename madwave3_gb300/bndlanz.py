@@ -27,6 +27,8 @@ zot that separates true from spurious copies.  State assignment (bndassign)
 and the plotting of the states need the product-channel functions and are
 not part of this module.
 """
+import math
+
 import numpy as np
 
 from .host.constants import conve1, eV2cm, ev_to_zot
@@ -227,6 +229,67 @@ def write_bnd(outdir, run, iv, energy_zot, vec, idproc=0):
         f.write(" %d %d\n" % (i.nangu, i.inc))
         for k in range(run.ntot):
             f.write("".join(" %7d" % x for x in (k + 1,) + tuple(lab[k])) + "\n")
+
+
+def plot_bnd(outdir, run, iv, vec):
+    """plot_bnd (main_boundlanz.f:620-811), three plot files of a bound state
+    (lines '(100(1x,e15.7))', a blank line after each block):
+      bndplot.iNNN     R, gamma (radians), sum over r1 and channels of psi^2, per R;
+      bndr1r2.iNNN     r1, R, sum over angles and channels of psi^2, per R;
+      bndbondx1x2.iNNN x1, x2, psi along the cut at a 135.5 degree bond angle, per x1:
+    for r1 = x1 and a second bond x2 on the r1 grid, R = (x2^2 + g^2 x1^2 -
+    2 cos(135.5) g x1 x2)^(1/2) with g = m1/(m0+m1), taken at the R index
+    INT((R - rmis2)/ah2) (the program's truncation, clamped to the grid) and at
+    the first angle whose cos gamma is nearest (x2 cos(135.5) - g x1)/R; the
+    value is psi (not squared) of the last stored point there in flat order, 0
+    where none is stored."""
+    import os
+    i = run.inp
+    na, n1, n2 = i.nangu, i.npun1, i.npun2
+    lab = _point_labels(run)
+    ir1, ir2, iang = lab[:, 5] - 1, lab[:, 6] - 1, lab[:, 7] - 1
+    vec = np.asarray(vec, np.float64)
+    p2 = vec * vec
+    cg = np.asarray(run.cgamma[:na], np.float64)
+    line = lambda vals: "".join(" " + _e15(v) for v in vals) + "\n"
+    by_ang = np.zeros((n2, na))
+    np.add.at(by_ang, (ir2, iang), p2)
+    with open(os.path.join(outdir, "bndplot.i%03d" % iv), "w") as f:
+        for jr2 in range(n2):
+            r2 = i.rmis2 + jr2 * run.ah2
+            for a in range(na):
+                f.write(line((r2, math.acos(cg[a]), by_ang[jr2, a])))
+            f.write("\n")
+    by_r1 = np.zeros((n2, n1))
+    np.add.at(by_r1, (ir2, ir1), p2)
+    with open(os.path.join(outdir, "bndr1r2.i%03d" % iv), "w") as f:
+        for jr2 in range(n2):
+            r2 = i.rmis2 + jr2 * run.ah2
+            for k in range(n1):
+                f.write(line((i.rmis1 + k * run.ah1, r2, by_r1[jr2, k])))
+            f.write("\n")
+    last = {}
+    for k in range(run.ntot):                  # later points overwrite earlier ones
+        last[(ir1[k], ir2[k], iang[k])] = vec[k]
+    xb = math.cos(135.5 * math.pi / 180.0)
+    gam = i.xm1 / (i.xm0 + i.xm1)
+    with open(os.path.join(outdir, "bndbondx1x2.i%03d" % iv), "w") as f:
+        for jr1 in range(n1):
+            x1 = i.rmis1 + jr1 * run.ah1
+            for jr2 in range(n1):
+                x2 = i.rmis1 + jr2 * run.ah1
+                rg = math.sqrt(x2 * x2 + x1 * x1 * gam * gam - 2.0 * xb * gam * x1 * x2)
+                k2 = min(max(int((rg - i.rmis2) / run.ah2), 1), n2)
+                ct = (x2 * xb - gam * x1) / rg
+                if abs(ct) > 1.0:
+                    ct = ct / abs(ct)
+                dis, ka = 1.0e10, 0
+                for a in range(na):
+                    d = abs(cg[a] - ct) ** 2
+                    if d < dis:
+                        dis, ka = d, a
+                f.write(line((x1, x2, last.get((jr1, k2 - 1, ka), 0.0))))
+            f.write("\n")
 
 
 def read_bound_state(run, outdir, iv, idproc=0):

@@ -328,6 +328,90 @@ def product_radialf_write(g, potelebond, nviniprod, nvmaxprod, jiniprod, jmaxpro
     return fdprod, ediatprod, np.full(njp, nvmaxprod, np.int32)
 
 
+NPUNT_ADIABATIC = 2000
+
+
+def bndbc1ele(vdiag, xm, rmis, rfin, nvini, nvmax, j, max_viblevels):
+    """Bound levels of several uncoupled electronic states for one j
+    (SRC/liboctdyn.f:1815-1941): per state the tridiagonal finite-difference
+    eigenvalues as guesses, each refined by schr, kept while V(rfin) - E >
+    0.01 hartree, up to max_viblevels(state) levels (or nvmax + 2 when it is
+    negative), appended state after state (not sorted across states) and
+    numbered from nvini - 1.  vdiag [nelec][npun] in hartree, xm in a.u.
+    Returns {level: (E hartree, state 1-based, v within the state, function [npun])}
+    for the levels numbered nvini..nvmax, and the last level number."""
+    nelec, npun = vdiag.shape
+    ah = (rfin - rmis) / float(npun - 1)
+    xl = 0.5 * float(j * (j + 1)) / xm
+    xz, xz1 = 0.5 / xm, 2.0 * xm
+    r = rmis + np.arange(npun, dtype=np.float64) * ah
+    out = {}
+    ivreal = nvini - 1
+    for ie in range(nelec):
+        vv = vdiag[ie] + xl / (r * r)
+        diag = -2.0 - 2.0 * xm * vv * ah * ah
+        alpha = np.sort(-xz * eigvalsh_tridiagonal(diag, np.ones(npun - 1)) / ah / ah)
+        maxvib = nvmax + 1 if max_viblevels[ie] < 0 else max_viblevels[ie] - 1
+        for iv in range(0, min(npun, maxvib) + 1):
+            if iv >= npun or not (vdiag[ie, npun - 1] - alpha[iv] > 1.0e-2):
+                continue
+            e2, _, p = schr(alpha[iv] * xz1, rmis, rfin, npun, 20, 1.0e-10, (vv * xz1).tolist())
+            ivreal += 1
+            if nvini <= ivreal <= nvmax:
+                out[ivreal] = (e2 / xz1, ie + 1, iv, np.array(p))
+    return out, ivreal
+
+
+def product_radialf_write_adiabatic(g, potelebond, nviniprod, nvmaxprod, jiniprod, jmaxprod, n2prod1, r1inf=100.0,
+                                    nelec=1, max_viblevels=None):
+    """Product (02) diatom states of uncoupled (adiabatic) electronic states,
+    the diabatic_prod_pot = 0 branch of product_radialf_write
+    (SRC/mod_baseYfunciones_01y2.f:1071-1250): the diagonal potentials of
+    potelebond on 2000 points of [rmis2, rfin2] with atom 1 at r1inf, per j
+    the levels of bndbc1ele, each level's function (nonzero only in its own
+    state) splined onto the first n2prod1 R points and discrete-normalised.
+    max_viblevels defaults as the namelist does (-1 per state; nvmaxprod -
+    nviniprod + 1 with one state).  Returns (fdprod[njp][nvp][nelec][n2prod1],
+    ediatprod[njp][nvp] in zot, nobcprod[njp], elecprodmax[njp][nvp] (the
+    level's state), vibelecprod[njp][nvp] (its v within the state))."""
+    inp = g.inp
+    if max_viblevels is None:
+        max_viblevels = [nvmaxprod - nviniprod + 1] if nelec == 1 else [-1] * nelec
+    npunt = NPUNT_ADIABATIC
+    rmis, rfin = inp.rmis2 / C.convl, inp.rfin2 / C.convl
+    ah = (rfin - rmis) / float(npunt - 1)
+    r = rmis + np.arange(npunt, dtype=np.float64) * ah
+    V = potelebond(np.full(npunt, r1inf / C.convl), r, 1.0)
+    vdiag = np.array([V[ie, ie] for ie in range(nelec)])
+    xm = g.xm1prod * C.convm
+    njp, nvp = jmaxprod - jiniprod + 1, nvmaxprod - nviniprod + 1
+    fdprod = np.zeros((njp, nvp, nelec, n2prod1))
+    ediatprod = np.zeros((njp, nvp))
+    nobcprod = np.full(njp, nviniprod - 1, np.int32)
+    elecprodmax = np.zeros((njp, nvp), np.int32)
+    vibelecprod = np.zeros((njp, nvp), np.int32)
+    r2 = (inp.rmis2 + np.arange(n2prod1, dtype=np.float64) * g.ah2) / C.convl
+    inside = (r2 >= r[0]) & (r2 <= r[-1])
+    for jj, j in enumerate(range(jiniprod, jmaxprod + 1)):
+        levels, ivreal = bndbc1ele(vdiag, xm, rmis, rfin, nviniprod, nvmaxprod, j, max_viblevels)
+        for iv in range(nviniprod, min(ivreal, nvmaxprod) + 1):
+            e, ie, v, p = levels[iv]
+            k = iv - nviniprod
+            ediatprod[jj, k] = e / C.conve * C.conve1
+            ff = p / math.sqrt(C.convl)
+            d = splset(ff, r)
+            vals = np.zeros(n2prod1)
+            vals[inside] = splinqq_many(ff, d, r, r2[inside])
+            xnorm = float(np.sum(vals * vals)) * g.ah2
+            if xnorm > 1.0e-8:
+                vals = vals * math.sqrt(g.ah2 / xnorm)
+            fdprod[jj, k, ie - 1] = vals
+            elecprodmax[jj, k] = ie
+            vibelecprod[jj, k] = v
+        nobcprod[jj] = min(ivreal, nvmaxprod)
+    return fdprod, ediatprod, nobcprod, elecprodmax, vibelecprod
+
+
 def write_func(outdir, inp, nobc, ediat, fd, ediatref, nelec=1):
     """func/bcwf and func/eref (SRC/mod_baseYfunciones_01y2.f:785-808)."""
     os.makedirs(os.path.join(outdir, "func"), exist_ok=True)

@@ -132,3 +132,51 @@ def test_assignment_distributions(tiny):
     assert abs(sum(a["disomg"].values()) - 1.0) < 1e-12
     assert abs(a["diselec"].sum() - 1.0) < 1e-12
     assert abs(a["cos_mean"] - run.cgamma[ang[0] - 1]) < 1e-12
+
+
+def _blocks(path, ncol=3):
+    """Blank-line separated blocks of a plot file, as arrays."""
+    out, cur = [], []
+    for line in open(path).read().split("\n"):
+        if line.strip():
+            cur.append([float(x) for x in line.split()])
+        elif cur:
+            out.append(np.array(cur))
+            cur = []
+    return out
+
+
+def test_plot_bnd_files(runs, tmp_path):
+    """plot_bnd's three files (main_boundlanz.f:620-811) on a seeded vector."""
+    import math
+    run = runs["tiny_j3"]
+    i = run.inp
+    vec = np.random.default_rng(17).standard_normal(run.ntot)
+    bndlanz.plot_bnd(str(tmp_path), run, 4, vec)
+    tot = float(np.sum(vec * vec))
+    lab = bndlanz._point_labels(run)
+    # summed over r1 (per R and angle) and over angles (per R and r1): each block an R
+    a = _blocks(str(tmp_path / "bndplot.i004"))
+    b = _blocks(str(tmp_path / "bndr1r2.i004"))
+    assert len(a) == i.npun2 and all(x.shape == (i.nangu, 3) for x in a)
+    assert len(b) == i.npun2 and all(x.shape == (i.npun1, 3) for x in b)
+    assert abs(sum(x[:, 2].sum() for x in a) - tot) <= 1e-6 * tot
+    assert abs(sum(x[:, 2].sum() for x in b) - tot) <= 1e-6 * tot
+    for jr2 in (0, i.npun2 // 2):
+        want = float(np.sum(vec[lab[:, 6] == jr2 + 1] ** 2))
+        assert abs(a[jr2][:, 2].sum() - want) <= 1e-6 * max(want, 1e-300)
+    assert np.allclose(a[0][:, 1], np.arccos(run.cgamma[: i.nangu]), rtol=1e-6)
+    # the bond cut: one block per x1, each value psi (not squared) of a stored point
+    # at that r1, or 0
+    c = _blocks(str(tmp_path / "bndbondx1x2.i004"))
+    assert len(c) == i.npun1 and all(x.shape == (i.npun1, 3) for x in c)
+    nonzero = 0
+    for jr1, blk in enumerate(c):
+        at = vec[lab[:, 5] == jr1 + 1]
+        for v in blk[:, 2]:
+            if v != 0.0:
+                nonzero += 1
+                assert np.min(np.abs(at - v)) <= 1e-6 * abs(v)
+    assert nonzero > 0
+    xb = math.cos(135.5 * math.pi / 180.0)
+    assert np.allclose(c[3][:, 0], i.rmis1 + 3 * run.ah1, rtol=1e-6) and xb < 0
