@@ -23,7 +23,6 @@ over every state, and the files CRPtot.res, CRPvib.res, CRPomg.res, PJ.res
 and CRP.vfVV.efE with k^2 = 2 mu E / hbar^2 (E in zot, mu the reactant
 arrangement's for iprod = 2) beside each energy (:400-480).
 """
-import math
 import os
 
 import numpy as np
