@@ -297,7 +297,7 @@ def product_radialf_write(g, potelebond, nviniprod, nvmaxprod, jiniprod, jmaxpro
     ediatprod[njp][nvp] in zot, nobcprod[njp])."""
     inp = g.inp
     if nelec != 1:
-        raise NotImplementedError("product_radialf_write is restated for one electronic state")
+        return _product_dvr_coupled(g, potelebond, nviniprod, nvmaxprod, jiniprod, jmaxprod, n2prod1, r1inf, nelec)
     npun = inp.npun2
     rmis = inp.rmis2 / C.convl
     rfin = inp.rfin2 / C.convl
@@ -412,6 +412,62 @@ def product_radialf_write_adiabatic(g, potelebond, nviniprod, nvmaxprod, jinipro
     return fdprod, ediatprod, nobcprod, elecprodmax, vibelecprod
 
 
+def _dvr_kinetic(npun, ah, xmu):
+    """bndbcele's particle-in-a-box DVR kinetic matrix (SRC/liboctdyn.f:1760-1779)."""
+    i = np.arange(1, npun + 1)
+    menos = (i[:, None] - i[None, :]).astype(np.float64)
+    mas = (i[:, None] + i[None, :]).astype(np.float64)
+    sign = np.where((i[:, None] - i[None, :]) % 2 == 0, 1.0, -1.0)
+    x1 = np.where(menos == 0.0, math.pi * math.pi / 6.0, 1.0 / np.where(menos == 0.0, 1.0, menos * menos))
+    return sign * (x1 + 1.0 / (mas * mas)) / (ah * ah) / xmu
+
+
+def _product_dvr_coupled(g, potelebond, nviniprod, nvmaxprod, jiniprod, jmaxprod, n2prod1, r1inf, nelec):
+    """product_radialf_write's diabatic branch for several coupled states
+    (bndbcele, SRC/liboctdyn.f:1687-1814): one block per state holding the DVR
+    kinetic matrix and the centrifugal term, the potential matrix coupling the
+    states at each point; the lowest nvmaxprod - nviniprod + 1 levels, each
+    eigenvector positive at its largest component, its state components
+    discrete-normalised as one vector over the npun2 points."""
+    inp = g.inp
+    npun = inp.npun2
+    rmis, rfin = inp.rmis2 / C.convl, inp.rfin2 / C.convl
+    ah = (rfin - rmis) / float(npun - 1)
+    xmu = g.xm1prod * C.convm
+    r = rmis + np.arange(npun, dtype=np.float64) * ah
+    V = potelebond(np.full(npun, r1inf / C.convl), r, 1.0)
+    T = _dvr_kinetic(npun, ah, xmu)
+    njp, nvp = jmaxprod - jiniprod + 1, nvmaxprod - nviniprod + 1
+    fdprod = np.zeros((njp, nvp, nelec, n2prod1))
+    ediatprod = np.zeros((njp, nvp))
+    for jj, j in enumerate(range(jiniprod, jmaxprod + 1)):
+        xl = 0.5 * float(j * (j + 1)) / xmu
+        H = np.zeros((nelec * npun, nelec * npun))
+        for e in range(nelec):
+            H[e * npun:(e + 1) * npun, e * npun:(e + 1) * npun] = T + np.diag(xl / (r * r))
+            for f in range(nelec):
+                H[e * npun:(e + 1) * npun, f * npun:(f + 1) * npun] += np.diag(V[e, f])
+        w, vec = np.linalg.eigh(H)
+        for k in range(nvp):
+            c = vec[:, k]
+            if c[np.argmax(np.abs(c))] < 0:
+                c = -c
+            ediatprod[jj, k] = w[k] / C.conve * C.conve1
+            fdprod[jj, k] = (c.reshape(nelec, npun) / math.sqrt(ah))[:, :n2prod1] * math.sqrt(g.ah2 / C.convl)
+    return fdprod, ediatprod, np.full(njp, nvmaxprod, np.int32)
+
+
+def product_labels(fdprod, nviniprod):
+    """elecprodmax and vibelecprod of diabatic product states
+    (SRC/mod_baseYfunciones_01y2.f:1190-1245): the state holding the largest
+    share of each level's norm (the first on ties), and the level number itself."""
+    njp, nvp = fdprod.shape[:2]
+    norms = np.sum(fdprod ** 2, axis=3)                     # [njp][nvp][nelec]
+    elec = np.argmax(norms, axis=2).astype(np.int32) + 1
+    vib = np.broadcast_to(nviniprod + np.arange(nvp, dtype=np.int32), (njp, nvp)).copy()
+    return elec, vib
+
+
 def write_func(outdir, inp, nobc, ediat, fd, ediatref, nelec=1):
     """func/bcwf and func/eref (SRC/mod_baseYfunciones_01y2.f:785-808)."""
     os.makedirs(os.path.join(outdir, "func"), exist_ok=True)
@@ -452,13 +508,15 @@ def write_prodwf(outdir, jiniprod, nviniprod, fdprod, ediatprod, nobcprod, elecp
         f.write("\n".join(lines) + "\n")
 
 
-def pot1(g, potelebond, vref, outdir, nelec=1):
+def pot1(g, potelebond, vref, outdir, nelec=1, states=None):
     """SRC/mod_pot_01y2.f:147-341 for one electronic state: V on the grid in
     zot minus vref, stored where it lies below Vcut (capped at Vcut otherwise);
     pot/pot.NNN.dat rows 'ir1 ir2 V' with ir2 outer and ir1 inner, and
-    pot/cont.pot.  Returns (npunreal, vmin, vmaxtot)."""
+    pot/cont.pot.  Several states: see _pot1_coupled (``states``: per state
+    (iomdiat, iomatom, sigdiat, sigatom) for cont.pot, default (0, 0, 1, 1)).
+    Returns (npunreal, vmin, vmaxtot)."""
     if nelec != 1:
-        raise NotImplementedError("pot1 is restated for one electronic state")
+        return _pot1_coupled(g, potelebond, vref, outdir, nelec, states)
     inp = g.inp
     os.makedirs(os.path.join(outdir, "pot"), exist_ok=True)
     n1, n2 = inp.npun1, inp.npun2
@@ -498,26 +556,107 @@ def pot1(g, potelebond, vref, outdir, nelec=1):
     return np.array(npunreal, np.int32), vmin, vmaxtot
 
 
-def write_case(outdir, inputfile, potelebond, bound_test="margin", input_text=None):
+def _pot1_coupled(g, potelebond, vref, outdir, nelec, states=None):
+    """pot1 for several electronic states (SRC/mod_pot_01y2.f:147-341): at each
+    grid point the potential matrix in zot with vref subtracted on the
+    diagonal; a state whose diagonal exceeds Vcut has its row and
+    column zeroed and the diagonal set to Vcut (in state order); the point is
+    stored when any eigenvalue of the matrix lies below Vcut, as 'ir1 ir2'
+    and the matrix column by column; vmin and vmaxtot are the extreme
+    eigenvalues over the grid (vmaxtot at least Vcut)."""
+    inp = g.inp
+    os.makedirs(os.path.join(outdir, "pot"), exist_ok=True)
+    n1, n2 = inp.npun1, inp.npun2
+    vcut = g.vcutmax
+    states = states or [(0, 0, 1.0, 1.0)] * nelec
+    r1 = inp.rmis1 + np.arange(n1, dtype=np.float64) * g.ah1
+    r2 = inp.rmis2 + np.arange(n2, dtype=np.float64) * g.ah2
+    rpeq = np.broadcast_to((r1 / C.convl)[None, :], (n2, n1))     # [ir2][ir1]
+    Rg = np.broadcast_to((r2 / C.convl)[:, None], (n2, n1))
+    gam = inp.xm1 / (inp.xm0 + inp.xm1)
+    vmin, vmaxtot = 1e10, vcut
+    npunreal = []
+    for iang in range(inp.nangu):
+        ctet = float(g.cgamma[iang])
+        X2 = np.sqrt(Rg * Rg + gam * gam * rpeq * rpeq + 2.0 * gam * Rg * rpeq * ctet)
+        calpha = (Rg * ctet + gam * rpeq) / X2
+        calpha = np.where(np.abs(calpha) > 1.0, calpha / np.abs(calpha), calpha)
+        with np.errstate(invalid="ignore"):
+            v = potelebond(rpeq, X2, calpha) / C.conve * C.conve1     # [ne][ne][n2][n1]
+        v = np.array(v, dtype=np.float64)
+        for e in range(nelec):
+            v[e, e] -= vref
+        for e in range(nelec):
+            hi = v[e, e] > vcut
+            for f in range(nelec):
+                v[e, f] = np.where(hi, 0.0, v[e, f])
+                v[f, e] = np.where(hi, 0.0, v[f, e])
+            v[e, e] = np.where(hi, vcut, v[e, e])
+        eig = np.moveaxis(np.linalg.eigvalsh(np.moveaxis(v, (0, 1), (-2, -1))), -1, 0)   # [ne][n2][n1]
+        vmaxtot = max(vmaxtot, float(np.nanmax(eig)))
+        vmin = min(vmin, float(np.nanmin(eig)))
+        keep = (eig < vcut).any(axis=0)
+        i2, i1 = np.nonzero(keep)
+        with open(os.path.join(outdir, "pot", "pot.%03d.dat" % (iang + 1)), "w") as f:
+            for a, b in zip(i1, i2):
+                vals = [float(v[ie, je, b, a]) for je in range(nelec) for ie in range(nelec)]
+                f.write("%d %d %s\n" % (a + 1, b + 1, " ".join(repr(x) for x in vals)))
+        npunreal.append(len(i1))
+    with open(os.path.join(outdir, "pot", "cont.pot"), "w") as f:
+        f.write("%d\n" % nelec)
+        for st in states:
+            f.write("%d %d %r %r\n" % (int(st[0]), int(st[1]), float(st[2]), float(st[3])))
+        f.write("%r %d %r\n" % (vmin, sum(npunreal), vmaxtot))
+        f.write("%r %r %d\n" % (inp.rmis1, inp.rfin1, n1))
+        f.write("%r %r %d\n" % (inp.rmis2, inp.rfin2, n2))
+        f.write("%d %d\n" % (inp.nangu, inp.inc))
+        f.write(" ".join("%d" % n for n in npunreal) + "\n")
+    return np.array(npunreal, np.int32), vmin, vmaxtot
+
+
+def write_case(outdir, inputfile, potelebond, bound_test="margin", input_text=None, product_form="dvr",
+               states=None):
     """pot.out for one input.dat (a path, or its text in ``input_text``) and a
-    surface: func/ and pot/ beside a copy of the input.  Returns a summary
-    (levels, eref, points per angle, vmin)."""
+    surface: func/ and pot/ beside a copy of the input, for the input's
+    nelecmax states (``states``: their (iomdiat, iomatom, sigdiat, sigatom)).
+    With iprod = 2 the product states are written to func/prodwf:
+    ``product_form`` "dvr" takes the box DVR of bndbcele (the form the shipped
+    H + HD run was made with), "namelist" follows &inputpotmass's
+    diabatic_prod_pot as the current source does (0, its default: the
+    uncoupled-state levels of bndbc1ele).  Returns a summary (levels, eref,
+    points per angle, vmin, product states)."""
     groups = namelist.parse(input_text) if input_text is not None else namelist.read(inputfile)
     inp, flat = _inputs(groups)
+    nelec = int(inp.nelecmax)
     os.makedirs(outdir, exist_ok=True)
     with open(os.path.join(outdir, "input.dat"), "w") as f:
         f.write(namelist.dumps(groups))
     g = _grid(inp)
     r2inf = float(flat.get("r2inf_radial_functions", 100.0))
-    nobc, ediat, fd, eref = radial_functions01_write(g, potelebond, r2inf=r2inf, bound_test=bound_test)
-    write_func(outdir, inp, nobc, ediat, fd, eref)
-    npunreal, vmin, vmaxtot = pot1(g, potelebond, eref, outdir)
+    nobc, ediat, fd, eref = radial_functions01_write(g, potelebond, r2inf=r2inf, nelec=nelec,
+                                                     bound_test=bound_test)
+    write_func(outdir, inp, nobc, ediat, fd, eref, nelec=nelec)
+    npunreal, vmin, vmaxtot = pot1(g, potelebond, eref, outdir, nelec=nelec, states=states)
     out = {"nobc": nobc, "ediat": ediat, "fd": fd, "ediatref": eref, "npunreal": npunreal,
            "vmin": vmin, "vmaxtot": vmaxtot, "cgamma": g.cgamma}
     prod = groups.get("inputprod", {})
     if int(prod.get("iprod", 0)) == 2:
-        out["product"] = product_radialf_write(
-            g, potelebond, int(prod.get("nviniprod", 0)), int(prod.get("nvmaxprod", 0)),
-            int(prod.get("jiniprod", 0)), int(prod.get("jmaxprod", 0)), int(prod.get("n2prod1", inp.npun2)),
-            r1inf=float(flat.get("r1inf_radial_functions", 100.0)))
+        nv0, nv1 = int(prod.get("nviniprod", 0)), int(prod.get("nvmaxprod", 0))
+        j0, j1 = int(prod.get("jiniprod", 0)), int(prod.get("jmaxprod", 0))
+        n2p = int(prod.get("n2prod1", inp.npun2))
+        r1inf = float(flat.get("r1inf_radial_functions", 100.0))
+        dia = int(groups.get("inputpotmass", {}).get("diabatic_prod_pot", 0))
+        if product_form == "dvr" or (product_form == "namelist" and dia > 0):
+            fdp, edp, nobp = product_radialf_write(g, potelebond, nv0, nv1, j0, j1, n2p, r1inf=r1inf, nelec=nelec)
+            elec, vib = product_labels(fdp, nv0)
+            out["product"] = (fdp, edp, nobp)
+        elif product_form == "namelist":
+            mv = prod.get("max_viblevels")
+            mv = None if mv is None else list(np.atleast_1d(mv).astype(int))
+            fdp, edp, nobp, elec, vib = product_radialf_write_adiabatic(g, potelebond, nv0, nv1, j0, j1, n2p,
+                                                                        r1inf=r1inf, nelec=nelec, max_viblevels=mv)
+            out["product"] = (fdp, edp, nobp)
+        else:
+            raise ValueError("product_form must be 'dvr' or 'namelist'")
+        write_prodwf(outdir, j0, nv0, fdp, edp, nobp, elec, vib)
     return out
