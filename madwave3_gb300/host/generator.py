@@ -336,6 +336,10 @@ CASES = {
     "tiny_ecor": dict(npun2=36, npun1=20, nangu=8, jmax=5, nvmax=2, netot=48, npun1min=8,
                       nelecmax=2, lambdas=(0, 1), Jtot=2, iommax=2, iparity=1, alpha0_bohr=1.2,
                       shifts_ev=(0.0, 0.3), coupling_ev=0.2, coupling_width_bohr=1.5),
+    # three states with Lambda = 0, 1, 0: each Lambda = 1 channel couples to two sources
+    "tiny_ecor3": dict(npun2=32, npun1=20, nangu=8, jmax=5, nvmax=2, netot=48, npun1min=8,
+                       nelecmax=3, lambdas=(0, 1, 0), Jtot=2, iommax=2, iparity=1, alpha0_bohr=1.2,
+                       shifts_ev=(0.0, 0.3, 0.5), coupling_ev=0.2, coupling_width_bohr=1.5),
 }
 
 

@@ -18,7 +18,7 @@ def case_dirs(tmp_path_factory):
     from madwave3_gb300.host import generator
     base = tmp_path_factory.mktemp("cases")
     out = {}
-    for name in ("tiny_j0", "tiny_j3", "tiny_e2", "tiny_ecor"):
+    for name in ("tiny_j0", "tiny_j3", "tiny_e2", "tiny_ecor", "tiny_ecor3"):
         d = str(base / name)
         generator.write_case(d, **generator.CASES[name])
         out[name] = d

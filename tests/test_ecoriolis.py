@@ -97,8 +97,20 @@ def test_case_has_coupled_channels(ecor_run):
             assert np.abs(X).max() > 0
 
 
-def test_oracle_term_matches_restatement(ecor_run):
-    run = ecor_run
+def test_three_states_give_two_sources(runs):
+    run = runs["tiny_ecor3"]
+    assert list(run.iomdiat) == [0, 1, 0]
+    targets = {}
+    for b, b2 in ecor_pairs(run):
+        targets.setdefault(b2, []).append(b)
+    # every Lambda = 1 channel takes both Lambda = 0 channels of its Omega
+    lam1 = [b for b in range(run.ncan) if run.iomdiat[run.nelebas[b] - 1] == 1]
+    assert lam1 and all(len(targets[b]) == 2 for b in lam1)
+
+
+@pytest.mark.parametrize("case", ["tiny_ecor", "tiny_ecor3"])
+def test_oracle_term_matches_restatement(runs, case):
+    run = runs[case]
     plain, ecor = Oracle(run), Oracle(run, ecoriolis=True)
     rng = np.random.default_rng(20261204)
     for _ in range(2):

@@ -110,3 +110,21 @@ def test_set_after_tables_exist_is_refused(runs):
     with pytest.raises(RuntimeError, match="mw3_set_ecoriolis"):
         prop.set_ecoriolis(True)
     prop.close()
+
+
+def test_two_sources_per_target(runs):
+    """tiny_ecor3 (Lambda = 0, 1, 0): every Lambda = 1 channel sums two sources
+    in one CTA before its update of H."""
+    run = runs["tiny_ecor3"]
+    p64, pmx = Propagator(run, "fp64"), Propagator(run, "mixed")
+    p64.set_ecoriolis(True)
+    pmx.set_ecoriolis(True)
+    ref = Oracle(run, ecoriolis=True)
+    rng = np.random.default_rng(23)
+    for _ in range(2):
+        psi = rng.uniform(-1, 1, run.ntot)
+        h = p64.hphi(psi)
+        assert rel(h, ref.hphi(psi)) < 1e-12
+        assert rel(pmx.hphi(psi), h) < 1e-6
+    p64.close()
+    pmx.close()
