@@ -120,3 +120,25 @@ def test_quirk_points_keep_psi_as_kinetic_term(runs):
     xj2 = o.xj2()[0, iang - 1, iang - 1, run.indr1[iang - 1, ir] - 1]
     xl2 = o.xl2p()[1, 0, iang - 1, iang - 1, run.indr2[iang - 1, ir] - 1]
     assert h[flat] == pytest.approx(1.0 + v + xj2 + xl2, rel=1e-14)
+
+
+def test_norm_trace_of_the_damped_recursion(tmp_path, runs):
+    """The check trace: without absorption psi_k = T_k(H_s) psi_0 with the scaled
+    spectrum inside [-1, 1], so ||psi_k|| never exceeds ||psi_0||; with the
+    absorbers the trace, oscillating from one iteration to the next as Chebyshev
+    vectors do, decays once the packet reaches them."""
+    import os
+    from madwave3_gb300.host import generator, setup
+    d = str(tmp_path / "undamped")
+    generator.write_case(d, **dict(generator.CASES["tiny_j0"], absorb_strength=0.0))
+    r0 = setup.load(os.path.join(d, "input.dat"))
+    o = Oracle(r0)
+    assert o.tables()["absfr1"].min() == 1.0 and o.tables()["absfr2"].min() == 1.0
+    o.start(r0.psi0)
+    n = o.run_iters(1500)
+    assert n.max() <= float(np.sum(r0.psi0 ** 2)) * (1.0 + 1e-12)
+    run = runs["tiny_j0"]
+    o = Oracle(run, threads=4)
+    o.start(run.psi0)
+    n = o.run_iters(3000)
+    assert n[-100:].mean() < 0.1 * n[:100].mean()
