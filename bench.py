@@ -495,7 +495,7 @@ def run_gpu(args, rank, world, local):
     if rank == 0 and world == 1 and args.gate_iterations > 0 and args.precision == "mixed":
         out["gate"] = precision_gate(args.gate_iterations)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(sample_waves(runs), budget_s=args.cpu_seconds)
+        out["cpu_baseline"] = cpu_baseline(sample_waves(runs), seconds=args.cpu_seconds)
     return out
 
 
@@ -534,12 +534,12 @@ def fp64_plain(runs, steps, warmup=3):
             "ms_per_step": ms / steps, "steps": steps, "warmup": warmup}
 
 
-def cpu_baseline(runs, budget_s=15.0):
+def cpu_baseline(runs, seconds=15.0):
     """The oracle (CPU restatement of the same step), all host threads, bounded sample."""
     from oracle.mw3ref import Oracle
     cores = os.cpu_count() or 1
     total_pts, total_t, its_done = 0, 0.0, 0
-    per_wave = budget_s / len(runs)
+    per_wave = seconds / len(runs)
     for r in runs:
         o = Oracle(r, threads=cores)
         o.start(r.psi0)

@@ -4,7 +4,7 @@
  * the list of restated reference routines.  Every loop below follows the
  * cited Fortran loop nest, including its operation order where that fixes the
  * rounding, and its quirks (points with ir1 > nopr1 that the DST leaves out,
- * the k = 0/1 terms the driver never accumulates).
+ * the k = 0/1 terms the main program never accumulates).
  */
 #include "mw3ref.h"
 

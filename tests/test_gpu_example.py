@@ -12,8 +12,8 @@ shipped source's test E > V(flux point) (with the test, P(E) comes out up to
 4e-3 lower near threshold; without it, within 5e-8 of the file), so the flux
 runs here with that test off (mw3_set_flux_gate).
 
-The FP64 path reproduces the norm trace to 1e-10 relative (the north-star
-bar for the plain FP64 path) and P(E) to the file's print precision; the
+The FP64 path reproduces the norm trace to 1e-10 relative (the bar for the
+plain FP64 path) and P(E) to the file's print precision; the
 mixed path (FP32 transforms) reproduces P(E) to 1e-4 absolute, the bar of
 the mixed form."""
 import numpy as np
