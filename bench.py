@@ -38,7 +38,7 @@ FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 # DRAM bytes per stored point and launch of the mixed path's top kernels, from
 # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the J=0..4
 # sweep; the per-block structure of the full sweep is the same, so the traffic
-# scales with the stored points (profiles/k_*_jsweep0-4_256x128x60_mixed.md)
+# scales with the stored points (the ncu summaries of each kernel on that sweep)
 TRAFFIC_PER_POINT = {"dst_R": 16.0, "angular": 16.6, "update": 27.9}
 
 WORKLOADS = {
