@@ -148,3 +148,48 @@ def test_program_on_a_case(runs, case_dirs, tmp_path):
     vib = np.loadtxt(str(rundir / "distriS2prod.vib"))
     assert vib.shape == (run.inp.netot, 2 + nvp)
     assert np.allclose(vib[:, 1], s2no, rtol=1e-6)
+
+
+def test_photodissociation_branch(runs, case_dirs, tmp_path):
+    """iphoto > 0: S2prodfac = 4 pfin / (pi mu') with no packet distribution, and
+    every table scaled by photonorm from the auto file (distriwvp.f:320-327, 436-438)."""
+    from madwave3_gb300 import photo
+    e = np.array([0.5, 1.0, 2.0])
+    ed = np.array([[0.2, 1.5]])                        # [v][j]
+    fac = distri.s2prodfac(e, ed, 0.1, 1500.0, iphoto=1)
+    ekf = e[:, None, None] - ed[None] + 0.1
+    want = np.where(ekf > 0, 4.0 * np.sqrt(np.maximum(ekf, 0) * 1500.0 * 2.0) / distri.HBR / (math.pi * 1500.0), 0.0)
+    assert np.allclose(fac, want, rtol=1e-14)
+    assert fac[0, 0, 1] == 0.0                          # closed channel
+    # the program reads photonorm from the wave's auto file
+    run = runs["tiny_j3"]
+    case = case_dirs["tiny_j3"]
+    pp, o, rows = oracle_history(run, 10)
+    g = namelist.read(os.path.join(case, "input.dat"))
+    g["inputprod"] = dict(iprod=2, nviniprod=pp.nviniprod, nvmaxprod=pp.nvmaxprod, jiniprod=pp.jiniprod,
+                          jmaxprod=pp.jmaxprod, iomminprod=pp.iomminprod, iommaxprod=pp.iommaxprod,
+                          rbalinprod=3.0, n2prod0=pp.n2prod0, n2prod1=pp.n2prod1, nangproj0=pp.nangproj0,
+                          nangproj1=pp.nangproj1)
+    g["inputprocess"] = dict(iphoto=1)
+    g["inputtime"] = dict(g["inputtime"], ntimes=10, nloop=1)
+    out = {}
+    for name, norm in (("a", 1.0), ("b", 0.25)):
+        rundir = tmp_path / name
+        rundir.mkdir()
+        (rundir / "input.dat").write_text(namelist.dumps(g))
+        contfiles.write_cvj_file(str(rundir / "Cvjprod.0001"), range(2, 12), rows)
+        i = run.inp
+        photo.write_auto_file(str(rundir / ("auto.v%02d.j%02d.J%03d" % (i.nvref, i.jref, i.Jtot))), norm, -0.1,
+                              run.emindlt, run.delta2, [1], [0.5])
+        njp, nvp = pp.jmaxprod - pp.jiniprod + 1, pp.nvmaxprod - pp.nviniprod + 1
+        eref_raw = distri._bcwf_energy(os.path.join(case, "func", "bcwf"), i.npun1, i.jini, i.nvini, i.nvref,
+                                       i.jref, i.ielecref)
+        potini.write_prodwf(str(tmp_path / ("p" + name)), pp.jiniprod, pp.nviniprod,
+                            np.zeros((njp, nvp, 1, pp.n2prod1)), np.full((njp, nvp), eref_raw - 0.2), pp.nobcprod)
+        fdir = tmp_path / ("f" + name)
+        fdir.mkdir()
+        (fdir / "bcwf").write_text(open(os.path.join(case, "func", "bcwf")).read())
+        (fdir / "prodwf").write_text(open(str(tmp_path / ("p" + name) / "func" / "prodwf")).read())
+        out[name] = distri.run_program(str(rundir), potdir=os.path.join(case, "pot"), funcdir=str(fdir))
+    assert out["a"][3].max() > 0
+    assert np.allclose(out["b"][3], 0.25 * out["a"][3], rtol=1e-14)
