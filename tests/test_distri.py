@@ -193,3 +193,30 @@ def test_photodissociation_branch(runs, case_dirs, tmp_path):
         out[name] = distri.run_program(str(rundir), potdir=os.path.join(case, "pot"), funcdir=str(fdir))
     assert out["a"][3].max() > 0
     assert np.allclose(out["b"][3], 0.25 * out["a"][3], rtol=1e-14)
+
+
+def test_distri_reproduces_printprob(runs):
+    """The main program's product total S2no (printprob, from the propagation's
+    zS2prod accumulators and ini_transcoor's S2prodfac) and distriwvp's, rebuilt
+    from the per-iteration Cvjprod records with its own packet distribution and
+    hbar literal, agree to the latter's ~1e-4 differences."""
+    from madwave3_gb300 import printprob
+    from madwave3_gb300.host import transcoor
+    run = runs["tiny_j3"]
+    i = run.inp
+    pp, o, rows = oracle_history(run, 60)
+    ft = o.flux_tables()
+    etot = ft["etot"]
+    njp, nvp = pp.jmaxprod - pp.jiniprod + 1, pp.nvmaxprod - pp.nviniprod + 1
+    ediatprod = -0.3 + 0.07 * np.arange(njp * nvp, dtype=np.float64).reshape(njp, nvp)   # zot, from eref
+    fac_main = transcoor.s2prodfac(run, etot, ft["apaqini"], ediatprod, pp.nobcprod, pp.nviniprod, pp.nvmaxprod)
+    zs2, _ = o.product()
+    s2no_main, _ = printprob.s2prod_products(zs2, fac_main, pp)
+    z = distri.chebyshev_sum(rows, etot, run.emindlt, run.delta2)
+    paq, pini = distri.packet_distribution(etot, i.rmis2, i.rfin2, i.rcolini_ang, i.ecol_ev, i.deltae_ev,
+                                           run.xm2reac, i.Jtot, i.jref, i.iomref)
+    fac_d = distri.s2prodfac(etot, ediatprod.T, 0.0, run.xm2prod, paq, pini, run.xm2reac)
+    _, _, s2no_d = distri.distributions(z, fac_d, pp.jiniprod, pp.iomminprod)
+    big = s2no_main > 1e-3 * s2no_main.max()
+    assert big.sum() > 10
+    assert np.allclose(s2no_d[big], s2no_main[big], rtol=1e-3)
