@@ -139,3 +139,13 @@ def test_roofline_charges_the_executing_unit():
     # FP64 path: the FP64 pipe at its nominal rate
     r = bench.dominant_roofline({"dst_r_pair": 5.0}, 10, model, cuda_core, "fp64", 1e8, peaks)
     assert r["bound"] == "fp64" and r["peak"] == bench.FP64_NOMINAL_TFLOPS
+
+
+def test_cpu_baseline_sample(runs):
+    """The bench's CPU-baseline leg (the oracle on every host core, a bounded
+    sample) returns a well-formed entry."""
+    sys.path.insert(0, ROOT)
+    import bench
+    out = bench.cpu_baseline(bench.sample_waves([runs["tiny_j0"]]), seconds=0.5)
+    assert out["kind"] == "port" and out["unit"] == "grid-pt*iter/s" and out["value"] > 0
+    assert out["cores"] >= 1 and "Chebyshev iterations" in out["sample"]
